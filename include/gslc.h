@@ -1,0 +1,185 @@
+/*
+ * gslc.h — C ABI of the GB300 SLC geocoder (libgslc.so).
+ *
+ * One fused sm_103a kernel geocodes a complex64 SLC onto a geographic grid:
+ * DEM biquintic interpolation, zero-Doppler geo2rdr against a Hermite orbit
+ * and a LUT2d Doppler, 8-tap windowed-sinc interpolation with carrier
+ * deramp/reramp and native-Doppler demodulation, and geometric flattening.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: 0 success, > 0 an argument
+ *    error, < 0 a CUDA or runtime error.  Nothing throws across the ABI and
+ *    nothing aborts; gslc_last_error() gives the message.
+ *  - Bulk arrays (SLC blocks, outputs, DEM raster, LUT samples, subswath
+ *    intervals) are DEVICE pointers.  Orbit state vectors and Poly2d
+ *    coefficients are HOST pointers; they are folded into launch parameters.
+ *  - Calls are ordered on the stream passed in (a cudaStream_t, may be 0).
+ *    One context per host thread; a context may be reused across calls.
+ *  - Arrays are C-contiguous row-major.  complex64 is interleaved (re, im).
+ */
+#ifndef GSLC_H
+#define GSLC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSLC_OK 0
+#define GSLC_EINVAL 1          /* argument error (ValueError on the Python side) */
+#define GSLC_EUNSUPPORTED 2    /* valid in the reference, not provided here */
+#define GSLC_EPROJ 3           /* projection inverse failed (reference throws) */
+#define GSLC_ECUDA (-1)        /* CUDA runtime error */
+#define GSLC_ETIMEOUT (-2)     /* a bounded device-side wait ran out */
+
+typedef struct gslc_ctx gslc_ctx;
+
+/* isce3::core::LUT2d<double> (cxx/isce3/core/LUT2d.h:18-112). */
+typedef struct {
+    int32_t have_data;      /* 0: default LUT — contains() is true, eval() = ref_value */
+    int32_t bounds_error;   /* LUT2d::boundsError() */
+    int32_t method;         /* 1 bilinear, 3 nearest (isce3 dataInterpMethod) */
+    int32_t nx, ny;         /* width, length */
+    int32_t _pad;
+    double x0, y0, dx, dy;  /* x = slant range (m), y = azimuth time (s) */
+    double ref_value;
+    const double* data;     /* device, ny*nx */
+} gslc_lut2d;
+
+/* isce3::core::Poly2d (cxx/isce3/core/Poly2d.h:40-70). */
+#define GSLC_POLY_MAX_COEFFS 64
+typedef struct {
+    int32_t x_order, y_order;   /* -1,-1: default polynomial, evaluates to 0 */
+    double x_mean, y_mean, x_norm, y_norm;
+    const double* coeffs;       /* host, (y_order+1)*(x_order+1); row i = y power i */
+} gslc_poly2d;
+
+/* geocodeSlc's AzRgFunc template argument: LUT2d<double> or Poly2d. */
+typedef struct {
+    int32_t kind;           /* 0 LUT2d, 1 Poly2d */
+    int32_t _pad;
+    gslc_lut2d lut;
+    gslc_poly2d poly;
+} gslc_azrg_func;
+
+/* isce3::product::RadarGridParameters (RadarGridParameters.h). */
+typedef struct {
+    double sensing_start, wavelength, prf, starting_range, range_pixel_spacing;
+    int32_t look_side;      /* -1 right, +1 left */
+    int32_t _pad;
+    int64_t length, width;
+} gslc_radar_grid;
+
+/* isce3::product::GeoGridParameters (GeoGridParameters.h). */
+typedef struct {
+    double start_x, start_y, spacing_x, spacing_y;
+    int32_t width, length, epsg, _pad;
+} gslc_geo_grid;
+
+/* isce3::core::Orbit, uniformly sampled (core/Orbit.h, core/Linspace.h). */
+typedef struct {
+    double t0, spacing;     /* time tag i = t0 + i*spacing (s since reference epoch) */
+    int32_t n;
+    int32_t method;         /* 0 Hermite (1 Legendre: GSLC_EUNSUPPORTED) */
+    const double* pos;      /* host, n*3 (m, ECEF) */
+    const double* vel;      /* host, n*3 (m/s) */
+} gslc_orbit;
+
+/* A DEM raster as GDAL exposes it to isce3::geometry::DEMRasterToInterpolator
+ * (geometry/loadDem.cpp:22-133): the whole raster, its geotransform, EPSG. */
+typedef struct {
+    int64_t width, length;  /* full raster size */
+    double gt[6];           /* GDAL geotransform; rotation terms must be 0 */
+    int32_t epsg, _pad;
+    /* Device samples of raster pixels [data_y_off, data_y_off + data_length) x
+     * [data_x_off, data_x_off + data_width), row stride data_stride floats.
+     * The window the geocoder needs must lie inside.  data may be NULL for
+     * gslc_compute_dem_window. */
+    const float* data;
+    int64_t data_x_off, data_y_off, data_width, data_length, data_stride;
+} gslc_dem_raster;
+
+/* The DEM window the reference loads for a geogrid (DEMInterpolator::loadDEM,
+ * geometry/DEMInterpolator.cpp:29-455), in raster pixel coordinates. */
+typedef struct {
+    int32_t have_raster;    /* 0: every height is the reference height 0 */
+    int32_t wraps;          /* 1: window straddles the DEM file discontinuity */
+    int64_t x_off, y_off, width, length;
+    double x_start, y_start, dx, dy;   /* pixel-centre start of the window */
+} gslc_dem_window;
+
+/* isce3::product::SubSwaths (SubSwaths.h). */
+typedef struct {
+    int32_t n;              /* number of subswaths; 0 means "every sample is subswath 1" */
+    int32_t _pad;
+    int64_t length, width;
+    const int32_t* valid;   /* device, n*length*2: [start, stop) range samples per line */
+} gslc_subswaths;
+
+/* Arguments of isce3::geocode::geocodeSlc, array mode
+ * (cxx/isce3/geocode/geocodeSlc.cpp:831-968), with the DEM raster in place of
+ * isce3::io::Raster. */
+typedef struct {
+    gslc_radar_grid radar_grid, sliced_radar_grid;
+    gslc_geo_grid geo_grid;
+    gslc_orbit orbit;
+    gslc_lut2d native_doppler, image_grid_doppler;
+    gslc_lut2d az_time_correction, srange_correction;
+    gslc_azrg_func az_carrier, rg_carrier;
+    double ellipsoid_a, ellipsoid_e2;
+    double threshold_geo2rdr;
+    int32_t numiter_geo2rdr;
+    int32_t flatten, reramp, flatten_with_corrected_srange;
+    int64_t first_azimuth_line, first_range_sample;
+    float invalid_re, invalid_im;
+    int32_t n_blocks;       /* number of (rdr, geo) block pairs sharing the geometry */
+    int32_t inplace_deramp; /* 1: deramp rdr blocks in place like the reference; 0: leave them */
+    int64_t rdr_length, rdr_width;
+    const void* const* rdr_blocks;  /* host array of n_blocks device pointers (complex64) */
+    void* const* geo_blocks;        /* host array of n_blocks device pointers (complex64, geo length*width) */
+    uint8_t* mask;                  /* device or NULL */
+    double* carrier_phase;          /* device or NULL */
+    double* flatten_phase;          /* device or NULL */
+    double* az_index;               /* device or NULL: radar line coordinate per geo pixel (NaN if invalid) */
+    double* rg_index;               /* device or NULL: radar sample coordinate per geo pixel */
+    gslc_dem_raster dem;
+    int32_t dem_margin;             /* DEM pixels of margin (reference default 50) */
+    int32_t geo2rdr_precision;      /* 0 FP64 (reference numerics), 1 float-float */
+    const gslc_subswaths* subswaths;  /* host pointer to descriptor, or NULL */
+} gslc_geocode_args;
+
+int gslc_ctx_create(int device, gslc_ctx** out);
+int gslc_ctx_destroy(gslc_ctx* ctx);
+const char* gslc_last_error(const gslc_ctx* ctx);
+const char* gslc_version(void);
+
+/* Host-only: the DEM window the geocoder loads for geo_grid
+ * (replaces geometry/loadDem.cpp:22-133 + DEMInterpolator.cpp:29-455). */
+int gslc_compute_dem_window(const gslc_dem_raster* dem, const gslc_geo_grid* geo_grid, int32_t margin,
+                    gslc_dem_window* out);
+
+/* Host-only: platform position/velocity at time t from the per-interval
+ * polynomial form of the Hermite interpolant the kernels evaluate (replaces
+ * isce3::core::Orbit::interpolate, core/Orbit.cpp:71-86, for Hermite).
+ * Returns GSLC_EINVAL outside the orbit's time span. */
+int gslc_orbit_interpolate(const gslc_orbit* orbit, double t, double* pos, double* vel);
+
+/* Host-only: the float sinc kernel table (SINC_SUB=8192 phases x 8 taps) the
+ * kernels use (core/Sinc2dInterpolator.cpp:12-40, cast to float at use). */
+int gslc_sinc_table(float* out);
+
+/* Plain form: geocode one geogrid from n_blocks SLC blocks.
+ * Replaces isce3::geocode::geocodeSlc<AzRgFunc>, array mode
+ * (cxx/isce3/geocode/geocodeSlc.cpp:831-968; bound to Python as
+ * isce3.ext.isce3.geocode._geocode_slc in
+ * python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:218-334). */
+int gslc_geocode_slc(gslc_ctx* ctx, const gslc_geocode_args* args, void* stream);
+
+/* Number of the library's own kernels launched by the last call on ctx. */
+int64_t gslc_last_launch_count(const gslc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSLC_H */

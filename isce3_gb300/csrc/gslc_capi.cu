@@ -1,0 +1,611 @@
+// C ABI of libgslc.so: contexts, argument checks, host-side precomputation
+// (sinc table, orbit polynomials, DEM window) and kernel launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/gslc.h"
+#include "gslc_kernels.cuh"
+
+using namespace gslc;
+
+struct gslc_ctx {
+    int device = 0;
+    float* d_sinc = nullptr;        // SINC_SUB * SINC_LEN
+    int32_t* d_err = nullptr;
+    int32_t* h_err = nullptr;       // pinned
+    double* d_orbit = nullptr;
+    size_t orbit_cap = 0;           // doubles
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int set_err(gslc_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+
+int cuda_err(gslc_ctx* c, cudaError_t e, const char* where) {
+    return set_err(c, GSLC_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// core/Sinc2dInterpolator.cpp:12-40 and :98-115 — Hann-weighted sinc,
+// SINC_LEN taps x SINC_SUB phases, each phase normalised to unit sum, then
+// cast to float at use (Sinc2dInterpolator.cpp:88-90).
+std::vector<float> make_sinc_table() {
+    const int filtercoef = SINC_SUB * SINC_LEN;
+    std::vector<double> filter(filtercoef, 0.0);
+    const double beta = 1.0, pedestal = 0.0;
+    const double wgthgt = (1.0 - pedestal) / 2.0;
+    const double soff = (filtercoef - 1.) / 2.;
+    for (int i = 0; i < filtercoef; i++) {
+        const double wgt = (1. - wgthgt) + (wgthgt * std::cos((M_PI * (i - soff)) / soff));
+        const double s = (std::floor(i - soff) * beta) / (1. * SINC_SUB);
+        const double fct = ((s != 0.) ? (std::sin(M_PI * s) / (M_PI * s)) : 1.);
+        filter[i] = fct * wgt;
+    }
+    std::vector<float> table((size_t)filtercoef);
+    for (int i = 0; i < SINC_SUB; ++i) {
+        double ssum = 0.0;
+        for (int j = 0; j < SINC_LEN; ++j) ssum += filter[i + SINC_SUB * j];
+        for (int j = 0; j < SINC_LEN; ++j) {
+            filter[i + SINC_SUB * j] /= ssum;
+            table[(size_t)i * SINC_LEN + j] = (float)filter[i + SINC_SUB * j];
+        }
+    }
+    return table;
+}
+
+// Data-independent part of _initSpline for n = 6
+// (core/Spline2dInterpolator.cpp:95-100), in FP32 like the reference.
+SplineConst make_spline_const() {
+    SplineConst k{};
+    float q_prev = 0.0f;
+    for (int i = 1; i < 5; ++i) {
+        volatile float half_q = 0.5f * q_prev;   // keep mul and add separately rounded
+        const float p = 1.0f / (half_q + 2.0f);
+        k.p[i] = p;
+        k.q[i] = -0.5f * p;
+        q_prev = k.q[i];
+    }
+    k.p[0] = k.q[0] = 0.0f;
+    return k;
+}
+
+// ---- double-double helpers (Knuth TwoSum, FMA-based TwoProd) --------------
+struct dd { double hi, lo; };
+dd two_sum(double a, double b) {
+    const double s = a + b, bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+dd dd_add(dd a, dd b) {
+    dd s = two_sum(a.hi, b.hi);
+    s.lo += a.lo + b.lo;
+    return two_sum(s.hi, s.lo);
+}
+dd dd_mul_d(dd a, double b) {
+    const double p = a.hi * b;
+    const double e = std::fma(a.hi, b, -p);
+    return two_sum(p, e + a.lo * b);
+}
+dd dd_div_d(dd a, double b) {
+    const double q1 = a.hi / b;
+    dd r = dd_add(a, dd_mul_d({q1, 0.0}, -b));
+    const double q2 = r.hi / b;
+    return two_sum(q1, q2);
+}
+
+// Integer-coefficient polynomials (exact in double for these sizes).
+using P8 = std::vector<double>;
+P8 pmul(const P8& a, const P8& b) {
+    P8 r(a.size() + b.size() - 1, 0.0);
+    for (size_t i = 0; i < a.size(); ++i)
+        for (size_t j = 0; j < b.size(); ++j) r[i + j] += a[i] * b[j];
+    return r;
+}
+// q(u + c): Taylor shift, exact for dyadic c and these magnitudes
+P8 pshift(const P8& q, double c) {
+    P8 r(q.size(), 0.0);
+    for (size_t k = 0; k < q.size(); ++k) {
+        // (u + c)^k = sum_m C(k,m) c^(k-m) u^m
+        double binom = 1.0;
+        for (size_t m = 0; m <= k; ++m) {
+            if (m > 0) binom = binom * (double)(k - m + 1) / (double)m;
+            r[m] += q[k] * binom * std::pow(c, (double)(k - m));
+        }
+    }
+    return r;
+}
+
+// Expansion of the 4-point Hermite interpolant
+// (core/detail/InterpolateOrbit.icc:10-109) on each state-vector interval.
+// With s = (t - t_idx)/spacing and nodes s = 0..3:
+//   pos(s) = sum_i L_i(s)^2 [(1 - 2 sigma_i (s - i)) P_i + spacing (s - i) V_i]
+// where L_i is the Lagrange basis and sigma_i = sum_{j != i} 1/(i - j).
+// Stored around u = s - 1.5 and P_ref = P_{idx+1}.
+void make_orbit_coeffs(const gslc_orbit& o, std::vector<double>& out) {
+    const int npieces = o.n - 3;
+    out.assign((size_t)npieces * ORB_STRIDE, 0.0);
+    const P8 s1{0.0, 1.0};
+    auto lin = [](double a, double b) { return P8{a, b}; };  // a + b s
+    P8 N[4] = {pmul(pmul(lin(-1, 1), lin(-2, 1)), lin(-3, 1)), pmul(pmul(s1, lin(-2, 1)), lin(-3, 1)),
+               pmul(pmul(s1, lin(-1, 1)), lin(-3, 1)), pmul(pmul(s1, lin(-1, 1)), lin(-2, 1))};
+    const P8 Lp[4] = {lin(3, 11), lin(0, 27), lin(81, -27), lin(36, -11)};  // 108 * L_i^2 factor * f0_i / N_i^2
+    const double cB[4] = {1, 9, 9, 1};                                      // 36 / D_i^2
+    P8 A[4], B[4];
+    for (int i = 0; i < 4; ++i) {
+        const P8 n2 = pmul(N[i], N[i]);
+        A[i] = pshift(pmul(n2, Lp[i]), 1.5);                   // = 108 * A_i(u)
+        P8 bi = pmul(n2, lin(-(double)i, 1));
+        for (double& v : bi) v *= cB[i];
+        B[i] = pshift(bi, 1.5);                                // = 36 * B_i(u)
+    }
+    for (int idx = 0; idx < npieces; ++idx) {
+        double* c = out.data() + (size_t)idx * ORB_STRIDE;
+        for (int d = 0; d < 3; ++d) {
+            const double pref = o.pos[(idx + 1) * 3 + d];
+            c[d] = pref;
+            double a[8];
+            for (int k = 0; k < 8; ++k) {
+                dd sa{0.0, 0.0}, sb{0.0, 0.0};
+                for (int i = 0; i < 4; ++i) {
+                    const double dp = o.pos[(idx + i) * 3 + d] - pref;
+                    sa = dd_add(sa, dd_mul_d({dp, 0.0}, A[i][k]));
+                    sb = dd_add(sb, dd_mul_d({o.vel[(idx + i) * 3 + d], 0.0}, B[i][k]));
+                }
+                dd term = dd_add(dd_div_d(sa, 108.0), dd_mul_d(dd_div_d(sb, 36.0), o.spacing));
+                a[k] = term.hi + term.lo;
+                c[3 + d * 8 + k] = a[k];
+            }
+            for (int k = 0; k < 7; ++k) c[27 + d * 7 + k] = (double)(k + 1) * a[k + 1] / o.spacing;
+        }
+    }
+}
+
+bool utm_setup(int code, Utm& u) {
+    // core/Projections.cpp:80-170
+    int zone;
+    if (code > 32600 && code <= 32660) { zone = code - 32600; u.isnorth = 1; }
+    else if (code > 32700 && code <= 32760) { zone = code - 32700; u.isnorth = 0; }
+    else return false;
+    u.lon0 = ((zone - 0.5) * (M_PI / 30.)) - M_PI;
+    const double f = WGS84_E2 / (1. + std::sqrt(1 - WGS84_E2));
+    const double n = f / (2. - f);
+    u.cgb[0] = n * (2 + n * ((-2. / 3.) + n * (-2 + n * ((116. / 45.) + n * ((26. / 45.) + n * (-2854. / 675.))))));
+    u.cbg[0] = n * (-2 + n * ((2. / 3.) + n * ((4. / 3.) + n * ((-82. / 45.) + n * ((32. / 45.) + n * (4642. / 4725.))))));
+    u.cgb[1] = std::pow(n, 2) * ((7. / 3.) + n * ((-8. / 5.) + n * ((-227. / 45.) + n * ((2704. / 315.) + n * (2323. / 945.)))));
+    u.cbg[1] = std::pow(n, 2) * ((5. / 3.) + n * ((-16. / 15.) + n * ((-13. / 9.) + n * ((904. / 315.) + n * (-1522. / 945.)))));
+    u.cgb[2] = std::pow(n, 3) * ((56. / 15.) + n * ((-136. / 35.) + n * ((-1262. / 105.) + n * (73814. / 2835.))));
+    u.cbg[2] = std::pow(n, 3) * ((-26. / 15.) + n * ((34. / 21.) + n * ((8. / 5.) + n * (-12686. / 2835.))));
+    u.cgb[3] = std::pow(n, 4) * ((4279. / 630.) + n * ((-332. / 35.) + n * (-399572 / 14175.)));
+    u.cbg[3] = std::pow(n, 4) * ((1237. / 630.) + n * ((-12. / 5.) + n * (-24832. / 14175.)));
+    u.cgb[4] = std::pow(n, 5) * ((4174. / 315.) + n * (-144838. / 6237.));
+    u.cbg[4] = std::pow(n, 5) * ((-734. / 315.) + n * (109598. / 31185.));
+    u.cgb[5] = std::pow(n, 6) * (601676. / 22275.);
+    u.cbg[5] = std::pow(n, 6) * (444337. / 155925.);
+    u.Qn = (0.9996 / (1. + n)) * (1. + n * n * ((1. / 4.) + n * n * ((1. / 64.) + ((n * n) / 256.))));
+    u.utg[0] = n * (-.5 + n * ((2. / 3.) + n * ((-37. / 96.) + n * ((1. / 360.) + n * ((81. / 512.) + n * (-96199. / 604800.))))));
+    u.gtu[0] = n * (.5 + n * ((-2. / 3.) + n * ((5. / 16.) + n * ((41. / 180.) + n * ((-127. / 288.) + n * (7891. / 37800.))))));
+    u.utg[1] = std::pow(n, 2) * ((-1. / 48.) + n * ((-1. / 15.) + n * ((437. / 1440.) + n * ((-46. / 105.) + n * (1118711. / 3870720.)))));
+    u.gtu[1] = std::pow(n, 2) * ((13. / 48.) + n * ((-3. / 5.) + n * ((557. / 1440.) + n * ((281. / 630.) + n * (-1983433. / 1935360.)))));
+    u.utg[2] = std::pow(n, 3) * ((-17. / 480.) + n * ((37. / 840.) + n * ((209. / 4480.) + n * (-5569. / 90720.))));
+    u.gtu[2] = std::pow(n, 3) * ((61. / 240.) + n * ((-103. / 140.) + n * ((15061. / 26880.) + n * (167603. / 181440.))));
+    u.utg[3] = std::pow(n, 4) * ((-4397. / 161280.) + n * ((11. / 504.) + n * (830251. / 7257600.)));
+    u.gtu[3] = std::pow(n, 4) * ((49561. / 161280.) + n * ((-179. / 168.) + n * (6601661. / 7257600.)));
+    u.utg[4] = std::pow(n, 5) * ((-4583. / 161280.) + n * (108847. / 3991680.));
+    u.gtu[4] = std::pow(n, 5) * ((34729. / 80640.) + n * (-3418889. / 1995840.));
+    u.utg[5] = std::pow(n, 6) * (-20648693. / 638668800.);
+    u.gtu[5] = std::pow(n, 6) * (212378941. / 319334400.);
+    const double Z = clens(u.cbg, 0.);
+    u.Zb = -u.Qn * (Z + clens(u.gtu, 2 * Z));
+    return true;
+}
+
+bool is_lonlat_or_utm(int epsg) { return epsg == 4326 || (epsg > 32600 && epsg <= 32660) || (epsg > 32700 && epsg <= 32760); }
+
+// Map <-> lon/lat(rad) for LonLat or UTM (core/Projections.h:127-140).
+bool proj_inverse(int epsg, const Utm& u, double x, double y, double& lon, double& lat) {
+    if (epsg == 4326) { lon = x * M_PI / 180.0; lat = y * M_PI / 180.0; return true; }
+    return utm_inverse(u, x, y, lon, lat);
+}
+bool proj_forward(int epsg, const Utm& u, double lon, double lat, double& x, double& y) {
+    if (epsg == 4326) { x = lon * 180.0 / M_PI; y = lat * 180.0 / M_PI; return true; }
+    return utm_forward(u, lon, lat, x, y);
+}
+
+Lut to_lut(const gslc_lut2d& l) {
+    Lut o{};
+    o.have_data = l.have_data;
+    o.bounds_error = l.bounds_error;
+    o.method = l.method;
+    o.nx = l.nx;
+    o.ny = l.ny;
+    o.x0 = l.x0; o.y0 = l.y0; o.dx = l.dx; o.dy = l.dy;
+    o.ref_value = l.ref_value;
+    o.data = l.data;
+    return o;
+}
+
+int check_lut(gslc_ctx* c, const gslc_lut2d& l, const char* name) {
+    if (!l.have_data) return 0;
+    if (l.method != 1 && l.method != 3)
+        return set_err(c, GSLC_EUNSUPPORTED, std::string(name) + ": only bilinear and nearest LUT2d interpolation");
+    if (l.nx < 1 || l.ny < 1 || !l.data) return set_err(c, GSLC_EINVAL, std::string(name) + ": LUT2d without data");
+    return 0;
+}
+
+int to_azrg(gslc_ctx* c, const gslc_azrg_func& f, AzRg& o, const char* name) {
+    std::memset(&o, 0, sizeof(o));
+    o.kind = f.kind;
+    if (f.kind == 0) {
+        if (int st = check_lut(c, f.lut, name)) return st;
+        o.lut = to_lut(f.lut);
+        o.is_zero = (!f.lut.have_data && f.lut.ref_value == 0.0) ? 1 : 0;
+    } else if (f.kind == 1) {
+        const gslc_poly2d& p = f.poly;
+        const int nc = (p.x_order + 1) * (p.y_order + 1);
+        if (p.x_order < -1 || p.y_order < -1) return set_err(c, GSLC_EINVAL, std::string(name) + ": bad Poly2d order");
+        if (nc > POLY_MAX) return set_err(c, GSLC_EUNSUPPORTED, std::string(name) + ": Poly2d has more than 64 coefficients");
+        o.poly.x_order = p.x_order;
+        o.poly.y_order = p.y_order;
+        o.poly.x_mean = p.x_mean; o.poly.y_mean = p.y_mean;
+        o.poly.x_norm = p.x_norm; o.poly.y_norm = p.y_norm;
+        for (int i = 0; i < nc; ++i) o.poly.c[i] = p.coeffs[i];
+        // the default Poly2d (order -1) evaluates to exactly 0 (core/Poly2d.h:56)
+        o.is_zero = nc <= 0 ? 1 : 0;
+    } else {
+        return set_err(c, GSLC_EINVAL, std::string(name) + ": unknown carrier kind");
+    }
+    return 0;
+}
+
+}  // namespace
+
+// ---- DEM window: geometry/loadDem.cpp:22-133 + DEMInterpolator.cpp:29-455 --
+extern "C" int gslc_compute_dem_window(const gslc_dem_raster* r, const gslc_geo_grid* g, int32_t margin, gslc_dem_window* out) {
+    if (!r || !g || !out) return GSLC_EINVAL;
+    std::memset(out, 0, sizeof(*out));
+    if (!is_lonlat_or_utm(r->epsg) || !is_lonlat_or_utm(g->epsg)) return GSLC_EUNSUPPORTED;
+    if (r->gt[2] != 0.0 || r->gt[4] != 0.0) return GSLC_EUNSUPPORTED;
+    const int lineStart = 0, blockLength = g->length, blockWidth = g->width;
+    double minX = std::numeric_limits<double>::max(), maxX = std::numeric_limits<double>::lowest();
+    double minY = std::numeric_limits<double>::max(), maxY = std::numeric_limits<double>::lowest();
+    if (r->epsg != g->epsg) {
+        Utm ug{}, ud{};
+        if (g->epsg != 4326) utm_setup(g->epsg, ug);
+        if (r->epsg != 4326) utm_setup(r->epsg, ud);
+        const int askip = std::max(static_cast<int>(blockLength / 10.), 1);
+        const int rskip = std::max(static_cast<int>(blockWidth / 10.), 1);
+        std::vector<int> li, pi;
+        for (int j = 0; j < blockWidth; j += rskip) { li.push_back(0); pi.push_back(j); }
+        for (int i = 0; i < blockLength; i += askip) { li.push_back(i); pi.push_back(blockWidth); }
+        for (int j = blockWidth; j > 0; j -= rskip) { li.push_back(blockLength - 1); pi.push_back(j); }
+        for (int i = blockLength; i > 0; i -= askip) { li.push_back(i); pi.push_back(0); }
+        for (size_t i = 0; i < li.size(); ++i) {
+            const double ox = g->start_x + g->spacing_x * pi[i];
+            const double oy = g->start_y + g->spacing_y * (lineStart + li[i]);
+            double lon, lat, dx, dy;
+            if (!proj_inverse(g->epsg, ug, ox, oy, lon, lat) || !proj_forward(r->epsg, ud, lon, lat, dx, dy))
+                return GSLC_EPROJ;
+            minX = std::min(minX, dx); maxX = std::max(maxX, dx);
+            minY = std::min(minY, dy); maxY = std::max(maxY, dy);
+        }
+    } else {
+        maxY = g->start_y + g->spacing_y * lineStart;
+        minY = g->start_y + g->spacing_y * (lineStart + blockLength - 1);
+        minX = g->start_x;
+        maxX = g->start_x + g->spacing_x * (blockWidth - 1);
+    }
+    minX -= margin * r->gt[1];
+    maxX += margin * r->gt[1];
+    minY -= margin * std::abs(r->gt[5]);
+    maxY += margin * std::abs(r->gt[5]);
+
+    // DEMInterpolator::loadDEM
+    double min_x = minX, max_x = maxX, min_y = minY, max_y = maxY;
+    const double delta_y = r->gt[5], delta_x = r->gt[1];
+    if (delta_x < 0) return GSLC_EINVAL;
+    const double dem_y0 = r->gt[3];
+    double dem_x0 = r->gt[0];
+    const bool ll = r->epsg == 4326;
+    if (ll) {
+        if (max_x - min_x > 360 + 2 * delta_x) max_x = min_x + 360 + delta_x;
+        if (min_x < -180 - delta_x || max_x < -180 - delta_x || max_x > 360 + delta_x) {
+            const double n_wraps = std::floor(max_x / 360);
+            min_x -= n_wraps * 360;
+            max_x -= n_wraps * 360;
+        }
+        if (min_x < -180 - delta_x || max_x < -180 - delta_x) { min_x += 360; max_x += 360; }
+        if (min_x > 0 && max_x < 0) max_x += 360;
+        if (dem_x0 > 360 + delta_x || dem_x0 < -180 - delta_x) dem_x0 = std::fmod(dem_x0, 360);
+    }
+    const double dem_yf = dem_y0 + r->length * delta_y;
+    const double dem_xf = dem_x0 + r->width * delta_x;
+    if (ll && min_x < dem_xf - 360 - delta_x) { min_x += 360; max_x += 360; }
+    else if (ll && min_x > 180 && max_x > dem_x0 + 360 + delta_x) { min_x -= 360; max_x -= 360; }
+    const bool disc = ll && (min_x <= dem_xf) && (dem_xf < max_x) && (min_x <= dem_x0 + 360) && (dem_x0 + 360 < max_x);
+    if (min_x < dem_x0) min_x = dem_x0;
+    if (max_x > dem_xf && !disc) max_x = dem_xf;
+    if (min_y < dem_yf) min_y = dem_yf;
+    if (max_y > dem_y0) max_y = dem_y0;
+    long min_x_idx = (long)std::floor((min_x - dem_x0) / delta_x);
+    long max_x_idx = (long)std::ceil((max_x - dem_x0) / delta_x);
+    long min_y_idx = (long)std::floor((max_y - dem_y0) / delta_y);
+    long max_y_idx = (long)std::ceil((min_y - dem_y0) / delta_y);
+    out->x_start = dem_x0 + (0.5 + min_x_idx) * delta_x;
+    out->y_start = dem_y0 + (0.5 + min_y_idx) * delta_y;
+    out->dx = delta_x;
+    out->dy = delta_y;
+    long width = max_x_idx - min_x_idx, length = max_y_idx - min_y_idx;
+    if (!disc && min_x_idx + width > r->width) width = r->width - min_x_idx;
+    if (!disc && min_y_idx + length > r->length) length = r->length - min_y_idx;
+    out->x_off = min_x_idx;
+    out->y_off = min_y_idx;
+    out->width = width;
+    out->length = length;
+    out->wraps = disc ? 1 : 0;
+    // A window with no pixels leaves the interpolator without a raster: every
+    // height is then the reference height (DEMInterpolator.cpp:393-397).
+    out->have_raster = (width > 0 && length > 0) ? 1 : 0;
+    if (out->have_raster && (min_x_idx < 0 || min_y_idx < 0)) return GSLC_EINVAL;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_orbit_interpolate(const gslc_orbit* o, double t, double* pos, double* vel) {
+    if (!o || !pos || !vel || o->n < 4 || !(o->spacing > 0) || o->method != 0) return GSLC_EINVAL;
+    std::vector<double> coef;
+    make_orbit_coeffs(*o, coef);
+    Orbit ob{};
+    ob.t0 = o->t0; ob.spacing = o->spacing; ob.inv_spacing = 1.0 / o->spacing;
+    ob.t_end = o->t0 + (o->n - 1) * o->spacing; ob.n = o->n; ob.n_pieces = o->n - 3; ob.coef = coef.data();
+    if (!(t >= ob.t0 && t <= ob.t_end)) return GSLC_EINVAL;
+    V3 p, v;
+    orbit_eval(ob, t, p, v);
+    pos[0] = p.x; pos[1] = p.y; pos[2] = p.z;
+    vel[0] = v.x; vel[1] = v.y; vel[2] = v.z;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_sinc_table(float* out) {
+    if (!out) return GSLC_EINVAL;
+    const std::vector<float> t = make_sinc_table();
+    std::memcpy(out, t.data(), t.size() * sizeof(float));
+    return GSLC_OK;
+}
+
+extern "C" const char* gslc_version(void) { return "gslc 0.1 (sm_103a)"; }
+
+extern "C" int gslc_ctx_create(int device, gslc_ctx** out) {
+    if (!out) return GSLC_EINVAL;
+    *out = nullptr;
+    gslc_ctx* c = new (std::nothrow) gslc_ctx();
+    if (!c) return GSLC_ECUDA;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete c; return GSLC_ECUDA; }
+    const std::vector<float> table = make_sinc_table();
+    e = cudaMalloc(&c->d_sinc, table.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_sinc, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int32_t) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(int32_t) * 4);
+    if (e != cudaSuccess) { gslc_ctx_destroy(c); return GSLC_ECUDA; }
+    *out = c;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_ctx_destroy(gslc_ctx* c) {
+    if (!c) return GSLC_OK;
+    cudaSetDevice(c->device);
+    if (c->d_sinc) cudaFree(c->d_sinc);
+    if (c->d_err) cudaFree(c->d_err);
+    if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->d_orbit) cudaFree(c->d_orbit);
+    delete c;
+    return GSLC_OK;
+}
+
+extern "C" const char* gslc_last_error(const gslc_ctx* c) { return c ? c->err.c_str() : "no context"; }
+extern "C" int64_t gslc_last_launch_count(const gslc_ctx* c) { return c ? c->launches : 0; }
+
+namespace {
+
+bool grid_ok(const gslc_radar_grid& g) {
+    return g.prf > 0 && g.range_pixel_spacing != 0 && g.length > 0 && g.width > 0 && g.wavelength > 0 &&
+           (g.look_side == -1 || g.look_side == 1);
+}
+double grid_stop(const gslc_radar_grid& g) { return g.sensing_start + (g.length - 1.0) / g.prf; }
+double grid_end(const gslc_radar_grid& g) { return g.starting_range + (g.width - 1.0) * g.range_pixel_spacing; }
+
+}  // namespace
+
+extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (!a) return set_err(c, GSLC_EINVAL, "null arguments");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const gslc_radar_grid& rg = a->radar_grid;
+    const gslc_radar_grid& srg = a->sliced_radar_grid;
+    const gslc_geo_grid& gg = a->geo_grid;
+    if (a->n_blocks < 1 || !a->rdr_blocks || !a->geo_blocks)
+        return set_err(c, GSLC_EINVAL, "number of geoDataBlocks != number of rdrDataBlocks");
+    if (!grid_ok(rg) || !grid_ok(srg)) return set_err(c, GSLC_EINVAL, "invalid radar grid");
+    if (gg.width < 0 || gg.length < 0) return set_err(c, GSLC_EINVAL, "invalid geogrid");
+    // geocodeSlc.cpp:548-580 (validate_slice)
+    if (srg.sensing_start < rg.sensing_start) return set_err(c, GSLC_EINVAL, "sliced grid sensing start < full grid sensing start");
+    if (grid_stop(srg) > grid_stop(rg)) return set_err(c, GSLC_EINVAL, "sliced grid sensing stop < full grid sensing stop");
+    if (srg.starting_range < rg.starting_range) return set_err(c, GSLC_EINVAL, "sliced grid staring range < full grid staring range");
+    if (grid_end(srg) > grid_end(rg)) return set_err(c, GSLC_EINVAL, "sliced grid ending range < full grid ending range");
+    if (srg.look_side != rg.look_side) return set_err(c, GSLC_EINVAL, "sliced grid look side != full grid look side");
+    if (srg.wavelength != rg.wavelength) return set_err(c, GSLC_EINVAL, "sliced grid wavelength != full grid wavelength");
+    if (!is_lonlat_or_utm(gg.epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
+    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
+    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
+        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (a->rdr_length < 0 || a->rdr_width < 0) return set_err(c, GSLC_EINVAL, "invalid radar block shape");
+    if (gg.width == 0 || gg.length == 0) return GSLC_OK;
+    for (const gslc_lut2d* l : {&a->native_doppler, &a->image_grid_doppler, &a->az_time_correction, &a->srange_correction})
+        if (int st = check_lut(c, *l, "LUT2d")) return st;
+
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+
+    GeoParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.gx0 = gg.start_x; p.gy0 = gg.start_y; p.gdx = gg.spacing_x; p.gdy = gg.spacing_y;
+    p.gw = gg.width; p.gl = gg.length;
+    p.geo_is_lonlat = gg.epsg == 4326;
+    if (!p.geo_is_lonlat) utm_setup(gg.epsg, p.utm);
+
+    // DEM window the reference would load (loadDem.cpp:22-133)
+    gslc_dem_window w;
+    int st = gslc_compute_dem_window(&a->dem, &gg, a->dem_margin, &w);
+    if (st == GSLC_EPROJ) return set_err(c, GSLC_EINVAL, "projection transformation between geogrid and DEM failed");
+    if (st != GSLC_OK) return set_err(c, st, "unsupported or invalid DEM raster");
+    if (w.wraps) return set_err(c, GSLC_EUNSUPPORTED, "DEM window crossing the DEM file discontinuity");
+    p.dem.have_raster = w.have_raster && a->dem.data != nullptr;
+    p.dem.epsg_is_lonlat = a->dem.epsg == 4326;
+    if (!p.dem.epsg_is_lonlat) utm_setup(a->dem.epsg, p.dem.utm);
+    if (p.dem.have_raster) {
+        const gslc_dem_raster& d = a->dem;
+        if (w.x_off < d.data_x_off || w.y_off < d.data_y_off || w.x_off + w.width > d.data_x_off + d.data_width ||
+            w.y_off + w.length > d.data_y_off + d.data_length || d.data_stride < d.data_width)
+            return set_err(c, GSLC_EINVAL, "DEM samples provided do not cover the DEM window of the geogrid");
+        p.dem.data = d.data + (w.y_off - d.data_y_off) * d.data_stride + (w.x_off - d.data_x_off);
+        p.dem.stride = d.data_stride;
+        p.dem.width = (int32_t)w.width;
+        p.dem.length = (int32_t)w.length;
+        p.dem.x_start = w.x_start; p.dem.y_start = w.y_start;
+        p.dem.dx = w.dx; p.dem.dy = w.dy;
+    }
+    p.dem.sc = make_spline_const();
+    p.ell_a = a->ellipsoid_a;
+    p.ell_e2 = a->ellipsoid_e2;
+
+    // orbit polynomials
+    std::vector<double> coef;
+    make_orbit_coeffs(a->orbit, coef);
+    if (coef.size() > c->orbit_cap) {
+        if (c->d_orbit) cudaFree(c->d_orbit);
+        c->d_orbit = nullptr;
+        e = cudaMalloc(&c->d_orbit, coef.size() * sizeof(double));
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc orbit");
+        c->orbit_cap = coef.size();
+    }
+    e = cudaMemcpyAsync(c->d_orbit, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "orbit upload");
+    Orbit& ob = p.orbit;
+    ob.t0 = a->orbit.t0;
+    ob.spacing = a->orbit.spacing;
+    ob.inv_spacing = 1.0 / a->orbit.spacing;
+    ob.t_end = a->orbit.t0 + (a->orbit.n - 1) * a->orbit.spacing;
+    ob.n = a->orbit.n;
+    ob.n_pieces = a->orbit.n - 3;
+    ob.coef = c->d_orbit;
+
+    // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)
+    p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
+    p.t_mid_in_orbit = (p.t_mid >= ob.t0 && p.t_mid <= ob.t_end) ? 1 : 0;
+    if (p.t_mid_in_orbit) {
+        Orbit host_ob = ob;
+        host_ob.coef = coef.data();
+        orbit_eval(host_ob, p.t_mid, p.pos0, p.vel0);
+    }
+    p.thr = a->threshold_geo2rdr;
+    p.maxiter = a->numiter_geo2rdr;
+    p.rg_t0 = rg.sensing_start; p.rg_prf = rg.prf; p.rg_r0 = rg.starting_range;
+    p.rg_dr = rg.range_pixel_spacing; p.rg_wvl = rg.wavelength;
+    p.rg_len = rg.length; p.rg_wid = rg.width;
+    p.look_side = rg.look_side;
+    // sliced grid contains() bounds (RadarGridParameters.cpp:27-35)
+    const double half_az = (1.0 / srg.prf) / 2, half_rg = srg.range_pixel_spacing / 2;
+    p.s_t0 = srg.sensing_start - half_az;
+    p.s_r0 = srg.starting_range - half_rg;
+    p.s_stop = grid_stop(srg) + half_az;
+    p.s_end = grid_end(srg) + half_rg;
+    p.nat_dop = to_lut(a->native_doppler);
+    p.img_dop = to_lut(a->image_grid_doppler);
+    p.az_corr = to_lut(a->az_time_correction);
+    p.sr_corr = to_lut(a->srange_correction);
+    if ((st = to_azrg(c, a->az_carrier, p.az_car, "az_carrier"))) return st;
+    if ((st = to_azrg(c, a->rg_carrier, p.rg_car, "rg_carrier"))) return st;
+    p.carriers_zero = p.az_car.is_zero && p.rg_car.is_zero;
+    p.flat_scale = 4.0 * (M_PI / rg.wavelength);
+    p.flatten = a->flatten; p.reramp = a->reramp; p.use_corr = a->flatten_with_corrected_srange;
+    p.inv_re = a->invalid_re; p.inv_im = a->invalid_im;
+    p.inL = a->rdr_length; p.inW = a->rdr_width;
+    p.az_first = a->first_azimuth_line; p.rg_first = a->first_range_sample;
+    p.mask = a->mask;
+    p.carrier_out = a->carrier_phase;
+    p.flatten_out = a->flatten_phase;
+    p.az_out = a->az_index;
+    p.rg_out = a->rg_index;
+    p.sinc = c->d_sinc;
+    if (a->subswaths) {
+        p.have_subsw = 1;
+        p.subsw_n = a->subswaths->n;
+        p.subsw_len = a->subswaths->length;
+        p.subsw_wid = a->subswaths->width;
+        p.subsw = a->subswaths->valid;
+        if (p.subsw_n > 0 && !p.subsw) return set_err(c, GSLC_EINVAL, "subswaths without valid-sample arrays");
+    }
+    p.err = c->d_err;
+    e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "memset");
+
+    // carrier deramp: the reference mutates the radar blocks in place
+    // (geocodeSlc.cpp:952-953); without inplace_deramp the deramped copy goes
+    // to stream-ordered scratch.
+    const int64_t nrdr = a->rdr_length * a->rdr_width;
+    std::vector<void*> scratch;
+    std::vector<const float2*> rdr(a->n_blocks);
+    for (int b = 0; b < a->n_blocks; ++b) rdr[b] = (const float2*)a->rdr_blocks[b];
+    if (!p.carriers_zero && nrdr > 0) {
+        for (int b = 0; b < a->n_blocks; ++b) {
+            float2* dst = (float2*)a->rdr_blocks[b];
+            if (!a->inplace_deramp) {
+                void* buf = nullptr;
+                e = cudaMallocAsync(&buf, nrdr * sizeof(float2), stream);
+                if (e != cudaSuccess) {
+                    for (void* s : scratch) cudaFreeAsync(s, stream);
+                    return cuda_err(c, e, "cudaMallocAsync deramp scratch");
+                }
+                scratch.push_back(buf);
+                dst = (float2*)buf;
+            }
+            DerampParams dp;
+            std::memset(&dp, 0, sizeof(dp));
+            dp.src = rdr[b]; dp.dst = dst;
+            dp.inL = a->rdr_length; dp.inW = a->rdr_width;
+            dp.az_first = a->first_azimuth_line; dp.rg_first = a->first_range_sample;
+            dp.rg_t0 = rg.sensing_start; dp.rg_prf = rg.prf; dp.rg_r0 = rg.starting_range; dp.rg_dr = rg.range_pixel_spacing;
+            dp.az_car = p.az_car; dp.rg_car = p.rg_car;
+            e = launch_deramp(dp, stream, &c->launches);
+            if (e != cudaSuccess) return cuda_err(c, e, "deramp launch");
+            rdr[b] = dst;
+        }
+    }
+    for (int b0 = 0; b0 < a->n_blocks; b0 += MAX_BLOCKS) {
+        p.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
+        for (int b = 0; b < p.nblk; ++b) {
+            p.rdr[b] = rdr[b0 + b];
+            p.geo[b] = (float2*)a->geo_blocks[b0 + b];
+        }
+        e = launch_geocode(p, a->geo2rdr_precision, stream, &c->launches);
+        if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
+    }
+    for (void* s : scratch) cudaFreeAsync(s, stream);
+    e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "geocode");
+    if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    return GSLC_OK;
+}

@@ -1,0 +1,358 @@
+// Fused SLC geocoding kernel (sm_103a) and the carrier deramp pre-pass.
+//
+// One thread per output geogrid pixel:
+//   map x/y -> lon/lat (LonLat or UTM inverse, core/Projections.cpp:200-232)
+//   -> DEM height (biquintic FP32, geometry/DEMInterpolator.cpp:617-659)
+//   -> geo2rdr Newton (geometry/detail/Geo2Rdr.icc:114-179), FP64
+//   -> corrections, radar-grid checks, subswath mask (geocode/geocodeSlc.cpp:55-228)
+//   -> per SLC block: 8x8 windowed-sinc with native-Doppler demodulation
+//      (geocodeSlc.cpp:409-511, core/Sinc2dInterpolator.cpp:45-96),
+//      then carrier reramp and flattening (geocodeSlc.cpp:298-394).
+// Nothing here is a dense contraction, so no tensor cores; the kernel is
+// bound by the FP64 pipe (geometry) and latency, not by HBM.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include "gslc_kernels.cuh"
+
+namespace gslc {
+
+namespace {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    // std::complex<float> product for finite operands: (ac - bd, ad + bc)
+    const float ac = fmul(a.x, b.x), bd = fmul(a.y, b.y), ad = fmul(a.x, b.y), bc = fmul(a.y, b.x);
+    return make_float2(fsub(ac, bd), fadd(ad, bc));
+}
+
+// cos/sin of a large FP64 phase: reduce by 2*pi in FP64 (Cody-Waite with a
+// two-term 2*pi), then evaluate in FP32.  Error ~1e-7 rad against the
+// reference's float(cos(double)).
+__device__ __forceinline__ float2 expi_fp64(double ph) {
+    constexpr double INV_2PI = 0.15915494309189535;
+    constexpr double TWO_PI_HI = 6.283185307179586;
+    constexpr double TWO_PI_LO = 2.4492935982947064e-16;
+    const double k = rint(ph * INV_2PI);
+    double r = fma(-k, TWO_PI_HI, ph);
+    r = fma(-k, TWO_PI_LO, r);
+    float s, c;
+    sincosf((float)r, &s, &c);
+    return make_float2(c, s);
+}
+
+// geometry/DEMInterpolator.cpp:593-659 + core/Spline2dInterpolator.cpp:32-67
+__device__ double dem_height(const Dem& d, double lon, double lat) {
+    const double ref = 0.0;
+    if (!d.have_raster) return ref;
+    double X, Y;
+    if (d.epsg_is_lonlat) {
+        X = (lon * 180.0) / PI;
+        Y = (lat * 180.0) / PI;
+        if (X > 360 || X < -360) X = fmod(X, 360.0);
+        if (X < -180) X += 360;
+        if (X - 360 >= d.x_start) X -= 360;
+        else if (X < d.x_start && X + 360 >= d.x_start) X += 360;
+        else if (X < d.x_start) return ref;
+    } else {
+        if (!utm_forward(d.utm, lon, lat, X, Y)) return ref;
+        if (X < d.x_start) return ref;
+    }
+    const double row = (Y - d.y_start) / d.dy;
+    const double col = (X - d.x_start) / d.dx;
+    const int irow = (int)floor(row), icol = (int)floor(col);
+    if (irow < 2 || irow >= d.length - 1) return ref;
+    if (icol < 2 || icol >= d.width - 1) return ref;
+    // order-6 spline window (Spline2dInterpolator.cpp:43-51)
+    const int i0 = (int)row - 2, j0 = (int)col - 2;
+    const float xx = (float)((col - (double)j0) - 2.0);
+    const float yy = (float)((row - (double)i0) - 2.0);
+    int cidx[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) cidx[j] = min(max(j0 + j, 0), d.width - 2) + 1;
+    float HC[6], A[6], R[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const int indi = min(max(i0 + i, 0), d.length - 2) + 1;
+        const float* rowp = d.data + (int64_t)indi * d.stride;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) A[j] = __ldg(rowp + cidx[j]);
+        init_spline6(A, R, d.sc);
+        HC[i] = spline6_at(xx, A, R);
+    }
+    init_spline6(HC, R, d.sc);
+    return (double)spline6_at(yy, HC, R);
+}
+
+// geometry/detail/Geo2Rdr.icc:50-112 (coarse search when the initial guess is
+// outside the orbit)
+__device__ bool update_aztime(const GeoParams& p, V3 xyz, double& t) {
+    const double tstart = p.orbit.t0, tend = p.orbit.t_end;
+    const double dt = (tend - tstart) / 14;
+    double r_closest = 1e16, t_closest = -1000.;
+    for (int k = 0; k < 15; ++k) {
+        const double tt = tstart + k * dt;
+        if (tt < tstart || tt > tend) continue;
+        V3 pos, vel;
+        orbit_eval(p.orbit, tt, pos, vel);
+        const V3 rvec = vsub(xyz, pos);
+        if (k == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
+        const double r = vnorm(rvec);
+        if (r < r_closest) { r_closest = r; t_closest = tt; }
+    }
+    t = (t_closest < 0.) ? 0.5 * (tstart + tend) : t_closest;
+    return true;
+}
+
+// geometry/detail/Geo2Rdr.icc:114-179 with geometry/geometry.cpp:241-251
+// (deltaRange = 1e-8 as passed by geocodeSlc.cpp:120-123).
+__device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
+    constexpr double dr = 1.0e-8;
+    t = p.t_mid;
+    bool first_shared = p.t_mid_in_orbit;
+    if (!p.t_mid_in_orbit && !update_aztime(p, xyz, t)) return false;
+    const bool dop_data = p.img_dop.have_data;
+    const bool dop_const = !dop_data && p.img_dop.ref_value == 0.0;
+    const double half_wvl = 0.5 * p.rg_wvl;
+    double dt = 0.0;
+    for (int i = 0; i < p.maxiter; ++i) {
+        t -= dt;
+        V3 pos, vel;
+        if (i == 0 && first_shared) {
+            pos = p.pos0;
+            vel = p.vel0;
+        } else {
+            if (!(t >= p.orbit.t0 && t <= p.orbit.t_end)) return false;  // FillNaN -> no convergence
+            orbit_eval(p.orbit, t, pos, vel);
+        }
+        const V3 rvec = vsub(xyz, pos);
+        R = vnorm(rvec);
+        if (i == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
+        if (dop_data && p.img_dop.bounds_error &&
+            !(lut_contains(p.img_dop, t, R) && lut_contains(p.img_dop, t, R + dr)))
+            return false;
+        const double dopfact = vdot(rvec, vel);
+        const double c1 = -vdot(vel, vel);
+        double fn, fnprime;
+        if (dop_const) {
+            fn = dopfact;        // fdop == 0 and fdopder == 0 exactly
+            fnprime = c1;
+        } else {
+            const double fdop = half_wvl * lut_eval(p.img_dop, t, R);
+            const double fdopder = (half_wvl * lut_eval(p.img_dop, t, R + dr) - fdop) / dr;
+            fn = dopfact - fdop * R;
+            const double c2 = (fdop / R) + fdopder;
+            fnprime = c1 + c2 * dopfact;
+        }
+        dt = fn / fnprime;
+        if (fabs(dt) < p.thr) return true;
+    }
+    return false;
+}
+
+// product/SubSwaths.cpp:58-96
+__device__ int subswath_of(const GeoParams& p, int az, int rg) {
+    if (rg < 0 || rg >= p.subsw_wid || az < 0 || az >= p.subsw_len) return 0;
+    if (p.subsw_n == 0) return 1;
+    for (int s = 0; s < p.subsw_n; ++s) {
+        const int32_t* v = p.subsw + ((int64_t)s * p.subsw_len + az) * 2;
+        if (rg >= __ldg(v) && rg < __ldg(v + 1)) return s + 1;
+    }
+    return 0;
+}
+
+// geocodeSlc.cpp:409-511 for one pixel and one block: 9x9 chip demodulated
+// by the native Doppler, Sinc2d over it (Sinc2dInterpolator.cpp:45-96), then
+// the Doppler added back.  Sum order is the reference's (i outer, j inner).
+__device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr, int intAz, int intRg,
+                             double fracAz, double fracRg, double doppFreq) {
+    const double x = 4.0 + fracRg, y = 4.0 + fracAz;
+    const int ix = (int)floor(x), iy = (int)floor(y);
+    const double fx = x - ix, fy = y - iy;
+    if (ix < 3 || ix > 4 || iy < 3 || iy > 4) return make_float2(0.f, 0.f);
+    const int ifx = min(max(0, (int)(fx * SINC_SUB)), SINC_SUB - 1);
+    const int ify = min(max(0, (int)(fy * SINC_SUB)), SINC_SUB - 1);
+    float kx[8], ky[8];
+    const float4* kxp = reinterpret_cast<const float4*>(p.sinc + ifx * SINC_LEN);
+    const float4* kyp = reinterpret_cast<const float4*>(p.sinc + ify * SINC_LEN);
+    {
+        float4 a = __ldg(kxp), b = __ldg(kxp + 1), c = __ldg(kyp), d = __ldg(kyp + 1);
+        kx[0] = a.x; kx[1] = a.y; kx[2] = a.z; kx[3] = a.w; kx[4] = b.x; kx[5] = b.y; kx[6] = b.z; kx[7] = b.w;
+        ky[0] = c.x; ky[1] = c.y; ky[2] = c.z; ky[3] = c.w; ky[4] = d.x; ky[5] = d.y; ky[6] = d.z; ky[7] = d.w;
+    }
+    const bool demod = doppFreq != 0.0;
+    // demodulation phasors for row offsets m = 0..4 (doppPhase = doppFreq*m)
+    float dc[5], ds[5];
+    if (demod) {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) sincosf((float)(doppFreq * m), &ds[m], &dc[m]);
+    }
+    // chip row r9 = iy + 4 - i maps to radar row intAz + iy - i; col c9 = ix + 4 - j
+    const float2* base = rdr + (int64_t)(intAz + iy) * p.inW + (intRg + ix);
+    float sre = 0.f, sim = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float2* rowp = base - (int64_t)i * p.inW;
+        float2 dv = make_float2(1.f, 0.f);
+        if (demod) {
+            const int m = iy - i;
+            const int am = m < 0 ? -m : m;
+            // doppVal = (cos(phase), -sin(phase)), phase = doppFreq * m
+            dv = make_float2(dc[am], m < 0 ? ds[am] : -ds[am]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            float2 a = __ldg(rowp - j);
+            if (demod) a = cmul(a, dv);
+            sre = fadd(sre, fmul(fmul(a.x, ky[i]), kx[j]));
+            sim = fadd(sim, fmul(fmul(a.y, ky[i]), kx[j]));
+        }
+    }
+    // A non-finite chip sample turns both parts of the reference's complex
+    // products into NaN (x*0 with x = inf or NaN).
+    if (!isfinite(sre) || !isfinite(sim)) return make_float2(CUDART_NAN_F, CUDART_NAN_F);
+    float2 cval = make_float2(sre, sim);
+    if (demod) {
+        float s, c;
+        sincosf((float)(doppFreq * fracAz), &s, &c);
+        cval = cmul(cval, make_float2(c, s));
+    }
+    return cval;
+}
+
+template <bool GEO_LONLAT>
+__global__ void __launch_bounds__(128) geocode_kernel(const __grid_constant__ GeoParams p) {
+    const int pixel = blockIdx.x * blockDim.x + threadIdx.x;
+    const int line = blockIdx.y * blockDim.y + threadIdx.y;
+    if (pixel >= p.gw || line >= p.gl) return;
+    const int64_t k = (int64_t)line * p.gw + pixel;
+
+    bool valid = false;
+    uint8_t mval = 255;
+    double azc = CUDART_NAN, rgc = CUDART_NAN;
+    double R_uncorr = (double)p.inv_re;
+
+    // pixel centre (geocodeSlc.cpp:100-103), same rounding as the reference
+    const double y = dadd(p.gy0, dmul(p.gdy, (double)line + 0.5));
+    const double x = dadd(p.gx0, dmul(p.gdx, (double)pixel + 0.5));
+    double lon, lat;
+    bool ok = true;
+    if (GEO_LONLAT) {
+        lon = (x * PI) / 180.0;
+        lat = (y * PI) / 180.0;
+    } else {
+        ok = utm_inverse(p.utm, x, y, lon, lat);
+        if (!ok) atomicOr(p.err, 1);
+    }
+    if (ok) {
+        const double h = dem_height(p.dem, lon, lat);
+        const V3 xyz = lonlat_to_xyz(p.ell_a, p.ell_e2, lon, lat, h);
+        double t, R;
+        if (geo2rdr(p, xyz, t, R)) {
+            if (!p.use_corr) R_uncorr = R;
+            if (lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
+            if (lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
+            const bool in_grid = t >= p.s_t0 && R >= p.s_r0 && t <= p.s_stop && R <= p.s_end;
+            if (in_grid && lut_contains(p.nat_dop, t, R)) {
+                azc = (t - p.rg_t0) * p.rg_prf;
+                rgc = (R - p.rg_r0) / p.rg_dr;
+                valid = true;
+                const int intAz = (int)floor(azc), intRg = (int)floor(rgc);
+                const bool corners = !(intRg < 4 || intRg >= p.rg_wid - 4 || intAz < 4 || intAz >= p.rg_len - 4);
+                if (p.have_subsw && p.mask) {
+                    int m = subswath_of(p, intAz, intRg);
+                    if (m != 0) {
+                        if (subswath_of(p, intAz - 4, intRg - 4) == 0 || subswath_of(p, intAz - 4, intRg + 4) == 0 ||
+                            subswath_of(p, intAz + 4, intRg - 4) == 0 || subswath_of(p, intAz + 4, intRg + 4) == 0)
+                            m = 0;
+                    }
+                    mval = (uint8_t)m;
+                } else if (corners) {
+                    mval = 1;
+                }
+            }
+        }
+    }
+    if (p.mask) p.mask[k] = mval;
+    if (p.az_out) p.az_out[k] = azc;
+    if (p.rg_out) p.rg_out[k] = rgc;
+
+    const float2 invalid = make_float2(p.inv_re, p.inv_im);
+    if (!valid) {
+        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
+        return;
+    }
+    // block-relative chip position (geocodeSlc.cpp:440-458, 335-348)
+    const double RgIndex = rgc - (double)p.rg_first, AzIndex = azc - (double)p.az_first;
+    const int intRgB = (int)RgIndex, intAzB = (int)AzIndex;
+    const double fracRg = RgIndex - intRgB, fracAz = AzIndex - intAzB;
+    bool interp = !(intRgB < 4 || intRgB >= p.inW - 4 || intAzB < 4 || intAzB >= p.inL - 4);
+    double rng = 0.0, az = 0.0;
+    if (interp) {
+        rng = dadd(p.rg_r0, dmul(rgc, p.rg_dr));
+        az = p.rg_t0 + azc / p.rg_prf;
+        interp = lut_contains(p.nat_dop, az, rng);
+    }
+    if (!interp) {
+        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
+        return;
+    }
+    const double doppFreq = ((lut_eval(p.nat_dop, az, rng) * 2) * PI) / p.rg_prf;
+    // reramp + flatten phase (geocodeSlc.cpp:362-392)
+    const double carrier = p.carriers_zero ? 0.0 : azrg_eval(p.rg_car, az, rng) + azrg_eval(p.az_car, az, rng);
+    const double flat = p.flat_scale * (p.use_corr ? rng : R_uncorr);
+    double total = 0.0;
+    if (p.reramp) total += carrier;
+    if (p.flatten) total += flat;
+    if (p.carrier_out) p.carrier_out[k] = carrier;
+    if (p.flatten_out) p.flatten_out[k] = flat;
+    const bool rot = total != 0.0;
+    float2 ph = make_float2(1.f, 0.f);
+    if (rot) ph = expi_fp64(total);
+    for (int b = 0; b < p.nblk; ++b) {
+        float2 v = sinc_pixel(p, p.rdr[b], intAzB, intRgB, fracAz, fracRg, doppFreq);
+        if (rot) v = cmul(v, ph);
+        p.geo[b][k] = v;
+    }
+}
+
+// geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier))
+__global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ DerampParams p) {
+    const int64_t n = p.inL * p.inW;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx / p.inW, j = idx - i * p.inW;
+        const double az = p.rg_t0 + (double)(i + p.az_first) / p.rg_prf;
+        const double rg = dadd(p.rg_r0, dmul((double)(j + p.rg_first), p.rg_dr));
+        const float phase = (float)(azrg_eval(p.rg_car, az, rg) + azrg_eval(p.az_car, az, rg));
+        float s, c;
+        sincosf(phase, &s, &c);
+        p.dst[idx] = cmul(p.src[idx], make_float2(c, -s));
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
+    (void)precision;
+    const dim3 block(32, 4);
+    const dim3 grid((p.gw + 31) / 32, (p.gl + 3) / 4);
+    if (p.geo_is_lonlat) geocode_kernel<true><<<grid, block, 0, s>>>(p);
+    else geocode_kernel<false><<<grid, block, 0, s>>>(p);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t n = p.inL * p.inW;
+    int64_t blocks = (n + 255) / 256;
+    const int64_t cap = (int64_t)sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    deramp_kernel<<<(unsigned)blocks, 256, 0, s>>>(p);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+}  // namespace gslc

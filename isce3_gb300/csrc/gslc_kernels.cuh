@@ -1,0 +1,74 @@
+// Launch parameters shared by the host launcher and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "gslc_math.cuh"
+
+namespace gslc {
+
+constexpr int MAX_BLOCKS = 16;   // (rdr, geo) block pairs per launch
+
+struct Dem {
+    const float* data;          // points at raster (y_off, x_off); row stride = stride
+    int64_t stride;
+    int32_t width, length;      // window size (spline clamps and bounds use these)
+    int32_t have_raster, epsg_is_lonlat;
+    double x_start, y_start, dx, dy;
+    Utm utm;                    // DEM projection when it is UTM
+    SplineConst sc;
+};
+
+struct GeoParams {
+    // geogrid
+    double gx0, gy0, gdx, gdy;
+    int32_t gw, gl;
+    int32_t geo_is_lonlat, _pad0;
+    Utm utm;
+    Dem dem;
+    double ell_a, ell_e2;
+    Orbit orbit;
+    // geo2rdr
+    double t_mid;               // RadarGridParameters::sensingMid(), initial guess
+    int32_t t_mid_in_orbit, maxiter;
+    double thr;
+    V3 pos0, vel0;              // orbit at t_mid (first Newton iterate is shared)
+    // radar grid (full) and sliced grid
+    double rg_t0, rg_prf, rg_r0, rg_dr, rg_wvl;
+    int64_t rg_len, rg_wid;
+    int32_t look_side, _pad1;
+    double s_t0, s_stop, s_r0, s_end, s_half_az, s_half_rg;
+    // LUTs
+    Lut nat_dop, img_dop, az_corr, sr_corr;
+    AzRg az_car, rg_car;
+    double flat_scale;          // 4.0 * (M_PI / wavelength)
+    int32_t flatten, reramp, use_corr, carriers_zero;
+    float inv_re, inv_im;
+    // radar blocks
+    int32_t nblk, _pad2;
+    int64_t inL, inW, az_first, rg_first;
+    const float2* rdr[MAX_BLOCKS];
+    float2* geo[MAX_BLOCKS];
+    uint8_t* mask;
+    double* carrier_out;
+    double* flatten_out;
+    double* az_out;
+    double* rg_out;
+    const float* sinc;          // [SINC_SUB][SINC_LEN]
+    const int32_t* subsw;       // [n][length][2] or NULL
+    int32_t subsw_n, have_subsw;
+    int64_t subsw_len, subsw_wid;
+    int32_t* err;               // device error word: bit 0 projection inverse failed
+};
+
+struct DerampParams {
+    const float2* src;
+    float2* dst;
+    int64_t inL, inW, az_first, rg_first;
+    double rg_t0, rg_prf, rg_r0, rg_dr;
+    AzRg az_car, rg_car;
+};
+
+// launchers (gslc_kernels.cu)
+cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
+cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);
+
+}  // namespace gslc

@@ -1,0 +1,292 @@
+// Host/device math for the SLC geocoder.
+//
+// Where the reference computes in FP32 (the biquintic DEM spline,
+// cxx/isce3/core/Spline2dInterpolator.cpp:32-108) the device code uses
+// round-to-nearest intrinsics so nvcc cannot contract or reorder: one ULP of
+// DEM height moves the flattening phase by ~4e-3 rad at L-band, far above the
+// 1e-4 rad parity tolerance.  FP64 geometry may contract to FMA; its
+// differences stay ~1e-16 relative.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+
+#ifdef __CUDACC__
+#define GSLC_HD __host__ __device__ __forceinline__
+#else
+#define GSLC_HD inline
+#endif
+
+namespace gslc {
+
+// ---- exact-order FP32 / FP64 primitives (device: _rn intrinsics) ----------
+#if defined(__CUDA_ARCH__)
+GSLC_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
+GSLC_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
+GSLC_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
+GSLC_HD float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+GSLC_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+GSLC_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+#else
+GSLC_HD float fadd(float a, float b) { return a + b; }
+GSLC_HD float fsub(float a, float b) { return a - b; }
+GSLC_HD float fmul(float a, float b) { return a * b; }
+GSLC_HD float fdiv(float a, float b) { return a / b; }
+GSLC_HD double dadd(double a, double b) { return a + b; }
+GSLC_HD double dmul(double a, double b) { return a * b; }
+#endif
+
+constexpr double PI = 3.14159265358979323846;
+constexpr double WGS84_A = 6378137.0;                 // core/Constants.h:41
+constexpr double WGS84_E2 = 0.006694379990141317;     // core/Constants.h:44
+constexpr int SINC_HALF = 4, SINC_LEN = 8, SINC_ONE = 9, SINC_SUB = 8192;  // core/Constants.h:32-35
+
+struct V3 { double x, y, z; };
+GSLC_HD V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+GSLC_HD double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+GSLC_HD V3 vcross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+GSLC_HD double vnorm(V3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// ---- LUT2d (core/LUT2d.{h,cpp}) ------------------------------------------
+struct Lut {
+    int32_t have_data, bounds_error, method, nx, ny, _pad;
+    double x0, y0, dx, dy, ref_value;
+    const double* data;
+};
+
+// core/LUT2d.h:84-95
+GSLC_HD bool lut_contains(const Lut& l, double y, double x) {
+    if (!l.have_data) return true;
+    const double i = (x - l.x0) / l.dx;
+    const double j = (y - l.y0) / l.dy;
+    return (i >= 0.0 && i <= l.nx - 1.0) && (j >= 0.0 && j <= l.ny - 1.0);
+}
+
+template <typename T>
+GSLC_HD T ld_ro(const T* p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+// core/LUT2d.cpp:124-158 with core/BilinearInterpolator.cpp:12-49 or
+// core/NearestNeighborInterpolator.cpp:12-22.  The bilinear divisions by
+// (x2-x1)*(y2-y1) == 1 are exact and omitted.
+GSLC_HD double lut_eval(const Lut& l, double y, double x) {
+    if (!l.have_data) return l.ref_value;
+    double xi = (x - l.x0) / l.dx;
+    double yi = (y - l.y0) / l.dy;
+    xi = fmin(fmax(xi, 0.0), l.nx - 1.0);
+    yi = fmin(fmax(yi, 0.0), l.ny - 1.0);
+    if (l.method == 3) {
+        long r = (long)round(yi), c = (long)round(xi);
+        return ld_ro(l.data + r * l.nx + c);
+    }
+    const int x1 = (int)floor(xi), x2 = (int)ceil(xi);
+    const int y1 = (int)floor(yi), y2 = (int)ceil(yi);
+    const double q11 = ld_ro(l.data + (long)y1 * l.nx + x1), q12 = ld_ro(l.data + (long)y2 * l.nx + x1);
+    const double q21 = ld_ro(l.data + (long)y1 * l.nx + x2), q22 = ld_ro(l.data + (long)y2 * l.nx + x2);
+    if (y1 == y2 && x1 == x2) return q11;
+    if (y1 == y2) return ((x2 - xi) / (x2 - x1)) * q11 + ((xi - x1) / (x2 - x1)) * q21;
+    if (x1 == x2) return ((y2 - yi) / (y2 - y1)) * q11 + ((yi - y1) / (y2 - y1)) * q12;
+    return q11 * ((x2 - xi) * (y2 - yi)) + q21 * ((xi - x1) * (y2 - yi)) +
+           q12 * ((x2 - xi) * (yi - y1)) + q22 * ((xi - x1) * (yi - y1));
+}
+
+// ---- Poly2d (core/Poly2d.cpp:8-24) ----------------------------------------
+constexpr int POLY_MAX = 64;
+struct Poly {
+    int32_t x_order, y_order;
+    double x_mean, y_mean, x_norm, y_norm;
+    double c[POLY_MAX];
+};
+
+GSLC_HD double poly_eval(const Poly& p, double y, double x) {
+    const double xval = (x - p.x_mean) / p.x_norm;
+    const double yval = (y - p.y_mean) / p.y_norm;
+    double scaley = 1., val = 0.;
+    for (int i = 0; i <= p.y_order; i++, scaley *= yval) {
+        double scalex = 1.;
+        for (int j = 0; j <= p.x_order; j++, scalex *= xval) val += scalex * scaley * p.c[i * (p.x_order + 1) + j];
+    }
+    return val;
+}
+
+struct AzRg {
+    int32_t kind;      // 0 LUT2d, 1 Poly2d
+    int32_t is_zero;   // evaluates to exactly 0 everywhere (default object)
+    Lut lut;
+    Poly poly;
+};
+
+GSLC_HD double azrg_eval(const AzRg& f, double y, double x) {
+    if (f.is_zero) return 0.0;
+    return f.kind == 1 ? poly_eval(f.poly, y, x) : lut_eval(f.lut, y, x);
+}
+
+// ---- Ellipsoid (core/Ellipsoid.h:117-120, 177-190) -------------------------
+GSLC_HD V3 lonlat_to_xyz(double a, double e2, double lon, double lat, double h) {
+    double slat, clat, slon, clon;
+#if defined(__CUDA_ARCH__)
+    sincos(lat, &slat, &clat);
+    sincos(lon, &slon, &clon);
+#else
+    slat = sin(lat); clat = cos(lat); slon = sin(lon); clon = cos(lon);
+#endif
+    const double re = a / sqrt(1.0 - e2 * (slat * slat));
+    return {(re + h) * clat * clon, (re + h) * clat * slon, ((re * (1.0 - e2)) + h) * slat};
+}
+
+// ---- Projections (core/Projections.{h,cpp}) -------------------------------
+struct Utm {
+    int32_t isnorth, _pad;
+    double lon0, Qn, Zb;
+    double cgb[6], cbg[6], utg[6], gtu[6];
+};
+
+// core/Projections.cpp:33-42 (real Clenshaw summation)
+GSLC_HD double clens(const double* a, double real) {
+    const double cr = cos(real);
+    double hr2 = 0., hr1 = a[5], hr = 0.;
+    for (int k = 4; k >= 0; --k) {
+        hr = -hr2 + (2. * hr1 * cr) + a[k];
+        hr2 = hr1;
+        hr1 = hr;
+    }
+    return sin(real) * hr;
+}
+
+// core/Projections.cpp:54-74 (complex Clenshaw summation).  The row/column
+// factors sin/cos(real) and sinh/cosh(imag) are evaluated once.
+GSLC_HD void clenS(const double* a, double sr, double cr, double shi, double chi, double& R, double& I) {
+    double hr2 = 0., hi2 = 0., hi1 = 0., hr1 = a[5], hr = 0., hi = 0.;
+    const double rr = 2. * cr * chi, ii = -2. * sr * shi;
+    for (int k = 4; k >= 0; --k) {
+        hr = -hr2 + (hr1 * rr) - (hi1 * ii) + a[k];
+        hi = -hi2 + (hr1 * ii) + (hi1 * rr);
+        hr2 = hr1; hi2 = hi1; hr1 = hr; hi1 = hi;
+    }
+    R = (sr * chi * hr) - (cr * shi * hi);
+    I = (sr * chi * hi) + (cr * shi * hr);
+}
+
+// core/Projections.cpp:200-232; returns false where the reference throws.
+GSLC_HD bool utm_inverse(const Utm& u, double x, double y, double& lon, double& lat) {
+    double Cn = (y - (u.isnorth ? 0. : 10000000.)) / WGS84_A;
+    double Ce = (x - 500000.) / WGS84_A;
+    Cn = (Cn - u.Zb) / u.Qn;
+    Ce /= u.Qn;
+    if (!(fabs(Ce) <= 2.623395162778)) return false;
+    double sr, cr;
+#if defined(__CUDA_ARCH__)
+    sincos(2 * Cn, &sr, &cr);
+#else
+    sr = sin(2 * Cn); cr = cos(2 * Cn);
+#endif
+    const double shi = sinh(2 * Ce), chi = cosh(2 * Ce);
+    double dCn, dCe;
+    clenS(u.utg, sr, cr, shi, chi, dCn, dCe);
+    Cn += dCn;
+    Ce = atan(sinh(Ce + dCe));
+    double sinCe, cosCe, sinCn, cosCn;
+#if defined(__CUDA_ARCH__)
+    sincos(Ce, &sinCe, &cosCe);
+    sincos(Cn, &sinCn, &cosCn);
+#else
+    sinCe = sin(Ce); cosCe = cos(Ce); sinCn = sin(Cn); cosCn = cos(Cn);
+#endif
+    Ce = atan2(sinCe, cosCe * cosCn);
+    Cn = atan2(sinCn * cosCe, hypot(sinCe, cosCe * cosCn));
+    lon = Ce + u.lon0;
+    lat = clens(u.cgb, 2 * Cn) + Cn;
+    return true;
+}
+
+// core/Projections.cpp:172-198
+GSLC_HD bool utm_forward(const Utm& u, double lon, double lat, double& x, double& y) {
+    const double gauss = clens(u.cbg, 2. * lat) + lat;
+    const double lam = lon - u.lon0;
+    double Cn = atan2(sin(gauss), cos(lam) * cos(gauss));
+    double Ce = atan2(sin(lam) * cos(gauss), hypot(sin(gauss), cos(gauss) * cos(lam)));
+    Ce = asinh(tan(Ce));
+    double dCn, dCe;
+    clenS(u.gtu, sin(2 * Cn), cos(2 * Cn), sinh(2 * Ce), cosh(2 * Ce), dCn, dCe);
+    Cn += dCn;
+    Ce += dCe;
+    if (!(fabs(Ce) <= 2.623395162778)) return false;
+    x = (u.Qn * Ce * WGS84_A) + 500000.;
+    y = (((u.Qn * Cn) + u.Zb) * WGS84_A) + (u.isnorth ? 0. : 10000000.);
+    return true;
+}
+
+// ---- Orbit as per-interval polynomials -------------------------------------
+// The 4-point Hermite interpolant of core/detail/InterpolateOrbit.icc:10-109
+// is, on each state-vector interval, one degree-7 polynomial in
+// u = (t - t_idx)/spacing - 1.5; velocity is its derivative.  The host
+// expands it once per interval (gslc_capi.cu) around P_ref = P_{idx+1}.
+constexpr int ORB_STRIDE = 48;   // pref[3], a[3][8], b[3][7] (b = d/dt coefficients)
+
+struct Orbit {
+    double t0, spacing, inv_spacing, t_end;
+    int32_t n, n_pieces;
+    const double* coef;          // n_pieces * ORB_STRIDE
+};
+
+GSLC_HD int orbit_piece(const Orbit& o, double t) {
+    // core/Linspace.icc:77-89 search(t) - 2, clamped (InterpolateOrbit.icc:18-19)
+    int idx = (int)((t - o.t0) * o.inv_spacing + 1) - 2;
+    idx = idx < 0 ? 0 : idx;
+    idx = idx > o.n - 4 ? o.n - 4 : idx;
+    return idx;
+}
+
+GSLC_HD void orbit_eval(const Orbit& o, double t, V3& pos, V3& vel) {
+    const int idx = orbit_piece(o, t);
+    const double* c = o.coef + (long)idx * ORB_STRIDE;
+    const double tidx = o.t0 + idx * o.spacing;
+    const double u = (t - tidx) * o.inv_spacing - 1.5;
+    double p[3], v[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double* a = c + 3 + d * 8;
+        double acc = ld_ro(a + 7);
+#pragma unroll
+        for (int k = 6; k >= 0; --k) acc = acc * u + ld_ro(a + k);
+        p[d] = ld_ro(c + d) + acc;
+        const double* b = c + 27 + d * 7;
+        double vacc = ld_ro(b + 6);
+#pragma unroll
+        for (int k = 5; k >= 0; --k) vacc = vacc * u + ld_ro(b + k);
+        v[d] = vacc;
+    }
+    pos = {p[0], p[1], p[2]};
+    vel = {v[0], v[1], v[2]};
+}
+
+// ---- Biquintic spline, FP32, exact reference order -------------------------
+// core/Spline2dInterpolator.cpp:89-108 (_initSpline) for n = 6.  p[i], q[i]
+// depend on nothing but n; the host computes them with the same FP32 ops.
+struct SplineConst { float p[5], q[5]; };
+
+GSLC_HD void init_spline6(const float Y[6], float R[6], const SplineConst& k) {
+    R[0] = 0.0f;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) {
+        const float t = fadd(fsub(Y[i + 1], fmul(2.0f, Y[i])), Y[i - 1]);
+        R[i] = fmul(fsub(fmul(3.0f, t), fmul(0.5f, R[i - 1])), k.p[i]);
+    }
+    R[5] = 0.0f;
+#pragma unroll
+    for (int i = 4; i > 0; --i) R[i] = fadd(fmul(k.q[i], R[i + 1]), R[i]);
+}
+
+// core/Spline2dInterpolator.cpp:69-87 (_spline) on the branch every in-range
+// DEM point takes: x - j0 lies in [2, 3), so j = 2.
+GSLC_HD float spline6_at(float xx, const float Y[6], const float R[6]) {
+    const float t0 = fsub(fsub(fsub(Y[2], Y[1]), fdiv(R[1], 3.0f)), fdiv(R[2], 6.0f));
+    const float t1 = fmul(xx, fadd(fmul(R[1], 0.5f), fmul(xx, fdiv(fsub(R[2], R[1]), 6.0f))));
+    return fadd(Y[1], fmul(xx, fadd(t0, t1)));
+}
+
+}  // namespace gslc

@@ -1,0 +1,255 @@
+"""Drop-in for ``isce3.geocode.geocode_slc`` backed by the sm_103a kernel.
+
+Argument names, defaults, the list/array validation and the error types follow
+python/packages/isce3/geocode/geocode_slc.py:11-240 and the pybind binding
+python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:218-334.  The C++ call
+it replaces is isce3::geocode::geocodeSlc (array mode,
+cxx/isce3/geocode/geocodeSlc.cpp:831-968); here it is gslc_geocode_slc in
+libgslc.so.
+
+Arrays may be NumPy (host; copied to the GPU and results copied back, like a
+call on host memory) or CUDA ``torch.Tensor`` (device-resident; no copies).
+One difference is deliberate: the reference deramps the caller's radar
+arrays in place (geocodeSlc.cpp:952-953); this call leaves them unchanged
+unless ``inplace_deramp=True`` is given for device tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import logging
+from types import SimpleNamespace
+from typing import Union
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import _marshal as M
+from .core import Ellipsoid, LUT2d, Orbit, Poly2d
+from .product import GeoGridParameters, RadarGridParameters, SubSwaths
+
+log = logging.getLogger("isce3_gb300.geocode.geocode_slc")
+
+ArrayLike = Union[np.ndarray, torch.Tensor]
+
+
+def _is_array(x) -> bool:
+    return isinstance(x, (np.ndarray, torch.Tensor))
+
+
+def _io_value_check(io):
+    """geocode_slc.py:11-58."""
+    chk = SimpleNamespace(is_list=False, is_array=False, n_items=0, shapes_consistent=False,
+                          dtypes_consistent=False, is_valid=False)
+    if isinstance(io, list):
+        chk.is_list = True
+        if io:
+            chk.n_items = len(io)
+            if all(_is_array(x) for x in io):
+                shapes = [tuple(x.shape) for x in io]
+                chk.shapes_consistent = all(s == shapes[0] for s in shapes)
+                dtypes = [x.dtype for x in io]
+                chk.dtypes_consistent = all(d == dtypes[0] for d in dtypes)
+                chk.is_valid = chk.shapes_consistent and chk.dtypes_consistent
+    elif _is_array(io):
+        chk.is_array = True
+        chk.n_items = 1
+        chk.shapes_consistent = chk.dtypes_consistent = chk.is_valid = True
+    return chk
+
+
+def _io_valid(geo, rdr):
+    """geocode_slc.py:61-92: log then raise ValueError."""
+    def contents(x):
+        return str(x)[10:-1]
+
+    def err(msg):
+        log.error(msg)
+        raise ValueError(msg)
+
+    if not rdr.is_valid:
+        err(f"radar input is invalid: {contents(rdr)}")
+    if not geo.is_valid:
+        err(f"geo input is invalid: {contents(geo)}")
+    if (geo.is_array and rdr.is_list) or (geo.is_list and rdr.is_array):
+        err("geo and radar inputs are not the same type")
+    if geo.is_list and rdr.is_list and geo.n_items != rdr.n_items:
+        err(f"length of geo input list ({geo.n_items}) and radar input list ({rdr.n_items}) do not match")
+
+
+def _output_array_valid(output_array, geo_array, which):
+    """geocode_slc.py:95-109."""
+    if output_array is None:
+        return
+    size = output_array.numel() if isinstance(output_array, torch.Tensor) else output_array.size
+    if size and tuple(output_array.shape) != tuple(geo_array.shape):
+        msg = f"{which} output array shape does not match geocoded array shape"
+        log.error(msg)
+        raise ValueError(msg)
+
+
+def _check_dtype(x, np_dtype, torch_dtype, what):
+    if isinstance(x, torch.Tensor):
+        if x.dtype != torch_dtype:
+            raise TypeError(f"{what} must be {torch_dtype}, got {x.dtype}")
+    elif x.dtype != np_dtype:
+        raise TypeError(f"{what} must be {np.dtype(np_dtype).name}, got {x.dtype}")
+
+
+class _Staged:
+    """A caller array as a device tensor, with copy-back for host outputs."""
+
+    def __init__(self, arr, dev, upload: bool, torch_dtype):
+        self.host = None
+        if isinstance(arr, torch.Tensor):
+            if arr.device.type != "cuda":
+                raise ValueError("torch tensors must be CUDA tensors")
+            if not arr.is_contiguous():
+                raise ValueError("arrays must be C-contiguous")
+            self.dev = arr
+        else:
+            if not arr.flags.c_contiguous:
+                raise ValueError("arrays must be C-contiguous")
+            self.host = arr
+            if upload:
+                self.dev = torch.from_numpy(arr).to(dev, non_blocking=True)
+            else:
+                self.dev = torch.empty(arr.shape, dtype=torch_dtype, device=dev)
+
+    def ptr(self) -> int:
+        return self.dev.data_ptr()
+
+    def copy_back(self):
+        if self.host is not None:
+            self.host[...] = self.dev.cpu().numpy()
+
+
+def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGridParameters,
+                geogrid: GeoGridParameters, orbit: Orbit, native_doppler: LUT2d, image_grid_doppler: LUT2d,
+                ellipsoid: Ellipsoid, threshold_geo2rdr: float, num_iter_geo2rdr: int,
+                mask_block=None, sliced_radargrid=None, subswaths: SubSwaths | None = None,
+                first_azimuth_line: int = 0, first_range_sample: int = 0, flatten: bool = True,
+                reramp: bool = True, az_carrier=None, rg_carrier=None, az_time_correction=None,
+                srange_correction=None, flatten_with_corrected_srange: bool = False,
+                invalid_value=np.nan + np.nan * 1j,
+                carrier_phase_block=None, flatten_phase_block=None, *,
+                geo2rdr_precision: str = "fp64", inplace_deramp: bool = False,
+                az_index_block=None, rg_index_block=None, dem_margin: int = 50,
+                device=None, stream: torch.cuda.Stream | None = None) -> None:
+    """Geocode radar SLC arrays sharing one radar grid onto one geogrid.
+
+    Parameters and semantics are those of ``isce3.geocode.geocode_slc``
+    (python/packages/isce3/geocode/geocode_slc.py:112-191).  Extra keyword-only
+    arguments: ``geo2rdr_precision`` ("fp64" reference numerics, or "ff"
+    float-float), ``inplace_deramp`` (mutate device radar tensors like the
+    reference), ``az_index_block``/``rg_index_block`` (f64 outputs of the radar
+    coordinates per geo pixel), ``dem_margin``, ``device`` and ``stream``.
+    """
+    az_carrier = LUT2d() if az_carrier is None else az_carrier
+    rg_carrier = LUT2d() if rg_carrier is None else rg_carrier
+    az_time_correction = LUT2d() if az_time_correction is None else az_time_correction
+    srange_correction = LUT2d() if srange_correction is None else srange_correction
+    if carrier_phase_block is None:
+        carrier_phase_block = np.array([], dtype=np.float64)
+    if flatten_phase_block is None:
+        flatten_phase_block = np.array([], dtype=np.float64)
+
+    geo_chk = _io_value_check(geo_data_blocks)
+    rdr_chk = _io_value_check(rdr_data_blocks)
+    _io_valid(geo_chk, rdr_chk)
+    if sliced_radargrid is None:
+        sliced_radargrid = radargrid
+    if geo_chk.is_array and rdr_chk.is_array:
+        geo_data_blocks = [geo_data_blocks]
+        rdr_data_blocks = [rdr_data_blocks]
+    for arr, which in zip([carrier_phase_block, flatten_phase_block, mask_block],
+                          ["carrier", "flattening", "mask"]):
+        _output_array_valid(arr, geo_data_blocks[0], which)
+    if type(az_carrier) is not type(rg_carrier):
+        raise TypeError("az_carrier and rg_carrier must both be LUT2d or both be Poly2d")
+    if not isinstance(az_carrier, (LUT2d, Poly2d)):
+        raise TypeError("carriers must be LUT2d or Poly2d")
+    for g in geo_data_blocks:
+        _check_dtype(g, np.complex64, torch.complex64, "geo_data_blocks")
+        if tuple(g.shape) != (geogrid.length, geogrid.width):
+            raise ValueError("geo_data_blocks shape does not match the geogrid")
+    for r in rdr_data_blocks:
+        _check_dtype(r, np.complex64, torch.complex64, "rdr_data_blocks")
+    if mask_block is not None:
+        _check_dtype(mask_block, np.uint8, torch.uint8, "mask_block")
+    precision = {"fp64": 0, "ff": 1, "float-float": 1}.get(geo2rdr_precision)
+    if precision is None:
+        raise ValueError(f"unknown geo2rdr_precision {geo2rdr_precision!r}")
+
+    dev = M.device_of(device)
+    lib = L.lib()
+    ctx = L.context(dev.index)
+    with torch.cuda.device(dev):
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        rdr = [_Staged(r, dev, True, torch.complex64) for r in rdr_data_blocks]
+        if any(r.host is not None for r in rdr) and inplace_deramp:
+            raise ValueError("inplace_deramp needs device-resident radar tensors")
+        geo = [_Staged(g, dev, False, torch.complex64) for g in geo_data_blocks]
+        outs = list(geo)
+
+        def opt_out(arr, np_dtype, t_dtype, what):
+            if arr is None:
+                return None
+            size = arr.numel() if isinstance(arr, torch.Tensor) else arr.size
+            if size == 0:
+                return None
+            _check_dtype(arr, np_dtype, t_dtype, what)
+            st = _Staged(arr, dev, True, t_dtype)   # upload: untouched pixels keep caller values
+            outs.append(st)
+            return st
+
+        mask = opt_out(mask_block, np.uint8, torch.uint8, "mask_block")
+        carrier = opt_out(carrier_phase_block, np.float64, torch.float64, "carrier_phase_block")
+        flat = opt_out(flatten_phase_block, np.float64, torch.float64, "flatten_phase_block")
+        azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block")
+        rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block")
+
+        holder = M.AzRgHolder()
+        a = L.GeocodeArgs()
+        a.radar_grid = M.radar_grid_desc(radargrid)
+        a.sliced_radar_grid = M.radar_grid_desc(sliced_radargrid)
+        a.geo_grid = M.geo_grid_desc(geogrid)
+        a.orbit = M.orbit_desc(orbit)
+        a.native_doppler = M.lut_desc(native_doppler, dev)
+        a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
+        a.az_time_correction = M.lut_desc(az_time_correction, dev)
+        a.srange_correction = M.lut_desc(srange_correction, dev)
+        a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
+        a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
+        a.ellipsoid_a, a.ellipsoid_e2 = ellipsoid.a, ellipsoid.e2
+        a.threshold_geo2rdr = float(threshold_geo2rdr)
+        a.numiter_geo2rdr = int(num_iter_geo2rdr)
+        a.flatten, a.reramp = int(bool(flatten)), int(bool(reramp))
+        a.flatten_with_corrected_srange = int(bool(flatten_with_corrected_srange))
+        a.first_azimuth_line, a.first_range_sample = int(first_azimuth_line), int(first_range_sample)
+        inv = complex(invalid_value)
+        a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
+        a.n_blocks = len(rdr)
+        a.inplace_deramp = int(bool(inplace_deramp))
+        a.rdr_length, a.rdr_width = rdr[0].dev.shape
+        rdr_ptrs = (C.c_void_p * len(rdr))(*[r.ptr() for r in rdr])
+        geo_ptrs = (C.c_void_p * len(geo))(*[g.ptr() for g in geo])
+        a.rdr_blocks = C.cast(rdr_ptrs, C.POINTER(C.c_void_p))
+        a.geo_blocks = C.cast(geo_ptrs, C.POINTER(C.c_void_p))
+        a.mask = mask.ptr() if mask else None
+        a.carrier_phase = carrier.ptr() if carrier else None
+        a.flatten_phase = flat.ptr() if flat else None
+        a.az_index = azi.ptr() if azi else None
+        a.rg_index = rgi.ptr() if rgi else None
+        a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
+        a.dem_margin = int(dem_margin)
+        a.geo2rdr_precision = precision
+        ss = None
+        if subswaths is not None:
+            ss = M.subswaths_desc(subswaths, dev)
+            a.subswaths = C.pointer(ss)
+        st = lib.gslc_geocode_slc(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
+        L.check(st, ctx, "geocode_slc")
+        for o in outs:
+            o.copy_back()
+        del dem_keep, holder

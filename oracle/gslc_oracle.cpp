@@ -1,0 +1,1034 @@
+// CPU oracle for SLC geocoding — TEST INFRASTRUCTURE ONLY (see gslc_oracle.h).
+//
+// Every function cites the reference file:line it restates.  Operation order
+// is kept where the reference computes in FP32 (DEM spline, deramp phase,
+// sinc accumulation, complex products), because FP32 rounding there moves the
+// flattening phase by more than the parity tolerance.  Compile with
+// -ffp-contract=off.
+#include "gslc_oracle.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+thread_local std::string g_err;
+int fail(const std::string& m) { g_err = m; return 1; }
+
+constexpr int SINC_HALF = 4;    // core/Constants.h:32
+constexpr int SINC_LEN = 8;     // core/Constants.h:33
+constexpr int SINC_ONE = 9;     // core/Constants.h:34
+constexpr int SINC_SUB = 8192;  // core/Constants.h:35
+const double NaN = std::numeric_limits<double>::quiet_NaN();
+
+struct V3 { double x, y, z; };
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double norm(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// complex<float> product the way GCC lowers it for finite operands:
+// (ac - bd) + (ad + bc)i, each product rounded (no FMA).
+struct cf { float re, im; };
+inline cf cmul(cf a, cf b) {
+    float ac = a.re * b.re, bd = a.im * b.im, ad = a.re * b.im, bc = a.im * b.re;
+    return {ac - bd, ad + bc};
+}
+
+// ---------------------------------------------------------------- Orbit
+// core/Linspace.h:56 operator[], core/Linspace.icc:77-89 search
+inline double orb_time(const orc_orbit* o, int i) { return o->t0 + i * o->spacing; }
+inline int orb_search(const orc_orbit* o, double t) {
+    double first = o->t0, last = orb_time(o, o->n - 1);
+    if (o->spacing >= 0) {
+        if (t < first) return 0;
+        if (t > last) return o->n;
+    } else {
+        if (t > first) return 0;
+        if (t < last) return o->n;
+    }
+    return (int)((t - first) / o->spacing + 1);
+}
+inline V3 orb_pos(const orc_orbit* o, int i) { return {o->pos[3*i], o->pos[3*i+1], o->pos[3*i+2]}; }
+inline V3 orb_vel(const orc_orbit* o, int i) { return {o->vel[3*i], o->vel[3*i+1], o->vel[3*i+2]}; }
+
+// core/detail/InterpolateOrbit.icc:10-109
+void hermite(const orc_orbit* o, double t, V3* position, V3* velocity) {
+    int idx = orb_search(o, t) - 2;
+    idx = std::min(std::max(idx, 0), o->n - 4);
+    double f1[4], f0[4], h[4], hdot[4], g1[4], g0[4];
+    for (int i = 0; i < 4; ++i) f1[i] = t - orb_time(o, idx + i);
+    for (int i = 0; i < 4; ++i) {
+        double sum = 0.;
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            sum += 1. / (orb_time(o, idx + i) - orb_time(o, idx + j));
+        }
+        f0[i] = 1. - 2. * sum * (t - orb_time(o, idx + i));
+    }
+    for (int i = 0; i < 4; ++i) {
+        h[i] = 1.;
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            h[i] *= (t - orb_time(o, idx + j)) / (orb_time(o, idx + i) - orb_time(o, idx + j));
+        }
+    }
+    if (position) {
+        V3 p{0., 0., 0.};
+        for (int i = 0; i < 4; ++i) {
+            V3 P = orb_pos(o, idx + i), Vv = orb_vel(o, idx + i);
+            // h*h*(P*f0 + V*f1), Vec3 ops are component-wise
+            double hh = h[i] * h[i];
+            p.x += hh * (P.x * f0[i] + Vv.x * f1[i]);
+            p.y += hh * (P.y * f0[i] + Vv.y * f1[i]);
+            p.z += hh * (P.z * f0[i] + Vv.z * f1[i]);
+        }
+        *position = p;
+    }
+    if (!velocity) return;
+    for (int i = 0; i < 4; ++i) {
+        hdot[i] = 0.;
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            double prod = 1. / (orb_time(o, idx + i) - orb_time(o, idx + j));
+            for (int k = 0; k < 4; ++k) {
+                if (k == i || k == j) continue;
+                prod *= (t - orb_time(o, idx + k)) / (orb_time(o, idx + i) - orb_time(o, idx + k));
+            }
+            hdot[i] += prod;
+        }
+    }
+    for (int i = 0; i < 4; ++i) g1[i] = h[i] + 2. * hdot[i] * (t - orb_time(o, idx + i));
+    for (int i = 0; i < 4; ++i) {
+        double sum = 0.;
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            sum += 1. / (orb_time(o, idx + i) - orb_time(o, idx + j));
+        }
+        g0[i] = 2. * (f0[i] * hdot[i] - sum * h[i]);
+    }
+    V3 v{0., 0., 0.};
+    for (int i = 0; i < 4; ++i) {
+        V3 P = orb_pos(o, idx + i), Vv = orb_vel(o, idx + i);
+        v.x += h[i] * (P.x * g0[i] + Vv.x * g1[i]);
+        v.y += h[i] * (P.y * g0[i] + Vv.y * g1[i]);
+        v.z += h[i] * (P.z * g0[i] + Vv.z * g1[i]);
+    }
+    *velocity = v;
+}
+
+// core/detail/InterpolateOrbit.icc:111-155
+void legendre(const orc_orbit* o, double t, V3* position, V3* velocity) {
+    int idx = orb_search(o, t) - 5;
+    idx = std::min(std::max(idx, 0), o->n - 9);
+    double trel = 8. * (t - orb_time(o, idx)) / (orb_time(o, idx + 8) - orb_time(o, idx));
+    double teller = 1.;
+    for (int i = 0; i < 9; ++i) teller *= trel - i;
+    if (teller == 0.) {
+        int i = (int)trel;
+        if (position) *position = orb_pos(o, idx + i);
+        if (velocity) *velocity = orb_vel(o, idx + i);
+        return;
+    }
+    static const double noemer[9] = {40320.0, -5040.0, 1440.0, -720.0, 576.0,
+                                      -720.0, 1440.0, -5040.0, 40320.0};
+    V3 p{0., 0., 0.}, v{0., 0., 0.};
+    for (int i = 0; i < 9; ++i) {
+        double coeff = (teller / noemer[i]) / (trel - i);
+        V3 P = orb_pos(o, idx + i), Vv = orb_vel(o, idx + i);
+        p.x += coeff * P.x; p.y += coeff * P.y; p.z += coeff * P.z;
+        v.x += coeff * Vv.x; v.y += coeff * Vv.y; v.z += coeff * Vv.z;
+    }
+    if (position) *position = p;
+    if (velocity) *velocity = v;
+}
+
+// core/detail/InterpolateOrbit.icc:157-193 (border mode FillNaN);
+// returns 0 on success.
+int orbit_interp(const orc_orbit* o, double t, V3* pos, V3* vel) {
+    int minsv = o->method == 1 ? 9 : 4;
+    if (o->n < minsv) return 2;
+    if (t < o->t0 || t > orb_time(o, o->n - 1)) {
+        if (pos) *pos = {NaN, NaN, NaN};
+        if (vel) *vel = {NaN, NaN, NaN};
+        return 1;
+    }
+    if (o->method == 1) legendre(o, t, pos, vel); else hermite(o, t, pos, vel);
+    return 0;
+}
+
+// ---------------------------------------------------------------- LUT2d
+// core/LUT2d.h:84-95
+bool lut_contains(const orc_lut2d* l, double y, double x) {
+    if (!l->have_data) return true;
+    const double i = (x - l->x0) / l->dx;
+    const double j = (y - l->y0) / l->dy;
+    return (i >= 0.0 && i <= l->nx - 1.0) && (j >= 0.0 && j <= l->ny - 1.0);
+}
+
+// core/BilinearInterpolator.cpp:12-49 (U = double)
+double bilinear(const double* z, int nx, double x, double y) {
+    int x1 = (int)std::floor(x), x2 = (int)std::ceil(x);
+    int y1 = (int)std::floor(y), y2 = (int)std::ceil(y);
+    double q11 = z[(size_t)y1 * nx + x1], q12 = z[(size_t)y2 * nx + x1];
+    double q21 = z[(size_t)y1 * nx + x2], q22 = z[(size_t)y2 * nx + x2];
+    if ((y1 == y2) && (x1 == x2)) return q11;
+    if (y1 == y2)
+        return ((double)((x2 - x) / (x2 - x1)) * q11) + ((double)((x - x1) / (x2 - x1)) * q21);
+    if (x1 == x2)
+        return ((double)((y2 - y) / (y2 - y1)) * q11) + ((double)((y - y1) / (y2 - y1)) * q12);
+    const double den = (double)((x2 - x1) * (y2 - y1));
+    return ((q11 * (double)((x2 - x) * (y2 - y))) / den) +
+           ((q21 * (double)((x - x1) * (y2 - y))) / den) +
+           ((q12 * (double)((x2 - x) * (y - y1))) / den) +
+           ((q22 * (double)((x - x1) * (y - y1))) / den);
+}
+
+// core/NearestNeighborInterpolator.cpp:12-22
+double nearest(const double* z, int nx, double x, double y) {
+    long row = (long)std::round(y), col = (long)std::round(x);
+    return z[(size_t)row * nx + col];
+}
+
+// core/LUT2d.cpp:124-158 (out-of-bounds only logs; index is clamped)
+double lut_eval(const orc_lut2d* l, double y, double x) {
+    double value = l->ref_value;
+    if (!l->have_data) return value;
+    double x_idx = (x - l->x0) / l->dx;
+    double y_idx = (y - l->y0) / l->dy;
+    x_idx = std::min(std::max(x_idx, 0.0), l->nx - 1.0);
+    y_idx = std::min(std::max(y_idx, 0.0), l->ny - 1.0);
+    if (l->method == 3) return nearest(l->data, l->nx, x_idx, y_idx);
+    return bilinear(l->data, l->nx, x_idx, y_idx);
+}
+
+// ---------------------------------------------------------------- Poly2d
+// core/Poly2d.cpp:8-24
+double poly_eval(const orc_poly2d* p, double y, double x) {
+    double xval = (x - p->x_mean) / p->x_norm;
+    double yval = (y - p->y_mean) / p->y_norm;
+    double scalex, scaley = 1., val = 0.;
+    for (int i = 0; i <= p->y_order; i++, scaley *= yval) {
+        scalex = 1.;
+        for (int j = 0; j <= p->x_order; j++, scalex *= xval)
+            val += scalex * scaley * p->coeffs[i * (p->x_order + 1) + j];
+    }
+    return val;
+}
+
+double azrg_eval(const orc_azrg* f, double y, double x) {
+    return f->kind == 1 ? poly_eval(&f->poly, y, x) : lut_eval(&f->lut, y, x);
+}
+
+// ---------------------------------------------------------------- Ellipsoid
+// core/Ellipsoid.h:117-120 (rEast) and :177-190 (lonLatToXyz)
+V3 lonlat_to_xyz(double a, double e2, V3 llh) {
+    double re = a / std::sqrt(1.0 - (e2 * std::pow(std::sin(llh.y), 2)));
+    V3 xyz;
+    xyz.x = (re + llh.z) * std::cos(llh.y) * std::cos(llh.x);
+    xyz.y = (re + llh.z) * std::cos(llh.y) * std::sin(llh.x);
+    xyz.z = ((re * (1.0 - e2)) + llh.z) * std::sin(llh.y);
+    return xyz;
+}
+
+// ---------------------------------------------------------------- Projections
+constexpr double WGS84_A = 6378137.0;                  // core/Constants.h:41
+constexpr double WGS84_E2 = 0.006694379990141317;      // core/Constants.h:44
+
+// core/Projections.cpp:33-42
+double clens(const double* a, int size, double real) {
+    const double* p;
+    double hr, hr1, hr2;
+    for (p = a + size, hr2 = 0., hr1 = *(--p), hr = 0.; a - p; hr2 = hr1, hr1 = hr)
+        hr = -hr2 + (2. * hr1 * std::cos(real)) + *(--p);
+    return std::sin(real) * hr;
+}
+
+// core/Projections.cpp:54-74
+double clenS(const double* a, int size, double real, double imag, double& R, double& I) {
+    const double* p;
+    double hr, hr1, hr2, hi, hi1, hi2;
+    for (p = a + size, hr2 = 0., hi2 = 0., hi1 = 0., hr1 = *(--p), hi1 = 0., hr = 0., hi = 0.;
+         a - p; hr2 = hr1, hi2 = hi1, hr1 = hr, hi1 = hi) {
+        hr = -hr2 + (2. * hr1 * std::cos(real) * std::cosh(imag)) -
+             (-2. * hi1 * std::sin(real) * std::sinh(imag)) + *(--p);
+        hi = -hi2 + (-2. * hr1 * std::sin(real) * std::sinh(imag)) +
+             (2. * hi1 * std::cos(real) * std::cosh(imag));
+    }
+    R = (std::sin(real) * std::cosh(imag) * hr) - (std::cos(real) * std::sinh(imag) * hi);
+    I = (std::sin(real) * std::cosh(imag) * hi) + (std::cos(real) * std::sinh(imag) * hr);
+    return R;
+}
+
+struct UTM {
+    int zone; bool isnorth;
+    double lon0, Qn, Zb, cgb[6], cbg[6], utg[6], gtu[6];
+};
+
+// core/Projections.cpp:80-170
+bool utm_setup(int code, UTM& u) {
+    if (code > 32600 && code <= 32660) { u.zone = code - 32600; u.isnorth = true; }
+    else if (code > 32700 && code <= 32760) { u.zone = code - 32700; u.isnorth = false; }
+    else return false;
+    u.lon0 = ((u.zone - 0.5) * (M_PI / 30.)) - M_PI;
+    double f = WGS84_E2 / (1. + std::sqrt(1 - WGS84_E2));
+    double n = f / (2. - f);
+    u.cgb[0] = n * (2 + n * ((-2. / 3.) + n * (-2 + n * ((116. / 45.) + n * ((26. / 45.) + n * (-2854. / 675.))))));
+    u.cbg[0] = n * (-2 + n * ((2. / 3.) + n * ((4. / 3.) + n * ((-82. / 45.) + n * ((32. / 45.) + n * (4642. / 4725.))))));
+    u.cgb[1] = std::pow(n, 2) * ((7. / 3.) + n * ((-8. / 5.) + n * ((-227. / 45.) + n * ((2704. / 315.) + n * (2323. / 945.)))));
+    u.cbg[1] = std::pow(n, 2) * ((5. / 3.) + n * ((-16. / 15.) + n * ((-13. / 9.) + n * ((904. / 315.) + n * (-1522. / 945.)))));
+    u.cgb[2] = std::pow(n, 3) * ((56. / 15.) + n * ((-136. / 35.) + n * ((-1262. / 105.) + n * (73814. / 2835.))));
+    u.cbg[2] = std::pow(n, 3) * ((-26. / 15.) + n * ((34. / 21.) + n * ((8. / 5.) + n * (-12686. / 2835.))));
+    u.cgb[3] = std::pow(n, 4) * ((4279. / 630.) + n * ((-332. / 35.) + n * (-399572 / 14175.)));
+    u.cbg[3] = std::pow(n, 4) * ((1237. / 630.) + n * ((-12. / 5.) + n * (-24832. / 14175.)));
+    u.cgb[4] = std::pow(n, 5) * ((4174. / 315.) + n * (-144838. / 6237.));
+    u.cbg[4] = std::pow(n, 5) * ((-734. / 315.) + n * (109598. / 31185.));
+    u.cgb[5] = std::pow(n, 6) * (601676. / 22275.);
+    u.cbg[5] = std::pow(n, 6) * (444337. / 155925.);
+    u.Qn = (0.9996 / (1. + n)) * (1. + n * n * ((1. / 4.) + n * n * ((1. / 64.) + ((n * n) / 256.))));
+    u.utg[0] = n * (-.5 + n * ((2. / 3.) + n * ((-37. / 96.) + n * ((1. / 360.) + n * ((81. / 512.) + n * (-96199. / 604800.))))));
+    u.gtu[0] = n * (.5 + n * ((-2. / 3.) + n * ((5. / 16.) + n * ((41. / 180.) + n * ((-127. / 288.) + n * (7891. / 37800.))))));
+    u.utg[1] = std::pow(n, 2) * ((-1. / 48.) + n * ((-1. / 15.) + n * ((437. / 1440.) + n * ((-46. / 105.) + n * (1118711. / 3870720.)))));
+    u.gtu[1] = std::pow(n, 2) * ((13. / 48.) + n * ((-3. / 5.) + n * ((557. / 1440.) + n * ((281. / 630.) + n * (-1983433. / 1935360.)))));
+    u.utg[2] = std::pow(n, 3) * ((-17. / 480.) + n * ((37. / 840.) + n * ((209. / 4480.) + n * (-5569. / 90720.))));
+    u.gtu[2] = std::pow(n, 3) * ((61. / 240.) + n * ((-103. / 140.) + n * ((15061. / 26880.) + n * (167603. / 181440.))));
+    u.utg[3] = std::pow(n, 4) * ((-4397. / 161280.) + n * ((11. / 504.) + n * (830251. / 7257600.)));
+    u.gtu[3] = std::pow(n, 4) * ((49561. / 161280.) + n * ((-179. / 168.) + n * (6601661. / 7257600.)));
+    u.utg[4] = std::pow(n, 5) * ((-4583. / 161280.) + n * (108847. / 3991680.));
+    u.gtu[4] = std::pow(n, 5) * ((34729. / 80640.) + n * (-3418889. / 1995840.));
+    u.utg[5] = std::pow(n, 6) * (-20648693. / 638668800.);
+    u.gtu[5] = std::pow(n, 6) * (212378941. / 319334400.);
+    double Z = clens(u.cbg, 6, 0.);
+    u.Zb = -u.Qn * (Z + clens(u.gtu, 6, 2 * Z));
+    return true;
+}
+
+// core/Projections.cpp:172-198
+int utm_forward(const UTM& u, V3 llh, V3& out) {
+    double gauss = clens(u.cbg, 6, 2. * llh.y) + llh.y;
+    double lam = llh.x - u.lon0;
+    double Cn = std::atan2(std::sin(gauss), std::cos(lam) * std::cos(gauss));
+    double Ce = std::atan2(std::sin(lam) * std::cos(gauss),
+                           std::hypot(std::sin(gauss), std::cos(gauss) * std::cos(lam)));
+    Ce = std::asinh(std::tan(Ce));
+    double dCn, dCe;
+    Cn += clenS(u.gtu, 6, 2 * Cn, 2 * Ce, dCn, dCe);
+    Ce += dCe;
+    if (std::fabs(Ce) <= 2.623395162778) {
+        out.x = (u.Qn * Ce * WGS84_A) + 500000.;
+        out.y = (((u.Qn * Cn) + u.Zb) * WGS84_A) + (u.isnorth ? 0. : 10000000.);
+        out.z = llh.z;
+        return 0;
+    }
+    return 1;
+}
+
+// core/Projections.cpp:200-232
+int utm_inverse(const UTM& u, V3 in, V3& llh) {
+    double Cn = (in.y - (u.isnorth ? 0. : 10000000.)) / WGS84_A;
+    double Ce = (in.x - 500000.) / WGS84_A;
+    Cn = (Cn - u.Zb) / u.Qn;
+    Ce /= u.Qn;
+    if (std::fabs(Ce) <= 2.623395162778) {
+        double dCn, dCe;
+        Cn += clenS(u.utg, 6, 2 * Cn, 2 * Ce, dCn, dCe);
+        Ce = std::atan(std::sinh(Ce + dCe));
+        double sinCe = std::sin(Ce);
+        double cosCe = std::cos(Ce);
+        Ce = std::atan2(sinCe, cosCe * std::cos(Cn));
+        Cn = std::atan2(std::sin(Cn) * cosCe, std::hypot(sinCe, cosCe * std::cos(Cn)));
+        llh.x = Ce + u.lon0;
+        llh.y = clens(u.cgb, 6, 2 * Cn) + Cn;
+        llh.z = in.z;
+        return 0;
+    }
+    return 1;
+}
+
+// Projection object: LonLat (core/Projections.h:127-140) or UTM.
+struct Proj {
+    int epsg = 0; UTM utm{};
+    bool init(int code) {
+        epsg = code;
+        if (code == 4326) return true;
+        if (code > 32600 && code < 32800) return utm_setup(code, utm);
+        return false;
+    }
+    int forward(V3 llh, V3& out) const {
+        if (epsg == 4326) {
+            out.x = llh.x * 180.0 / M_PI; out.y = llh.y * 180.0 / M_PI; out.z = llh.z;
+            return 0;
+        }
+        return utm_forward(utm, llh, out);
+    }
+    int inverse(V3 in, V3& llh) const {
+        if (epsg == 4326) {
+            llh.x = in.x * M_PI / 180.0; llh.y = in.y * M_PI / 180.0; llh.z = in.z;
+            return 0;
+        }
+        return utm_inverse(utm, in, llh);
+    }
+};
+
+// ---------------------------------------------------------------- Spline2d
+// core/Spline2dInterpolator.cpp:89-108 (_initSpline)
+template <typename U>
+void init_spline(const U* Y, int n, U* R, U* Q) {
+    Q[0] = U(0.0);
+    R[0] = U(0.0);
+    for (int i = 1; i < n - 1; ++i) {
+        const U p = static_cast<U>(1.0) / (static_cast<U>(0.5) * Q[i - 1] + static_cast<U>(2.0));
+        Q[i] = static_cast<U>(-0.5) * p;
+        R[i] = (static_cast<U>(3.0) * (Y[i + 1] - static_cast<U>(2.0) * Y[i] + Y[i - 1]) -
+                static_cast<U>(0.5) * R[i - 1]) * p;
+    }
+    R[n - 1] = U(0.0);
+    for (int i = (n - 2); i > 0; --i) R[i] = Q[i] * R[i + 1] + R[i];
+}
+
+// core/Spline2dInterpolator.cpp:69-87 (_spline)
+template <typename U>
+U spline(double x, const U* Y, int n, const U* R) {
+    const U denom = static_cast<U>(6.0);
+    if (x < 1.0) {
+        return Y[0] + static_cast<U>(x - 1.0) * (Y[1] - Y[0] - (R[1] / denom));
+    } else if (x > n) {
+        return Y[n - 1] + (static_cast<U>(x - n) * (Y[n - 1] - Y[n - 2] + (R[n - 2] / denom)));
+    } else {
+        int j = int(std::floor(x));
+        U xx = static_cast<U>(x - j);
+        U t0 = Y[j] - Y[j - 1] - (R[j - 1] / static_cast<U>(3.0)) - (R[j] / denom);
+        U t1 = xx * ((R[j - 1] / static_cast<U>(2.0)) + (xx * ((R[j] - R[j - 1]) / denom)));
+        return Y[j - 1] + (xx * (t0 + t1));
+    }
+}
+
+// core/Spline2dInterpolator.cpp:32-67 (interp_impl, order 6)
+template <typename U>
+U spline2d(const U* z, int ny, int nx, double x, double y) {
+    const int order = 6;
+    int i0 = (int)y, j0 = (int)x;      // order even: truncation
+    i0 = i0 - (order / 2) + 1;
+    j0 = j0 - (order / 2) + 1;
+    U A[order], R[order], Q[order], HC[order];
+    for (int i = 0; i < order; ++i) {
+        const int indi = std::min(std::max(i0 + i, 0), ny - 2);
+        for (int j = 0; j < order; ++j) {
+            const int indj = std::min(std::max(j0 + j, 0), nx - 2);
+            A[j] = z[(size_t)(indi + 1) * nx + (indj + 1)];
+        }
+        init_spline(A, order, R, Q);
+        HC[i] = spline(x - j0, A, order, R);
+    }
+    init_spline(HC, order, R, Q);
+    return static_cast<U>(spline(y - i0, HC, order, R));
+}
+
+// ---------------------------------------------------------------- Sinc2d
+// core/Sinc2dInterpolator.cpp:98-115 (_sinc_coef) and :12-40 (ctor)
+struct SincTable {
+    std::vector<double> k;   // [SINC_SUB][SINC_LEN]
+    SincTable() : k((size_t)SINC_SUB * SINC_LEN) {
+        const int filtercoef = SINC_SUB * SINC_LEN;
+        std::vector<double> filter(filtercoef, 0.0);
+        const double beta = 1.0, pedestal = 0.0;
+        const double wgthgt = (1.0 - pedestal) / 2.0;
+        const double soff = (filtercoef - 1.) / 2.;
+        for (int i = 0; i < filtercoef; i++) {
+            double wgt = (1. - wgthgt) + (wgthgt * std::cos((M_PI * (i - soff)) / soff));
+            double s = (std::floor(i - soff) * beta) / (1. * SINC_SUB);
+            double fct = ((s != 0.) ? (std::sin(M_PI * s) / (M_PI * s)) : 1.);
+            filter[i] = fct * wgt;
+        }
+        for (size_t i = 0; i < (size_t)SINC_SUB; ++i) {
+            double ssum = 0.0;
+            for (size_t j = 0; j < (size_t)SINC_LEN; ++j) ssum += filter[i + SINC_SUB * j];
+            for (size_t j = 0; j < (size_t)SINC_LEN; ++j) {
+                filter[i + SINC_SUB * j] /= ssum;
+                k[i * SINC_LEN + j] = filter[i + SINC_SUB * j];
+            }
+        }
+    }
+};
+const SincTable& sinc_table() { static SincTable t; return t; }
+
+// core/Sinc2dInterpolator.cpp:45-96 for U = complex<float>; the chip is the
+// 9x9 Matrix built in geocodeSlc.cpp:476-494.
+cf sinc2d_chip(const cf* chip, int rows, int cols, double x, double y) {
+    const SincTable& T = sinc_table();
+    const int half = SINC_LEN / 2;
+    const int ix = (int)std::floor(x), iy = (int)std::floor(y);
+    const double fx = x - ix, fy = y - iy;
+    cf ret{0.f, 0.f};
+    if ((ix < (half - 1)) || (ix > (cols - half - 1))) return ret;
+    if ((iy < (half - 1)) || (iy > (rows - half - 1))) return ret;
+    const int xx = ix + half, yy = iy + half;
+    int ifracx = std::min(std::max(0, int(fx * SINC_SUB)), SINC_SUB - 1);
+    int ifracy = std::min(std::max(0, int(fy * SINC_SUB)), SINC_SUB - 1);
+    for (int i = 0; i < SINC_LEN; i++) {
+        for (int j = 0; j < SINC_LEN; j++) {
+            cf a = chip[(yy - i) * cols + (xx - j)];
+            cf ky{(float)T.k[(size_t)ifracy * SINC_LEN + i], 0.f};
+            cf kx{(float)T.k[(size_t)ifracx * SINC_LEN + j], 0.f};
+            cf term = cmul(cmul(a, ky), kx);
+            ret.re = ret.re + term.re;
+            ret.im = ret.im + term.im;
+        }
+    }
+    return ret;
+}
+
+// U = double flavour, used only by the interpolator known-answer test.
+double sinc2d_double(const double* z, int rows, int cols, double x, double y) {
+    const SincTable& T = sinc_table();
+    const int half = SINC_LEN / 2;
+    const int ix = (int)std::floor(x), iy = (int)std::floor(y);
+    const double fx = x - ix, fy = y - iy;
+    if ((ix < (half - 1)) || (ix > (cols - half - 1))) return 0.0;
+    if ((iy < (half - 1)) || (iy > (rows - half - 1))) return 0.0;
+    const int xx = ix + half, yy = iy + half;
+    int ifracx = std::min(std::max(0, int(fx * SINC_SUB)), SINC_SUB - 1);
+    int ifracy = std::min(std::max(0, int(fy * SINC_SUB)), SINC_SUB - 1);
+    double ret = 0.0;
+    for (int i = 0; i < SINC_LEN; i++)
+        for (int j = 0; j < SINC_LEN; j++)
+            ret += z[(size_t)(yy - i) * cols + (xx - j)] * T.k[(size_t)ifracy * SINC_LEN + i] *
+                   T.k[(size_t)ifracx * SINC_LEN + j];
+    return ret;
+}
+
+// ---------------------------------------------------------------- DEM
+struct DEM {
+    bool have_raster = false;
+    double ref_height = 0.0;
+    int epsg = 4326;
+    Proj proj;
+    double xstart = 0, ystart = 0, deltax = 0, deltay = 0;
+    long width = 0, length = 0;
+    std::vector<float> dem;
+};
+
+// geometry/DEMInterpolator.cpp:29-455 (loadDEM with bounding box)
+int load_dem(DEM& d, const orc_dem_raster* r, double min_x, double max_x, double min_y, double max_y) {
+    const double delta_y = r->gt[5];
+    const double delta_x = r->gt[1];
+    if (delta_x < 0) return 1;
+    const double dem_y0 = r->gt[3];
+    double dem_x0 = r->gt[0];
+    int epsgcode = r->epsg;
+    d.epsg = epsgcode;
+    d.proj.init(epsgcode);
+    if (epsgcode == 4326) {
+        if (max_x - min_x > 360 + 2 * delta_x) max_x = min_x + 360 + delta_x;
+        if (min_x < -180 - delta_x || max_x < -180 - delta_x || max_x > 360 + delta_x) {
+            double n_wraps = std::floor(max_x / 360);
+            min_x -= n_wraps * 360;
+            max_x -= n_wraps * 360;
+        }
+        if (min_x < -180 - delta_x || max_x < -180 - delta_x) { min_x += 360; max_x += 360; }
+        if (min_x > 0 && max_x < 0) max_x += 360;
+        if (dem_x0 > 360 + delta_x || dem_x0 < -180 - delta_x) dem_x0 = std::fmod(dem_x0, 360);
+    }
+    const double dem_yf = dem_y0 + r->length * delta_y;
+    const double dem_xf = dem_x0 + r->width * delta_x;
+    if (epsgcode == 4326 && min_x < dem_xf - 360 - delta_x) { min_x += 360; max_x += 360; }
+    else if (epsgcode == 4326 && min_x > 180 && max_x > dem_x0 + 360 + delta_x) { min_x -= 360; max_x -= 360; }
+    bool disc = (epsgcode == 4326) && (min_x <= dem_xf) && (dem_xf < max_x) &&
+                (min_x <= dem_x0 + 360) && (dem_x0 + 360 < max_x);
+    if (min_x < dem_x0) min_x = dem_x0;
+    if (max_x > dem_xf && !disc) max_x = dem_xf;
+    if (min_y < dem_yf) min_y = dem_yf;
+    if (max_y > dem_y0) max_y = dem_y0;
+    long min_x_idx = (long)std::floor((min_x - dem_x0) / delta_x);
+    long max_x_idx = (long)std::ceil((max_x - dem_x0) / delta_x);
+    long min_y_idx = (long)std::floor((max_y - dem_y0) / delta_y);
+    long max_y_idx = (long)std::ceil((min_y - dem_y0) / delta_y);
+    d.xstart = dem_x0 + (0.5 + min_x_idx) * delta_x;
+    d.ystart = dem_y0 + (0.5 + min_y_idx) * delta_y;
+    d.deltax = delta_x;
+    d.deltay = delta_y;
+    long width = max_x_idx - min_x_idx;
+    long length = max_y_idx - min_y_idx;
+    if (!disc && min_x_idx + width > r->width) { width = r->width - min_x_idx; max_x_idx = min_x_idx + width; }
+    if (!disc && min_y_idx + length > r->length) { length = r->length - min_y_idx; max_y_idx = min_y_idx + length; }
+    if (width <= 0 || length <= 0) return 2;
+    d.width = width; d.length = length;
+    d.dem.assign((size_t)width * length, 0.f);
+    // GDAL getBlock of a window that is partly outside the raster is an
+    // error in the reference; here the window is inside by construction
+    // except for negative offsets, which GDAL would also reject.
+    if (min_x_idx < 0 || min_y_idx < 0) return 3;
+    if (!disc) {
+        for (long i = 0; i < length; ++i)
+            std::memcpy(&d.dem[(size_t)i * width], &r->data[(size_t)(min_y_idx + i) * r->width + min_x_idx],
+                        sizeof(float) * width);
+    } else {
+        std::fill(d.dem.begin(), d.dem.end(), std::numeric_limits<float>::quiet_NaN());
+        const long wl = r->width - min_x_idx;
+        for (long i = 0; i < length && wl > 0; ++i)
+            for (long j = 0; j < wl; ++j)
+                d.dem[(size_t)i * width + j] = r->data[(size_t)(min_y_idx + i) * r->width + min_x_idx + j];
+        const double ideal = (r->width - 360.0 / delta_x);
+        const long wnext = std::lround(ideal);
+        if (std::abs(ideal - wnext) > 1e-5) return 4;
+        const long x0r = std::max(0L, wnext);
+        const long x1r = std::min((long)(r->width - 1), (long)std::ceil((max_x - 360 - dem_x0) / delta_x));
+        const long wr = x1r - x0r;
+        if (wr > 1) {
+            for (long i = 0; i < length; ++i)
+                for (long j = 0; j < wr; ++j) {
+                    const long dj = (long)((x0r + j) + 360.0 / delta_x - min_x_idx);
+                    if (dj > width - 1) continue;
+                    d.dem[(size_t)i * width + dj] = r->data[(size_t)(min_y_idx + i) * r->width + x0r + j];
+                }
+        }
+    }
+    d.have_raster = true;
+    return 0;
+}
+
+// geometry/loadDem.cpp:22-133 (DEMRasterToInterpolator, BIQUINTIC)
+int dem_raster_to_interp(DEM& d, const orc_dem_raster* r, const orc_geo_grid* g, int lineStart,
+                         int blockLength, int blockWidth, int margin) {
+    d = DEM();
+    d.ref_height = 0.0;
+    double minX = std::numeric_limits<double>::max();
+    double maxX = std::numeric_limits<double>::lowest();
+    double minY = std::numeric_limits<double>::max();
+    double maxY = std::numeric_limits<double>::lowest();
+    if (r->epsg != g->epsg) {
+        Proj proj, demproj;
+        if (!proj.init(g->epsg) || !demproj.init(r->epsg)) return fail("unsupported EPSG");
+        const int askip = std::max(static_cast<int>(blockLength / 10.), 1);
+        const int rskip = std::max(static_cast<int>(blockWidth / 10.), 1);
+        std::vector<int> lineInd, pixInd;
+        for (int j = 0; j < blockWidth; j += rskip) { lineInd.push_back(0); pixInd.push_back(j); }
+        for (int i = 0; i < blockLength; i += askip) { lineInd.push_back(i); pixInd.push_back(blockWidth); }
+        for (int j = blockWidth; j > 0; j -= rskip) { lineInd.push_back(blockLength - 1); pixInd.push_back(j); }
+        for (int i = blockLength; i > 0; i -= askip) { lineInd.push_back(i); pixInd.push_back(0); }
+        for (size_t i = 0; i < lineInd.size(); i++) {
+            V3 outpt{g->start_x + g->spacing_x * pixInd[i],
+                     g->start_y + g->spacing_y * (lineStart + lineInd[i]), 0.0};
+            V3 tmp, dempt;
+            if (proj.inverse(outpt, tmp) != 0 || demproj.forward(tmp, dempt) != 0)
+                return fail("projection transformation between geogrid and DEM failed");
+            minX = std::min(minX, dempt.x); maxX = std::max(maxX, dempt.x);
+            minY = std::min(minY, dempt.y); maxY = std::max(maxY, dempt.y);
+        }
+    } else {
+        maxY = g->start_y + g->spacing_y * lineStart;
+        minY = g->start_y + g->spacing_y * (lineStart + blockLength - 1);
+        minX = g->start_x;
+        maxX = g->start_x + g->spacing_x * (blockWidth - 1);
+    }
+    minX -= margin * r->gt[1];
+    maxX += margin * r->gt[1];
+    minY -= margin * std::abs(r->gt[5]);
+    maxY += margin * std::abs(r->gt[5]);
+    int st = load_dem(d, r, minX, maxX, minY, maxY);
+    if (st != 0) d.have_raster = false;   // interpolation then returns refHeight
+    d.epsg = r->epsg;
+    d.proj.init(r->epsg);
+    return 0;
+}
+
+// geometry/DEMInterpolator.cpp:617-659
+double dem_interp_xy(const DEM& d, double x, double y) {
+    double value = d.ref_height;
+    if (!d.have_raster) return value;
+    if (d.epsg == 4326 && (x > 360 || x < -360)) x = std::fmod(x, 360);
+    if (d.epsg == 4326 && x < -180) x += 360;
+    if (d.epsg == 4326 && x - 360 >= d.xstart) {
+        x -= 360;
+    } else if (d.epsg == 4326 && x < d.xstart && x + 360 >= d.xstart) {
+        x += 360;
+    } else if (x < d.xstart) {
+        return d.ref_height;
+    }
+    const double row = (y - d.ystart) / d.deltay;
+    const double col = (x - d.xstart) / d.deltax;
+    const int irow = int(std::floor(row));
+    const int icol = int(std::floor(col));
+    if (irow < 2 || irow >= int(d.length - 1)) return d.ref_height;
+    if (icol < 2 || icol >= int(d.width - 1)) return d.ref_height;
+    return (double)spline2d<float>(d.dem.data(), (int)d.length, (int)d.width, col, row);
+}
+
+// geometry/DEMInterpolator.cpp:593-611
+double dem_interp_lonlat(const DEM& d, double lon, double lat) {
+    if (!d.have_raster) return d.ref_height;
+    V3 xyz{0, 0, 0};
+    d.proj.forward({lon, lat, 0.0}, xyz);
+    return dem_interp_xy(d, xyz.x, xyz.y);
+}
+
+// ---------------------------------------------------------------- geo2rdr
+enum { G_OK = 0, G_OOB = 1, G_LOOK = 2, G_NOCONV = 3 };
+
+// geometry/detail/Geo2Rdr.icc:11-48
+int doppler_aztime_diff(double* dt, double t, double r, V3 rvec, V3 vel, const orc_lut2d* dop,
+                        double wvl, double dr) {
+    if (dop->bounds_error) {
+        if (!(lut_contains(dop, t, r) && lut_contains(dop, t, r + dr))) return G_OOB;
+    }
+    const double dopfact = dot(rvec, vel);
+    const double fdop = 0.5 * wvl * lut_eval(dop, t, r);
+    const double fdopder = (0.5 * wvl * lut_eval(dop, t, r + dr) - fdop) / dr;
+    const double fn = dopfact - fdop * r;
+    const double c1 = -dot(vel, vel);
+    const double c2 = (fdop / r) + fdopder;
+    const double fnprime = c1 + c2 * dopfact;
+    *dt = fn / fnprime;
+    return G_OK;
+}
+
+// geometry/detail/Geo2Rdr.icc:50-112
+int update_aztime(double* t, const orc_orbit* o, V3 xyz, int side) {
+    const int num = 15;
+    const double tstart = o->t0, tend = orb_time(o, o->n - 1);
+    const double dt = (tend - tstart) / (num - 1);
+    double r_closest = 1e16, t_closest = -1000.;
+    for (int k = 0; k < num; ++k) {
+        const double tt = tstart + k * dt;
+        if (tt < tstart || tt > tend) continue;
+        V3 pos, vel;
+        orbit_interp(o, tt, &pos, &vel);
+        const V3 rvec = sub(xyz, pos);
+        if (k == 0) {
+            if ((side == -1) != (dot(cross(rvec, vel), pos) > 0.)) return G_LOOK;
+        }
+        const double r = norm(rvec);
+        if (r < r_closest) { r_closest = r; t_closest = tt; }
+    }
+    *t = (t_closest < 0.) ? 0.5 * (tstart + tend) : t_closest;
+    return G_OK;
+}
+
+// geometry/detail/Geo2Rdr.icc:114-179
+int geo2rdr_detail(double* t, double* r, V3 llh, double a, double e2, const orc_orbit* o,
+                   const orc_lut2d* dop, double wvl, int side, double t0, double thr, int maxiter,
+                   double dr) {
+    const V3 xyz = lonlat_to_xyz(a, e2, llh);
+    if (t0 >= o->t0 && t0 <= orb_time(o, o->n - 1)) {
+        *t = t0;
+    } else {
+        int st = update_aztime(t, o, xyz, side);
+        if (st != G_OK) return st;
+    }
+    double dt = 0.0;
+    for (int i = 0; i < maxiter; ++i) {
+        *t -= dt;
+        V3 pos, vel;
+        orbit_interp(o, *t, &pos, &vel);
+        const V3 rvec = sub(xyz, pos);
+        *r = norm(rvec);
+        if (i == 0) {
+            if ((side == -1) != (dot(cross(rvec, vel), pos) > 0.)) return G_LOOK;
+        }
+        int st = doppler_aztime_diff(&dt, *t, *r, rvec, vel, dop, wvl, dr);
+        if (st != G_OK) return st;
+        if (std::abs(dt) < thr) return G_OK;
+    }
+    return G_NOCONV;
+}
+
+// ---------------------------------------------------------------- radar grid
+inline double rg_sensing_stop(const orc_radar_grid& g) { return g.sensing_start + (g.length - 1.0) / g.prf; }
+inline double rg_ending_range(const orc_radar_grid& g) { return g.starting_range + (g.width - 1.0) * g.range_pixel_spacing; }
+inline double rg_sensing_mid(const orc_radar_grid& g) { return 0.5 * (g.sensing_start + rg_sensing_stop(g)); }
+// product/RadarGridParameters.cpp:27-35
+bool rg_contains(const orc_radar_grid& g, double az, double sr) {
+    const double half_az = (1.0 / g.prf) / 2;
+    const double half_rg = g.range_pixel_spacing / 2;
+    return az >= g.sensing_start - half_az && sr >= g.starting_range - half_rg &&
+           az <= rg_sensing_stop(g) + half_az && sr <= rg_ending_range(g) + half_rg;
+}
+
+// product/SubSwaths.cpp:58-96
+int subswath_of(const orc_subswaths* s, int az, int rg) {
+    if (rg < 0 || rg >= s->width || az < 0 || az >= s->length) return 0;
+    if (s->n == 0) return 1;
+    for (int k = 1; k <= s->n; ++k) {
+        const int32_t* v = s->valid + (size_t)(k - 1) * s->length * 2;
+        const int start = v[(size_t)az * 2], stop = v[(size_t)az * 2 + 1];
+        if (rg >= start && rg < stop) return k;
+    }
+    return 0;
+}
+
+// geocode/geocodeSlc.cpp:548-580
+int validate_slice(const orc_radar_grid& full, const orc_radar_grid& s) {
+    if (s.sensing_start < full.sensing_start) return fail("sliced grid sensing start < full grid sensing start");
+    if (rg_sensing_stop(s) > rg_sensing_stop(full)) return fail("sliced grid sensing stop < full grid sensing stop");
+    if (s.starting_range < full.starting_range) return fail("sliced grid staring range < full grid staring range");
+    if (rg_ending_range(s) > rg_ending_range(full)) return fail("sliced grid ending range < full grid ending range");
+    if (s.look_side != full.look_side) return fail("sliced grid look side != full grid look side");
+    if (s.wavelength != full.wavelength) return fail("sliced grid wavelength != full grid wavelength");
+    return 0;
+}
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+// ================================================================ geocode
+extern "C" int orc_geocode_slc(orc_geocode_args* a) {
+    g_err.clear();
+    const orc_radar_grid& rg = a->radar_grid;
+    const orc_radar_grid& srg = a->sliced_radar_grid;
+    const orc_geo_grid& gg = a->geo_grid;
+    const size_t L = gg.length, W = gg.width;
+    const size_t N = L * W;
+    if (a->n_blocks < 1) return fail("number of geoDataBlocks != number of rdrDataBlocks");
+#ifdef _OPENMP
+    if (a->nthreads > 0) omp_set_num_threads(a->nthreads);
+#endif
+    // geocodeSlc.cpp:873-877
+    for (int b = 0; b < a->n_blocks; ++b)
+        for (size_t k = 0; k < N; ++k) { a->geo_blocks[b][2*k] = a->invalid_re; a->geo_blocks[b][2*k+1] = a->invalid_im; }
+    if (a->mask) std::memset(a->mask, 255, N);
+    if (validate_slice(rg, srg)) return 1;
+    Proj proj;
+    if (!proj.init(gg.epsg)) return fail("Unknown EPSG code (in factory): " + std::to_string(gg.epsg));
+    (void)sinc_table();
+    DEM dem;
+    if (dem_raster_to_interp(dem, &a->dem, &gg, 0, (int)L, (int)W, a->dem_margin)) return 1;
+
+    std::vector<double> rgIdx(N, NaN), azIdx(N, NaN);
+    std::vector<double> uncorr;
+    const bool useCorr = a->flatten_with_corrected_srange != 0;
+    if (!useCorr) uncorr.assign(N, (double)a->invalid_re);
+
+    // ---- computeGeogridRadarIndicesAndMask, geocodeSlc.cpp:55-228
+    double t_start = now();
+    const int chipHalf = SINC_ONE / 2;
+    int proj_fail = 0;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long line = 0; line < (long)L; ++line) {
+        for (size_t pixel = 0; pixel < W; ++pixel) {
+            const size_t k = (size_t)line * W + pixel;
+            double y = gg.start_y + gg.spacing_y * (line + 0.5);
+            double x = gg.start_x + gg.spacing_x * (pixel + 0.5);
+            double aztime = rg_sensing_mid(rg), srange = 0.0;
+            V3 llh;
+            if (proj.inverse({x, y, 0.0}, llh) != 0) {
+#pragma omp atomic write
+                proj_fail = 1;
+                continue;
+            }
+            llh.z = dem_interp_lonlat(dem, llh.x, llh.y);
+            int st = geo2rdr_detail(&aztime, &srange, llh, a->ell_a, a->ell_e2, &a->orbit,
+                                    &a->image_grid_doppler, rg.wavelength, rg.look_side, aztime,
+                                    a->threshold_geo2rdr, a->numiter_geo2rdr, 1.0e-8);
+            if (st != G_OK) continue;
+            if (!useCorr) uncorr[k] = srange;
+            if (lut_contains(&a->az_time_correction, aztime, srange))
+                aztime += lut_eval(&a->az_time_correction, aztime, srange);
+            if (lut_contains(&a->srange_correction, aztime, srange))
+                srange += lut_eval(&a->srange_correction, aztime, srange);
+            if (!rg_contains(srg, aztime, srange) || !lut_contains(&a->native_doppler, aztime, srange))
+                continue;
+            double azc = (aztime - rg.sensing_start) * rg.prf;
+            double rgc = (srange - rg.starting_range) / rg.range_pixel_spacing;
+            const int intAz = (int)std::floor(azc);
+            const int intRg = (int)std::floor(rgc);
+            bool corners = true;
+            if ((intRg < chipHalf) || (intRg >= (rg.width - chipHalf)) || (intAz < chipHalf) ||
+                (intAz >= (rg.length - chipHalf)))
+                corners = false;
+            if (a->subswaths && a->mask) {
+                unsigned char m = (unsigned char)subswath_of(a->subswaths, intAz, intRg);
+                if (m != 0) {
+                    const int ext[2] = {-chipHalf, chipHalf};
+                    for (int ai = 0; ai < 2; ++ai)
+                        for (int ri = 0; ri < 2; ++ri)
+                            if (subswath_of(a->subswaths, intAz + ext[ai], intRg + ext[ri]) == 0) { m = 0; break; }
+                }
+                a->mask[k] = m;
+            } else if (corners && a->mask) {
+                a->mask[k] = 1;
+            }
+            rgIdx[k] = rgc;
+            azIdx[k] = azc;
+        }
+    }
+    if (proj_fail) return fail("Inverse projection transformation failed");
+    a->phase_seconds[0] = now() - t_start;
+    a->phase_seconds[1] = a->phase_seconds[2] = a->phase_seconds[3] = 0.0;
+
+    if (a->out_az_index) std::memcpy(a->out_az_index, azIdx.data(), N * sizeof(double));
+    if (a->out_rg_index) std::memcpy(a->out_rg_index, rgIdx.data(), N * sizeof(double));
+    if (a->out_uncorrected_srange && !useCorr) std::memcpy(a->out_uncorrected_srange, uncorr.data(), N * sizeof(double));
+
+    const long inL = a->rdr_length, inW = a->rdr_width;
+    const size_t azFirst = a->first_azimuth_line, rgFirst = a->first_range_sample;
+    for (int b = 0; b < a->n_blocks; ++b) {
+        cf* rdr = reinterpret_cast<cf*>(a->rdr_blocks[b]);
+        cf* geo = reinterpret_cast<cf*>(a->geo_blocks[b]);
+        // ---- carrierPhaseDeramp, geocodeSlc.cpp:240-274
+        t_start = now();
+#pragma omp parallel for
+        for (long ii = 0; ii < inL * inW; ++ii) {
+            size_t i = ii / inW, j = ii % inW;
+            const size_t i_az = i + azFirst;
+            const double az = rg.sensing_start + i_az / rg.prf;
+            const size_t j_rg = j + rgFirst;
+            const double r = rg.starting_range + j_rg * rg.range_pixel_spacing;
+            const float carrierPhase = azrg_eval(&a->rg_carrier, az, r) + azrg_eval(&a->az_carrier, az, r);
+            const cf c{std::cos(carrierPhase), -std::sin(carrierPhase)};
+            rdr[ii] = cmul(rdr[ii], c);
+        }
+        a->phase_seconds[1] += now() - t_start;
+        // ---- interpolate, geocodeSlc.cpp:409-511
+        t_start = now();
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (long ii = 0; ii < (long)N; ++ii) {
+            const double uRg = rgIdx[ii], uAz = azIdx[ii];
+            if (std::isnan(uRg) || std::isnan(uAz)) continue;
+            double RgIndex = uRg - (double)rgFirst;
+            double AzIndex = uAz - (double)azFirst;
+            const int intRg = (int)RgIndex, intAz = (int)AzIndex;
+            const double fracRg = RgIndex - intRg, fracAz = AzIndex - intAz;
+            if ((intRg < SINC_HALF) || (intRg >= (inW - SINC_HALF))) continue;
+            if ((intAz < SINC_HALF) || (intAz >= (inL - SINC_HALF))) continue;
+            const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
+            const double az = rg.sensing_start + uAz / rg.prf;
+            if (!lut_contains(&a->native_doppler, az, rng)) continue;
+            const double doppFreq = lut_eval(&a->native_doppler, az, rng) * 2 * M_PI / rg.prf;
+            cf chip[SINC_ONE * SINC_ONE];
+            for (int r9 = 0; r9 < SINC_ONE; ++r9) {
+                const int chipRow = intAz + r9 - SINC_HALF;
+                const double doppPhase = doppFreq * (r9 - SINC_HALF);
+                const cf dv{(float)std::cos(doppPhase), (float)-std::sin(doppPhase)};
+                for (int c9 = 0; c9 < SINC_ONE; ++c9) {
+                    const int chipCol = intRg + c9 - SINC_HALF;
+                    chip[r9 * SINC_ONE + c9] = cmul(rdr[(size_t)chipRow * inW + chipCol], dv);
+                }
+            }
+            const cf cval = sinc2d_chip(chip, SINC_ONE, SINC_ONE, SINC_HALF + fracRg, SINC_HALF + fracAz);
+            const double back = doppFreq * fracAz;
+            const cf bv{(float)std::cos(back), (float)std::sin(back)};
+            geo[ii] = cmul(cval, bv);
+        }
+        a->phase_seconds[2] += now() - t_start;
+        // ---- carrierPhaseRerampAndFlatten, geocodeSlc.cpp:298-394
+        t_start = now();
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (long ii = 0; ii < (long)N; ++ii) {
+            const double uRg = rgIdx[ii], uAz = azIdx[ii];
+            if (std::isnan(uRg) || std::isnan(uAz)) continue;
+            const double RgIndex = uRg - (double)rgFirst, AzIndex = uAz - (double)azFirst;
+            const int intRg = (int)RgIndex, intAz = (int)AzIndex;
+            if ((intRg < chipHalf) || (intRg >= (inW - chipHalf))) continue;
+            if ((intAz < chipHalf) || (intAz >= (inL - chipHalf))) continue;
+            const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
+            const double az = rg.sensing_start + uAz / rg.prf;
+            if (!lut_contains(&a->native_doppler, az, rng)) continue;
+            const double carrierPhase = azrg_eval(&a->rg_carrier, az, rng) + azrg_eval(&a->az_carrier, az, rng);
+            const double sRngFlatten = useCorr ? rng : uncorr[ii];
+            const double flattenPhase = 4.0 * (M_PI / rg.wavelength) * sRngFlatten;
+            double totalPhase = 0.0;
+            if (a->reramp) totalPhase += carrierPhase;
+            if (a->flatten) totalPhase += flattenPhase;
+            if (a->carrier_phase) a->carrier_phase[ii] = carrierPhase;
+            if (a->flatten_phase) a->flatten_phase[ii] = flattenPhase;
+            const cf c{(float)std::cos(totalPhase), (float)std::sin(totalPhase)};
+            geo[ii] = cmul(geo[ii], c);
+        }
+        a->phase_seconds[3] += now() - t_start;
+    }
+    return 0;
+}
+
+extern "C" const char* orc_last_error(void) { return g_err.c_str(); }
+
+// ================================================================ components
+extern "C" int orc_orbit_interpolate(const orc_orbit* o, double t, double* pos, double* vel) {
+    V3 p{NaN, NaN, NaN}, v{NaN, NaN, NaN};
+    int st = orbit_interp(o, t, &p, &v);
+    pos[0] = p.x; pos[1] = p.y; pos[2] = p.z;
+    vel[0] = v.x; vel[1] = v.y; vel[2] = v.z;
+    return st;
+}
+
+extern "C" double orc_interp2d_double(int method, const double* z, int ny, int nx, double x, double y) {
+    switch (method) {
+        case 1: return bilinear(z, nx, x, y);
+        case 3: return nearest(z, nx, x, y);
+        case 4: return spline2d<double>(z, ny, nx, x, y);
+        case 5: return sinc2d_double(z, ny, nx, x, y);
+        default: return NaN;
+    }
+}
+
+extern "C" float orc_spline2d_float(const float* z, int ny, int nx, double x, double y) {
+    return spline2d<float>(z, ny, nx, x, y);
+}
+
+extern "C" double orc_lut2d_eval(const orc_lut2d* l, double y, double x) { return lut_eval(l, y, x); }
+extern "C" int orc_lut2d_contains(const orc_lut2d* l, double y, double x) { return lut_contains(l, y, x) ? 1 : 0; }
+extern "C" double orc_poly2d_eval(const orc_poly2d* p, double y, double x) { return poly_eval(p, y, x); }
+
+extern "C" int orc_proj_forward(int epsg, const double* llh, double* xyz) {
+    Proj p;
+    if (!p.init(epsg)) return -1;
+    V3 o{0, 0, 0};
+    int st = p.forward({llh[0], llh[1], llh[2]}, o);
+    xyz[0] = o.x; xyz[1] = o.y; xyz[2] = o.z;
+    return st;
+}
+
+extern "C" int orc_proj_inverse(int epsg, const double* xyz, double* llh) {
+    Proj p;
+    if (!p.init(epsg)) return -1;
+    V3 o{0, 0, 0};
+    int st = p.inverse({xyz[0], xyz[1], xyz[2]}, o);
+    llh[0] = o.x; llh[1] = o.y; llh[2] = o.z;
+    return st;
+}
+
+extern "C" void orc_lonlat_to_xyz(double a, double e2, const double* llh, double* xyz) {
+    V3 o = lonlat_to_xyz(a, e2, {llh[0], llh[1], llh[2]});
+    xyz[0] = o.x; xyz[1] = o.y; xyz[2] = o.z;
+}
+
+extern "C" int orc_geo2rdr(const double* llh, double a, double e2, const orc_orbit* orbit,
+                           const orc_lut2d* doppler, double* aztime, double* srange,
+                           double wavelength, int look_side, double threshold, int maxiter,
+                           double delta_range) {
+    double t0 = *aztime;
+    int st = geo2rdr_detail(aztime, srange, {llh[0], llh[1], llh[2]}, a, e2, orbit, doppler,
+                            wavelength, look_side, t0, threshold, maxiter, delta_range);
+    return st == G_OK ? 1 : 0;
+}
+
+extern "C" void orc_sinc_table(float* out) {
+    const SincTable& T = sinc_table();
+    for (size_t i = 0; i < T.k.size(); ++i) out[i] = (float)T.k[i];
+}
+
+extern "C" int orc_dem_subset(const orc_dem_raster* dem, const orc_geo_grid* g, int margin,
+                              int64_t* x_off, int64_t* y_off, int64_t* width, int64_t* length,
+                              double* x_start, double* y_start) {
+    DEM d;
+    if (dem_raster_to_interp(d, dem, g, 0, g->length, g->width, margin)) return 1;
+    if (!d.have_raster) { *width = 0; *length = 0; return 0; }
+    *x_off = (int64_t)std::llround((d.xstart - dem->gt[0]) / dem->gt[1] - 0.5);
+    *y_off = (int64_t)std::llround((d.ystart - dem->gt[3]) / dem->gt[5] - 0.5);
+    *width = d.width; *length = d.length;
+    *x_start = d.xstart; *y_start = d.ystart;
+    return 0;
+}

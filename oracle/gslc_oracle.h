@@ -1,0 +1,147 @@
+/*
+ * CPU oracle for SLC geocoding — TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain C++17/OpenMP restatement of isce3's array-mode SLC
+ * geocoder (cxx/isce3/geocode/geocodeSlc.cpp:55-511, 831-968) and of every
+ * callee on that path.  It exists to check the CUDA product path; only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+ * it.  The product never calls it and has no CPU fallback.
+ *
+ * Parity status: the reference cannot be compiled here (it needs Eigen,
+ * GDAL, HDF5 and pyre), so the end-to-end restatement is pinned by the
+ * reference's own runnable known-answer data for the pieces on the path
+ * (tests/data/interpolator/data.txt for bilinear/biquintic/sinc, the
+ * circular-orbit Hermite KAT of tests/cxx/isce3/core/orbit/orbit.cpp:495-552)
+ * and by the synthetic lon/lat-as-phase KAT of
+ * tests/cxx/isce3/geocode/geocodeSlc.cpp:231-297 restated on synthetic
+ * geometry.  The full geocode path itself is "parity unpinned" against a
+ * running reference.
+ *
+ * Numerics follow the reference operation by operation.  Build with
+ * -ffp-contract=off (no FMA contraction), like the reference's x86-64 build.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int32_t have_data;      /* 0: default-constructed LUT, eval -> ref_value */
+    int32_t bounds_error;   /* LUT2d::boundsError() */
+    int32_t method;         /* 1 bilinear, 3 nearest (isce3 dataInterpMethod) */
+    int32_t nx, ny;         /* width, length */
+    double x0, y0, dx, dy;
+    double ref_value;
+    const double* data;     /* ny*nx row-major, host */
+} orc_lut2d;
+
+typedef struct {
+    int32_t x_order, y_order;   /* -1,-1 : default Poly2d (evaluates to 0) */
+    double x_mean, y_mean, x_norm, y_norm;
+    const double* coeffs;       /* (y_order+1)*(x_order+1), row = y power */
+} orc_poly2d;
+
+typedef struct {
+    int32_t kind;           /* 0 LUT2d, 1 Poly2d */
+    orc_lut2d lut;
+    orc_poly2d poly;
+} orc_azrg;
+
+typedef struct {
+    double sensing_start, wavelength, prf, starting_range, range_pixel_spacing;
+    int32_t look_side;      /* -1 right, +1 left (isce3 LookSide) */
+    int64_t length, width;
+} orc_radar_grid;
+
+typedef struct {
+    double start_x, start_y, spacing_x, spacing_y;
+    int32_t width, length, epsg;
+} orc_geo_grid;
+
+typedef struct {
+    double t0, spacing;     /* state-vector time tags: t0 + i*spacing */
+    int32_t n;
+    int32_t method;         /* 0 Hermite, 1 Legendre */
+    const double* pos;      /* n*3 */
+    const double* vel;      /* n*3 */
+} orc_orbit;
+
+/* A DEM raster as GDAL would expose it: full array + geotransform + EPSG. */
+typedef struct {
+    const float* data;      /* length*width, row-major */
+    int64_t width, length;
+    double gt[6];
+    int32_t epsg;
+} orc_dem_raster;
+
+typedef struct {
+    int32_t n;              /* number of subswaths; 0 -> every sample is sw 1 */
+    int64_t length, width;
+    const int32_t* valid;   /* n * length * 2 : [start, stop) per line */
+} orc_subswaths;
+
+typedef struct {
+    orc_radar_grid radar_grid, sliced_radar_grid;
+    orc_geo_grid geo_grid;
+    orc_orbit orbit;
+    orc_lut2d native_doppler, image_grid_doppler, az_time_correction, srange_correction;
+    orc_azrg az_carrier, rg_carrier;
+    double ell_a, ell_e2;
+    double threshold_geo2rdr;
+    int32_t numiter_geo2rdr;
+    int64_t first_azimuth_line, first_range_sample;
+    int32_t flatten, reramp, flatten_with_corrected_srange;
+    float invalid_re, invalid_im;
+    int32_t n_blocks;
+    int64_t rdr_length, rdr_width;
+    float* const* rdr_blocks;   /* complex64 interleaved; deramped IN PLACE like the reference */
+    float* const* geo_blocks;   /* complex64 interleaved, geo length*width */
+    uint8_t* mask;              /* may be NULL */
+    double* carrier_phase;      /* may be NULL */
+    double* flatten_phase;      /* may be NULL */
+    orc_dem_raster dem;
+    const orc_subswaths* subswaths;  /* may be NULL */
+    /* optional diagnostics (NULL to skip): radar coordinates per geo pixel */
+    double* out_az_index;
+    double* out_rg_index;
+    double* out_uncorrected_srange;
+    int32_t dem_margin;         /* DEMRasterToInterpolator default: 50 */
+    int32_t nthreads;           /* 0: OpenMP default */
+    double phase_seconds[4];    /* out: index pass, deramp, interpolate, reramp */
+} orc_geocode_args;
+
+/* Returns 0 on success; >0 argument error (message via orc_last_error). */
+int orc_geocode_slc(orc_geocode_args* a);
+const char* orc_last_error(void);
+
+/* ---- component entry points used by the pinning tests ---- */
+int orc_orbit_interpolate(const orc_orbit* o, double t, double* pos, double* vel);
+/* interpolators over a double matrix (ny x nx); method: 1 bilinear, 3 nearest,
+ * 4 biquintic (order 6), 5 sinc (8 taps, 8192 phases) */
+double orc_interp2d_double(int method, const double* z, int ny, int nx, double x, double y);
+/* the same biquintic, in float, as the DEM interpolator runs it */
+float orc_spline2d_float(const float* z, int ny, int nx, double x, double y);
+double orc_lut2d_eval(const orc_lut2d* l, double y, double x);
+int orc_lut2d_contains(const orc_lut2d* l, double y, double x);
+double orc_poly2d_eval(const orc_poly2d* p, double y, double x);
+/* projections: forward = lon/lat(rad)/h -> map x/y/h; returns 0 on success */
+int orc_proj_forward(int epsg, const double* llh, double* xyz);
+int orc_proj_inverse(int epsg, const double* xyz, double* llh);
+void orc_lonlat_to_xyz(double a, double e2, const double* llh, double* xyz);
+/* geo2rdr with LUT2d Doppler; returns 1 on convergence (geometry.cpp:241-251) */
+int orc_geo2rdr(const double* llh, double a, double e2, const orc_orbit* orbit,
+                const orc_lut2d* doppler, double* aztime, double* srange,
+                double wavelength, int look_side, double threshold, int maxiter,
+                double delta_range);
+/* sinc kernel table (8192 x 8, float-cast as used), for inspection */
+void orc_sinc_table(float* out);
+/* DEM subset the geocoder loads for a geogrid (loadDem.cpp:22-133) */
+int orc_dem_subset(const orc_dem_raster* dem, const orc_geo_grid* g, int margin,
+                   int64_t* x_off, int64_t* y_off, int64_t* width, int64_t* length,
+                   double* x_start, double* y_start);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,336 @@
+"""ctypes front end of the CPU oracle (oracle/gslc_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg use it as the checker.  The product (isce3_gb300) never
+imports it.  It takes the same host objects as isce3_gb300.geocode.geocode_slc
+(read by attribute) and runs the C++ restatement of the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libgslc_oracle.so"
+
+
+def build(force: bool = False) -> Path:
+    src = [HERE / "gslc_oracle.cpp", HERE / "gslc_oracle.h"]
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(p.stat().st_mtime for p in src):
+        r = subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+class Lut(C.Structure):
+    _fields_ = [("have_data", C.c_int32), ("bounds_error", C.c_int32), ("method", C.c_int32),
+                ("nx", C.c_int32), ("ny", C.c_int32), ("x0", C.c_double), ("y0", C.c_double),
+                ("dx", C.c_double), ("dy", C.c_double), ("ref_value", C.c_double), ("data", C.c_void_p)]
+
+
+class Poly(C.Structure):
+    _fields_ = [("x_order", C.c_int32), ("y_order", C.c_int32), ("x_mean", C.c_double), ("y_mean", C.c_double),
+                ("x_norm", C.c_double), ("y_norm", C.c_double), ("coeffs", C.c_void_p)]
+
+
+class AzRg(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("lut", Lut), ("poly", Poly)]
+
+
+class RadarGrid(C.Structure):
+    _fields_ = [("sensing_start", C.c_double), ("wavelength", C.c_double), ("prf", C.c_double),
+                ("starting_range", C.c_double), ("range_pixel_spacing", C.c_double), ("look_side", C.c_int32),
+                ("length", C.c_int64), ("width", C.c_int64)]
+
+
+class GeoGrid(C.Structure):
+    _fields_ = [("start_x", C.c_double), ("start_y", C.c_double), ("spacing_x", C.c_double),
+                ("spacing_y", C.c_double), ("width", C.c_int32), ("length", C.c_int32), ("epsg", C.c_int32)]
+
+
+class OrbitS(C.Structure):
+    _fields_ = [("t0", C.c_double), ("spacing", C.c_double), ("n", C.c_int32), ("method", C.c_int32),
+                ("pos", C.c_void_p), ("vel", C.c_void_p)]
+
+
+class DemRaster(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int64), ("length", C.c_int64), ("gt", C.c_double * 6),
+                ("epsg", C.c_int32)]
+
+
+class SubSw(C.Structure):
+    _fields_ = [("n", C.c_int32), ("length", C.c_int64), ("width", C.c_int64), ("valid", C.c_void_p)]
+
+
+class Args(C.Structure):
+    _fields_ = [("radar_grid", RadarGrid), ("sliced_radar_grid", RadarGrid), ("geo_grid", GeoGrid),
+                ("orbit", OrbitS), ("native_doppler", Lut), ("image_grid_doppler", Lut),
+                ("az_time_correction", Lut), ("srange_correction", Lut), ("az_carrier", AzRg),
+                ("rg_carrier", AzRg), ("ell_a", C.c_double), ("ell_e2", C.c_double),
+                ("threshold_geo2rdr", C.c_double), ("numiter_geo2rdr", C.c_int32),
+                ("first_azimuth_line", C.c_int64), ("first_range_sample", C.c_int64),
+                ("flatten", C.c_int32), ("reramp", C.c_int32), ("flatten_with_corrected_srange", C.c_int32),
+                ("invalid_re", C.c_float), ("invalid_im", C.c_float), ("n_blocks", C.c_int32),
+                ("rdr_length", C.c_int64), ("rdr_width", C.c_int64), ("rdr_blocks", C.POINTER(C.c_void_p)),
+                ("geo_blocks", C.POINTER(C.c_void_p)), ("mask", C.c_void_p), ("carrier_phase", C.c_void_p),
+                ("flatten_phase", C.c_void_p), ("dem", DemRaster), ("subswaths", C.POINTER(SubSw)),
+                ("out_az_index", C.c_void_p), ("out_rg_index", C.c_void_p),
+                ("out_uncorrected_srange", C.c_void_p), ("dem_margin", C.c_int32), ("nthreads", C.c_int32),
+                ("phase_seconds", C.c_double * 4)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB))
+        _lib.orc_geocode_slc.restype = C.c_int
+        _lib.orc_geocode_slc.argtypes = [C.POINTER(Args)]
+        _lib.orc_last_error.restype = C.c_char_p
+        _lib.orc_orbit_interpolate.argtypes = [C.POINTER(OrbitS), C.c_double, C.c_void_p, C.c_void_p]
+        _lib.orc_interp2d_double.restype = C.c_double
+        _lib.orc_interp2d_double.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        _lib.orc_spline2d_float.restype = C.c_float
+        _lib.orc_spline2d_float.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        _lib.orc_lut2d_eval.restype = C.c_double
+        _lib.orc_lut2d_eval.argtypes = [C.POINTER(Lut), C.c_double, C.c_double]
+        _lib.orc_lut2d_contains.argtypes = [C.POINTER(Lut), C.c_double, C.c_double]
+        _lib.orc_poly2d_eval.restype = C.c_double
+        _lib.orc_poly2d_eval.argtypes = [C.POINTER(Poly), C.c_double, C.c_double]
+        _lib.orc_proj_forward.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        _lib.orc_proj_inverse.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        _lib.orc_lonlat_to_xyz.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+        _lib.orc_geo2rdr.argtypes = [C.c_void_p, C.c_double, C.c_double, C.POINTER(OrbitS), C.POINTER(Lut),
+                                     C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double]
+        _lib.orc_sinc_table.argtypes = [C.c_void_p]
+        _lib.orc_dem_subset.argtypes = [C.POINTER(DemRaster), C.POINTER(GeoGrid), C.c_int] + [C.c_void_p] * 6
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class _Keep(list):
+    def arr(self, a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self.append(a)
+        return a
+
+
+def lut_struct(lut, keep: _Keep) -> Lut:
+    s = Lut()
+    s.have_data = int(lut.have_data)
+    s.bounds_error = int(lut.bounds_error)
+    s.method = int(lut.interp_method)
+    s.ref_value = float(lut.ref_value)
+    if lut.have_data:
+        d = keep.arr(lut.data, np.float64)
+        s.nx, s.ny = d.shape[1], d.shape[0]
+        s.x0, s.y0, s.dx, s.dy = lut.x_start, lut.y_start, lut.x_spacing, lut.y_spacing
+        s.data = _ptr(d)
+    return s
+
+
+def poly_struct(p, keep: _Keep) -> Poly:
+    s = Poly()
+    s.x_order, s.y_order = p.x_order, p.y_order
+    s.x_mean, s.y_mean, s.x_norm, s.y_norm = p.x_mean, p.y_mean, p.x_std, p.y_std
+    c = keep.arr(p.coeffs if p.coeffs.size else np.zeros(1), np.float64)
+    s.coeffs = _ptr(c)
+    return s
+
+
+def azrg_struct(f, keep: _Keep) -> AzRg:
+    s = AzRg()
+    if hasattr(f, "x_order"):
+        s.kind = 1
+        s.poly = poly_struct(f, keep)
+    else:
+        s.kind = 0
+        s.lut = lut_struct(f, keep)
+    return s
+
+
+def radar_struct(g) -> RadarGrid:
+    s = RadarGrid()
+    s.sensing_start, s.wavelength, s.prf = g.sensing_start, g.wavelength, g.prf
+    s.starting_range, s.range_pixel_spacing = g.starting_range, g.range_pixel_spacing
+    s.look_side, s.length, s.width = int(g.lookside), g.length, g.width
+    return s
+
+
+def geo_struct(g) -> GeoGrid:
+    s = GeoGrid()
+    s.start_x, s.start_y, s.spacing_x, s.spacing_y = g.start_x, g.start_y, g.spacing_x, g.spacing_y
+    s.width, s.length, s.epsg = g.width, g.length, g.epsg
+    return s
+
+
+def orbit_struct(o, keep: _Keep) -> OrbitS:
+    s = OrbitS()
+    s.t0, s.spacing, s.n = o.t0, o.spacing, o.size
+    s.method = int(o.interp_method)
+    s.pos = _ptr(keep.arr(o.position, np.float64))
+    s.vel = _ptr(keep.arr(o.velocity, np.float64))
+    return s
+
+
+def dem_struct(r, keep: _Keep) -> DemRaster:
+    s = DemRaster()
+    d = keep.arr(r.data, np.float32)
+    s.data = _ptr(d)
+    s.length, s.width = d.shape
+    for i, v in enumerate(r.get_geotransform()):
+        s.gt[i] = v
+    s.epsg = r.get_epsg()
+    return s
+
+
+def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
+                image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block=None,
+                sliced_radargrid=None, subswaths=None, first_azimuth_line=0, first_range_sample=0, flatten=True,
+                reramp=True, az_carrier=None, rg_carrier=None, az_time_correction=None, srange_correction=None,
+                flatten_with_corrected_srange=False, invalid_value=np.nan + np.nan * 1j,
+                carrier_phase_block=None, flatten_phase_block=None, *, az_index_block=None, rg_index_block=None,
+                uncorrected_srange_block=None, dem_margin=50, nthreads=0, inplace_deramp=False):
+    """Run the oracle with geocode_slc's arguments; outputs are written in place.
+
+    Radar blocks are deramped on copies unless ``inplace_deramp``.  Returns
+    the per-phase wall times (index pass, deramp, interpolate, reramp) in s.
+    """
+    from isce3_gb300.core import LUT2d
+    az_carrier = az_carrier if az_carrier is not None else LUT2d()
+    rg_carrier = rg_carrier if rg_carrier is not None else LUT2d()
+    az_time_correction = az_time_correction if az_time_correction is not None else LUT2d()
+    srange_correction = srange_correction if srange_correction is not None else LUT2d()
+    if not isinstance(geo_data_blocks, list):
+        geo_data_blocks, rdr_data_blocks = [geo_data_blocks], [rdr_data_blocks]
+    keep = _Keep()
+    rdr = [r if inplace_deramp else np.array(r, dtype=np.complex64, copy=True) for r in rdr_data_blocks]
+    keep.extend(rdr)
+    a = Args()
+    a.radar_grid = radar_struct(radargrid)
+    a.sliced_radar_grid = radar_struct(sliced_radargrid or radargrid)
+    a.geo_grid = geo_struct(geogrid)
+    a.orbit = orbit_struct(orbit, keep)
+    a.native_doppler = lut_struct(native_doppler, keep)
+    a.image_grid_doppler = lut_struct(image_grid_doppler, keep)
+    a.az_time_correction = lut_struct(az_time_correction, keep)
+    a.srange_correction = lut_struct(srange_correction, keep)
+    a.az_carrier = azrg_struct(az_carrier, keep)
+    a.rg_carrier = azrg_struct(rg_carrier, keep)
+    a.ell_a, a.ell_e2 = ellipsoid.a, ellipsoid.e2
+    a.threshold_geo2rdr, a.numiter_geo2rdr = threshold_geo2rdr, num_iter_geo2rdr
+    a.first_azimuth_line, a.first_range_sample = first_azimuth_line, first_range_sample
+    a.flatten, a.reramp = int(flatten), int(reramp)
+    a.flatten_with_corrected_srange = int(flatten_with_corrected_srange)
+    inv = complex(invalid_value)
+    a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
+    a.n_blocks = len(rdr)
+    a.rdr_length, a.rdr_width = rdr[0].shape
+    rp = (C.c_void_p * len(rdr))(*[_ptr(r) for r in rdr])
+    gp = (C.c_void_p * len(geo_data_blocks))(*[_ptr(g) for g in geo_data_blocks])
+    a.rdr_blocks = C.cast(rp, C.POINTER(C.c_void_p))
+    a.geo_blocks = C.cast(gp, C.POINTER(C.c_void_p))
+
+    def opt(x):
+        return _ptr(x) if x is not None and x.size else None
+    a.mask = opt(mask_block)
+    a.carrier_phase = opt(carrier_phase_block)
+    a.flatten_phase = opt(flatten_phase_block)
+    a.out_az_index = opt(az_index_block)
+    a.out_rg_index = opt(rg_index_block)
+    a.out_uncorrected_srange = opt(uncorrected_srange_block)
+    a.dem = dem_struct(dem_raster, keep)
+    a.dem_margin = dem_margin
+    a.nthreads = nthreads
+    if subswaths is not None:
+        ss = SubSw()
+        ss.n, ss.length, ss.width = subswaths.num_sub_swaths, subswaths.length, subswaths.width
+        packed = keep.arr(subswaths.packed(), np.int32)
+        ss.valid = _ptr(packed)
+        keep.append(ss)
+        a.subswaths = C.pointer(ss)
+    st = lib().orc_geocode_slc(C.byref(a))
+    if st != 0:
+        raise ValueError(lib().orc_last_error().decode())
+    return list(a.phase_seconds)
+
+
+def orbit_interpolate(orbit, t):
+    keep = _Keep()
+    o = orbit_struct(orbit, keep)
+    pos, vel = np.zeros(3), np.zeros(3)
+    st = lib().orc_orbit_interpolate(C.byref(o), float(t), _ptr(pos), _ptr(vel))
+    return pos, vel, st
+
+
+def interp2d(method: int, z: np.ndarray, x: float, y: float) -> float:
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    return lib().orc_interp2d_double(method, _ptr(z), z.shape[0], z.shape[1], x, y)
+
+
+def spline2d_float(z: np.ndarray, x: float, y: float) -> np.float32:
+    z = np.ascontiguousarray(z, dtype=np.float32)
+    return np.float32(lib().orc_spline2d_float(_ptr(z), z.shape[0], z.shape[1], x, y))
+
+
+def lut_eval(lut, y, x) -> float:
+    keep = _Keep()
+    s = lut_struct(lut, keep)
+    return lib().orc_lut2d_eval(C.byref(s), y, x)
+
+
+def poly_eval(p, y, x) -> float:
+    keep = _Keep()
+    s = poly_struct(p, keep)
+    return lib().orc_poly2d_eval(C.byref(s), y, x)
+
+
+def proj_inverse(epsg, x, y):
+    inp, out = np.array([x, y, 0.0]), np.zeros(3)
+    st = lib().orc_proj_inverse(epsg, _ptr(inp), _ptr(out))
+    return out[0], out[1], st
+
+
+def proj_forward(epsg, lon, lat):
+    inp, out = np.array([lon, lat, 0.0]), np.zeros(3)
+    st = lib().orc_proj_forward(epsg, _ptr(inp), _ptr(out))
+    return out[0], out[1], st
+
+
+def geo2rdr(llh, ellipsoid, orbit, doppler, wavelength, side, t0, threshold=1e-8, maxiter=50, delta_range=10.0):
+    keep = _Keep()
+    o = orbit_struct(orbit, keep)
+    d = lut_struct(doppler, keep)
+    llh = np.asarray(llh, dtype=np.float64)
+    t, r = np.array([t0], dtype=np.float64), np.zeros(1)
+    ok = lib().orc_geo2rdr(_ptr(llh), ellipsoid.a, ellipsoid.e2, C.byref(o), C.byref(d), _ptr(t), _ptr(r),
+                           wavelength, int(side), threshold, maxiter, delta_range)
+    return t[0], r[0], ok
+
+
+def sinc_table() -> np.ndarray:
+    out = np.zeros((8192, 8), dtype=np.float32)
+    lib().orc_sinc_table(_ptr(out))
+    return out
+
+
+def timed_geocode(*args, **kw):
+    t0 = time.perf_counter()
+    phases = geocode_slc(*args, **kw)
+    return time.perf_counter() - t0, phases
+
+
+def ncores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1
