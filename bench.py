@@ -1,0 +1,464 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 SLC geocoder on the frame-scale workload.
+
+Workload ("frame", the single-GPU configuration the metric is quoted on): a
+16384 x 8192 complex64 SLC (circular complex Gaussian, seeded) geocoded onto
+an 8000 x 8000 UTM (EPSG:32611) 10 m geogrid over a 1 arc-second EPSG:4326
+fBm DEM (0-3000 m), with a 32 x 32 native-Doppler LUT2d (quadratic in range,
++-50 Hz) and a linear azimuth carrier.  One step = one plain geocode_slc call
+over the whole frame (64M output pixels).
+
+Printed JSON (one line):
+- value: output px/s with inputs resident in HBM (CUDA events, K steps);
+- e2e: the same through the drop-in call with pinned host buffers, H2D of the
+  SLC and DEM window and D2H of the geocoded frame and mask inside the timing;
+- roofline: the fused geocode kernel's algorithmic bytes per launch over its
+  CUDA-event duration, against the measured HBM copy bandwidth; plus the FP64
+  pipe it is actually bound by;
+- cpu_baseline: the CPU oracle (a restatement of the reference's OpenMP
+  geocodeSlc) on a bounded sample of geogrid rows, all host cores;
+- parity_sample: the GPU frame against the oracle on that sample.
+``--impl reference`` times the oracle alone (the reference's CPU algorithm) on
+the same workload, metric and units.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "geocoded px/s (batched/served vs plain, 1 GB300, ≤1e-4 rad); p50/p99 latency"
+UNIT = "px/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gslc", "reference"], default="gslc")
+    p.add_argument("--workload", choices=["frame", "small"], default="frame")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def make_scene(workload: str):
+    from isce3_gb300 import synth
+    if workload == "frame":
+        return synth.scene_c2(seed=2)
+    return synth.scene_c2(seed=2, length=4096, width=2048, geo=2000, spacing=12.0)
+
+
+def workload_config(sc, args, world):
+    g = sc.geogrid
+    return {"workload": f"plain geocode_slc, {sc.radar_grid.length}x{sc.radar_grid.width} c64 SLC -> "
+                        f"{g.length}x{g.width} UTM EPSG:{g.epsg} {g.spacing_x:g} m",
+            "slc_shape": [sc.radar_grid.length, sc.radar_grid.width], "geogrid_shape": [g.length, g.width],
+            "epsg": g.epsg, "dem": f"{sc.dem.length}x{sc.dem.width} EPSG:4326 fBm 0-3000 m",
+            "native_doppler": "LUT2d 32x32 quadratic in range +-50 Hz", "az_carrier": "Poly2d linear",
+            "geo2rdr": "fp64", "form": "plain", "l2": "inputs larger than L2 (1 GiB SLC, 512 MiB output)",
+            "replicas": world, "seed": sc.seed}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [ln.split(",") for ln in Path(self.path).read_text().splitlines() if ln.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU side
+def radar_bbox(az, rg, shape, margin=9):
+    """Radar block covering the chips of the given coordinates (the reference
+    raster mode pads its block by 5 lines/samples, geocodeSlc.cpp:740-750;
+    the sinc chip adds 4)."""
+    v = np.isfinite(az) & np.isfinite(rg)
+    if not v.any():
+        return 0, 1, 0, 1
+    a0 = max(int(np.floor(az[v].min())) - margin, 0)
+    a1 = min(int(np.ceil(az[v].max())) + margin + 1, shape[0])
+    r0 = max(int(np.floor(rg[v].min())) - margin, 0)
+    r1 = min(int(np.ceil(rg[v].max())) + margin + 1, shape[1])
+    return a0, a1, r0, r1
+
+
+def sample_rows_block(oracle, sc, row0, nrows):
+    """Geogrid rows [row0, row0+nrows) and the radar sub-block they need, the
+    way the reference's block generator feeds geocode_slc."""
+    g = sc.geogrid[row0:row0 + nrows, 0:sc.geogrid.width]
+    coarse = sc.geogrid[row0:row0 + nrows:1, 0:sc.geogrid.width]
+    az = np.zeros((coarse.length, coarse.width))
+    rg = np.zeros_like(az)
+    dummy = np.zeros((16, 16), np.complex64)
+    geo = np.zeros((coarse.length, coarse.width), np.complex64)
+    oracle.geocode_slc(geo, dummy, sc.dem, sc.radar_grid, coarse, sc.orbit, sc.native_doppler,
+                       sc.image_grid_doppler, sc.ellipsoid, sc.threshold, sc.maxiter,
+                       az_index_block=az, rg_index_block=rg, az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    return g, radar_bbox(az, rg, sc.slc.shape)
+
+
+def run_oracle_sample(oracle, sc, g, box, outputs=False):
+    a0, a1, r0, r1 = box
+    block = np.ascontiguousarray(sc.slc[a0:a1, r0:r1])
+    geo = np.zeros((g.length, g.width), np.complex64)
+    mask = np.zeros((g.length, g.width), np.uint8)
+    az = np.zeros((g.length, g.width)) if outputs else None
+    rg = np.zeros((g.length, g.width)) if outputs else None
+    t0 = time.perf_counter()
+    phases = oracle.geocode_slc(geo, block, sc.dem, sc.radar_grid, g, sc.orbit, sc.native_doppler,
+                                sc.image_grid_doppler, sc.ellipsoid, sc.threshold, sc.maxiter, mask_block=mask,
+                                first_azimuth_line=a0, first_range_sample=r0, az_carrier=sc.az_carrier,
+                                rg_carrier=sc.rg_carrier, az_index_block=az, rg_index_block=rg,
+                                inplace_deramp=True)
+    dt = time.perf_counter() - t0
+    return dt, phases, dict(geo=geo, mask=mask, az=az, rg=rg)
+
+
+def calibrate_rows(oracle, sc, target_s, max_rows=512):
+    """Geogrid rows (centred) whose oracle run takes about target_s seconds."""
+    mid = sc.geogrid.length // 2
+    rows = 4
+    g, box = sample_rows_block(oracle, sc, mid - rows // 2, rows)
+    dt, _, _ = run_oracle_sample(oracle, sc, g, box)
+    rows = int(np.clip(rows * target_s / max(dt, 1e-3), 4, max_rows))
+    row0 = mid - rows // 2
+    g, box = sample_rows_block(oracle, sc, row0, rows)
+    return row0, rows, g, box
+
+
+def cpu_baseline(sc, target_s):
+    from oracle import oracle
+    oracle.build()
+    row0, rows, g, box = calibrate_rows(oracle, sc, target_s)
+    dt, phases, out = run_oracle_sample(oracle, sc, g, box, outputs=True)
+    npx = g.length * g.width
+    info = {"value": npx / dt, "unit": UNIT, "cores": oracle.ncores(), "kind": "port",
+            "sample": f"geogrid rows {row0}..{row0 + rows - 1} (x{g.width}) of the frame with their radar "
+                      f"sub-block {box[1] - box[0]}x{box[3] - box[2]}; {npx} px in {dt:.2f} s",
+            "phase_seconds": {"index": phases[0], "deramp": phases[1], "interpolate": phases[2],
+                              "reramp": phases[3]},
+            "arch": os.uname().machine}
+    return info, (row0, rows, box, out)
+
+
+# ---------------------------------------------------------------- GPU side
+def slc_footprint(az, rg, shape):
+    """SLC samples read by the 8x8 sinc chips of all valid pixels, assuming
+    each radar line's footprint is one interval (true for a swath)."""
+    import torch
+    v = torch.isfinite(az) & torch.isfinite(rg)
+    ia = torch.floor(az[v]).long().clamp(0, shape[0] - 1)
+    ir = torch.floor(rg[v]).long().clamp(0, shape[1] - 1)
+    big = torch.iinfo(torch.int64).max
+    lo = torch.full((shape[0],), big, dtype=torch.int64, device=az.device)
+    hi = torch.full((shape[0],), -1, dtype=torch.int64, device=az.device)
+    lo.scatter_reduce_(0, ia, ir, reduce="amin")
+    hi.scatter_reduce_(0, ia, ir, reduce="amax")
+    lo, hi = lo.cpu().numpy(), hi.cpu().numpy()
+    n = 0
+    for r in range(shape[0]):
+        a, b = max(r - 4, 0), min(r + 4, shape[0])        # chip rows intAz-3 .. intAz+4
+        l_, h_ = lo[a:b].min(), hi[a:b].max()
+        if h_ >= 0:
+            n += min(h_ + 4, shape[1] - 1) - max(l_ - 3, 0) + 1
+    return int(n)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from isce3_gb300 import _lib as L
+    from isce3_gb300.geocode import geocode_slc
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    sc = make_scene(args.workload)
+    g = sc.geogrid
+    npx = g.length * g.width
+    lib = L.lib()
+    ctx = L.context(dev.index)
+    L.check(lib.gslc_ctx_set_timing(ctx, 1), ctx)
+    slc_d = torch.from_numpy(sc.slc).to(dev)
+    geo_d = torch.empty((g.length, g.width), dtype=torch.complex64, device=dev)
+    mask_d = torch.empty((g.length, g.width), dtype=torch.uint8, device=dev)
+    common = (sc.dem, sc.radar_grid, g, sc.orbit, sc.native_doppler, sc.image_grid_doppler, sc.ellipsoid,
+              sc.threshold, sc.maxiter)
+    kw = dict(az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+
+    # one diagnostic call for radar coordinates (algorithmic bytes, parity sample)
+    az_d = torch.empty((g.length, g.width), dtype=torch.float64, device=dev)
+    rg_d = torch.empty_like(az_d)
+    geocode_slc(geo_d, slc_d, *common, mask_block=mask_d, az_index_block=az_d, rg_index_block=rg_d, **kw)
+    n_valid = int(torch.isfinite(az_d).sum())
+    n_slc = slc_footprint(az_d, rg_d, sc.slc.shape)
+    dem_keep = [v for v in sc.dem.__dict__.get("_gslc_dev", {}).values()]
+    dem_bytes = sum(t.numel() * 4 for t in dem_keep)
+    alg_bytes = 8 * npx + 1 * npx + 8 * n_slc + dem_bytes
+
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        geocode_slc(geo_d, slc_d, *common, mask_block=mask_d, **kw)
+    sampler = ClockSampler(dev.index)
+    kernel_ms, deramp_ms, launches = [], [], 0
+    _barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        geocode_slc(geo_d, slc_d, *common, mask_block=mask_d, **kw)
+        a, b = _kernel_ms(lib, ctx)
+        kernel_ms.append(a)
+        deramp_ms.append(b)
+        launches += int(lib.gslc_last_launch_count(ctx))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    _barrier(world)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = _max_over_ranks(ms, world)
+    res = dict(npx=npx, n_valid=n_valid, ms=ms, kernel_ms=float(np.mean(kernel_ms)),
+               deramp_ms=float(np.mean(deramp_ms)), launches=launches, clocks=clocks, alg_bytes=alg_bytes,
+               n_slc=n_slc, dem_bytes=dem_bytes)
+    fp = C_double()
+    L.check(lib.gslc_probe_fp64_gflops(ctx, fp), ctx)
+    res["fp64_peak_gflops"] = fp.value
+    res["geo_d"], res["mask_d"], res["az_d"], res["rg_d"] = geo_d, mask_d, az_d, rg_d
+    res["e2e"] = None if args.no_e2e else run_e2e(args, sc, dev, common, kw)
+    return sc, res
+
+
+def C_double():
+    import ctypes
+    return ctypes.c_double()
+
+
+def _kernel_ms(lib, ctx):
+    import ctypes
+    a, b = ctypes.c_float(), ctypes.c_float()
+    lib.gslc_last_kernel_ms(ctx, ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def run_e2e(args, sc, dev, common, kw):
+    """Drop-in call on pinned host buffers; H2D and D2H inside the timing."""
+    import torch
+    from isce3_gb300.geocode import geocode_slc
+    g = sc.geogrid
+    slc_h = torch.empty(sc.slc.shape, dtype=torch.complex64, pin_memory=True)
+    slc_h.numpy()[...] = sc.slc
+    geo_h = torch.empty((g.length, g.width), dtype=torch.complex64, pin_memory=True)
+    mask_h = torch.empty((g.length, g.width), dtype=torch.uint8, pin_memory=True)
+    caches = [sc.dem, sc.native_doppler, sc.image_grid_doppler]
+
+    def step():
+        for c in caches:            # inputs are re-sent every step
+            c.__dict__.pop("_gslc_dev", None)
+        geocode_slc(geo_h, slc_h, *common, mask_block=mask_h, **kw)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        torch.cuda.synchronize()
+        t.append(time.perf_counter() - t0)
+    dem_bytes = sum(v.numel() * 4 for v in sc.dem.__dict__.get("_gslc_dev", {}).values())
+    lut_bytes = sc.native_doppler.data.nbytes
+    h2d = slc_h.numel() * 8 + dem_bytes + lut_bytes
+    d2h = geo_h.numel() * 8 + mask_h.numel()
+    sec = float(np.mean(t))
+    return {"value": g.length * g.width / sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": sec * 1e3, "p50_ms": float(np.median(t)) * 1e3,
+            "timing": "host wall clock around the drop-in call, synchronized"}
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def parity_sample(res, row0, rows, box, out):
+    """GPU frame rows against the oracle's run on the same rows."""
+    sl = slice(row0, row0 + rows)
+    geo = res["geo_d"][sl].cpu().numpy()
+    mask = res["mask_d"][sl].cpu().numpy()
+    az = res["az_d"][sl].cpu().numpy()
+    rg = res["rg_d"][sl].cpu().numpy()
+    go, mo, ao, ro = out["geo"], out["mask"], out["az"], out["rg"]
+
+    def tidx(c):
+        with np.errstate(invalid="ignore"):
+            f = c - np.trunc(c)
+            return np.nan_to_num(np.floor((4.0 + f - np.floor(4.0 + f)) * 8192)).astype(np.int64)
+    both = np.isfinite(az) & np.isfinite(ao)
+    flips = both & ((tidx(az) != tidx(ao)) | (tidx(rg) != tidx(ro)))
+    ok = both & ~flips & np.isfinite(go) & np.isfinite(geo)
+    rms = float(np.sqrt(np.mean(np.abs(go[ok]) ** 2))) if ok.any() else 1.0
+    err = np.abs(geo[ok] - go[ok])
+    big = np.abs(go[ok]) >= 1e-2 * rms
+    ph = np.abs(np.angle(geo[ok][big] * np.conj(go[ok][big])))
+    return {"rows": [row0, row0 + rows], "px": int(geo.size), "valid": int(both.sum()),
+            "mask_mismatch": int((mask != mo).sum()),
+            "validity_mismatch": int((np.isfinite(az) != np.isfinite(ao)).sum()),
+            "max_phase_err_rad": float(ph.max()) if ph.size else 0.0,
+            "max_rel_err": float((err / np.maximum(np.abs(go[ok]), 1e-2 * rms)).max()) if ok.any() else 0.0,
+            "n_out_of_tol": int(np.sum(err > 1e-5 * np.abs(go[ok]) + 1e-6 * rms)),
+            "sinc_table_flips": int(flips.sum()), "flip_fraction": float(flips.sum() / max(both.sum(), 1))}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU algorithm (the oracle restatement, OpenMP, all host
+    cores) on the same workload: each step one bounded sample of geogrid rows."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    sc = make_scene(args.workload)
+    target = max(1.0, min(args.cpu_seconds, 120.0 / max(args.steps + args.warmup, 1)))
+    row0, rows, g, box = calibrate_rows(oracle, sc, target)
+    for _ in range(args.warmup):
+        run_oracle_sample(oracle, sc, g, box)
+    times = [run_oracle_sample(oracle, sc, g, box)[0] for _ in range(args.steps)]
+    npx = g.length * g.width
+    sec = float(np.mean(times))
+    value = npx / sec
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+            "config": workload_config(sc, args, 1),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.ncores(), "kind": "port",
+                             "sample": f"geogrid rows {row0}..{row0 + rows - 1} (x{g.width}) with their radar "
+                                       f"sub-block per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "isce3 itself cannot be built here (Eigen/GDAL/HDF5/pyre absent); the timed CPU code is "
+                    "the oracle's C++/OpenMP restatement of geocodeSlc"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    if not torch.cuda.is_available():
+        print(json.dumps({"metric": METRIC, "error": "no CUDA GPU"}))
+        sys.exit(1)
+    from isce3_gb300 import _lib as L
+    L.build()
+    sc, res = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    cpu, par = None, None
+    if not args.no_cpu:
+        cpu, (row0, rows, box, out) = cpu_baseline(sc, args.cpu_seconds)
+        par = parity_sample(res, row0, rows, box, out)
+    hbm_peak, peak_kind = peaks()
+    kernel_s = res["kernel_ms"] * 1e-3
+    achieved = res["alg_bytes"] / kernel_s / 1e9
+    value = res["npx"] * world / (res["ms"] * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": workload_config(sc, args, world),
+        "valid_px_per_s": res["n_valid"] * world / (res["ms"] * 1e-3),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": f"{peak_kind} hbm_gbs",
+                     "kernel": "geocode_kernel (fused)", "kernel_ms": res["kernel_ms"],
+                     "alg_bytes_per_launch": res["alg_bytes"],
+                     "alg_bytes_terms": {"geo_out": 8 * res["npx"], "mask": res["npx"], "slc": 8 * res["n_slc"],
+                                         "dem_window": res["dem_bytes"]},
+                     "binding": "fp64 pipe (geo2rdr); see fp64"},
+        "fp64": {"peak_gflops_measured": res["fp64_peak_gflops"], "probe": "gslc_probe_fp64_gflops DFMA loop"},
+        "deramp_ms": res["deramp_ms"],
+        "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
+        "cpu_baseline": cpu, "parity_sample": par,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -179,6 +179,17 @@ int gslc_geocode_slc(gslc_ctx* ctx, const gslc_geocode_args* args, void* stream)
 /* Number of the library's own kernels launched by the last call on ctx. */
 int64_t gslc_last_launch_count(const gslc_ctx* ctx);
 
+/* Measurement: when enabled, each geocode call records CUDA events on its
+ * stream around the fused geocode kernel(s) and the deramp pre-pass;
+ * gslc_last_kernel_ms reads their durations after the call returns. */
+int gslc_ctx_set_timing(gslc_ctx* ctx, int32_t enable);
+int gslc_last_kernel_ms(const gslc_ctx* ctx, float* geocode_ms, float* deramp_ms);
+
+/* Measurement: sustained FP64 FMA rate of this GPU (GFLOP/s, 2 flops per
+ * FMA) from a dependent-chain DFMA loop over all SMs; the denominator of the
+ * FP64 roofline the geocode kernel is reported against. */
+int gslc_probe_fp64_gflops(gslc_ctx* ctx, double* gflops);
+
 #ifdef __cplusplus
 }
 #endif

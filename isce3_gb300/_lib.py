@@ -146,6 +146,9 @@ _EXPORTS = {
     "gslc_orbit_interpolate": (C.c_int, [C.POINTER(OrbitDesc), C.c_double, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]),
     "gslc_sinc_table": (C.c_int, [C.c_void_p]),
+    "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
 }
 
 _lock = threading.Lock()

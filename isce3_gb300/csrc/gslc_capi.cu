@@ -23,6 +23,9 @@ struct gslc_ctx {
     double* d_orbit = nullptr;
     size_t orbit_cap = 0;           // doubles
     int64_t launches = 0;
+    int timing = 0;                 // record CUDA events around the kernels
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float ms_geocode = 0.f, ms_deramp = 0.f;
     std::string err;
 };
 
@@ -408,6 +411,8 @@ extern "C" int gslc_ctx_destroy(gslc_ctx* c) {
     if (c->d_err) cudaFree(c->d_err);
     if (c->h_err) cudaFreeHost(c->h_err);
     if (c->d_orbit) cudaFree(c->d_orbit);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
     delete c;
     return GSLC_OK;
 }
@@ -568,6 +573,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     std::vector<void*> scratch;
     std::vector<const float2*> rdr(a->n_blocks);
     for (int b = 0; b < a->n_blocks; ++b) rdr[b] = (const float2*)a->rdr_blocks[b];
+    if (c->timing) cudaEventRecord(c->ev[2], stream);
     if (!p.carriers_zero && nrdr > 0) {
         for (int b = 0; b < a->n_blocks; ++b) {
             float2* dst = (float2*)a->rdr_blocks[b];
@@ -593,6 +599,10 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
             rdr[b] = dst;
         }
     }
+    if (c->timing) {
+        cudaEventRecord(c->ev[3], stream);
+        cudaEventRecord(c->ev[0], stream);
+    }
     for (int b0 = 0; b0 < a->n_blocks; b0 += MAX_BLOCKS) {
         p.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
         for (int b = 0; b < p.nblk; ++b) {
@@ -602,10 +612,64 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
         e = launch_geocode(p, a->geo2rdr_precision, stream, &c->launches);
         if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
     }
+    if (c->timing) cudaEventRecord(c->ev[1], stream);
     for (void* s : scratch) cudaFreeAsync(s, stream);
     e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return cuda_err(c, e, "geocode");
+    if (c->timing) {
+        cudaEventElapsedTime(&c->ms_geocode, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&c->ms_deramp, c->ev[2], c->ev[3]);
+    }
     if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    return GSLC_OK;
+}
+
+extern "C" int gslc_ctx_set_timing(gslc_ctx* c, int32_t enable) {
+    if (!c) return GSLC_EINVAL;
+    cudaSetDevice(c->device);
+    if (enable && !c->ev[0]) {
+        for (auto& e : c->ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return set_err(c, GSLC_ECUDA, "cudaEventCreate");
+    }
+    c->timing = enable ? 1 : 0;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_last_kernel_ms(const gslc_ctx* c, float* geocode_ms, float* deramp_ms) {
+    if (!c || !c->timing) return GSLC_EINVAL;
+    if (geocode_ms) *geocode_ms = c->ms_geocode;
+    if (deramp_ms) *deramp_ms = c->ms_deramp;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_probe_fp64_gflops(gslc_ctx* c, double* gflops) {
+    if (!c || !gflops) return GSLC_EINVAL;
+    cudaSetDevice(c->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int blocks = sms * 8, iters = 4096;
+    double* out = nullptr;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaMalloc(&out, (size_t)blocks * 256 * sizeof(double));
+    if (e != cudaSuccess) return cuda_err(c, e, "probe alloc");
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0, 0);
+        e = probe_fp64(out, blocks, iters, 0);
+        cudaEventRecord(e1, 0);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return cuda_err(c, e, "probe launch");
+    const double flops = 2.0 * 8.0 * iters * (double)blocks * 256.0;
+    *gflops = flops / (best * 1e-3) / 1e9;
     return GSLC_OK;
 }

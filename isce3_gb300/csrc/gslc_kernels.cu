@@ -329,7 +329,27 @@ __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ Der
     }
 }
 
+// FP64 FMA throughput probe: 8 independent dependent chains per thread.
+__global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
+
+cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s) {
+    dfma_probe_kernel<<<blocks, 256, 0, s>>>(out, iters, 0.9999999, 1e-7);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
     (void)precision;

@@ -70,5 +70,6 @@ struct DerampParams {
 // launchers (gslc_kernels.cu)
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);
+cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s);
 
 }  // namespace gslc

@@ -37,6 +37,10 @@ def _is_array(x) -> bool:
     return isinstance(x, (np.ndarray, torch.Tensor))
 
 
+def _size(x) -> int:
+    return x.numel() if isinstance(x, torch.Tensor) else x.size
+
+
 def _io_value_check(io):
     """geocode_slc.py:11-58."""
     chk = SimpleNamespace(is_list=False, is_array=False, n_items=0, shapes_consistent=False,
@@ -97,31 +101,39 @@ def _check_dtype(x, np_dtype, torch_dtype, what):
 
 
 class _Staged:
-    """A caller array as a device tensor, with copy-back for host outputs."""
+    """A caller array as a device tensor, with copy-back for host outputs.
+
+    Host arrays may be NumPy arrays or CPU torch tensors; pinned CPU tensors
+    copy by DMA without staging.
+    """
 
     def __init__(self, arr, dev, upload: bool, torch_dtype):
         self.host = None
-        if isinstance(arr, torch.Tensor):
-            if arr.device.type != "cuda":
-                raise ValueError("torch tensors must be CUDA tensors")
+        if isinstance(arr, torch.Tensor) and arr.device.type == "cuda":
             if not arr.is_contiguous():
                 raise ValueError("arrays must be C-contiguous")
             self.dev = arr
+            return
+        if isinstance(arr, torch.Tensor):
+            if not arr.is_contiguous():
+                raise ValueError("arrays must be C-contiguous")
+            host = arr
         else:
             if not arr.flags.c_contiguous:
                 raise ValueError("arrays must be C-contiguous")
-            self.host = arr
-            if upload:
-                self.dev = torch.from_numpy(arr).to(dev, non_blocking=True)
-            else:
-                self.dev = torch.empty(arr.shape, dtype=torch_dtype, device=dev)
+            host = torch.from_numpy(arr)
+        self.host = host
+        if upload:
+            self.dev = host.to(dev, non_blocking=host.is_pinned())
+        else:
+            self.dev = torch.empty(tuple(host.shape), dtype=torch_dtype, device=dev)
 
     def ptr(self) -> int:
         return self.dev.data_ptr()
 
     def copy_back(self):
         if self.host is not None:
-            self.host[...] = self.dev.cpu().numpy()
+            self.host.copy_(self.dev)
 
 
 def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGridParameters,
@@ -186,28 +198,45 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
     ctx = L.context(dev.index)
     with torch.cuda.device(dev):
         s = stream if stream is not None else torch.cuda.current_stream(dev)
+        with torch.cuda.stream(s):
+            _geocode_on_stream(lib, ctx, s, dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid,
+                               sliced_radargrid, geogrid, orbit, native_doppler, image_grid_doppler, ellipsoid,
+                               threshold_geo2rdr, num_iter_geo2rdr, mask_block, subswaths, first_azimuth_line,
+                               first_range_sample, flatten, reramp, az_carrier, rg_carrier, az_time_correction,
+                               srange_correction, flatten_with_corrected_srange, invalid_value,
+                               carrier_phase_block, flatten_phase_block, precision, inplace_deramp,
+                               az_index_block, rg_index_block, dem_margin)
+
+
+def _geocode_on_stream(lib, ctx, s, dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid,
+                       sliced_radargrid, geogrid, orbit, native_doppler, image_grid_doppler, ellipsoid,
+                       threshold_geo2rdr, num_iter_geo2rdr, mask_block, subswaths, first_azimuth_line,
+                       first_range_sample, flatten, reramp, az_carrier, rg_carrier, az_time_correction,
+                       srange_correction, flatten_with_corrected_srange, invalid_value,
+                       carrier_phase_block, flatten_phase_block, precision, inplace_deramp,
+                       az_index_block, rg_index_block, dem_margin):
+    if True:
         rdr = [_Staged(r, dev, True, torch.complex64) for r in rdr_data_blocks]
         if any(r.host is not None for r in rdr) and inplace_deramp:
             raise ValueError("inplace_deramp needs device-resident radar tensors")
         geo = [_Staged(g, dev, False, torch.complex64) for g in geo_data_blocks]
         outs = list(geo)
 
-        def opt_out(arr, np_dtype, t_dtype, what):
-            if arr is None:
-                return None
-            size = arr.numel() if isinstance(arr, torch.Tensor) else arr.size
-            if size == 0:
+        def opt_out(arr, np_dtype, t_dtype, what, upload):
+            if arr is None or _size(arr) == 0:
                 return None
             _check_dtype(arr, np_dtype, t_dtype, what)
-            st = _Staged(arr, dev, True, t_dtype)   # upload: untouched pixels keep caller values
+            st = _Staged(arr, dev, upload, t_dtype)
             outs.append(st)
             return st
 
-        mask = opt_out(mask_block, np.uint8, torch.uint8, "mask_block")
-        carrier = opt_out(carrier_phase_block, np.float64, torch.float64, "carrier_phase_block")
-        flat = opt_out(flatten_phase_block, np.float64, torch.float64, "flatten_phase_block")
-        azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block")
-        rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block")
+        # the mask and radar coordinates are written at every pixel; the phase
+        # outputs only at valid ones, so those keep the caller's other values
+        mask = opt_out(mask_block, np.uint8, torch.uint8, "mask_block", False)
+        carrier = opt_out(carrier_phase_block, np.float64, torch.float64, "carrier_phase_block", True)
+        flat = opt_out(flatten_phase_block, np.float64, torch.float64, "flatten_phase_block", True)
+        azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block", False)
+        rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block", False)
 
         holder = M.AzRgHolder()
         a = L.GeocodeArgs()

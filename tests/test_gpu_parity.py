@@ -1,0 +1,199 @@
+"""GPU parity: the sm_103a kernel (through the C ABI) against the CPU oracle.
+
+Every case runs the same seeded inputs through isce3_gb300.geocode.geocode_slc
+(which calls gslc_geocode_slc in libgslc.so) and through the oracle, then
+applies tests/parity.py: masks and validity bit-exact, complex values within
+1e-5 relative (+1e-6 rms), phase within 1e-4 rad, sinc-table flips counted
+and bounded.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from isce3_gb300 import synth  # noqa: E402
+from isce3_gb300.core import DataInterpMethod, LUT2d, Poly2d  # noqa: E402
+from isce3_gb300.geocode import geocode_slc  # noqa: E402
+from isce3_gb300.product import SubSwaths  # noqa: E402
+
+from parity import assert_parity, compare  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+def _run_both(oracle_mod, sc, slc_blocks, rg=None, geogrid=None, dem=None, n_out=1, **kw):
+    """Run product and oracle with identical arguments; return both outputs."""
+    rg = rg or sc.radar_grid
+    g = geogrid or sc.geogrid
+    dem = dem or sc.dem
+    shape = (g.length, g.width)
+    nd = kw.pop("native_doppler", sc.native_doppler)
+    igd = kw.pop("image_grid_doppler", sc.image_grid_doppler)
+    out = {}
+    for side in ("gpu", "ora"):
+        geo = [np.zeros(shape, np.complex64) for _ in range(n_out)]
+        mask = np.zeros(shape, np.uint8)
+        az = np.zeros(shape)
+        rgi = np.zeros(shape)
+        carrier = np.full(shape, -7.0)
+        flat = np.full(shape, -7.0)
+        blocks = [b.copy() for b in slc_blocks]
+        args = (geo if n_out > 1 else geo[0], blocks if n_out > 1 else blocks[0], dem, rg, g, sc.orbit, nd, igd,
+                sc.ellipsoid, kw.get("threshold", sc.threshold), kw.get("maxiter", sc.maxiter))
+        extra = {k: v for k, v in kw.items() if k not in ("threshold", "maxiter")}
+        if side == "gpu":
+            geocode_slc(*args, mask_block=mask, carrier_phase_block=carrier, flatten_phase_block=flat,
+                        az_index_block=az, rg_index_block=rgi, **extra)
+        else:
+            extra.pop("geo2rdr_precision", None)
+            oracle_mod.geocode_slc(*args, mask_block=mask, carrier_phase_block=carrier, flatten_phase_block=flat,
+                                   az_index_block=az, rg_index_block=rgi, **extra)
+        out[side] = dict(geo=geo, mask=mask, az=az, rg=rgi, carrier=carrier, flat=flat)
+    return out["gpu"], out["ora"]
+
+
+def _check(gpu, ora, az_first=0, rg_first=0, max_flip=1e-3):
+    reports = []
+    for gg, go in zip(gpu["geo"], ora["geo"]):
+        r = compare(gg, go, gpu["az"], ora["az"], gpu["rg"], ora["rg"], gpu["mask"], ora["mask"],
+                    az_first, rg_first)
+        print(r)
+        assert_parity(r, max_flip)
+        reports.append(r)
+    # carrier / flattening phase outputs: written on the same pixels, FP64
+    for k in ("carrier", "flat"):
+        wg, wo = gpu[k] != -7.0, ora[k] != -7.0
+        np.testing.assert_array_equal(wg, wo)
+        if wg.any():
+            scale = max(1.0, float(np.abs(ora[k][wo]).max()))
+            assert np.abs(gpu[k][wg] - ora[k][wo]).max() <= 1e-13 * scale + 1e-9
+    return reports
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return synth.scene_c1()
+
+
+def test_c1_plain(oracle_mod, c1):
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc])
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 100000
+    assert r["max_rel_err"] < 1e-5
+
+
+def test_c1_device_tensors_match_host_arrays(c1):
+    """Device-resident torch inputs give the same bits as the host path."""
+    g = c1.geogrid
+    host = np.zeros((g.length, g.width), np.complex64)
+    geocode_slc(host, c1.slc, c1.dem, c1.radar_grid, g, c1.orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-8, 25)
+    dev_out = torch.zeros((g.length, g.width), dtype=torch.complex64, device="cuda")
+    dev_in = torch.from_numpy(c1.slc).cuda()
+    geocode_slc(dev_out, dev_in, c1.dem, c1.radar_grid, g, c1.orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-8, 25)
+    np.testing.assert_array_equal(dev_out.cpu().numpy().view(np.uint64), host.view(np.uint64))
+    np.testing.assert_array_equal(dev_in.cpu().numpy(), c1.slc)   # input not mutated
+
+
+def test_c1_doppler_carriers_corrections_blocks(oracle_mod, c1):
+    """Squinted grid (image-grid Doppler = native), Poly2d carriers, correction
+    LUTs, two blocks of a radar sub-block with offsets, flatten with the
+    corrected range, custom invalid value."""
+    rg = c1.radar_grid
+    rr = np.linspace(rg.starting_range - 50 * rg.range_pixel_spacing, rg.end_range + 50 * rg.range_pixel_spacing, 16)
+    tt = np.linspace(rg.sensing_start - 50 / rg.prf, rg.sensing_stop + 50 / rg.prf, 12)
+    u = (rr - rr.mean()) / (rr.max() - rr.mean())
+    dop = LUT2d(rr, tt, np.tile(-40.0 + 80.0 * u ** 2, (12, 1)) + 3.0 * np.linspace(-1, 1, 12)[:, None])
+    az_car = Poly2d([[0.0, 1e-4], [2 * np.pi * 250.0, 0.0]], x_mean=rg.mid_range, y_mean=rg.sensing_mid)
+    rg_car = Poly2d([[0.5, 2e-3, 1e-7]], x_mean=rg.mid_range, y_mean=0.0)
+    s_vec = np.linspace(rg.starting_range, rg.end_range, 9)
+    t_vec = np.linspace(rg.sensing_start, rg.sensing_stop, 7)
+    corr_r = LUT2d(s_vec, t_vec, 0.37 + 0.01 * np.arange(63).reshape(7, 9), DataInterpMethod.BILINEAR)
+    corr_t = LUT2d(s_vec, t_vec, np.full((7, 9), 2.1e-5), DataInterpMethod.NEAREST)
+    a0, r0 = 100, 150
+    sub = [c1.slc[a0:a0 + 800, r0:r0 + 700], (c1.slc[a0:a0 + 800, r0:r0 + 700] * np.complex64(0.3 - 0.7j))]
+    gpu, ora = _run_both(oracle_mod, c1, sub, n_out=2, native_doppler=dop, image_grid_doppler=dop,
+                         az_carrier=az_car, rg_carrier=rg_car, az_time_correction=corr_t,
+                         srange_correction=corr_r, first_azimuth_line=a0, first_range_sample=r0,
+                         flatten_with_corrected_srange=True, invalid_value=np.complex64(-1 + 2j))
+    _check(gpu, ora, az_first=a0, rg_first=r0)
+
+
+@pytest.mark.parametrize("flatten,reramp", [(False, True), (True, False), (False, False)])
+def test_c1_flags(oracle_mod, c1, flatten, reramp):
+    az_car = Poly2d([[0.0], [2 * np.pi * 100.0]], y_mean=c1.radar_grid.sensing_mid)
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], flatten=flatten, reramp=reramp, az_carrier=az_car,
+                         rg_carrier=Poly2d())
+    _check(gpu, ora)
+
+
+def test_sliced_grid_and_subswaths(oracle_mod, c1):
+    rg = c1.radar_grid
+    sliced = rg.offset_and_resize(100, 80, 700, 800)
+    sw = SubSwaths(rg.length, rg.width, 2)
+    lo = (100 + 50 * np.sin(np.arange(rg.length) / 90.0)).astype(np.int32)
+    sw.set_valid_samples_array(1, np.stack([lo, np.full(rg.length, 500, np.int32)], axis=1))
+    sw.set_valid_samples_array(2, np.stack([np.full(rg.length, 520, np.int32), np.full(rg.length, 990, np.int32)],
+                                           axis=1))
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], sliced_radargrid=sliced, subswaths=sw)
+    _check(gpu, ora)
+    assert set(np.unique(gpu["mask"])) >= {0, 1, 2, 255}
+
+
+def test_utm_geogrid_and_lut_doppler(oracle_mod):
+    """Reduced frame scene: UTM 32611 geogrid over an EPSG:4326 DEM, native
+    Doppler LUT2d (quadratic in range) and a linear azimuth carrier."""
+    sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0)
+    gpu, ora = _run_both(oracle_mod, sc, [sc.slc], az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 10000
+
+
+def test_known_answer_lonlat_phase_gpu(c1):
+    """The lon-as-phase KAT run through the GPU path (1e-6 rad)."""
+    g = c1.geogrid
+    slc = synth.kat_slc(c1, "x", 0.0)
+    dem = synth.constant_dem_like(c1.dem, 0.0)
+    geo = np.zeros((g.length, g.width), np.complex64)
+    geocode_slc(geo, slc, dem, c1.radar_grid, g, c1.orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-9, 25, flatten=False)
+    truth = np.radians(g.start_x + g.spacing_x * (np.arange(g.width) + 0.5))[None, :]
+    v = np.isfinite(geo)
+    assert v.sum() > 0.4 * v.size
+    err = np.angle(geo * np.exp(-1j * truth))[v]
+    assert np.abs(err).max() < 1e-6
+
+
+def test_edge_cases(oracle_mod, c1):
+    g = c1.geogrid
+    # geogrid entirely outside the swath: all invalid, mask 255
+    far = g[0:32, 0:32]
+    far.start_x += 5.0
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], geogrid=far, dem=synth.constant_dem_like(c1.dem, 0.0))
+    assert np.all(gpu["mask"] == 255) and np.all(np.isnan(gpu["geo"][0]))
+    _check(gpu, ora)
+    # NaN and inf samples in the SLC propagate like the reference
+    bad = c1.slc.copy()
+    bad[500:503, 500:540] = np.complex64(complex(np.nan, 1.0))
+    bad[600, 600] = np.complex64(complex(np.inf, 0.0))
+    gpu, ora = _run_both(oracle_mod, c1, [bad])
+    _check(gpu, ora)
+    # radar block smaller than one sinc chip: nothing interpolated
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc[:6, :6].copy()])
+    assert np.all(~np.isfinite(gpu["geo"][0]))
+    _check(gpu, ora)
+    # empty geogrid is a no-op
+    empty = np.zeros((0, g.width), np.complex64)
+    geocode_slc(empty, c1.slc, c1.dem, c1.radar_grid, g[0:0, 0:g.width], c1.orbit, LUT2d(), LUT2d(),
+                c1.ellipsoid, 1e-8, 25)
+
+
+def test_projection_failure_raises(c1):
+    """A UTM geogrid far outside its zone fails the inverse projection; the
+    reference throws (Projections.h ProjectionBase::inverse), so do we."""
+    from isce3_gb300.product import GeoGridParameters
+    g = GeoGridParameters(-1.2e7, 4.0e6, 10.0, -10.0, 8, 8, 32611)
+    geo = np.zeros((8, 8), np.complex64)
+    with pytest.raises(ValueError):
+        geocode_slc(geo, c1.slc, c1.dem, c1.radar_grid, g, c1.orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-8, 25)
