@@ -315,7 +315,10 @@ extern "C" int gslc_compute_dem_window(const gslc_dem_raster* r, const gslc_geo_
     // DEMInterpolator::loadDEM
     double min_x = minX, max_x = maxX, min_y = minY, max_y = maxY;
     const double delta_y = r->gt[5], delta_x = r->gt[1];
-    if (delta_x < 0) return GSLC_EINVAL;
+    // a negative x spacing makes loadDEM warn and return InvalidDem; the
+    // interpolator then has no raster and yields the reference height
+    // (DEMInterpolator.cpp:43-49)
+    if (delta_x < 0) return GSLC_OK;
     const double dem_y0 = r->gt[3];
     double dem_x0 = r->gt[0];
     const bool ll = r->epsg == 4326;

@@ -168,7 +168,7 @@ def scene_c1(seed: int = 1, length=1024, width=1024, geo=512, dem_px=256, n_targ
     lon, lat = _swath_bounds(model, grid, 750.0)
     geogrid = lonlat_geogrid(lon, lat, geo, geo)
     bounds = (geogrid.start_x, geogrid.end_x, geogrid.end_y, geogrid.start_y)
-    dem = lonlat_dem(bounds, (dem_px, dem_px), rng, 0.8, 1500.0, margin_px=60)
+    dem = lonlat_dem(bounds, (dem_px, dem_px), rng, 0.8, 1500.0, margin_px=min(60, dem_px // 4))
     data = None
     if slc:
         data = complex_gaussian((length, width), rng)
