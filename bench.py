@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gslc", "reference"], default="gslc")
-    p.add_argument("--workload", choices=["frame", "small"], default="frame")
+    p.add_argument("--workload", choices=["frame", "medium", "small"], default="frame")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -59,6 +59,8 @@ def make_scene(workload: str):
     from isce3_gb300 import synth
     if workload == "frame":
         return synth.scene_c2(seed=2)
+    if workload == "medium":     # profiling size: 256 MiB SLC, 4000 x 4000 output
+        return synth.scene_c2(seed=2, length=8192, width=4096, geo=4000, spacing=10.0)
     return synth.scene_c2(seed=2, length=4096, width=2048, geo=2000, spacing=12.0)
 
 
@@ -356,31 +358,16 @@ def _max_over_ranks(x, world):
 
 def parity_sample(res, row0, rows, box, out):
     """GPU frame rows against the oracle's run on the same rows."""
+    from oracle.compare import compare
     sl = slice(row0, row0 + rows)
     geo = res["geo_d"][sl].cpu().numpy()
     mask = res["mask_d"][sl].cpu().numpy()
     az = res["az_d"][sl].cpu().numpy()
     rg = res["rg_d"][sl].cpu().numpy()
-    go, mo, ao, ro = out["geo"], out["mask"], out["az"], out["rg"]
-
-    def tidx(c):
-        with np.errstate(invalid="ignore"):
-            f = c - np.trunc(c)
-            return np.nan_to_num(np.floor((4.0 + f - np.floor(4.0 + f)) * 8192)).astype(np.int64)
-    both = np.isfinite(az) & np.isfinite(ao)
-    flips = both & ((tidx(az) != tidx(ao)) | (tidx(rg) != tidx(ro)))
-    ok = both & ~flips & np.isfinite(go) & np.isfinite(geo)
-    rms = float(np.sqrt(np.mean(np.abs(go[ok]) ** 2))) if ok.any() else 1.0
-    err = np.abs(geo[ok] - go[ok])
-    big = np.abs(go[ok]) >= 1e-2 * rms
-    ph = np.abs(np.angle(geo[ok][big] * np.conj(go[ok][big])))
-    return {"rows": [row0, row0 + rows], "px": int(geo.size), "valid": int(both.sum()),
-            "mask_mismatch": int((mask != mo).sum()),
-            "validity_mismatch": int((np.isfinite(az) != np.isfinite(ao)).sum()),
-            "max_phase_err_rad": float(ph.max()) if ph.size else 0.0,
-            "max_rel_err": float((err / np.maximum(np.abs(go[ok]), 1e-2 * rms)).max()) if ok.any() else 0.0,
-            "n_out_of_tol": int(np.sum(err > 1e-5 * np.abs(go[ok]) + 1e-6 * rms)),
-            "sinc_table_flips": int(flips.sum()), "flip_fraction": float(flips.sum() / max(both.sum(), 1))}
+    r = compare(geo, out["geo"], az, out["az"], rg, out["rg"], mask, out["mask"])
+    r["rows"] = [row0, row0 + rows]
+    r["tolerance"] = "|d| <= 1e-5|ref| + 1e-6 rms; phase <= 1e-4 rad; masks exact; flips/splits counted"
+    return r
 
 
 def run_reference(args, rank, world):
