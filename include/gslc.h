@@ -20,6 +20,7 @@
 #ifndef GSLC_H
 #define GSLC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -189,6 +190,26 @@ int gslc_last_kernel_ms(const gslc_ctx* ctx, float* geocode_ms, float* deramp_ms
  * FMA) from a dependent-chain DFMA loop over all SMs; the denominator of the
  * FP64 roofline the geocode kernel is reported against. */
 int gslc_probe_fp64_gflops(gslc_ctx* ctx, double* gflops);
+
+/* Allocation-free plain form.  No counterpart in the reference: an addition
+ * for callers that must not allocate device memory while they run (serving
+ * loops that reserve HBM up front under a fixed budget, hosts that forbid
+ * allocation after start-up, frameworks that own the memory pool).  Same
+ * arguments, kernels and results as gslc_geocode_slc, but no context: its
+ * scratch lives in file-scope device arrays of the library (about 32.4 MiB
+ * per GPU that loads it, held until exit):
+ *  - the deramped copy of the radar blocks when carriers are present and
+ *    inplace_deramp is 0: at most 4194304 complex samples over all blocks;
+ *  - orbit polynomials for at most 256 state vectors; the sinc table; an
+ *    error word cleared by every call.
+ * Larger inputs are rejected with GSLC_EINVAL and a message in errbuf.  It
+ * calls no cudaMalloc, cudaFree or other allocating routine.  The first call
+ * on a device (the current one) looks up the arrays' device addresses and
+ * uploads the sinc table synchronously, so make it before any stream
+ * capture.  All calls share the arrays: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * errbuf (may be NULL) receives the error message, errbuf_len bytes at most. */
+int gslc_geocode_slc_noalloc(const gslc_geocode_args* args, void* stream, char* errbuf, size_t errbuf_len);
 
 #ifdef __cplusplus
 }

@@ -149,6 +149,7 @@ _EXPORTS = {
     "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 
 _lock = threading.Lock()

@@ -676,3 +676,133 @@ extern "C" int gslc_probe_fp64_gflops(gslc_ctx* c, double* gflops) {
     *gflops = flops / (best * 1e-3) / 1e9;
     return GSLC_OK;
 }
+
+#include <mutex>
+
+// ===========================================================================
+// Allocation-free entry point.
+//
+// For callers that must not allocate device memory while they run: serving
+// or real-time loops that reserve all of HBM up front under a fixed budget
+// (a cudaMalloc there can fail, or stall the device to synchronise), hosts
+// whose memory policy forbids allocation after start-up, and frameworks that
+// own the device memory pool and hand the geocoder only their own buffers.
+// gslc_geocode_slc needs a context, and its constructor and the carrier
+// deramp allocate; this variant runs the same kernels with all of its
+// scratch in the file-scope device arrays below, held by every GPU that
+// loads the library until the process exits (about 32.4 MiB in total).
+// ===========================================================================
+namespace {
+
+constexpr int64_t NOALLOC_MAX_DERAMP = int64_t(1) << 22;   // complex samples (32 MiB)
+constexpr int NOALLOC_MAX_STATE_VECTORS = 256;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// deramped radar samples, all blocks back to back
+static __device__ __align__(256) float2 g_noalloc_deramp[NOALLOC_MAX_DERAMP];
+// sinc kernel table, SINC_SUB x SINC_LEN
+static __device__ __align__(256) float g_noalloc_sinc[SINC_SUB * SINC_LEN];
+// orbit polynomial pieces
+static __device__ __align__(256) double g_noalloc_orbit[(NOALLOC_MAX_STATE_VECTORS - 3) * ORB_STRIDE];
+// error word (bit 0: projection inverse failed); cleared at every call
+static __device__ __align__(256) int32_t g_noalloc_err[4];
+
+struct NoallocDevice {
+    bool ready = false;
+    float2* deramp = nullptr;
+    float* sinc = nullptr;
+    double* orbit = nullptr;
+    int32_t* err = nullptr;
+};
+NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mutex;
+
+int noalloc_fail(char* buf, size_t len, int code, const char* msg) {
+    if (buf && len > 0) {
+        std::strncpy(buf, msg, len - 1);
+        buf[len - 1] = '\0';
+    }
+    return code;
+}
+
+// Once per device, with that device current: the device addresses of the
+// static arrays (the host-side names are not device addresses) and the sinc
+// table upload.  Synchronous, so the first call on a device must not be
+// inside a stream capture.
+int noalloc_setup(int dev, NoallocDevice& d, char* buf, size_t len) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (d.ready) return GSLC_OK;
+    cudaError_t e = cudaGetSymbolAddress((void**)&d.deramp, g_noalloc_deramp);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.sinc, g_noalloc_sinc);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.orbit, g_noalloc_orbit);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.err, g_noalloc_err);
+    if (e != cudaSuccess) return noalloc_fail(buf, len, GSLC_ECUDA, cudaGetErrorString(e));
+    const std::vector<float> table = make_sinc_table();
+    e = cudaMemcpy(d.sinc, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return noalloc_fail(buf, len, GSLC_ECUDA, cudaGetErrorString(e));
+    d.ready = true;
+    (void)dev;
+    return GSLC_OK;
+}
+
+}  // namespace
+
+extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream, char* errbuf, size_t errbuf_len) {
+    if (errbuf && errbuf_len) errbuf[0] = '\0';
+    if (!a) return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL, "null arguments");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return noalloc_fail(errbuf, errbuf_len, GSLC_ECUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return noalloc_fail(errbuf, errbuf_len, GSLC_EUNSUPPORTED, "device index beyond 64");
+    NoallocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        if (int st = noalloc_setup(dev, d, errbuf, errbuf_len)) return st;
+    }
+    if (a->orbit.n > NOALLOC_MAX_STATE_VECTORS)
+        return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL,
+                            "orbit has more than 256 state vectors (allocation-free limit)");
+    if (a->n_blocks < 1 || !a->rdr_blocks || !a->geo_blocks)
+        return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL, "number of geoDataBlocks != number of rdrDataBlocks");
+
+    // A context whose buffers are the static arrays: the regular path then
+    // has nothing to allocate (orbit capacity suffices, deramp is in place).
+    gslc_ctx c;
+    c.device = dev;
+    c.d_sinc = d.sinc;
+    c.d_err = d.err;
+    static thread_local int32_t h_err[4];
+    c.h_err = h_err;
+    c.d_orbit = d.orbit;
+    c.orbit_cap = (size_t)(NOALLOC_MAX_STATE_VECTORS - 3) * ORB_STRIDE;
+
+    gslc_geocode_args args = *a;
+    std::vector<const void*> blocks(a->rdr_blocks, a->rdr_blocks + a->n_blocks);
+    AzRg az{}, rg{};
+    bool carriers = false;
+    if (!to_azrg(&c, a->az_carrier, az, "az_carrier") && !to_azrg(&c, a->rg_carrier, rg, "rg_carrier"))
+        carriers = !(az.is_zero && rg.is_zero);
+    const int64_t nrdr = a->rdr_length * a->rdr_width;
+    if (carriers && !a->inplace_deramp && nrdr > 0) {
+        // deramp works on a copy in the static scratch; the caller's blocks stay as given
+        if (nrdr * a->n_blocks > NOALLOC_MAX_DERAMP)
+            return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL,
+                                "radar blocks exceed the allocation-free deramp scratch (4194304 complex samples)");
+        for (int b = 0; b < a->n_blocks; ++b) {
+            float2* dst = d.deramp + (int64_t)b * nrdr;
+            e = cudaMemcpyAsync(dst, a->rdr_blocks[b], nrdr * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                (cudaStream_t)stream);
+            if (e != cudaSuccess) return noalloc_fail(errbuf, errbuf_len, GSLC_ECUDA, cudaGetErrorString(e));
+            blocks[b] = dst;
+        }
+        args.inplace_deramp = 1;
+    }
+    args.rdr_blocks = blocks.data();
+    const int st = gslc_geocode_slc(&c, &args, stream);
+    c.d_sinc = nullptr;   // the static arrays are not the context's to free
+    c.d_err = nullptr;
+    c.d_orbit = nullptr;
+    c.h_err = nullptr;
+    if (st != GSLC_OK) return noalloc_fail(errbuf, errbuf_len, st, c.err.c_str());
+    return GSLC_OK;
+}

@@ -1,0 +1,119 @@
+"""The allocation-free entry point gslc_geocode_slc_noalloc, called through
+the C ABI, gives the same result as gslc_geocode_slc.
+
+It exists for callers that must not allocate device memory while they run
+(serving loops with a fixed HBM budget, hosts that forbid allocation after
+start-up, frameworks that own the memory pool); its scratch is static device
+memory shared by every call.  The test makes two calls in a row that both use
+that scratch (carrier deramp) with different sizes, so a second call that
+inherited stale scratch contents would show.  It runs alone in a fresh
+process as well as after the other tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from isce3_gb300 import _lib as L, _marshal as M, synth  # noqa: E402
+from isce3_gb300.core import LUT2d, Poly2d  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+def _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep):
+    """GeocodeArgs for device tensors, as isce3_gb300.geocode builds them."""
+    holder = M.AzRgHolder()
+    a = L.GeocodeArgs()
+    a.radar_grid = M.radar_grid_desc(sc.radar_grid)
+    a.sliced_radar_grid = M.radar_grid_desc(sc.radar_grid)
+    a.geo_grid = M.geo_grid_desc(sc.geogrid)
+    a.orbit = M.orbit_desc(sc.orbit)
+    a.native_doppler = M.lut_desc(sc.native_doppler, dev)
+    a.image_grid_doppler = M.lut_desc(sc.image_grid_doppler, dev)
+    a.az_time_correction = M.lut_desc(LUT2d(), dev)
+    a.srange_correction = M.lut_desc(LUT2d(), dev)
+    a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
+    a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
+    a.ellipsoid_a, a.ellipsoid_e2 = sc.ellipsoid.a, sc.ellipsoid.e2
+    a.threshold_geo2rdr, a.numiter_geo2rdr = sc.threshold, sc.maxiter
+    a.flatten, a.reramp = 1, 1
+    a.invalid_re, a.invalid_im = np.float32(np.nan), np.float32(np.nan)
+    a.n_blocks = 1
+    a.rdr_length, a.rdr_width = slc.shape
+    rp = (C.c_void_p * 1)(slc.data_ptr())
+    gp = (C.c_void_p * 1)(geo.data_ptr())
+    a.rdr_blocks = C.cast(rp, C.POINTER(C.c_void_p))
+    a.geo_blocks = C.cast(gp, C.POINTER(C.c_void_p))
+    a.mask = mask.data_ptr()
+    a.dem, dem_t = M.dem_raster_desc(sc.dem, sc.geogrid, 50, dev)
+    a.dem_margin = 50
+    keep.extend([holder, rp, gp, dem_t])
+    return a
+
+
+def _run(sc, az_carrier, rg_carrier, noalloc):
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = sc.geogrid
+    slc = torch.from_numpy(sc.slc).to(dev)
+    geo = torch.zeros((g.length, g.width), dtype=torch.complex64, device=dev)
+    mask = torch.zeros((g.length, g.width), dtype=torch.uint8, device=dev)
+    keep = []
+    a = _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    lib = L.lib()
+    if noalloc:
+        err = C.create_string_buffer(512)
+        st = lib.gslc_geocode_slc_noalloc(C.byref(a), stream, err, len(err))
+        assert st == 0, err.value.decode()
+    else:
+        ctx = L.context(dev.index)
+        L.check(lib.gslc_geocode_slc(ctx, C.byref(a), stream), ctx)
+    torch.cuda.synchronize()
+    assert torch.equal(slc.cpu(), torch.from_numpy(sc.slc)), "radar input modified"
+    return geo.cpu().numpy(), mask.cpu().numpy()
+
+
+def _compare(ref, got):
+    (g0, m0), (g1, m1) = ref, got
+    np.testing.assert_array_equal(m0, m1)
+    v = np.isfinite(g0)
+    np.testing.assert_array_equal(v, np.isfinite(g1))
+    assert v.sum() > 1000
+    rms = np.sqrt(np.mean(np.abs(g0[v]) ** 2))
+    # tolerance of the parity tests: 1e-5 relative + 1e-6 rms
+    assert np.all(np.abs(g1[v] - g0[v]) <= 1e-5 * np.abs(g0[v]) + 1e-6 * rms)
+
+
+def test_noalloc_matches_regular_entry_point_twice():
+    sc1 = synth.scene_c1(seed=11, length=1024, width=1024, geo=256, dem_px=128)
+    sc2 = synth.scene_c1(seed=12, length=768, width=640, geo=192, dem_px=96)
+    mid1, mid2 = sc1.radar_grid.sensing_mid, sc2.radar_grid.sensing_mid
+    cases = [
+        (sc1, Poly2d([[0.0], [2 * np.pi * 200.0]], y_mean=mid1), Poly2d([[0.3, 1e-3]], x_mean=sc1.radar_grid.mid_range)),
+        (sc2, Poly2d([[0.1], [-2 * np.pi * 90.0]], y_mean=mid2), Poly2d([[0.0, -2e-3]], x_mean=sc2.radar_grid.mid_range)),
+    ]
+    for sc, azc, rgc in cases:             # two calls in a row, different sizes
+        ref = _run(sc, azc, rgc, noalloc=False)
+        got = _run(sc, azc, rgc, noalloc=True)
+        _compare(ref, got)
+
+
+def test_noalloc_rejects_oversized_input():
+    sc = synth.scene_c1(seed=13, length=2048, width=2100, geo=64, dem_px=96)   # 4.3M samples > 4194304
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = sc.geogrid
+    slc = torch.from_numpy(sc.slc).to(dev)
+    geo = torch.zeros((g.length, g.width), dtype=torch.complex64, device=dev)
+    mask = torch.zeros((g.length, g.width), dtype=torch.uint8, device=dev)
+    keep = []
+    a = _args(sc, slc, geo, mask, Poly2d([[0.0], [1.0]]), Poly2d([[0.0]]), dev, keep)
+    err = C.create_string_buffer(512)
+    st = L.lib().gslc_geocode_slc_noalloc(C.byref(a), C.c_void_p(torch.cuda.current_stream().cuda_stream), err,
+                                          len(err))
+    assert st == L.GSLC_EINVAL
+    assert b"allocation-free deramp scratch" in err.value
