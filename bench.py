@@ -172,14 +172,15 @@ def run_oracle_sample(oracle, sc, g, box, outputs=False):
     return dt, phases, dict(geo=geo, mask=mask, az=az, rg=rg)
 
 
-def calibrate_rows(oracle, sc, target_s, max_rows=512):
+def calibrate_rows(oracle, sc, target_s, max_rows=None):
     """Geogrid rows (centred) whose oracle run takes about target_s seconds."""
+    max_rows = max_rows or sc.geogrid.length
     mid = sc.geogrid.length // 2
     rows = 4
     g, box = sample_rows_block(oracle, sc, mid - rows // 2, rows)
     dt, _, _ = run_oracle_sample(oracle, sc, g, box)
     rows = int(np.clip(rows * target_s / max(dt, 1e-3), 4, max_rows))
-    row0 = mid - rows // 2
+    row0 = max(0, min(mid - rows // 2, sc.geogrid.length - rows))
     g, box = sample_rows_block(oracle, sc, row0, rows)
     return row0, rows, g, box
 

@@ -209,6 +209,8 @@ bool utm_setup(int code, Utm& u) {
     u.gtu[5] = std::pow(n, 6) * (212378941. / 319334400.);
     const double Z = clens(u.cbg, 0.);
     u.Zb = -u.Qn * (Z + clens(u.gtu, 2 * Z));
+    u.slon0 = std::sin(u.lon0);
+    u.clon0 = std::cos(u.lon0);
     return true;
 }
 
@@ -233,6 +235,8 @@ Lut to_lut(const gslc_lut2d& l) {
     o.ny = l.ny;
     o.x0 = l.x0; o.y0 = l.y0; o.dx = l.dx; o.dy = l.dy;
     o.ref_value = l.ref_value;
+    o.inv_dx = 1.0 / l.dx;
+    o.inv_dy = 1.0 / l.dy;
     o.data = l.data;
     return o;
 }
@@ -261,6 +265,8 @@ int to_azrg(gslc_ctx* c, const gslc_azrg_func& f, AzRg& o, const char* name) {
         o.poly.y_order = p.y_order;
         o.poly.x_mean = p.x_mean; o.poly.y_mean = p.y_mean;
         o.poly.x_norm = p.x_norm; o.poly.y_norm = p.y_norm;
+        o.poly.inv_x_norm = 1.0 / p.x_norm;
+        o.poly.inv_y_norm = 1.0 / p.y_norm;
         for (int i = 0; i < nc; ++i) o.poly.c[i] = p.coeffs[i];
         // the default Poly2d (order -1) evaluates to exactly 0 (core/Poly2d.h:56)
         o.is_zero = nc <= 0 ? 1 : 0;
@@ -547,6 +553,8 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     if ((st = to_azrg(c, a->rg_carrier, p.rg_car, "rg_carrier"))) return st;
     p.carriers_zero = p.az_car.is_zero && p.rg_car.is_zero;
     p.flat_scale = 4.0 * (M_PI / rg.wavelength);
+    p.inv_prf = 1.0 / rg.prf;
+    p.two_pi_over_prf = 2.0 * M_PI / rg.prf;
     p.flatten = a->flatten; p.reramp = a->reramp; p.use_corr = a->flatten_with_corrected_srange;
     p.inv_re = a->invalid_re; p.inv_im = a->invalid_im;
     p.inL = a->rdr_length; p.inW = a->rdr_width;
@@ -596,6 +604,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
             dp.inL = a->rdr_length; dp.inW = a->rdr_width;
             dp.az_first = a->first_azimuth_line; dp.rg_first = a->first_range_sample;
             dp.rg_t0 = rg.sensing_start; dp.rg_prf = rg.prf; dp.rg_r0 = rg.starting_range; dp.rg_dr = rg.range_pixel_spacing;
+            dp.inv_prf = 1.0 / rg.prf;
             dp.az_car = p.az_car; dp.rg_car = p.rg_car;
             e = launch_deramp(dp, stream, &c->launches);
             if (e != cudaSuccess) return cuda_err(c, e, "deramp launch");

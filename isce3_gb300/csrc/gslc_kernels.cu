@@ -39,29 +39,41 @@ __device__ __forceinline__ float2 expi_fp64(double ph) {
     return make_float2(c, s);
 }
 
-// geometry/DEMInterpolator.cpp:593-659 + core/Spline2dInterpolator.cpp:32-67
-__device__ double dem_height(const Dem& d, double lon, double lat) {
-    const double ref = 0.0;
-    if (!d.have_raster) return ref;
+// DEM column coordinate from longitude for an EPSG:4326 DEM
+// (geometry/DEMInterpolator.cpp:593-611 forward, :627-646 wrap and west edge).
+// Returns false where the reference returns the reference height.
+__device__ __forceinline__ bool dem_col_lonlat(const Dem& d, double lon, double& col) {
+    double X = (lon * 180.0) / PI;
+    if (X > 360 || X < -360) X = fmod(X, 360.0);
+    if (X < -180) X += 360;
+    if (X - 360 >= d.x_start) X -= 360;
+    else if (X < d.x_start && X + 360 >= d.x_start) X += 360;
+    else if (X < d.x_start) return false;
+    col = (X - d.x_start) / d.dx;
+    return true;
+}
+
+__device__ __forceinline__ double dem_row_lonlat(const Dem& d, double lat) {
+    return (((lat * 180.0) / PI) - d.y_start) / d.dy;
+}
+
+// Both coordinates for a UTM DEM (forward projection per pixel).
+__device__ __forceinline__ bool dem_coords_utm(const Dem& d, double lon, double lat, double& row, double& col) {
     double X, Y;
-    if (d.epsg_is_lonlat) {
-        X = (lon * 180.0) / PI;
-        Y = (lat * 180.0) / PI;
-        if (X > 360 || X < -360) X = fmod(X, 360.0);
-        if (X < -180) X += 360;
-        if (X - 360 >= d.x_start) X -= 360;
-        else if (X < d.x_start && X + 360 >= d.x_start) X += 360;
-        else if (X < d.x_start) return ref;
-    } else {
-        if (!utm_forward(d.utm, lon, lat, X, Y)) return ref;
-        if (X < d.x_start) return ref;
-    }
-    const double row = (Y - d.y_start) / d.dy;
-    const double col = (X - d.x_start) / d.dx;
+    if (!utm_forward(d.utm, lon, lat, X, Y)) return false;
+    if (X < d.x_start) return false;
+    row = (Y - d.y_start) / d.dy;
+    col = (X - d.x_start) / d.dx;
+    return true;
+}
+
+// Bounds checks (DEMInterpolator.cpp:648-655) and the order-6 biquintic
+// spline in FP32 (core/Spline2dInterpolator.cpp:32-67).
+__device__ double dem_spline(const Dem& d, double row, double col) {
+    const double ref = 0.0;
     const int irow = (int)floor(row), icol = (int)floor(col);
     if (irow < 2 || irow >= d.length - 1) return ref;
     if (icol < 2 || icol >= d.width - 1) return ref;
-    // order-6 spline window (Spline2dInterpolator.cpp:43-51)
     const int i0 = (int)row - 2, j0 = (int)col - 2;
     const float xx = (float)((col - (double)j0) - 2.0);
     const float yy = (float)((row - (double)i0) - 2.0);
@@ -103,11 +115,13 @@ __device__ bool update_aztime(const GeoParams& p, V3 xyz, double& t) {
 }
 
 // geometry/detail/Geo2Rdr.icc:114-179 with geometry/geometry.cpp:241-251
-// (deltaRange = 1e-8 as passed by geocodeSlc.cpp:120-123).
+// (deltaRange = 1e-8 as passed by geocodeSlc.cpp:120-123).  With a
+// zero image-grid Doppler the slant range enters only the returned iterate,
+// so it is formed once, after convergence.
 __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
     constexpr double dr = 1.0e-8;
     t = p.t_mid;
-    bool first_shared = p.t_mid_in_orbit;
+    const bool first_shared = p.t_mid_in_orbit;
     if (!p.t_mid_in_orbit && !update_aztime(p, xyz, t)) return false;
     const bool dop_data = p.img_dop.have_data;
     const bool dop_const = !dop_data && p.img_dop.ref_value == 0.0;
@@ -124,24 +138,27 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
             orbit_eval(p.orbit, t, pos, vel);
         }
         const V3 rvec = vsub(xyz, pos);
-        R = vnorm(rvec);
         if (i == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
+        if (dop_const) {
+            // fdop == 0 and fdopder == 0 exactly: fn = rvec.vel, fn' = -vel.vel
+            dt = vdot(rvec, vel) / (-vdot(vel, vel));
+            if (fabs(dt) < p.thr) {
+                R = vnorm(rvec);
+                return true;
+            }
+            continue;
+        }
+        R = vnorm(rvec);
         if (dop_data && p.img_dop.bounds_error &&
             !(lut_contains(p.img_dop, t, R) && lut_contains(p.img_dop, t, R + dr)))
             return false;
         const double dopfact = vdot(rvec, vel);
         const double c1 = -vdot(vel, vel);
-        double fn, fnprime;
-        if (dop_const) {
-            fn = dopfact;        // fdop == 0 and fdopder == 0 exactly
-            fnprime = c1;
-        } else {
-            const double fdop = half_wvl * lut_eval(p.img_dop, t, R);
-            const double fdopder = (half_wvl * lut_eval(p.img_dop, t, R + dr) - fdop) / dr;
-            fn = dopfact - fdop * R;
-            const double c2 = (fdop / R) + fdopder;
-            fnprime = c1 + c2 * dopfact;
-        }
+        const double fdop = half_wvl * lut_eval(p.img_dop, t, R);
+        const double fdopder = (half_wvl * lut_eval(p.img_dop, t, R + dr) - fdop) / dr;
+        const double fn = dopfact - fdop * R;
+        const double c2 = (fdop / R) + fdopder;
+        const double fnprime = c1 + c2 * dopfact;
         dt = fn / fnprime;
         if (fabs(dt) < p.thr) return true;
     }
@@ -218,10 +235,62 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
     return cval;
 }
 
+// Block shape: 32 geogrid columns x 8 lines.  Terms that depend only on the
+// column (easting/longitude) or only on the line (northing/latitude) are
+// evaluated once per block column/line into shared memory.
+constexpr int GBX = 32, GBY = 8;
+
 template <bool GEO_LONLAT>
-__global__ void __launch_bounds__(128) geocode_kernel(const __grid_constant__ GeoParams p) {
-    const int pixel = blockIdx.x * blockDim.x + threadIdx.x;
-    const int line = blockIdx.y * blockDim.y + threadIdx.y;
+__global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
+    __shared__ double s_col[4][GBX];
+    __shared__ double s_row[5][GBY];
+    __shared__ int s_colok[GBX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int pixel = blockIdx.x * GBX + tx;
+    const int line = blockIdx.y * GBY + ty;
+    const bool dem_ll = p.dem.have_raster && p.dem.epsg_is_lonlat;
+
+    if (ty == 0) {
+        // pixel centre easting/longitude (geocodeSlc.cpp:103), same rounding as the reference
+        const int pc = min(pixel, p.gw - 1);
+        const double x = dadd(p.gx0, dmul(p.gdx, (double)pc + 0.5));
+        if (GEO_LONLAT) {
+            const double lon = (x * PI) / 180.0;          // LonLat::inverse (Projections.h:136-140)
+            double sl, cl;
+            sincos(lon, &sl, &cl);
+            double col = 0.0;
+            s_colok[tx] = dem_ll ? (dem_col_lonlat(p.dem, lon, col) ? 1 : 0) : 1;
+            s_col[0][tx] = lon;
+            s_col[1][tx] = sl;
+            s_col[2][tx] = cl;
+            s_col[3][tx] = col;
+        } else {
+            const UtmCol c = utm_inverse_col(p.utm, x);
+            s_col[0][tx] = c.Ce;
+            s_col[1][tx] = c.shi;
+            s_col[2][tx] = c.chi;
+            s_colok[tx] = c.ok;
+        }
+    } else if (ty == 1 && tx < GBY) {
+        const int lr = min((int)(blockIdx.y * GBY + tx), p.gl - 1);
+        const double y = dadd(p.gy0, dmul(p.gdy, (double)lr + 0.5));   // geocodeSlc.cpp:100
+        if (GEO_LONLAT) {
+            const double lat = (y * PI) / 180.0;
+            double sl, cl;
+            sincos(lat, &sl, &cl);
+            s_row[0][tx] = lat;
+            s_row[1][tx] = sl;
+            s_row[2][tx] = cl;
+            s_row[3][tx] = p.ell_a / sqrt(1.0 - p.ell_e2 * (sl * sl));    // rEast (Ellipsoid.h:117-120)
+            s_row[4][tx] = dem_ll ? dem_row_lonlat(p.dem, lat) : 0.0;
+        } else {
+            const UtmRow r = utm_inverse_row(p.utm, y);
+            s_row[0][tx] = r.Cn;
+            s_row[1][tx] = r.sr;
+            s_row[2][tx] = r.cr;
+        }
+    }
+    __syncthreads();
     if (pixel >= p.gw || line >= p.gl) return;
     const int64_t k = (int64_t)line * p.gw + pixel;
 
@@ -230,21 +299,45 @@ __global__ void __launch_bounds__(128) geocode_kernel(const __grid_constant__ Ge
     double azc = CUDART_NAN, rgc = CUDART_NAN;
     double R_uncorr = (double)p.inv_re;
 
-    // pixel centre (geocodeSlc.cpp:100-103), same rounding as the reference
-    const double y = dadd(p.gy0, dmul(p.gdy, (double)line + 0.5));
-    const double x = dadd(p.gx0, dmul(p.gdx, (double)pixel + 0.5));
-    double lon, lat;
     bool ok = true;
+    V3 xyz;
     if (GEO_LONLAT) {
-        lon = (x * PI) / 180.0;
-        lat = (y * PI) / 180.0;
+        double h = 0.0;
+        if (p.dem.have_raster) {
+            if (dem_ll) {
+                if (s_colok[tx]) h = dem_spline(p.dem, s_row[4][ty], s_col[3][tx]);
+            } else {
+                double row, col;
+                if (dem_coords_utm(p.dem, s_col[0][tx], s_row[0][ty], row, col)) h = dem_spline(p.dem, row, col);
+            }
+        }
+        // lonLatToXyz (Ellipsoid.h:177-190) with the line's rEast and the sines/cosines above
+        const double re = s_row[3][ty], slat = s_row[1][ty], clat = s_row[2][ty];
+        xyz = {(re + h) * clat * s_col[2][tx], (re + h) * clat * s_col[1][tx],
+               ((re * (1.0 - p.ell_e2)) + h) * slat};
     } else {
-        ok = utm_inverse(p.utm, x, y, lon, lat);
-        if (!ok) atomicOr(p.err, 1);
+        ok = s_colok[tx];
+        if (!ok) {
+            atomicOr(p.err, 1);
+        } else {
+            UtmCol c;
+            c.Ce = s_col[0][tx]; c.shi = s_col[1][tx]; c.chi = s_col[2][tx]; c.ok = 1;
+            UtmRow r;
+            r.Cn = s_row[0][ty]; r.sr = s_row[1][ty]; r.cr = s_row[2][ty];
+            const LonLatSC ll = utm_inverse_px(p.utm, r, c);
+            double h = 0.0;
+            if (p.dem.have_raster) {
+                double row, col;
+                if (dem_ll) {
+                    if (dem_col_lonlat(p.dem, ll.lon, col)) h = dem_spline(p.dem, dem_row_lonlat(p.dem, ll.lat), col);
+                } else if (dem_coords_utm(p.dem, ll.lon, ll.lat, row, col)) {
+                    h = dem_spline(p.dem, row, col);
+                }
+            }
+            xyz = lonlat_to_xyz_sc(p.ell_a, p.ell_e2, ll.slon, ll.clon, ll.slat, ll.clat, h);
+        }
     }
     if (ok) {
-        const double h = dem_height(p.dem, lon, lat);
-        const V3 xyz = lonlat_to_xyz(p.ell_a, p.ell_e2, lon, lat, h);
         double t, R;
         if (geo2rdr(p, xyz, t, R)) {
             if (!p.use_corr) R_uncorr = R;
@@ -288,14 +381,15 @@ __global__ void __launch_bounds__(128) geocode_kernel(const __grid_constant__ Ge
     double rng = 0.0, az = 0.0;
     if (interp) {
         rng = dadd(p.rg_r0, dmul(rgc, p.rg_dr));
-        az = p.rg_t0 + azc / p.rg_prf;
+        az = p.rg_t0 + azc * p.inv_prf;
         interp = lut_contains(p.nat_dop, az, rng);
     }
     if (!interp) {
         for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
         return;
     }
-    const double doppFreq = ((lut_eval(p.nat_dop, az, rng) * 2) * PI) / p.rg_prf;
+    // Doppler in radians per line: eval * 2 * pi / prf (geocodeSlc.cpp:473-474)
+    const double doppFreq = lut_eval(p.nat_dop, az, rng) * p.two_pi_over_prf;
     // reramp + flatten phase (geocodeSlc.cpp:362-392)
     const double carrier = p.carriers_zero ? 0.0 : azrg_eval(p.rg_car, az, rng) + azrg_eval(p.az_car, az, rng);
     const double flat = p.flat_scale * (p.use_corr ? rng : R_uncorr);
@@ -314,18 +408,67 @@ __global__ void __launch_bounds__(128) geocode_kernel(const __grid_constant__ Ge
     }
 }
 
-// geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier))
+// A carrier on one radar line: Poly2d collapses to a polynomial in the
+// normalised range, d_j = sum_i c_ij yval^i (core/Poly2d.cpp:8-24 regrouped).
+constexpr int LINE_POLY_MAX = 8;
+struct LinePoly {
+    int n;                       // x_order + 1, or 0 when evaluated per sample
+    double d[LINE_POLY_MAX];
+};
+
+__device__ __forceinline__ void line_poly(const AzRg& f, double az, LinePoly& lp) {
+    lp.n = 0;
+    if (f.is_zero || f.kind != 1 || f.poly.x_order + 1 > LINE_POLY_MAX) return;
+    const Poly& q = f.poly;
+    const double yval = (az - q.y_mean) * q.inv_y_norm;
+    lp.n = q.x_order + 1;
+#pragma unroll
+    for (int j = 0; j < LINE_POLY_MAX; ++j) {
+        if (j >= lp.n) break;
+        double acc = 0.0, sy = 1.0;
+        for (int i = 0; i <= q.y_order; ++i, sy *= yval) acc += sy * q.c[i * lp.n + j];
+        lp.d[j] = acc;
+    }
+}
+
+__device__ __noinline__ double carrier_general(const AzRg& f, double az, double rg) { return azrg_eval(f, az, rg); }
+
+__device__ __forceinline__ double carrier_at(const AzRg& f, const LinePoly& lp, double az, double rg) {
+    if (f.is_zero) return 0.0;
+    if (lp.n == 0) return carrier_general(f, az, rg);
+    const double xval = (rg - f.poly.x_mean) * f.poly.inv_x_norm;
+    double acc = lp.d[lp.n - 1];
+    for (int j = lp.n - 2; j >= 0; --j) acc = acc * xval + lp.d[j];
+    return acc;
+}
+
+// geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier)).
+// Grid: x covers a line in chunks of 4 * blockDim.x samples, y the lines.
 __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ DerampParams p) {
-    const int64_t n = p.inL * p.inW;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = idx / p.inW, j = idx - i * p.inW;
-        const double az = p.rg_t0 + (double)(i + p.az_first) / p.rg_prf;
-        const double rg = dadd(p.rg_r0, dmul((double)(j + p.rg_first), p.rg_dr));
-        const float phase = (float)(azrg_eval(p.rg_car, az, rg) + azrg_eval(p.az_car, az, rg));
-        float s, c;
-        sincosf(phase, &s, &c);
-        p.dst[idx] = cmul(p.src[idx], make_float2(c, -s));
+    for (int64_t i = blockIdx.y; i < p.inL; i += gridDim.y) {
+        const double az = p.rg_t0 + (double)(i + p.az_first) * p.inv_prf;
+        LinePoly lr, la;
+        line_poly(p.rg_car, az, lr);
+        line_poly(p.az_car, az, la);
+        const float2* src = p.src + i * p.inW;
+        float2* dst = p.dst + i * p.inW;
+        const int64_t j0 = (int64_t)blockIdx.x * blockDim.x * 4 + threadIdx.x;
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {     // loads first: four samples in flight per thread
+            const int64_t j = j0 + (int64_t)u * blockDim.x;
+            v[u] = j < p.inW ? __ldg(src + j) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t j = j0 + (int64_t)u * blockDim.x;
+            if (j >= p.inW) break;
+            const double rg = dadd(p.rg_r0, dmul((double)(j + p.rg_first), p.rg_dr));
+            const float phase = (float)(carrier_at(p.rg_car, lr, az, rg) + carrier_at(p.az_car, la, az, rg));
+            float sn, cs;
+            sincosf(phase, &sn, &cs);
+            dst[j] = cmul(v[u], make_float2(cs, -sn));
+        }
     }
 }
 
@@ -353,8 +496,8 @@ cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s) {
 
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
     (void)precision;
-    const dim3 block(32, 4);
-    const dim3 grid((p.gw + 31) / 32, (p.gl + 3) / 4);
+    const dim3 block(GBX, GBY);
+    const dim3 grid((p.gw + GBX - 1) / GBX, (p.gl + GBY - 1) / GBY);
     if (p.geo_is_lonlat) geocode_kernel<true><<<grid, block, 0, s>>>(p);
     else geocode_kernel<false><<<grid, block, 0, s>>>(p);
     if (launches) ++*launches;
@@ -362,15 +505,10 @@ cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, in
 }
 
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t n = p.inL * p.inW;
-    int64_t blocks = (n + 255) / 256;
-    const int64_t cap = (int64_t)sms * 8;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    deramp_kernel<<<(unsigned)blocks, 256, 0, s>>>(p);
+    const int64_t chunks = (p.inW + 1023) / 1024;
+    const int64_t lines = p.inL < 65535 ? p.inL : 65535;
+    if (chunks < 1 || lines < 1) return cudaSuccess;
+    deramp_kernel<<<dim3((unsigned)chunks, (unsigned)lines), 256, 0, s>>>(p);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

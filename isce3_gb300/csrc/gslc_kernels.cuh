@@ -40,6 +40,7 @@ struct GeoParams {
     Lut nat_dop, img_dop, az_corr, sr_corr;
     AzRg az_car, rg_car;
     double flat_scale;          // 4.0 * (M_PI / wavelength)
+    double inv_prf, two_pi_over_prf;
     int32_t flatten, reramp, use_corr, carriers_zero;
     float inv_re, inv_im;
     // radar blocks
@@ -63,7 +64,7 @@ struct DerampParams {
     const float2* src;
     float2* dst;
     int64_t inL, inW, az_first, rg_first;
-    double rg_t0, rg_prf, rg_r0, rg_dr;
+    double rg_t0, rg_prf, rg_r0, rg_dr, inv_prf;
     AzRg az_car, rg_car;
 };
 

@@ -50,14 +50,17 @@ GSLC_HD double vnorm(V3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 struct Lut {
     int32_t have_data, bounds_error, method, nx, ny, _pad;
     double x0, y0, dx, dy, ref_value;
+    double inv_dx, inv_dy;      // 1/dx, 1/dy
     const double* data;
 };
 
-// core/LUT2d.h:84-95
+// core/LUT2d.h:84-95.  The index is formed with the reciprocal spacing; it
+// can differ from the reference's quotient by an ulp, which matters only for
+// a point within an ulp of the table's edge.
 GSLC_HD bool lut_contains(const Lut& l, double y, double x) {
     if (!l.have_data) return true;
-    const double i = (x - l.x0) / l.dx;
-    const double j = (y - l.y0) / l.dy;
+    const double i = (x - l.x0) * l.inv_dx;
+    const double j = (y - l.y0) * l.inv_dy;
     return (i >= 0.0 && i <= l.nx - 1.0) && (j >= 0.0 && j <= l.ny - 1.0);
 }
 
@@ -75,8 +78,8 @@ GSLC_HD T ld_ro(const T* p) {
 // (x2-x1)*(y2-y1) == 1 are exact and omitted.
 GSLC_HD double lut_eval(const Lut& l, double y, double x) {
     if (!l.have_data) return l.ref_value;
-    double xi = (x - l.x0) / l.dx;
-    double yi = (y - l.y0) / l.dy;
+    double xi = (x - l.x0) * l.inv_dx;
+    double yi = (y - l.y0) * l.inv_dy;
     xi = fmin(fmax(xi, 0.0), l.nx - 1.0);
     yi = fmin(fmax(yi, 0.0), l.ny - 1.0);
     if (l.method == 3) {
@@ -88,8 +91,8 @@ GSLC_HD double lut_eval(const Lut& l, double y, double x) {
     const double q11 = ld_ro(l.data + (long)y1 * l.nx + x1), q12 = ld_ro(l.data + (long)y2 * l.nx + x1);
     const double q21 = ld_ro(l.data + (long)y1 * l.nx + x2), q22 = ld_ro(l.data + (long)y2 * l.nx + x2);
     if (y1 == y2 && x1 == x2) return q11;
-    if (y1 == y2) return ((x2 - xi) / (x2 - x1)) * q11 + ((xi - x1) / (x2 - x1)) * q21;
-    if (x1 == x2) return ((y2 - yi) / (y2 - y1)) * q11 + ((yi - y1) / (y2 - y1)) * q12;
+    if (y1 == y2) return (x2 - xi) * q11 + (xi - x1) * q21;
+    if (x1 == x2) return (y2 - yi) * q11 + (yi - y1) * q12;
     return q11 * ((x2 - xi) * (y2 - yi)) + q21 * ((xi - x1) * (y2 - yi)) +
            q12 * ((x2 - xi) * (yi - y1)) + q22 * ((xi - x1) * (yi - y1));
 }
@@ -99,12 +102,14 @@ constexpr int POLY_MAX = 64;
 struct Poly {
     int32_t x_order, y_order;
     double x_mean, y_mean, x_norm, y_norm;
+    double inv_x_norm, inv_y_norm;
     double c[POLY_MAX];
 };
 
+// core/Poly2d.cpp:8-24, normalised with reciprocals
 GSLC_HD double poly_eval(const Poly& p, double y, double x) {
-    const double xval = (x - p.x_mean) / p.x_norm;
-    const double yval = (y - p.y_mean) / p.y_norm;
+    const double xval = (x - p.x_mean) * p.inv_x_norm;
+    const double yval = (y - p.y_mean) * p.inv_y_norm;
     double scaley = 1., val = 0.;
     for (int i = 0; i <= p.y_order; i++, scaley *= yval) {
         double scalex = 1.;
@@ -138,10 +143,17 @@ GSLC_HD V3 lonlat_to_xyz(double a, double e2, double lon, double lat, double h) 
     return {(re + h) * clat * clon, (re + h) * clat * slon, ((re * (1.0 - e2)) + h) * slat};
 }
 
+// lonLatToXyz from precomputed sines and cosines
+GSLC_HD V3 lonlat_to_xyz_sc(double a, double e2, double slon, double clon, double slat, double clat, double h) {
+    const double re = a / sqrt(1.0 - e2 * (slat * slat));
+    return {(re + h) * clat * clon, (re + h) * clat * slon, ((re * (1.0 - e2)) + h) * slat};
+}
+
 // ---- Projections (core/Projections.{h,cpp}) -------------------------------
 struct Utm {
     int32_t isnorth, _pad;
     double lon0, Qn, Zb;
+    double slon0, clon0;        // sin/cos of the central meridian
     double cgb[6], cbg[6], utg[6], gtu[6];
 };
 
@@ -201,6 +213,83 @@ GSLC_HD bool utm_inverse(const Utm& u, double x, double y, double& lon, double& 
     lon = Ce + u.lon0;
     lat = clens(u.cgb, 2 * Cn) + Cn;
     return true;
+}
+
+// The UTM inverse split by what it depends on.  Easting-only terms
+// (Projections.cpp:203-210): normalised easting and sinh/cosh of twice it.
+struct UtmCol { double Ce, shi, chi; int ok; };
+GSLC_HD UtmCol utm_inverse_col(const Utm& u, double x) {
+    UtmCol c;
+    c.Ce = ((x - 500000.) / WGS84_A) / u.Qn;
+    c.ok = fabs(c.Ce) <= 2.623395162778;
+    c.shi = sinh(2 * c.Ce);
+    c.chi = cosh(2 * c.Ce);
+    return c;
+}
+// Northing-only terms: normalised northing and sin/cos of twice it.
+struct UtmRow { double Cn, sr, cr; };
+GSLC_HD UtmRow utm_inverse_row(const Utm& u, double y) {
+    UtmRow r;
+    r.Cn = ((y - (u.isnorth ? 0. : 10000000.)) / WGS84_A - u.Zb) / u.Qn;
+#if defined(__CUDA_ARCH__)
+    sincos(2 * r.Cn, &r.sr, &r.cr);
+#else
+    r.sr = sin(2 * r.Cn); r.cr = cos(2 * r.Cn);
+#endif
+    return r;
+}
+
+// Per-pixel remainder of the UTM inverse, with the transcendentals the
+// reference chains replaced by identities:
+//   atan(sinh x): sin = tanh x, cos = sech x (Gudermannian), from expm1;
+//   sin/cos of the Gaussian latitude are the atan2 operands (B^2 + H^2 = 1);
+//   sin/cos of the latitude rotate those by the small Clenshaw correction d
+//   (|d| < 3.4e-3, series to d^6: error < 1e-20);
+//   sin/cos of the longitude rotate (sinCe, A)/H by the central meridian.
+// Returns lon, lat (rad) and their sines and cosines.
+struct LonLatSC { double lon, lat, slon, clon, slat, clat; };
+GSLC_HD LonLatSC utm_inverse_px(const Utm& u, const UtmRow& r, const UtmCol& c) {
+    double dCn, dCe;
+    clenS(u.utg, r.sr, r.cr, c.shi, c.chi, dCn, dCe);
+    const double Cn1 = r.Cn + dCn;
+    const double xg = c.Ce + dCe;
+    const double em = expm1(xg);
+    const double num = em * (2.0 + em);            // e^(2x) - 1
+    const double q = 1.0 / (num + 2.0);            // 1 / (e^(2x) + 1)
+    const double sinCe = num * q;                  // tanh x
+    const double cosCe = (2.0 + 2.0 * em) * q;     // sech x
+    double sinCn, cosCn;
+#if defined(__CUDA_ARCH__)
+    sincos(Cn1, &sinCn, &cosCn);
+#else
+    sinCn = sin(Cn1); cosCn = cos(Cn1);
+#endif
+    const double A = cosCe * cosCn;
+    const double H = hypot(sinCe, A);
+    const double B = sinCn * cosCe;
+    LonLatSC o;
+    o.lon = atan2(sinCe, A) + u.lon0;
+    const double Cg = atan2(B, H);
+    // clens(cgb, 2 Cg) (Projections.cpp:33-42) with sin/cos(2 Cg) = (2BH, H^2 - B^2)
+    const double s2 = 2.0 * B * H, tc = 2.0 * ((H - B) * (H + B));
+    double hr2 = 0., hr1 = u.cgb[5], hr = 0.;
+    for (int k = 4; k >= 0; --k) {
+        hr = -hr2 + hr1 * tc + u.cgb[k];
+        hr2 = hr1;
+        hr1 = hr;
+    }
+    const double d = s2 * hr;
+    o.lat = Cg + d;
+    const double d2 = d * d;
+    const double sd = d * (1.0 - d2 * (1.0 / 6.0 - d2 * (1.0 / 120.0)));
+    const double cd = 1.0 - d2 * (0.5 - d2 * (1.0 / 24.0 - d2 * (1.0 / 720.0)));
+    o.slat = B * cd + H * sd;
+    o.clat = H * cd - B * sd;
+    const double iH = 1.0 / H;
+    const double sl = sinCe * iH, cl = A * iH;
+    o.slon = sl * u.clon0 + cl * u.slon0;
+    o.clon = cl * u.clon0 - sl * u.slon0;
+    return o;
 }
 
 // core/Projections.cpp:172-198
