@@ -286,6 +286,27 @@ def run_gpu(args, rank, world):
     res = dict(npx=npx, n_valid=n_valid, ms=ms, kernel_ms=float(np.mean(kernel_ms)),
                deramp_ms=float(np.mean(deramp_ms)), launches=launches, clocks=clocks, alg_bytes=alg_bytes,
                n_slc=n_slc, dem_bytes=dem_bytes)
+
+    # float-float geo2rdr beside it: same inputs, timed the same way
+    geo_f = torch.empty_like(geo_d)
+    mask_f = torch.empty_like(mask_d)
+    az_f, rg_f = torch.empty_like(az_d), torch.empty_like(rg_d)
+    geocode_slc(geo_f, slc_d, *common, mask_block=mask_f, az_index_block=az_f, rg_index_block=rg_f,
+                geo2rdr_precision="ff", **kw)
+    for _ in range(args.warmup):
+        geocode_slc(geo_f, slc_d, *common, mask_block=mask_f, geo2rdr_precision="ff", **kw)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kms = []
+    f0.record(stream)
+    for _ in range(args.steps):
+        geocode_slc(geo_f, slc_d, *common, mask_block=mask_f, geo2rdr_precision="ff", **kw)
+        kms.append(_kernel_ms(lib, ctx)[0])
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_ff = f0.elapsed_time(f1) / args.steps
+    res["ff"] = dict(ms=ms_ff, kernel_ms=float(np.mean(kms)), value=npx * world / (ms_ff * 1e-3),
+                     geo_d=geo_f, mask_d=mask_f, az_d=az_f, rg_d=rg_f)
     fp = C_double()
     L.check(lib.gslc_probe_fp64_gflops(ctx, fp), ctx)
     res["fp64_peak_gflops"] = fp.value
@@ -420,9 +441,11 @@ def main():
     if rank != 0:
         return
     cpu, par = None, None
+    par_ff = None
     if not args.no_cpu:
         cpu, (row0, rows, box, out) = cpu_baseline(sc, args.cpu_seconds)
         par = parity_sample(res, row0, rows, box, out)
+        par_ff = parity_sample(res["ff"], row0, rows, box, out)
     hbm_peak, peak_kind = peaks()
     kernel_s = res["kernel_ms"] * 1e-3
     achieved = res["alg_bytes"] / kernel_s / 1e9
@@ -442,6 +465,9 @@ def main():
                      "binding": "fp64 pipe (geo2rdr); see fp64"},
         "fp64": {"peak_gflops_measured": res["fp64_peak_gflops"], "probe": "gslc_probe_fp64_gflops DFMA loop"},
         "deramp_ms": res["deramp_ms"],
+        "geo2rdr_ff": {"value": res["ff"]["value"], "unit": UNIT, "ms_per_step": res["ff"]["ms"],
+                       "kernel_ms": res["ff"]["kernel_ms"], "parity_sample": par_ff,
+                       "note": "float-float (double-word FP32) Newton iterations, FP64 first iterate and range"},
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "cpu_baseline": cpu, "parity_sample": par,
     }

@@ -507,6 +507,20 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     // orbit polynomials
     std::vector<double> coef;
     make_orbit_coeffs(a->orbit, coef);
+    // float-pair copy of the polynomial coefficients for the float-float geo2rdr,
+    // stored after the doubles (ORB_FF_STRIDE float2 per piece = 45 doubles' room)
+    {
+        const int np = a->orbit.n - 3;
+        const size_t nd = coef.size();
+        coef.resize(nd + (size_t)np * ORB_FF_STRIDE, 0.0);
+        float2* ffc = reinterpret_cast<float2*>(coef.data() + nd);
+        for (int idx = 0; idx < np; ++idx)
+            for (int k = 0; k < ORB_FF_STRIDE; ++k) {
+                const double v = coef[(size_t)idx * ORB_STRIDE + 3 + k];
+                const float hi = (float)v;
+                ffc[(size_t)idx * ORB_FF_STRIDE + k] = make_float2(hi, (float)(v - (double)hi));
+            }
+    }
     if (coef.size() > c->orbit_cap) {
         if (c->d_orbit) cudaFree(c->d_orbit);
         c->d_orbit = nullptr;
@@ -524,6 +538,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     ob.n = a->orbit.n;
     ob.n_pieces = a->orbit.n - 3;
     ob.coef = c->d_orbit;
+    ob.coef_ff = reinterpret_cast<const float2*>(c->d_orbit + (size_t)(a->orbit.n - 3) * ORB_STRIDE);
 
     // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)
     p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
@@ -712,7 +727,7 @@ static __device__ __align__(256) float2 g_noalloc_deramp[NOALLOC_MAX_DERAMP];
 // sinc kernel table, SINC_SUB x SINC_LEN
 static __device__ __align__(256) float g_noalloc_sinc[SINC_SUB * SINC_LEN];
 // orbit polynomial pieces
-static __device__ __align__(256) double g_noalloc_orbit[(NOALLOC_MAX_STATE_VECTORS - 3) * ORB_STRIDE];
+static __device__ __align__(256) double g_noalloc_orbit[(NOALLOC_MAX_STATE_VECTORS - 3) * (ORB_STRIDE + ORB_FF_STRIDE)];
 // error word (bit 0: projection inverse failed); cleared at every call
 static __device__ __align__(256) int32_t g_noalloc_err[4];
 
@@ -783,7 +798,7 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     static thread_local int32_t h_err[4];
     c.h_err = h_err;
     c.d_orbit = d.orbit;
-    c.orbit_cap = (size_t)(NOALLOC_MAX_STATE_VECTORS - 3) * ORB_STRIDE;
+    c.orbit_cap = (size_t)(NOALLOC_MAX_STATE_VECTORS - 3) * (ORB_STRIDE + ORB_FF_STRIDE);
 
     gslc_geocode_args args = *a;
     std::vector<const void*> blocks(a->rdr_blocks, a->rdr_blocks + a->n_blocks);

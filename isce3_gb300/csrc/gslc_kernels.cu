@@ -165,6 +165,94 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
     return false;
 }
 
+// The same Newton path in float-float.  Iteration 0 uses the shared FP64
+// state at sensingMid; later iterations evaluate the orbit polynomial, the
+// range vector relative to the interval's reference position, the Doppler
+// residual and the step in double-word FP32 (~2^-44 relative), keeping the
+// azimuth time as a double-word offset s from the interval's first node.
+// The FP64 pipe then carries only the first iterate, interval changes and
+// the final slant range.  Used when the image-grid Doppler is zero (the
+// NISAR GSLC convention); otherwise the FP64 path runs.
+__device__ __forceinline__ void orbit_eval_ff(const Orbit& o, int idx, ff u, ff pr[3], ff v[3]) {
+    const float2* c = o.coef_ff + (int64_t)idx * ORB_FF_STRIDE;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float2 q = __ldg(c + d * 8 + 7);
+        ff acc = {q.x, q.y};
+#pragma unroll
+        for (int k = 6; k >= 0; --k) {
+            q = __ldg(c + d * 8 + k);
+            acc = ff_fma(acc, u, {q.x, q.y});
+        }
+        pr[d] = acc;
+        q = __ldg(c + 24 + d * 7 + 6);
+        ff vacc = {q.x, q.y};
+#pragma unroll
+        for (int k = 5; k >= 0; --k) {
+            q = __ldg(c + 24 + d * 7 + k);
+            vacc = ff_fma(vacc, u, {q.x, q.y});
+        }
+        v[d] = vacc;
+    }
+}
+
+__device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
+    const Orbit& o = p.orbit;
+    // iteration 0: t = sensingMid, shared position/velocity (FP64)
+    t = p.t_mid;
+    {
+        const V3 rvec = vsub(xyz, p.pos0);
+        if ((p.look_side == -1) != (vdot(vcross(rvec, p.vel0), p.pos0) > 0.)) return false;
+        const double dt = vdot(rvec, p.vel0) / (-vdot(p.vel0, p.vel0));
+        if (fabs(dt) < p.thr) {
+            R = vnorm(rvec);
+            return true;
+        }
+        t -= dt;
+    }
+    const float thr = (float)p.thr;
+    const ff inv_sp = ff_from_double(o.inv_spacing);
+    int piece = -1;
+    double tidx = 0.0;
+    ff s = {0.f, 0.f}, D[3];
+    float s_lo = 0.f, s_hi = 0.f;              // s range of the current piece
+    for (int i = 1; i < p.maxiter; ++i) {
+        const float sf = s.hi + s.lo;
+        if (piece < 0 || !(sf >= s_lo && sf < s_hi)) {
+            // (re)enter an orbit interval: FP64 time, range check, reference position
+            if (piece >= 0) t = tidx + ((double)s.hi + (double)s.lo);
+            if (!(t >= o.t0 && t <= o.t_end)) return false;   // FillNaN -> no convergence
+            piece = orbit_piece(o, t);
+            tidx = o.t0 + piece * o.spacing;
+            const double* pref = o.coef + (int64_t)piece * ORB_STRIDE;
+            D[0] = ff_from_double(xyz.x - __ldg(pref + 0));
+            D[1] = ff_from_double(xyz.y - __ldg(pref + 1));
+            D[2] = ff_from_double(xyz.z - __ldg(pref + 2));
+            s = ff_from_double(t - tidx);
+            // the piece serves u in [-1.5, 1.5] (first/last) or [-0.5, 0.5)
+            const float sp = (float)o.spacing;
+            s_lo = piece == 0 ? 0.f : sp;
+            s_hi = piece == o.n - 4 ? 3.f * sp : 2.f * sp;
+            if (piece == o.n - 4) s_hi = (float)(o.t_end - tidx);
+        }
+        const ff u = ff_add(ff_mul(s, inv_sp), {-1.5f, 0.f});
+        ff pr[3], v[3];
+        orbit_eval_ff(o, piece, u, pr, v);
+        const ff r0 = ff_add(D[0], ff_neg(pr[0])), r1 = ff_add(D[1], ff_neg(pr[1])), r2 = ff_add(D[2], ff_neg(pr[2]));
+        const ff fn = ff_add(ff_add(ff_mul(r0, v[0]), ff_mul(r1, v[1])), ff_mul(r2, v[2]));
+        const ff vv = ff_add(ff_add(ff_mul(v[0], v[0]), ff_mul(v[1], v[1])), ff_mul(v[2], v[2]));
+        const ff dt = ff_div(fn, ff_neg(vv));
+        if (fabsf(dt.hi) < thr) {
+            t = tidx + ((double)s.hi + (double)s.lo);
+            const double x0 = ff_to_double(r0), x1 = ff_to_double(r1), x2 = ff_to_double(r2);
+            R = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+            return true;
+        }
+        s = ff_add(s, ff_neg(dt));
+    }
+    return false;
+}
+
 // product/SubSwaths.cpp:58-96
 __device__ int subswath_of(const GeoParams& p, int az, int rg) {
     if (rg < 0 || rg >= p.subsw_wid || az < 0 || az >= p.subsw_len) return 0;
@@ -240,7 +328,7 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
 // evaluated once per block column/line into shared memory.
 constexpr int GBX = 32, GBY = 8;
 
-template <bool GEO_LONLAT>
+template <bool GEO_LONLAT, bool FF>
 __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
     __shared__ double s_col[4][GBX];
     __shared__ double s_row[5][GBY];
@@ -339,7 +427,10 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constan
     }
     if (ok) {
         double t, R;
-        if (geo2rdr(p, xyz, t, R)) {
+        bool conv;
+        if (FF) conv = geo2rdr_ff(p, xyz, t, R);
+        else conv = geo2rdr(p, xyz, t, R);
+        if (conv) {
             if (!p.use_corr) R_uncorr = R;
             if (lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
             if (lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
@@ -495,11 +586,18 @@ cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s) {
 }
 
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
-    (void)precision;
     const dim3 block(GBX, GBY);
     const dim3 grid((p.gw + GBX - 1) / GBX, (p.gl + GBY - 1) / GBY);
-    if (p.geo_is_lonlat) geocode_kernel<true><<<grid, block, 0, s>>>(p);
-    else geocode_kernel<false><<<grid, block, 0, s>>>(p);
+    // the float-float path covers zero image-grid Doppler with the first
+    // iterate at sensingMid; anything else runs in FP64
+    const bool ff = precision == 1 && p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0;
+    if (p.geo_is_lonlat) {
+        if (ff) geocode_kernel<true, true><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<true, false><<<grid, block, 0, s>>>(p);
+    } else {
+        if (ff) geocode_kernel<false, true><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<false, false><<<grid, block, 0, s>>>(p);
+    }
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -315,11 +315,13 @@ GSLC_HD bool utm_forward(const Utm& u, double lon, double lat, double& x, double
 // u = (t - t_idx)/spacing - 1.5; velocity is its derivative.  The host
 // expands it once per interval (gslc_capi.cu) around P_ref = P_{idx+1}.
 constexpr int ORB_STRIDE = 48;   // pref[3], a[3][8], b[3][7] (b = d/dt coefficients)
+constexpr int ORB_FF_STRIDE = 45;  // a[3][8], b[3][7] split into float pairs
 
 struct Orbit {
     double t0, spacing, inv_spacing, t_end;
     int32_t n, n_pieces;
     const double* coef;          // n_pieces * ORB_STRIDE
+    const float2* coef_ff;       // n_pieces * ORB_FF_STRIDE: a[3][8], b[3][7] as (hi, lo)
 };
 
 GSLC_HD int orbit_piece(const Orbit& o, double t) {
@@ -352,6 +354,54 @@ GSLC_HD void orbit_eval(const Orbit& o, double t, V3& pos, V3& vel) {
     pos = {p[0], p[1], p[2]};
     vel = {v[0], v[1], v[2]};
 }
+
+// ---- float-float (double-word FP32) arithmetic ------------------------------
+// Dekker (1971) products and Knuth's TwoSum, in the double-word forms of
+// Joldes, Muller & Popescu, "Tight and rigorous error bounds for basic
+// building blocks of double-word arithmetic" (ACM TOMS 44(2), 2017):
+// relative error of add/mul about 2^-44.  Only plain IEEE add/mul and fmaf
+// are used, so nvcc cannot reassociate them.
+struct ff { float hi, lo; };
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_from_double(double d) {
+    const float hi = __double2float_rn(d);
+    return {hi, __double2float_rn(d - (double)hi)};
+}
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ ff ff_add(ff x, ff y) {                   // AccurateDWPlusDW
+    ff s = ff_two_sum(x.hi, y.hi);
+    const ff t = ff_two_sum(x.lo, y.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = ff_fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return ff_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ ff ff_mul(ff x, ff y) {                   // DWTimesDW
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, e);
+    e = fmaf(x.lo, y.hi, e);
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ ff ff_fma(ff x, ff y, ff z) { return ff_add(ff_mul(x, y), z); }
+__device__ __forceinline__ ff ff_div(ff a, ff b) {                   // DWDivDW (long division)
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const ff r = ff_add(a, ff_neg(ff_mul(b, {q1, 0.f})));
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    return ff_fast_two_sum(q1, q2);
+}
+#endif
 
 // ---- Biquintic spline, FP32, exact reference order -------------------------
 // core/Spline2dInterpolator.cpp:89-108 (_initSpline) for n = 6.  p[i], q[i]

@@ -81,8 +81,9 @@ def c1():
     return synth.scene_c1()
 
 
-def test_c1_plain(oracle_mod, c1):
-    gpu, ora = _run_both(oracle_mod, c1, [c1.slc])
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+def test_c1_plain(oracle_mod, c1, precision):
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], geo2rdr_precision=precision)
     r = _check(gpu, ora)[0]
     assert r["n_valid"] > 100000
     assert r["max_rel_err"] < 1e-5
@@ -124,11 +125,12 @@ def test_c1_doppler_carriers_corrections_blocks(oracle_mod, c1):
     _check(gpu, ora, az_first=a0, rg_first=r0)
 
 
-@pytest.mark.parametrize("flatten,reramp", [(False, True), (True, False), (False, False)])
-def test_c1_flags(oracle_mod, c1, flatten, reramp):
+@pytest.mark.parametrize("flatten,reramp,precision", [(False, True, "fp64"), (True, False, "fp64"),
+                                                     (False, False, "fp64"), (True, True, "ff")])
+def test_c1_flags(oracle_mod, c1, flatten, reramp, precision):
     az_car = Poly2d([[0.0], [2 * np.pi * 100.0]], y_mean=c1.radar_grid.sensing_mid)
     gpu, ora = _run_both(oracle_mod, c1, [c1.slc], flatten=flatten, reramp=reramp, az_carrier=az_car,
-                         rg_carrier=Poly2d())
+                         rg_carrier=Poly2d(), geo2rdr_precision=precision)
     _check(gpu, ora)
 
 
@@ -145,11 +147,13 @@ def test_sliced_grid_and_subswaths(oracle_mod, c1):
     assert set(np.unique(gpu["mask"])) >= {0, 1, 2, 255}
 
 
-def test_utm_geogrid_and_lut_doppler(oracle_mod):
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+def test_utm_geogrid_and_lut_doppler(oracle_mod, precision):
     """Reduced frame scene: UTM 32611 geogrid over an EPSG:4326 DEM, native
     Doppler LUT2d (quadratic in range) and a linear azimuth carrier."""
     sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0)
-    gpu, ora = _run_both(oracle_mod, sc, [sc.slc], az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    gpu, ora = _run_both(oracle_mod, sc, [sc.slc], az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier,
+                         geo2rdr_precision=precision)
     r = _check(gpu, ora)[0]
     assert r["n_valid"] > 10000
 
