@@ -191,6 +191,34 @@ int gslc_last_kernel_ms(const gslc_ctx* ctx, float* geocode_ms, float* deramp_ms
  * FP64 roofline the geocode kernel is reported against. */
 int gslc_probe_fp64_gflops(gslc_ctx* ctx, double* gflops);
 
+/* Batched form.  A batch holds many geocode requests (bursts, tiles of
+ * uneven size; each a gslc_geocode_args with its own radar grid, radar
+ * blocks, geogrid window and outputs).  One launch runs the deramp passes and
+ * ONE persistent kernel whose blocks pop runs of 32x8-pixel tiles of any
+ * request from a device counter; by default the whole sequence is captured
+ * in a CUDA graph at creation and replayed by gslc_batch_launch.  Each
+ * request's outputs equal its plain gslc_geocode_slc call.  Pointers in the
+ * requests are bound at creation: relaunching recomputes the same outputs
+ * from the (possibly updated) contents of the same buffers.  No counterpart
+ * in the reference, which geocodes one block per call
+ * (geocodeSlc.cpp:831-968, driven block by block by
+ * python/packages/nisar/workflows/gslc.py:173-214). */
+typedef struct gslc_batch gslc_batch;
+typedef struct {
+    int32_t tiles_per_pop;   /* tiles a block takes per counter pop; 0: 2 */
+    int32_t blocks_per_sm;   /* persistent blocks per SM; 0: occupancy maximum */
+    int32_t use_graph;       /* 1: capture and replay a CUDA graph; 0: launch directly */
+    int32_t _pad;
+} gslc_batch_tuning;
+
+int gslc_batch_create(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
+                      int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, gslc_batch** out);
+int gslc_batch_launch(gslc_batch* batch, void* stream);     /* enqueue only */
+int gslc_batch_status(gslc_batch* batch, void* stream);     /* synchronise the stream, report errors */
+int gslc_batch_info(const gslc_batch* batch, int64_t* n_tiles, int32_t* blocks, int32_t* tiles_per_pop,
+                    int64_t* launches);
+int gslc_batch_destroy(gslc_batch* batch);
+
 /* Allocation-free plain form.  No counterpart in the reference: an addition
  * for callers that must not allocate device memory while they run (serving
  * loops that reserve HBM up front under a fixed budget, hosts that forbid

@@ -134,6 +134,11 @@ class GeocodeArgs(C.Structure):
                 ("subswaths", C.POINTER(SubSwathsDesc))]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("tiles_per_pop", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
+                ("_pad", C.c_int32)]
+
+
 _EXPORTS = {
     "gslc_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "gslc_ctx_destroy": (C.c_int, [C.c_void_p]),
@@ -150,6 +155,13 @@ _EXPORTS = {
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),
+    "gslc_batch_create": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_int32, C.c_int32,
+                                    C.POINTER(BatchTuning), C.POINTER(C.c_void_p)]),
+    "gslc_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gslc_batch_status": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gslc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int64)]),
+    "gslc_batch_destroy": (C.c_int, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -440,12 +440,14 @@ double grid_end(const gslc_radar_grid& g) { return g.starting_range + (g.width -
 
 }  // namespace
 
-extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream_) {
-    if (!c) return GSLC_EINVAL;
-    c->err.clear();
-    c->launches = 0;
+namespace {
+
+// Validation and launch parameters of one geocode call: everything except
+// the device addresses of the orbit polynomials (bind_orbit), the sinc table
+// and the error word.  GSLC_EMPTY_GRID means there is nothing to do.
+constexpr int GSLC_EMPTY_GRID = 100;
+int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::vector<double>& coef) {
     if (!a) return set_err(c, GSLC_EINVAL, "null arguments");
-    cudaStream_t stream = (cudaStream_t)stream_;
     const gslc_radar_grid& rg = a->radar_grid;
     const gslc_radar_grid& srg = a->sliced_radar_grid;
     const gslc_geo_grid& gg = a->geo_grid;
@@ -465,14 +467,10 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
         return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
     if (a->rdr_length < 0 || a->rdr_width < 0) return set_err(c, GSLC_EINVAL, "invalid radar block shape");
-    if (gg.width == 0 || gg.length == 0) return GSLC_OK;
+    if (gg.width == 0 || gg.length == 0) return GSLC_EMPTY_GRID;
     for (const gslc_lut2d* l : {&a->native_doppler, &a->image_grid_doppler, &a->az_time_correction, &a->srange_correction})
         if (int st = check_lut(c, *l, "LUT2d")) return st;
 
-    cudaError_t e = cudaSetDevice(c->device);
-    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
-
-    GeoParams p;
     std::memset(&p, 0, sizeof(p));
     p.gx0 = gg.start_x; p.gy0 = gg.start_y; p.gdx = gg.spacing_x; p.gdy = gg.spacing_y;
     p.gw = gg.width; p.gl = gg.length;
@@ -505,7 +503,6 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     p.ell_e2 = a->ellipsoid_e2;
 
     // orbit polynomials
-    std::vector<double> coef;
     make_orbit_coeffs(a->orbit, coef);
     // float-pair copy of the polynomial coefficients for the float-float geo2rdr,
     // stored after the doubles (ORB_FF_STRIDE float2 per piece = 45 doubles' room)
@@ -521,15 +518,6 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
                 ffc[(size_t)idx * ORB_FF_STRIDE + k] = make_float2(hi, (float)(v - (double)hi));
             }
     }
-    if (coef.size() > c->orbit_cap) {
-        if (c->d_orbit) cudaFree(c->d_orbit);
-        c->d_orbit = nullptr;
-        e = cudaMalloc(&c->d_orbit, coef.size() * sizeof(double));
-        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc orbit");
-        c->orbit_cap = coef.size();
-    }
-    e = cudaMemcpyAsync(c->d_orbit, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return cuda_err(c, e, "orbit upload");
     Orbit& ob = p.orbit;
     ob.t0 = a->orbit.t0;
     ob.spacing = a->orbit.spacing;
@@ -537,8 +525,8 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     ob.t_end = a->orbit.t0 + (a->orbit.n - 1) * a->orbit.spacing;
     ob.n = a->orbit.n;
     ob.n_pieces = a->orbit.n - 3;
-    ob.coef = c->d_orbit;
-    ob.coef_ff = reinterpret_cast<const float2*>(c->d_orbit + (size_t)(a->orbit.n - 3) * ORB_STRIDE);
+    ob.coef = nullptr;      // bound to device memory by bind_orbit
+    ob.coef_ff = nullptr;
 
     // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)
     p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
@@ -579,7 +567,6 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     p.flatten_out = a->flatten_phase;
     p.az_out = a->az_index;
     p.rg_out = a->rg_index;
-    p.sinc = c->d_sinc;
     if (a->subswaths) {
         p.have_subsw = 1;
         p.subsw_n = a->subswaths->n;
@@ -588,6 +575,42 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
         p.subsw = a->subswaths->valid;
         if (p.subsw_n > 0 && !p.subsw) return set_err(c, GSLC_EINVAL, "subswaths without valid-sample arrays");
     }
+    return GSLC_OK;
+}
+
+// Point the launch parameters at orbit polynomials resident at d_coef
+// (doubles, then the float pairs, as make_orbit_coeffs + prepare lay them out).
+void bind_orbit(GeoParams& p, const double* d_coef) {
+    p.orbit.coef = d_coef;
+    p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+}
+
+}  // namespace
+
+extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    GeoParams p;
+    std::vector<double> coef;
+    int st = prepare_geocode(c, a, p, coef);
+    if (st == GSLC_EMPTY_GRID) return GSLC_OK;
+    if (st != GSLC_OK) return st;
+    const gslc_radar_grid& rg = a->radar_grid;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    if (coef.size() > c->orbit_cap) {
+        if (c->d_orbit) cudaFree(c->d_orbit);
+        c->d_orbit = nullptr;
+        e = cudaMalloc(&c->d_orbit, coef.size() * sizeof(double));
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc orbit");
+        c->orbit_cap = coef.size();
+    }
+    e = cudaMemcpyAsync(c->d_orbit, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "orbit upload");
+    bind_orbit(p, c->d_orbit);
+    p.sinc = c->d_sinc;
     p.err = c->d_err;
     e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
     if (e != cudaSuccess) return cuda_err(c, e, "memset");
@@ -828,5 +851,257 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     c.d_orbit = nullptr;
     c.h_err = nullptr;
     if (st != GSLC_OK) return noalloc_fail(errbuf, errbuf_len, st, c.err.c_str());
+    return GSLC_OK;
+}
+
+// ===========================================================================
+// Batched form: many geocode requests (bursts, tiles of uneven size) in one
+// persistent launch over a device tile counter, optionally captured with
+// their deramp passes in a CUDA graph and replayed.
+// ===========================================================================
+struct gslc_batch {
+    gslc_ctx* ctx = nullptr;
+    int device = 0;
+    bool lonlat = false, ff = false;
+    int blocks = 0;
+    BatchQueue q{};
+    GeoParams* d_items = nullptr;
+    long long* d_tile_start = nullptr;
+    long long* d_counter = nullptr;
+    double* d_orbit = nullptr;
+    float2* d_scratch = nullptr;
+    int32_t* d_err = nullptr;
+    int32_t* h_err = nullptr;
+    std::vector<DerampParams> deramps;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    int64_t launches_per_run = 0;
+    long long n_tiles = 0;
+    std::string err;
+};
+
+namespace {
+
+int batch_fail(gslc_batch* b, gslc_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    if (b) b->err = m;
+    return code;
+}
+
+cudaError_t batch_enqueue(gslc_batch* b, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter, 0, sizeof(long long), s);
+    for (const DerampParams& dp : b->deramps) {
+        if (e != cudaSuccess) break;
+        e = launch_deramp(dp, s, nullptr);
+    }
+    if (e == cudaSuccess) e = launch_geocode_persistent(b->q, b->lonlat, b->ff, b->blocks, s, nullptr);
+    return e;
+}
+
+}  // namespace
+
+extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, int32_t n, int32_t precision,
+                                 const gslc_batch_tuning* tuning, gslc_batch** out) {
+    if (!c || !out) return GSLC_EINVAL;
+    *out = nullptr;
+    c->err.clear();
+    if (!items || n < 1) return set_err(c, GSLC_EINVAL, "empty batch");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    gslc_batch* b = new (std::nothrow) gslc_batch();
+    if (!b) return set_err(c, GSLC_ECUDA, "out of host memory");
+    b->ctx = c;
+    b->device = c->device;
+
+    std::vector<GeoParams> params;
+    std::vector<std::vector<double>> coefs;
+    std::vector<int> owner;                 // item index of each params entry
+    size_t coef_total = 0, scratch_total = 0;
+    bool any_ll = false, any_utm = false;
+    for (int i = 0; i < n; ++i) {
+        GeoParams p;
+        std::vector<double> coef;
+        const int st = prepare_geocode(c, &items[i], p, coef);
+        if (st == GSLC_EMPTY_GRID) continue;
+        if (st != GSLC_OK) {
+            gslc_batch_destroy(b);
+            return st;
+        }
+        (p.geo_is_lonlat ? any_ll : any_utm) = true;
+        const gslc_geocode_args& a = items[i];
+        const int64_t nrdr = a.rdr_length * a.rdr_width;
+        if (!p.carriers_zero && nrdr > 0 && !a.inplace_deramp) scratch_total += (size_t)nrdr * a.n_blocks;
+        for (int b0 = 0; b0 < a.n_blocks; b0 += MAX_BLOCKS) {
+            GeoParams q = p;
+            q.nblk = std::min(MAX_BLOCKS, a.n_blocks - b0);
+            params.push_back(q);
+            owner.push_back(i);
+        }
+        coef_total += coef.size();
+        coefs.push_back(std::move(coef));
+    }
+    if (any_ll && any_utm) {
+        gslc_batch_destroy(b);
+        return set_err(c, GSLC_EUNSUPPORTED, "a batch mixes EPSG:4326 and UTM geogrids");
+    }
+    b->lonlat = any_ll;
+    b->ff = precision == 1;
+    if (params.empty()) {
+        *out = b;
+        return GSLC_OK;
+    }
+    e = cudaMalloc(&b->d_orbit, coef_total * sizeof(double));
+    if (e == cudaSuccess && scratch_total) e = cudaMalloc(&b->d_scratch, scratch_total * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_items, params.size() * sizeof(GeoParams));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_start, (params.size() + 1) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(int32_t) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_err, sizeof(int32_t) * 4);
+    if (e != cudaSuccess) {
+        gslc_batch_destroy(b);
+        return cuda_err(c, e, "batch allocation");
+    }
+    // orbit polynomials of each item, then bind every params entry
+    std::vector<size_t> coef_off;
+    size_t off = 0;
+    for (const auto& cf : coefs) {
+        coef_off.push_back(off);
+        e = cudaMemcpy(b->d_orbit + off, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) break;
+        off += cf.size();
+    }
+    // item index -> coefs index (items with empty grids have no coef)
+    std::vector<int> coef_of_item(n, -1);
+    {
+        int k = 0;
+        for (int i = 0, j = 0; i < n && j < (int)owner.size(); ++i)
+            if (owner[j] == i) {
+                coef_of_item[i] = k++;
+                while (j < (int)owner.size() && owner[j] == i) ++j;
+            }
+    }
+    size_t scratch_off = 0;
+    std::vector<long long> tile_start(params.size() + 1, 0);
+    int last_item = -1, block_base = 0;
+    for (size_t j = 0; j < params.size(); ++j) {
+        GeoParams& p = params[j];
+        const int i = owner[j];
+        const gslc_geocode_args& a = items[i];
+        block_base = (i == last_item) ? block_base + MAX_BLOCKS : 0;
+        last_item = i;
+        bind_orbit(p, b->d_orbit + coef_off[coef_of_item[i]]);
+        p.sinc = c->d_sinc;
+        p.err = b->d_err;
+        const int64_t nrdr = a.rdr_length * a.rdr_width;
+        for (int k = 0; k < p.nblk; ++k) {
+            const float2* src = (const float2*)a.rdr_blocks[block_base + k];
+            const float2* use = src;
+            if (!p.carriers_zero && nrdr > 0) {
+                float2* dst = a.inplace_deramp ? const_cast<float2*>(src) : b->d_scratch + scratch_off;
+                if (!a.inplace_deramp) scratch_off += nrdr;
+                DerampParams dp;
+                std::memset(&dp, 0, sizeof(dp));
+                dp.src = src; dp.dst = dst;
+                dp.inL = a.rdr_length; dp.inW = a.rdr_width;
+                dp.az_first = a.first_azimuth_line; dp.rg_first = a.first_range_sample;
+                const gslc_radar_grid& rg = a.radar_grid;
+                dp.rg_t0 = rg.sensing_start; dp.rg_prf = rg.prf; dp.rg_r0 = rg.starting_range;
+                dp.rg_dr = rg.range_pixel_spacing; dp.inv_prf = 1.0 / rg.prf;
+                dp.az_car = p.az_car; dp.rg_car = p.rg_car;
+                b->deramps.push_back(dp);
+                use = dst;
+            }
+            p.rdr[k] = use;
+            p.geo[k] = (float2*)a.geo_blocks[block_base + k];
+        }
+        const long long tiles = (long long)((p.gw + TILE_X - 1) / TILE_X) * ((p.gl + TILE_Y - 1) / TILE_Y);
+        tile_start[j + 1] = tile_start[j] + tiles;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_items, params.data(), params.size() * sizeof(GeoParams), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_tile_start, tile_start.data(), tile_start.size() * sizeof(long long),
+                       cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        gslc_batch_destroy(b);
+        return cuda_err(c, e, "batch upload");
+    }
+    b->n_tiles = tile_start.back();
+    b->q.items = b->d_items;
+    b->q.tile_start = b->d_tile_start;
+    b->q.n_items = (int32_t)params.size();
+    b->q.n_tiles = b->n_tiles;
+    b->q.counter = b->d_counter;
+    b->q.tiles_per_pop = (tuning && tuning->tiles_per_pop > 0) ? tuning->tiles_per_pop : 2;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int occ = std::max(1, persistent_blocks_per_sm(b->lonlat, b->ff));
+    const int per_sm = (tuning && tuning->blocks_per_sm > 0) ? std::min(tuning->blocks_per_sm, occ) : occ;
+    b->blocks = sms * per_sm;
+    b->launches_per_run = (int64_t)b->deramps.size() + 1;
+    if (!tuning || tuning->use_graph) {
+        e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e2 = batch_enqueue(b, b->capture_stream);
+            e = cudaStreamEndCapture(b->capture_stream, &b->graph);
+            if (e2 != cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) {
+            gslc_batch_destroy(b);
+            return cuda_err(c, e, "batch graph capture");
+        }
+    }
+    *out = b;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_batch_launch(gslc_batch* b, void* stream) {
+    if (!b) return GSLC_EINVAL;
+    if (!b->q.n_items) return GSLC_OK;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = b->exec ? cudaGraphLaunch(b->exec, (cudaStream_t)stream) : batch_enqueue(b, (cudaStream_t)stream);
+    if (e != cudaSuccess) return batch_fail(b, b->ctx, GSLC_ECUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+    if (b->ctx) b->ctx->launches = b->launches_per_run;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_batch_status(gslc_batch* b, void* stream) {
+    if (!b) return GSLC_EINVAL;
+    if (!b->q.n_items) return GSLC_OK;
+    cudaError_t e = cudaMemcpyAsync(b->h_err, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return batch_fail(b, b->ctx, GSLC_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
+    if (b->h_err[0] & 1) return batch_fail(b, b->ctx, GSLC_EPROJ, "Inverse projection transformation failed");
+    return GSLC_OK;
+}
+
+extern "C" int gslc_batch_info(const gslc_batch* b, int64_t* n_tiles, int32_t* blocks, int32_t* tiles_per_pop,
+                               int64_t* launches) {
+    if (!b) return GSLC_EINVAL;
+    if (n_tiles) *n_tiles = b->n_tiles;
+    if (blocks) *blocks = b->blocks;
+    if (tiles_per_pop) *tiles_per_pop = b->q.tiles_per_pop;
+    if (launches) *launches = b->launches_per_run;
+    return GSLC_OK;
+}
+
+extern "C" int gslc_batch_destroy(gslc_batch* b) {
+    if (!b) return GSLC_OK;
+    cudaSetDevice(b->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    cudaFree(b->d_items);
+    cudaFree(b->d_tile_start);
+    cudaFree(b->d_counter);
+    cudaFree(b->d_orbit);
+    cudaFree(b->d_scratch);
+    cudaFree(b->d_err);
+    if (b->h_err) cudaFreeHost(b->h_err);
+    delete b;
     return GSLC_OK;
 }

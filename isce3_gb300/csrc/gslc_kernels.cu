@@ -328,14 +328,15 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
 // evaluated once per block column/line into shared memory.
 constexpr int GBX = 32, GBY = 8;
 
+// One GBX x GBY tile (tile column bx, tile line by) of one geocode request.
 template <bool GEO_LONLAT, bool FF>
-__global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
+__device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by) {
     __shared__ double s_col[4][GBX];
     __shared__ double s_row[5][GBY];
     __shared__ int s_colok[GBX];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int pixel = blockIdx.x * GBX + tx;
-    const int line = blockIdx.y * GBY + ty;
+    const int pixel = bx * GBX + tx;
+    const int line = by * GBY + ty;
     const bool dem_ll = p.dem.have_raster && p.dem.epsg_is_lonlat;
 
     if (ty == 0) {
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constan
             s_colok[tx] = c.ok;
         }
     } else if (ty == 1 && tx < GBY) {
-        const int lr = min((int)(blockIdx.y * GBY + tx), p.gl - 1);
+        const int lr = min(by * GBY + tx, p.gl - 1);
         const double y = dadd(p.gy0, dmul(p.gdy, (double)lr + 0.5));   // geocodeSlc.cpp:100
         if (GEO_LONLAT) {
             const double lat = (y * PI) / 180.0;
@@ -499,6 +500,43 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constan
     }
 }
 
+template <bool GEO_LONLAT, bool FF>
+__global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
+    geocode_block<GEO_LONLAT, FF>(p, blockIdx.x, blockIdx.y);
+}
+
+// Persistent form: blocks pop runs of tiles of any request in the batch from
+// one counter until the batch is exhausted.  Requests keep their own
+// parameters, so each request's output equals its plain call.
+template <bool GEO_LONLAT, bool FF>
+__global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_constant__ BatchQueue q) {
+    __shared__ long long s_base;
+    for (;;) {
+        if (threadIdx.x == 0 && threadIdx.y == 0)
+            s_base = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(q.counter),
+                                          (unsigned long long)q.tiles_per_pop);
+        __syncthreads();
+        const long long base = s_base;
+        __syncthreads();
+        if (base >= q.n_tiles) return;
+        const long long end = min(base + (long long)q.tiles_per_pop, q.n_tiles);
+        for (long long tile = base; tile < end; ++tile) {
+            // request owning the tile: last prefix start <= tile (warp-uniform search)
+            int lo = 0, hi = q.n_items - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (q.tile_start[mid] <= tile) lo = mid;
+                else hi = mid - 1;
+            }
+            const GeoParams& p = q.items[lo];
+            const long long local = tile - q.tile_start[lo];
+            const int tiles_x = (p.gw + GBX - 1) / GBX;
+            geocode_block<GEO_LONLAT, FF>(p, (int)(local % tiles_x), (int)(local / tiles_x));
+            __syncthreads();
+        }
+    }
+}
+
 // A carrier on one radar line: Poly2d collapses to a polynomial in the
 // normalised range, d_j = sum_i c_ij yval^i (core/Poly2d.cpp:8-24 regrouped).
 constexpr int LINE_POLY_MAX = 8;
@@ -600,6 +638,28 @@ cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, in
     }
     if (launches) ++*launches;
     return cudaGetLastError();
+}
+
+cudaError_t launch_geocode_persistent(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s,
+                                      int64_t* launches) {
+    const dim3 block(GBX, GBY);
+    if (lonlat) {
+        if (ff) geocode_persistent<true, true><<<blocks, block, 0, s>>>(q);
+        else geocode_persistent<true, false><<<blocks, block, 0, s>>>(q);
+    } else {
+        if (ff) geocode_persistent<false, true><<<blocks, block, 0, s>>>(q);
+        else geocode_persistent<false, false><<<blocks, block, 0, s>>>(q);
+    }
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+int persistent_blocks_per_sm(bool lonlat, bool ff) {
+    int n = 0;
+    const void* f = lonlat ? (ff ? (const void*)geocode_persistent<true, true> : (const void*)geocode_persistent<true, false>)
+                           : (ff ? (const void*)geocode_persistent<false, true> : (const void*)geocode_persistent<false, false>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, GBX * GBY, 0);
+    return n;
 }
 
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches) {

@@ -68,9 +68,23 @@ struct DerampParams {
     AzRg az_car, rg_car;
 };
 
+// A batch of requests for the persistent kernel: per-request parameters in
+// device memory, the prefix sum of their tile counts, and the tile counter.
+struct BatchQueue {
+    const GeoParams* items;      // n_items
+    const long long* tile_start; // n_items + 1, tile_start[0] = 0
+    int32_t n_items, tiles_per_pop;
+    long long n_tiles;
+    long long* counter;          // zeroed before each launch
+};
+
 // launchers (gslc_kernels.cu)
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);
 cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s);
+cudaError_t launch_geocode_persistent(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s,
+                                      int64_t* launches);
+int persistent_blocks_per_sm(bool lonlat, bool ff);
+constexpr int TILE_X = 32, TILE_Y = 8;   // geogrid pixels per tile
 
 }  // namespace gslc

@@ -157,6 +157,29 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
     reference), ``az_index_block``/``rg_index_block`` (f64 outputs of the radar
     coordinates per geo pixel), ``dem_margin``, ``device`` and ``stream``.
     """
+    call = _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
+                           image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
+                           sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
+                           az_carrier, rg_carrier, az_time_correction, srange_correction,
+                           flatten_with_corrected_srange, invalid_value, carrier_phase_block, flatten_phase_block,
+                           geo2rdr_precision, inplace_deramp, az_index_block, rg_index_block, dem_margin)
+    dev = M.device_of(device)
+    lib = L.lib()
+    ctx = L.context(dev.index)
+    with torch.cuda.device(dev):
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        with torch.cuda.stream(s):
+            _geocode_on_stream(lib, ctx, s, dev, *call)
+
+
+def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
+                    image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
+                    sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
+                    az_carrier, rg_carrier, az_time_correction, srange_correction, flatten_with_corrected_srange,
+                    invalid_value, carrier_phase_block, flatten_phase_block, geo2rdr_precision, inplace_deramp,
+                    az_index_block, rg_index_block, dem_margin):
+    """Defaults and validation of geocode_slc (geocode_slc.py:192-213); the
+    arguments of _build_args in its order."""
     az_carrier = LUT2d() if az_carrier is None else az_carrier
     rg_carrier = LUT2d() if rg_carrier is None else rg_carrier
     az_time_correction = LUT2d() if az_time_correction is None else az_time_correction
@@ -193,92 +216,92 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
     if precision is None:
         raise ValueError(f"unknown geo2rdr_precision {geo2rdr_precision!r}")
 
-    dev = M.device_of(device)
-    lib = L.lib()
-    ctx = L.context(dev.index)
-    with torch.cuda.device(dev):
-        s = stream if stream is not None else torch.cuda.current_stream(dev)
-        with torch.cuda.stream(s):
-            _geocode_on_stream(lib, ctx, s, dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid,
-                               sliced_radargrid, geogrid, orbit, native_doppler, image_grid_doppler, ellipsoid,
-                               threshold_geo2rdr, num_iter_geo2rdr, mask_block, subswaths, first_azimuth_line,
-                               first_range_sample, flatten, reramp, az_carrier, rg_carrier, az_time_correction,
-                               srange_correction, flatten_with_corrected_srange, invalid_value,
-                               carrier_phase_block, flatten_phase_block, precision, inplace_deramp,
-                               az_index_block, rg_index_block, dem_margin)
+    return (rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sliced_radargrid, geogrid, orbit,
+            native_doppler, image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
+            subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
+            az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
+            carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
+            rg_index_block, dem_margin)
 
 
-def _geocode_on_stream(lib, ctx, s, dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid,
-                       sliced_radargrid, geogrid, orbit, native_doppler, image_grid_doppler, ellipsoid,
-                       threshold_geo2rdr, num_iter_geo2rdr, mask_block, subswaths, first_azimuth_line,
-                       first_range_sample, flatten, reramp, az_carrier, rg_carrier, az_time_correction,
-                       srange_correction, flatten_with_corrected_srange, invalid_value,
-                       carrier_phase_block, flatten_phase_block, precision, inplace_deramp,
-                       az_index_block, rg_index_block, dem_margin):
-    if True:
-        rdr = [_Staged(r, dev, True, torch.complex64) for r in rdr_data_blocks]
-        if any(r.host is not None for r in rdr) and inplace_deramp:
-            raise ValueError("inplace_deramp needs device-resident radar tensors")
-        geo = [_Staged(g, dev, False, torch.complex64) for g in geo_data_blocks]
-        outs = list(geo)
+def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sliced_radargrid, geogrid, orbit,
+                native_doppler, image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
+                subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
+                az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
+                carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
+                rg_index_block, dem_margin):
+    """Stage arrays on ``dev`` and fill a gslc_geocode_args.
 
-        def opt_out(arr, np_dtype, t_dtype, what, upload):
-            if arr is None or _size(arr) == 0:
-                return None
-            _check_dtype(arr, np_dtype, t_dtype, what)
-            st = _Staged(arr, dev, upload, t_dtype)
-            outs.append(st)
-            return st
+    Returns (args, outputs to copy back, objects to keep alive)."""
+    rdr = [_Staged(r, dev, True, torch.complex64) for r in rdr_data_blocks]
+    if any(r.host is not None for r in rdr) and inplace_deramp:
+        raise ValueError("inplace_deramp needs device-resident radar tensors")
+    geo = [_Staged(g, dev, False, torch.complex64) for g in geo_data_blocks]
+    outs = list(geo)
 
-        # the mask and radar coordinates are written at every pixel; the phase
-        # outputs only at valid ones, so those keep the caller's other values
-        mask = opt_out(mask_block, np.uint8, torch.uint8, "mask_block", False)
-        carrier = opt_out(carrier_phase_block, np.float64, torch.float64, "carrier_phase_block", True)
-        flat = opt_out(flatten_phase_block, np.float64, torch.float64, "flatten_phase_block", True)
-        azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block", False)
-        rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block", False)
+    def opt_out(arr, np_dtype, t_dtype, what, upload):
+        if arr is None or _size(arr) == 0:
+            return None
+        _check_dtype(arr, np_dtype, t_dtype, what)
+        st = _Staged(arr, dev, upload, t_dtype)
+        outs.append(st)
+        return st
 
-        holder = M.AzRgHolder()
-        a = L.GeocodeArgs()
-        a.radar_grid = M.radar_grid_desc(radargrid)
-        a.sliced_radar_grid = M.radar_grid_desc(sliced_radargrid)
-        a.geo_grid = M.geo_grid_desc(geogrid)
-        a.orbit = M.orbit_desc(orbit)
-        a.native_doppler = M.lut_desc(native_doppler, dev)
-        a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
-        a.az_time_correction = M.lut_desc(az_time_correction, dev)
-        a.srange_correction = M.lut_desc(srange_correction, dev)
-        a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
-        a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
-        a.ellipsoid_a, a.ellipsoid_e2 = ellipsoid.a, ellipsoid.e2
-        a.threshold_geo2rdr = float(threshold_geo2rdr)
-        a.numiter_geo2rdr = int(num_iter_geo2rdr)
-        a.flatten, a.reramp = int(bool(flatten)), int(bool(reramp))
-        a.flatten_with_corrected_srange = int(bool(flatten_with_corrected_srange))
-        a.first_azimuth_line, a.first_range_sample = int(first_azimuth_line), int(first_range_sample)
-        inv = complex(invalid_value)
-        a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
-        a.n_blocks = len(rdr)
-        a.inplace_deramp = int(bool(inplace_deramp))
-        a.rdr_length, a.rdr_width = rdr[0].dev.shape
-        rdr_ptrs = (C.c_void_p * len(rdr))(*[r.ptr() for r in rdr])
-        geo_ptrs = (C.c_void_p * len(geo))(*[g.ptr() for g in geo])
-        a.rdr_blocks = C.cast(rdr_ptrs, C.POINTER(C.c_void_p))
-        a.geo_blocks = C.cast(geo_ptrs, C.POINTER(C.c_void_p))
-        a.mask = mask.ptr() if mask else None
-        a.carrier_phase = carrier.ptr() if carrier else None
-        a.flatten_phase = flat.ptr() if flat else None
-        a.az_index = azi.ptr() if azi else None
-        a.rg_index = rgi.ptr() if rgi else None
-        a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
-        a.dem_margin = int(dem_margin)
-        a.geo2rdr_precision = precision
-        ss = None
-        if subswaths is not None:
-            ss = M.subswaths_desc(subswaths, dev)
-            a.subswaths = C.pointer(ss)
-        st = lib.gslc_geocode_slc(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
-        L.check(st, ctx, "geocode_slc")
-        for o in outs:
-            o.copy_back()
-        del dem_keep, holder
+    # the mask and radar coordinates are written at every pixel; the phase
+    # outputs only at valid ones, so those keep the caller's other values
+    mask = opt_out(mask_block, np.uint8, torch.uint8, "mask_block", False)
+    carrier = opt_out(carrier_phase_block, np.float64, torch.float64, "carrier_phase_block", True)
+    flat = opt_out(flatten_phase_block, np.float64, torch.float64, "flatten_phase_block", True)
+    azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block", False)
+    rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block", False)
+
+    holder = M.AzRgHolder()
+    a = L.GeocodeArgs()
+    a.radar_grid = M.radar_grid_desc(radargrid)
+    a.sliced_radar_grid = M.radar_grid_desc(sliced_radargrid)
+    a.geo_grid = M.geo_grid_desc(geogrid)
+    a.orbit = M.orbit_desc(orbit)
+    a.native_doppler = M.lut_desc(native_doppler, dev)
+    a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
+    a.az_time_correction = M.lut_desc(az_time_correction, dev)
+    a.srange_correction = M.lut_desc(srange_correction, dev)
+    a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
+    a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
+    a.ellipsoid_a, a.ellipsoid_e2 = ellipsoid.a, ellipsoid.e2
+    a.threshold_geo2rdr = float(threshold_geo2rdr)
+    a.numiter_geo2rdr = int(num_iter_geo2rdr)
+    a.flatten, a.reramp = int(bool(flatten)), int(bool(reramp))
+    a.flatten_with_corrected_srange = int(bool(flatten_with_corrected_srange))
+    a.first_azimuth_line, a.first_range_sample = int(first_azimuth_line), int(first_range_sample)
+    inv = complex(invalid_value)
+    a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
+    a.n_blocks = len(rdr)
+    a.inplace_deramp = int(bool(inplace_deramp))
+    a.rdr_length, a.rdr_width = rdr[0].dev.shape
+    rdr_ptrs = (C.c_void_p * len(rdr))(*[r.ptr() for r in rdr])
+    geo_ptrs = (C.c_void_p * len(geo))(*[g.ptr() for g in geo])
+    a.rdr_blocks = C.cast(rdr_ptrs, C.POINTER(C.c_void_p))
+    a.geo_blocks = C.cast(geo_ptrs, C.POINTER(C.c_void_p))
+    a.mask = mask.ptr() if mask else None
+    a.carrier_phase = carrier.ptr() if carrier else None
+    a.flatten_phase = flat.ptr() if flat else None
+    a.az_index = azi.ptr() if azi else None
+    a.rg_index = rgi.ptr() if rgi else None
+    a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
+    a.dem_margin = int(dem_margin)
+    a.geo2rdr_precision = precision
+    ss = None
+    if subswaths is not None:
+        ss = M.subswaths_desc(subswaths, dev)
+        a.subswaths = C.pointer(ss)
+    keep = [holder, rdr, geo, rdr_ptrs, geo_ptrs, dem_keep, ss]
+    return a, outs, keep
+
+
+def _geocode_on_stream(lib, ctx, s, dev, *args):
+    a, outs, keep = _build_args(dev, *args)
+    st = lib.gslc_geocode_slc(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
+    L.check(st, ctx, "geocode_slc")
+    for o in outs:
+        o.copy_back()
+    del keep

@@ -260,3 +260,73 @@ def kat_slc(scene, axis="x", height=0.0):
 
 def constant_dem_like(raster: Raster, value: float) -> Raster:
     return Raster(np.full_like(raster.data, np.float32(value)), raster.get_geotransform(), raster.get_epsg())
+
+
+def scene_bursts(seed: int = 4, n_az: int = 9, n_sw: int = 3, grid_px: int = 12000, spacing: float = 10.0,
+                 lines=(1200, 1800), samples=(16000, 24000), prf: float = 760.0, dem_arcsec: float = 1.0,
+                 device=None, epsg: int = 32611):
+    """TOPS-like burst set onto one shared UTM grid.
+
+    ``n_sw`` subswaths x ``n_az`` bursts; burst sizes are seeded uniform in
+    ``lines`` x ``samples``; C-band (0.0555 m), 2.33 m range spacing, PRF
+    ``prf`` (760 Hz: nine nominal 1500-line bursts then span ~120 km of
+    ground track); subswath starting ranges 16 km apart so three 46.6 km
+    slant-range swaths cover the grid's width; a quadratic azimuth steering
+    carrier per burst (Poly2d, 2000 Hz/s); zero Doppler; fBm DEM.  Each burst
+    gets the window of the shared grid its footprint covers (plus margin) and
+    complex64 Gaussian samples generated on ``device`` (torch, seeded).
+    """
+    import torch
+    rng = np.random.default_rng(seed)
+    model = CircularOrbitModel(lat0_deg=35.0, lon0_deg=-121.8)
+    wvl, dr = 0.0555, 2.33
+    n = n_az * n_sw
+    L_b = rng.integers(lines[0], lines[1] + 1, n)
+    W_b = rng.integers(samples[0], samples[1] + 1, n)
+    t_burst = 1500.0 / prf
+    t_first = 100.0
+    mid_t = t_first + 0.5 * n_az * t_burst
+    orbit = model.orbit(mid_t, 41, 10.0)
+    grids = []
+    for s in range(n_sw):
+        for k in range(n_az):
+            i = s * n_az + k
+            grids.append(RadarGridParameters(t_first + k * t_burst, wvl, prf, 800e3 + s * 16e3, dr, LookSide.Right,
+                                             int(L_b[i]), int(W_b[i]), EPOCH))
+    # shared grid centred on the whole burst set
+    corners = [_swath_bounds(model, g, 1500.0, n=3) for g in grids]
+    lon_all = np.concatenate([c[0] for c in corners])
+    lat_all = np.concatenate([c[1] for c in corners])
+    geogrid = _utm_grid_around(lon_all.mean(), lat_all.mean(), epsg, grid_px, grid_px, spacing)
+    d = dem_arcsec / 3600.0
+    x0, x1 = lon_all.min() - 0.1, lon_all.max() + 0.1
+    y0, y1 = lat_all.min() - 0.1, lat_all.max() + 0.1
+    nx, ny = int(np.ceil((x1 - x0) / d)), int(np.ceil((y1 - y0) / d))
+    dem = Raster(fbm_surface((ny, nx), 0.8, rng, 0.0, 3000.0), [x0, d, 0.0, y1, 0.0, -d], 4326)
+    gen = torch.Generator(device=device if device is not None else "cpu")
+    gen.manual_seed(seed)
+    bursts = []
+    for i, g in enumerate(grids):
+        lon, lat = _swath_bounds(model, g, 1500.0, n=5)
+        lo2, la2 = _swath_bounds(model, g, 0.0, n=5)
+        lon, lat = np.concatenate([lon, lo2]), np.concatenate([lat, la2])
+        ex, ny_ = utm_forward_host(epsg, np.radians(lon), np.radians(lat))
+        c0 = int(np.floor((ex.min() - geogrid.start_x) / spacing)) - 8
+        c1 = int(np.ceil((ex.max() - geogrid.start_x) / spacing)) + 8
+        r0 = int(np.floor((geogrid.start_y - ny_.max()) / spacing)) - 8
+        r1 = int(np.ceil((geogrid.start_y - ny_.min()) / spacing)) + 8
+        c0, c1 = max(c0, 0), min(c1, geogrid.width)
+        r0, r1 = max(r0, 0), min(r1, geogrid.length)
+        if c1 <= c0 or r1 <= r0:
+            continue
+        window = geogrid[r0:r1, c0:c1]
+        tm = g.sensing_mid
+        carrier = Poly2d([[0.0], [0.0], [np.pi * 2000.0]], x_mean=0.0, y_mean=tm, x_std=1.0, y_std=1.0)
+        slc = None
+        if device is not None:
+            slc = torch.randn((g.length, g.width), dtype=torch.complex64, device=device, generator=gen)
+        bursts.append(SimpleNamespace(radar_grid=g, window=window, window_offset=(r0, c0), az_carrier=carrier,
+                                      rg_carrier=Poly2d(np.zeros((1, 1))), slc=slc))
+    return SimpleNamespace(name="bursts", seed=seed, model=model, orbit=orbit, geogrid=geogrid, dem=dem,
+                           bursts=bursts, native_doppler=LUT2d(), image_grid_doppler=LUT2d(), ellipsoid=Ellipsoid(),
+                           threshold=1e-8, maxiter=25, prf=prf)

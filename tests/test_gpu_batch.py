@@ -1,0 +1,80 @@
+"""Batched form: one persistent, graph-captured launch over uneven bursts
+gives, for every burst, exactly the output of its plain geocode_slc call."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from isce3_gb300 import synth  # noqa: E402
+from isce3_gb300.batch import BatchTuning, GeocodeBatch, GeocodeRequest  # noqa: E402
+from isce3_gb300.geocode import geocode_slc  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def bursts():
+    return synth.scene_bursts(seed=5, n_az=3, n_sw=2, grid_px=1500, spacing=30.0, lines=(300, 420),
+                              samples=(2400, 3000), device="cuda")
+
+
+def _outputs(sc):
+    outs = []
+    for b in sc.bursts:
+        w = b.window
+        outs.append((torch.empty((w.length, w.width), dtype=torch.complex64, device="cuda"),
+                     torch.empty((w.length, w.width), dtype=torch.uint8, device="cuda")))
+    return outs
+
+
+def _requests(sc, outs):
+    return [GeocodeRequest(o[0], b.slc, sc.dem, b.radar_grid, b.window, sc.orbit, sc.native_doppler,
+                           sc.image_grid_doppler, sc.ellipsoid, sc.threshold, sc.maxiter,
+                           dict(mask_block=o[1], az_carrier=b.az_carrier, rg_carrier=b.rg_carrier))
+            for b, o in zip(sc.bursts, outs)]
+
+
+def _plain(sc, precision):
+    outs = _outputs(sc)
+    for b, (g, m) in zip(sc.bursts, outs):
+        geocode_slc(g, b.slc, sc.dem, b.radar_grid, b.window, sc.orbit, sc.native_doppler, sc.image_grid_doppler,
+                    sc.ellipsoid, sc.threshold, sc.maxiter, mask_block=m, az_carrier=b.az_carrier,
+                    rg_carrier=b.rg_carrier, geo2rdr_precision=precision)
+    return outs
+
+
+def _same(a, b):
+    for (g0, m0), (g1, m1) in zip(a, b):
+        assert torch.equal(m0, m1)
+        assert torch.equal(torch.view_as_real(g0).view(torch.int32), torch.view_as_real(g1).view(torch.int32))
+
+
+@pytest.mark.parametrize("precision,graph,pop", [("fp64", True, 2), ("ff", True, 4), ("fp64", False, 1)])
+def test_batch_equals_plain_calls(bursts, precision, graph, pop):
+    ref = _plain(bursts, precision)
+    outs = _outputs(bursts)
+    batch = GeocodeBatch(_requests(bursts, outs), precision, BatchTuning(tiles_per_pop=pop, use_graph=graph))
+    info = batch.info()
+    assert info["tiles"] > 0 and info["launches_per_run"] == len(bursts.bursts) + 1
+    for _ in range(2):                       # a replay recomputes the same bits
+        for g, m in outs:
+            g.fill_(0)
+            m.fill_(0)
+        batch.run()
+        _same(ref, outs)
+    valid = sum(int((m == 1).sum()) for _, m in outs)
+    assert valid > 0.2 * sum(m.numel() for _, m in outs)
+    batch.close()
+
+
+def test_batch_rejects_host_arrays(bursts):
+    b = bursts.bursts[0]
+    w = b.window
+    geo = np.zeros((w.length, w.width), np.complex64)
+    req = GeocodeRequest(geo, b.slc, bursts.dem, b.radar_grid, w, bursts.orbit, bursts.native_doppler,
+                         bursts.image_grid_doppler, bursts.ellipsoid, 1e-8, 25)
+    with pytest.raises(ValueError):
+        GeocodeBatch([req])
