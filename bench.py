@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the burst (batched vs plain) measurement")
+    p.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
     return p.parse_args()
 
 
@@ -378,6 +380,108 @@ def _max_over_ranks(x, world):
     return x
 
 
+def run_bursts(args):
+    """27 uneven TOPS-like bursts onto one 12000 x 12000 UTM grid: plain
+    per-burst calls against one batched persistent graph launch."""
+    import torch
+    from isce3_gb300 import synth
+    from isce3_gb300.autotune import time_batch, tune
+    from isce3_gb300.batch import GeocodeBatch, GeocodeRequest
+    from isce3_gb300.geocode import geocode_slc
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if args.workload == "frame":
+        sc = synth.scene_bursts(seed=4, device=dev)
+    else:
+        sc = synth.scene_bursts(seed=4, n_az=3, n_sw=3, grid_px=3000, spacing=20.0, lines=(500, 700),
+                                samples=(4000, 6000), device=dev)
+    outs = [(torch.empty((b.window.length, b.window.width), dtype=torch.complex64, device=dev),
+             torch.empty((b.window.length, b.window.width), dtype=torch.uint8, device=dev)) for b in sc.bursts]
+    npx = sum(b.window.length * b.window.width for b in sc.bursts)
+    common = (sc.dem,)
+    res = {"bursts": len(sc.bursts), "output_px": npx, "grid": [sc.geogrid.length, sc.geogrid.width],
+           "burst_lines": [min(b.radar_grid.length for b in sc.bursts), max(b.radar_grid.length for b in sc.bursts)],
+           "burst_samples": [min(b.radar_grid.width for b in sc.bursts), max(b.radar_grid.width for b in sc.bursts)],
+           "prf_hz": sc.prf, "wavelength_m": 0.0555, "range_spacing_m": 2.33,
+           "carrier": "Poly2d quadratic in azimuth time (2000 Hz/s)"}
+    steps = max(2, min(args.steps, 3))
+    for prec in ("fp64", "ff"):
+        def plain_pass():
+            for b, (g, m) in zip(sc.bursts, outs):
+                geocode_slc(g, b.slc, *common, b.radar_grid, b.window, sc.orbit, sc.native_doppler,
+                            sc.image_grid_doppler, sc.ellipsoid, sc.threshold, sc.maxiter, mask_block=m,
+                            az_carrier=b.az_carrier, rg_carrier=b.rg_carrier, geo2rdr_precision=prec)
+        plain_pass()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            plain_pass()
+        torch.cuda.synchronize()
+        ms_plain = (time.perf_counter() - t0) / steps * 1e3
+        ref = [(g.clone(), m.clone()) for g, m in outs]
+        valid = sum(int((m == 1).sum()) for _, m in outs)
+        reqs = [GeocodeRequest(g, b.slc, sc.dem, b.radar_grid, b.window, sc.orbit, sc.native_doppler,
+                               sc.image_grid_doppler, sc.ellipsoid, sc.threshold, sc.maxiter,
+                               dict(mask_block=m, az_carrier=b.az_carrier, rg_carrier=b.rg_carrier))
+                for b, (g, m) in zip(sc.bursts, outs)]
+        best, tried = tune(reqs, prec)
+        batch = GeocodeBatch(reqs, prec, best)
+        t0 = time.perf_counter()
+        ms_batch = time_batch(batch, steps)
+        wall_batch = (time.perf_counter() - t0) / (steps + 1) * 1e3
+        same = all(torch.equal(m0, m1) and torch.equal(torch.view_as_real(g0), torch.view_as_real(g1))
+                   for (g0, m0), (g1, m1) in zip(ref, outs))
+        info = batch.info()
+        batch.close()
+        res[prec] = {"plain_ms": ms_plain, "plain_px_per_s": npx / (ms_plain * 1e-3),
+                     "plain_timing": "host wall clock over sequential synchronous geocode_slc calls",
+                     "batched_ms": ms_batch, "batched_px_per_s": npx / (ms_batch * 1e-3),
+                     "batched_timing": "CUDA events around graph launches",
+                     "batched_wall_ms": wall_batch,
+                     "speedup": ms_plain / ms_batch, "valid_px": valid, "batched_equals_plain": bool(same),
+                     "tuning": {"tiles_per_pop": best.tiles_per_pop, "blocks_per_sm": best.blocks_per_sm,
+                                "tried_ms": {f"{k[0]}x{k[1]}" if isinstance(k, tuple) else k: v
+                                             for k, v in tried.items()}},
+                     "tiles": info["tiles"], "blocks": info["blocks"], "launches_per_run": info["launches_per_run"]}
+        del ref
+        torch.cuda.empty_cache()
+    return res
+
+
+def run_serving(args):
+    """Poisson arrivals (200 req/s) of geocode requests over 8 resident SLCs:
+    continuous-batching server against the plain per-request path."""
+    import torch
+    from isce3_gb300 import synth
+    from isce3_gb300.serve import GeocodeServer, ResidentStore, ServeRequest, serve_plain
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if args.workload == "frame":
+        sc = synth.scene_serving(seed=5, device=dev)
+        n_req = 200
+    else:
+        sc = synth.scene_serving(seed=5, n_slc=4, lines=(2048, 4096), samples=(2048, 4096), device=dev)
+        n_req = 60
+    store = ResidentStore(sc.dem, dev)
+    for s_ in sc.slcs:
+        store.add(s_.key, s_.slc, s_.radar_grid, s_.orbit, native_doppler=s_.native_doppler,
+                  az_carrier=s_.az_carrier, rg_carrier=s_.rg_carrier, copy=False)
+    torch.cuda.synchronize()
+    trace = synth.serving_trace(sc, n_requests=n_req, rate_hz=200.0, seed=6)
+    warm = synth.serving_trace(sc, n_requests=16, rate_hz=2000.0, side=(256, 1024), seed=7)
+    out = {"slcs": len(sc.slcs), "resident_bytes": store.nbytes, "requests": n_req, "rate_hz": 200.0,
+           "side_px": [256, 4096], "spacing_m": [10, 30], "budget_bytes": 150 * 10 ** 9,
+           "slc_shapes": [list(s_.radar_grid.shape) for s_ in sc.slcs]}
+    for prec in ("fp64", "ff"):
+        GeocodeServer(store, geo2rdr_precision=prec).serve([ServeRequest(k, g, t) for k, g, t in warm])
+        serve_plain(store, [ServeRequest(k, g, t) for k, g, t in warm], prec)
+        server = GeocodeServer(store, budget_bytes=150 * 10 ** 9, max_in_flight=4, max_batch=64,
+                               geo2rdr_precision=prec)
+        served = server.serve([ServeRequest(k, g, t) for k, g, t in trace])
+        plain = serve_plain(store, [ServeRequest(k, g, t) for k, g, t in trace], prec)
+        out[prec] = {"served": served, "plain": plain,
+                     "px_per_s_ratio": served["px_per_s"] / plain["px_per_s"] if plain["px_per_s"] else None}
+    return out
+
+
 def parity_sample(res, row0, rows, box, out):
     """GPU frame rows against the oracle's run on the same rows."""
     from oracle.compare import compare
@@ -446,6 +550,12 @@ def main():
         cpu, (row0, rows, box, out) = cpu_baseline(sc, args.cpu_seconds)
         par = parity_sample(res, row0, rows, box, out)
         par_ff = parity_sample(res["ff"], row0, rows, box, out)
+    batched = None
+    if not args.no_batched:
+        batched = run_bursts(args)
+    served = None
+    if not args.no_served:
+        served = run_serving(args)
     hbm_peak, peak_kind = peaks()
     kernel_s = res["kernel_ms"] * 1e-3
     achieved = res["alg_bytes"] / kernel_s / 1e9
@@ -468,6 +578,8 @@ def main():
         "geo2rdr_ff": {"value": res["ff"]["value"], "unit": UNIT, "ms_per_step": res["ff"]["ms"],
                        "kernel_ms": res["ff"]["kernel_ms"], "parity_sample": par_ff,
                        "note": "float-float (double-word FP32) Newton iterations, FP64 first iterate and range"},
+        "batched": batched,
+        "served": served,
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "cpu_baseline": cpu, "parity_sample": par,
     }

@@ -148,6 +148,9 @@ typedef struct {
     int32_t dem_margin;             /* DEM pixels of margin (reference default 50) */
     int32_t geo2rdr_precision;      /* 0 FP64 (reference numerics), 1 float-float */
     const gslc_subswaths* subswaths;  /* host pointer to descriptor, or NULL */
+    int32_t rdr_deramped;           /* 1: blocks already carry the deramp of these carriers (resident
+                                       stores deramp once); the reramp still applies */
+    int32_t _pad2;
 } gslc_geocode_args;
 
 int gslc_ctx_create(int device, gslc_ctx** out);
@@ -176,6 +179,15 @@ int gslc_sinc_table(float* out);
  * isce3.ext.isce3.geocode._geocode_slc in
  * python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:218-334). */
 int gslc_geocode_slc(gslc_ctx* ctx, const gslc_geocode_args* args, void* stream);
+
+/* carrierPhaseDeramp (cxx/isce3/geocode/geocodeSlc.cpp:240-274) on its own:
+ * dst = src * exp(-i float(rg_carrier(t, r) + az_carrier(t, r))) for a
+ * length x width block starting at (first_line, first_sample) of radar_grid.
+ * src == dst works in place.  With zero carriers it copies.  Resident stores
+ * deramp an SLC once and then geocode it with rdr_deramped = 1. */
+int gslc_deramp_block(gslc_ctx* ctx, const gslc_radar_grid* radar_grid, const gslc_azrg_func* az_carrier,
+                      const gslc_azrg_func* rg_carrier, int64_t first_line, int64_t first_sample,
+                      const void* src, void* dst, int64_t length, int64_t width, void* stream);
 
 /* Number of the library's own kernels launched by the last call on ctx. */
 int64_t gslc_last_launch_count(const gslc_ctx* ctx);
@@ -211,8 +223,12 @@ typedef struct {
     int32_t _pad;
 } gslc_batch_tuning;
 
+/* Device buffers are allocated and filled in the order of `stream`
+ * (cudaMallocAsync / cudaMemcpyAsync), so creating, launching and destroying
+ * batches never synchronises the device: launch a batch on its creation
+ * stream (or after it); destroy releases its buffers in that stream's order. */
 int gslc_batch_create(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
-                      int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, gslc_batch** out);
+                      int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, void* stream, gslc_batch** out);
 int gslc_batch_launch(gslc_batch* batch, void* stream);     /* enqueue only */
 int gslc_batch_status(gslc_batch* batch, void* stream);     /* synchronise the stream, report errors */
 int gslc_batch_info(const gslc_batch* batch, int64_t* n_tiles, int32_t* blocks, int32_t* tiles_per_pop,

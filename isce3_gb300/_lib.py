@@ -131,7 +131,7 @@ class GeocodeArgs(C.Structure):
                 ("mask", C.c_void_p), ("carrier_phase", C.c_void_p), ("flatten_phase", C.c_void_p),
                 ("az_index", C.c_void_p), ("rg_index", C.c_void_p), ("dem", DemRaster),
                 ("dem_margin", C.c_int32), ("geo2rdr_precision", C.c_int32),
-                ("subswaths", C.POINTER(SubSwathsDesc))]
+                ("subswaths", C.POINTER(SubSwathsDesc)), ("rdr_deramped", C.c_int32), ("_pad2", C.c_int32)]
 
 
 class BatchTuning(C.Structure):
@@ -156,12 +156,15 @@ _EXPORTS = {
     "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),
     "gslc_batch_create": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_int32, C.c_int32,
-                                    C.POINTER(BatchTuning), C.POINTER(C.c_void_p)]),
+                                    C.POINTER(BatchTuning), C.c_void_p, C.POINTER(C.c_void_p)]),
     "gslc_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gslc_batch_status": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gslc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int64)]),
     "gslc_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gslc_deramp_block": (C.c_int, [C.c_void_p, C.POINTER(RadarGrid), C.POINTER(AzRgFunc), C.POINTER(AzRgFunc),
+                                    C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                    C.c_void_p]),
 }
 
 _lock = threading.Lock()

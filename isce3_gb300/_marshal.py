@@ -102,7 +102,11 @@ def orbit_desc(o: Orbit) -> L.OrbitDesc:
 
 
 def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.device):
-    """Descriptor with only the DEM window of ``geogrid`` resident on ``dev``."""
+    """Descriptor with only the DEM window of ``geogrid`` resident on ``dev``
+    (or the whole raster, when ``raster.to_device`` made it resident)."""
+    res = getattr(raster, "resident", None)
+    if res is not None and res.device == dev:
+        return dem_raster_desc_resident(res, raster.get_geotransform(), raster.get_epsg()), res
     d = L.DemRaster()
     d.width, d.length = raster.width, raster.length
     gt = raster.get_geotransform()

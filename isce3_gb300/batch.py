@@ -49,7 +49,7 @@ class GeocodeRequest:
                   az_time_correction=None, srange_correction=None, flatten_with_corrected_srange=False,
                   invalid_value=complex(float("nan"), float("nan")), carrier_phase_block=None,
                   flatten_phase_block=None, inplace_deramp=False, az_index_block=None, rg_index_block=None,
-                  dem_margin=50)
+                  dem_margin=50, rdr_deramped=False)
         unknown = set(self.kwargs) - set(kw)
         if unknown:
             raise TypeError(f"unknown geocode_slc arguments {sorted(unknown)}")
@@ -62,7 +62,8 @@ class GeocodeRequest:
                                kw["rg_carrier"], kw["az_time_correction"], kw["srange_correction"],
                                kw["flatten_with_corrected_srange"], kw["invalid_value"],
                                kw["carrier_phase_block"], kw["flatten_phase_block"], precision,
-                               kw["inplace_deramp"], kw["az_index_block"], kw["rg_index_block"], kw["dem_margin"])
+                               kw["inplace_deramp"], kw["az_index_block"], kw["rg_index_block"], kw["dem_margin"],
+                               kw["rdr_deramped"])
 
 
 @dataclass
@@ -82,7 +83,7 @@ class GeocodeBatch:
     """A bound batch of geocode requests; ``launch()`` runs them all at once."""
 
     def __init__(self, requests: list[GeocodeRequest], geo2rdr_precision: str = "fp64",
-                 tuning: BatchTuning | None = None, device=None):
+                 tuning: BatchTuning | None = None, device=None, stream: torch.cuda.Stream | None = None):
         self.dev = M.device_of(device)
         self.precision = geo2rdr_precision
         self.tuning = tuning or BatchTuning()
@@ -102,11 +103,15 @@ class GeocodeBatch:
                     raise ValueError("batched requests need CUDA tensors for their outputs")
                 arr[i] = a
                 self._keep.append(keep)
-            torch.cuda.synchronize(self.dev)       # staged metadata is resident before binding
+            # the batch's buffers are ordered on this stream (staging ran on the current one)
+            self.stream = stream or torch.cuda.current_stream(self.dev)
+            if self.stream != torch.cuda.current_stream(self.dev):
+                self.stream.wait_stream(torch.cuda.current_stream(self.dev))
             h = C.c_void_p()
             tc = self.tuning.to_c()
             prec = 1 if geo2rdr_precision in ("ff", "float-float") else 0
-            st = self.lib.gslc_batch_create(self.ctx, arr, n, prec, C.byref(tc), C.byref(h))
+            st = self.lib.gslc_batch_create(self.ctx, arr, n, prec, C.byref(tc), C.c_void_p(self.stream.cuda_stream),
+                                            C.byref(h))
             L.check(st, self.ctx, "gslc_batch_create")
         self.handle = h
         self._args = arr
@@ -118,11 +123,11 @@ class GeocodeBatch:
         return {"tiles": nt.value, "blocks": bl.value, "tiles_per_pop": tp.value, "launches_per_run": nl.value}
 
     def launch(self, stream: torch.cuda.Stream | None = None) -> None:
-        s = stream or torch.cuda.current_stream(self.dev)
+        s = stream or self.stream
         L.check(self.lib.gslc_batch_launch(self.handle, C.c_void_p(s.cuda_stream)), self.ctx, "gslc_batch_launch")
 
     def wait(self, stream: torch.cuda.Stream | None = None) -> None:
-        s = stream or torch.cuda.current_stream(self.dev)
+        s = stream or self.stream
         L.check(self.lib.gslc_batch_status(self.handle, C.c_void_p(s.cuda_stream)), self.ctx, "gslc_batch")
 
     def run(self, stream=None) -> None:

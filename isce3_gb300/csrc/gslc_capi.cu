@@ -623,7 +623,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     std::vector<const float2*> rdr(a->n_blocks);
     for (int b = 0; b < a->n_blocks; ++b) rdr[b] = (const float2*)a->rdr_blocks[b];
     if (c->timing) cudaEventRecord(c->ev[2], stream);
-    if (!p.carriers_zero && nrdr > 0) {
+    if (!p.carriers_zero && nrdr > 0 && !a->rdr_deramped) {
         for (int b = 0; b < a->n_blocks; ++b) {
             float2* dst = (float2*)a->rdr_blocks[b];
             if (!a->inplace_deramp) {
@@ -830,7 +830,7 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     if (!to_azrg(&c, a->az_carrier, az, "az_carrier") && !to_azrg(&c, a->rg_carrier, rg, "rg_carrier"))
         carriers = !(az.is_zero && rg.is_zero);
     const int64_t nrdr = a->rdr_length * a->rdr_width;
-    if (carriers && !a->inplace_deramp && nrdr > 0) {
+    if (carriers && !a->inplace_deramp && !a->rdr_deramped && nrdr > 0) {
         // deramp works on a copy in the static scratch; the caller's blocks stay as given
         if (nrdr * a->n_blocks > NOALLOC_MAX_DERAMP)
             return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL,
@@ -871,7 +871,8 @@ struct gslc_batch {
     double* d_orbit = nullptr;
     float2* d_scratch = nullptr;
     int32_t* d_err = nullptr;
-    int32_t* h_err = nullptr;
+    int32_t h_err[4] = {0, 0, 0, 0};
+    cudaStream_t stream = nullptr;  // creation stream: allocation and release order
     std::vector<DerampParams> deramps;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -903,7 +904,7 @@ cudaError_t batch_enqueue(gslc_batch* b, cudaStream_t s) {
 }  // namespace
 
 extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, int32_t n, int32_t precision,
-                                 const gslc_batch_tuning* tuning, gslc_batch** out) {
+                                 const gslc_batch_tuning* tuning, void* stream_, gslc_batch** out) {
     if (!c || !out) return GSLC_EINVAL;
     *out = nullptr;
     c->err.clear();
@@ -914,6 +915,8 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
     if (!b) return set_err(c, GSLC_ECUDA, "out of host memory");
     b->ctx = c;
     b->device = c->device;
+    b->stream = (cudaStream_t)stream_;
+    const cudaStream_t st_ = b->stream;
 
     std::vector<GeoParams> params;
     std::vector<std::vector<double>> coefs;
@@ -932,7 +935,8 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
         (p.geo_is_lonlat ? any_ll : any_utm) = true;
         const gslc_geocode_args& a = items[i];
         const int64_t nrdr = a.rdr_length * a.rdr_width;
-        if (!p.carriers_zero && nrdr > 0 && !a.inplace_deramp) scratch_total += (size_t)nrdr * a.n_blocks;
+        if (!p.carriers_zero && nrdr > 0 && !a.inplace_deramp && !a.rdr_deramped)
+            scratch_total += (size_t)nrdr * a.n_blocks;
         for (int b0 = 0; b0 < a.n_blocks; b0 += MAX_BLOCKS) {
             GeoParams q = p;
             q.nblk = std::min(MAX_BLOCKS, a.n_blocks - b0);
@@ -952,13 +956,13 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
         *out = b;
         return GSLC_OK;
     }
-    e = cudaMalloc(&b->d_orbit, coef_total * sizeof(double));
-    if (e == cudaSuccess && scratch_total) e = cudaMalloc(&b->d_scratch, scratch_total * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_items, params.size() * sizeof(GeoParams));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_start, (params.size() + 1) * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(int32_t) * 4);
-    if (e == cudaSuccess) e = cudaMallocHost(&b->h_err, sizeof(int32_t) * 4);
+    e = cudaMallocAsync((void**)&b->d_orbit, coef_total * sizeof(double), st_);
+    if (e == cudaSuccess && scratch_total)
+        e = cudaMallocAsync((void**)&b->d_scratch, scratch_total * sizeof(float2), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_items, params.size() * sizeof(GeoParams), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_tile_start, (params.size() + 1) * sizeof(long long), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_counter, sizeof(long long), st_);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_err, sizeof(int32_t) * 4, st_);
     if (e != cudaSuccess) {
         gslc_batch_destroy(b);
         return cuda_err(c, e, "batch allocation");
@@ -968,7 +972,8 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
     size_t off = 0;
     for (const auto& cf : coefs) {
         coef_off.push_back(off);
-        e = cudaMemcpy(b->d_orbit + off, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice);
+        // pageable sources are staged by the runtime before the call returns
+        e = cudaMemcpyAsync(b->d_orbit + off, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
         if (e != cudaSuccess) break;
         off += cf.size();
     }
@@ -998,7 +1003,7 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
         for (int k = 0; k < p.nblk; ++k) {
             const float2* src = (const float2*)a.rdr_blocks[block_base + k];
             const float2* use = src;
-            if (!p.carriers_zero && nrdr > 0) {
+            if (!p.carriers_zero && nrdr > 0 && !a.rdr_deramped) {
                 float2* dst = a.inplace_deramp ? const_cast<float2*>(src) : b->d_scratch + scratch_off;
                 if (!a.inplace_deramp) scratch_off += nrdr;
                 DerampParams dp;
@@ -1020,10 +1025,11 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
         tile_start[j + 1] = tile_start[j] + tiles;
     }
     if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_items, params.data(), params.size() * sizeof(GeoParams), cudaMemcpyHostToDevice);
+        e = cudaMemcpyAsync(b->d_items, params.data(), params.size() * sizeof(GeoParams), cudaMemcpyHostToDevice,
+                            st_);
     if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_tile_start, tile_start.data(), tile_start.size() * sizeof(long long),
-                       cudaMemcpyHostToDevice);
+        e = cudaMemcpyAsync(b->d_tile_start, tile_start.data(), tile_start.size() * sizeof(long long),
+                            cudaMemcpyHostToDevice, st_);
     if (e != cudaSuccess) {
         gslc_batch_destroy(b);
         return cuda_err(c, e, "batch upload");
@@ -1073,6 +1079,7 @@ extern "C" int gslc_batch_status(gslc_batch* b, void* stream) {
     if (!b) return GSLC_EINVAL;
     if (!b->q.n_items) return GSLC_OK;
     cudaError_t e = cudaMemcpyAsync(b->h_err, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    // (a pageable destination: the copy has completed when the call returns)
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return batch_fail(b, b->ctx, GSLC_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
     if (b->h_err[0] & 1) return batch_fail(b, b->ctx, GSLC_EPROJ, "Inverse projection transformation failed");
@@ -1095,13 +1102,39 @@ extern "C" int gslc_batch_destroy(gslc_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
-    cudaFree(b->d_items);
-    cudaFree(b->d_tile_start);
-    cudaFree(b->d_counter);
-    cudaFree(b->d_orbit);
-    cudaFree(b->d_scratch);
-    cudaFree(b->d_err);
-    if (b->h_err) cudaFreeHost(b->h_err);
+    for (void* ptr : {(void*)b->d_items, (void*)b->d_tile_start, (void*)b->d_counter, (void*)b->d_orbit,
+                      (void*)b->d_scratch, (void*)b->d_err})
+        if (ptr) cudaFreeAsync(ptr, b->stream);
     delete b;
     return GSLC_OK;
+}
+
+// geocodeSlc.cpp:240-274 (carrierPhaseDeramp) as a call of its own: dst =
+// src * exp(-i float(rg_carrier + az_carrier)) for a block whose first sample
+// is (first_line, first_sample) of radar_grid.  src == dst deramps in place.
+extern "C" int gslc_deramp_block(gslc_ctx* c, const gslc_radar_grid* rg, const gslc_azrg_func* az_carrier,
+                                 const gslc_azrg_func* rg_carrier, int64_t first_line, int64_t first_sample,
+                                 const void* src, void* dst, int64_t length, int64_t width, void* stream) {
+    if (!c || !rg || !az_carrier || !rg_carrier || !src || !dst || length < 0 || width < 0) return GSLC_EINVAL;
+    c->err.clear();
+    DerampParams dp;
+    std::memset(&dp, 0, sizeof(dp));
+    if (int st = to_azrg(c, *az_carrier, dp.az_car, "az_carrier")) return st;
+    if (int st = to_azrg(c, *rg_carrier, dp.rg_car, "rg_carrier")) return st;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    dp.src = (const float2*)src;
+    dp.dst = (float2*)dst;
+    dp.inL = length; dp.inW = width;
+    dp.az_first = first_line; dp.rg_first = first_sample;
+    dp.rg_t0 = rg->sensing_start; dp.rg_prf = rg->prf; dp.rg_r0 = rg->starting_range;
+    dp.rg_dr = rg->range_pixel_spacing; dp.inv_prf = 1.0 / rg->prf;
+    if (dp.az_car.is_zero && dp.rg_car.is_zero) {
+        if (src != dst) e = cudaMemcpyAsync(dst, src, length * width * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                            (cudaStream_t)stream);
+        return e == cudaSuccess ? GSLC_OK : cuda_err(c, e, "copy");
+    }
+    c->launches = 0;
+    e = launch_deramp(dp, (cudaStream_t)stream, &c->launches);
+    return e == cudaSuccess ? GSLC_OK : cuda_err(c, e, "deramp launch");
 }

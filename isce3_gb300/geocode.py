@@ -146,7 +146,7 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
                 invalid_value=np.nan + np.nan * 1j,
                 carrier_phase_block=None, flatten_phase_block=None, *,
                 geo2rdr_precision: str = "fp64", inplace_deramp: bool = False,
-                az_index_block=None, rg_index_block=None, dem_margin: int = 50,
+                az_index_block=None, rg_index_block=None, dem_margin: int = 50, rdr_deramped: bool = False,
                 device=None, stream: torch.cuda.Stream | None = None) -> None:
     """Geocode radar SLC arrays sharing one radar grid onto one geogrid.
 
@@ -155,14 +155,17 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
     arguments: ``geo2rdr_precision`` ("fp64" reference numerics, or "ff"
     float-float), ``inplace_deramp`` (mutate device radar tensors like the
     reference), ``az_index_block``/``rg_index_block`` (f64 outputs of the radar
-    coordinates per geo pixel), ``dem_margin``, ``device`` and ``stream``.
+    coordinates per geo pixel), ``dem_margin``, ``rdr_deramped`` (the radar
+    blocks already carry the carrier deramp, as resident stores keep them),
+    ``device`` and ``stream``.
     """
     call = _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
                            image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
                            sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
                            az_carrier, rg_carrier, az_time_correction, srange_correction,
                            flatten_with_corrected_srange, invalid_value, carrier_phase_block, flatten_phase_block,
-                           geo2rdr_precision, inplace_deramp, az_index_block, rg_index_block, dem_margin)
+                           geo2rdr_precision, inplace_deramp, az_index_block, rg_index_block, dem_margin,
+                           rdr_deramped)
     dev = M.device_of(device)
     lib = L.lib()
     ctx = L.context(dev.index)
@@ -177,7 +180,7 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
                     sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
                     az_carrier, rg_carrier, az_time_correction, srange_correction, flatten_with_corrected_srange,
                     invalid_value, carrier_phase_block, flatten_phase_block, geo2rdr_precision, inplace_deramp,
-                    az_index_block, rg_index_block, dem_margin):
+                    az_index_block, rg_index_block, dem_margin, rdr_deramped=False):
     """Defaults and validation of geocode_slc (geocode_slc.py:192-213); the
     arguments of _build_args in its order."""
     az_carrier = LUT2d() if az_carrier is None else az_carrier
@@ -221,7 +224,7 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
             subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
             az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
             carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
-            rg_index_block, dem_margin)
+            rg_index_block, dem_margin, rdr_deramped)
 
 
 def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sliced_radargrid, geogrid, orbit,
@@ -229,7 +232,7 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
                 subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
                 az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
                 carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
-                rg_index_block, dem_margin):
+                rg_index_block, dem_margin, rdr_deramped=False):
     """Stage arrays on ``dev`` and fill a gslc_geocode_args.
 
     Returns (args, outputs to copy back, objects to keep alive)."""
@@ -277,6 +280,7 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
     a.n_blocks = len(rdr)
     a.inplace_deramp = int(bool(inplace_deramp))
+    a.rdr_deramped = int(bool(rdr_deramped))
     a.rdr_length, a.rdr_width = rdr[0].dev.shape
     rdr_ptrs = (C.c_void_p * len(rdr))(*[r.ptr() for r in rdr])
     geo_ptrs = (C.c_void_p * len(geo))(*[g.ptr() for g in geo])

@@ -67,6 +67,13 @@ class Raster:
     def dy(self) -> float:
         return self._gt[5]
 
+    def to_device(self, device) -> "Raster":
+        """Keep the whole raster resident on ``device``; geocode calls then
+        index it in place instead of uploading their DEM window."""
+        import torch
+        self.resident = torch.from_numpy(self.data).to(device)
+        return self
+
     def save(self, path) -> None:
         p = Path(path)
         np.save(p.with_suffix(".npy"), self.data)

@@ -330,3 +330,63 @@ def scene_bursts(seed: int = 4, n_az: int = 9, n_sw: int = 3, grid_px: int = 120
     return SimpleNamespace(name="bursts", seed=seed, model=model, orbit=orbit, geogrid=geogrid, dem=dem,
                            bursts=bursts, native_doppler=LUT2d(), image_grid_doppler=LUT2d(), ellipsoid=Ellipsoid(),
                            threshold=1e-8, maxiter=25, prf=prf)
+
+
+def scene_serving(seed: int = 5, n_slc: int = 8, lines=(4096, 16384), samples=(4096, 12000), device=None,
+                  epsg: int = 32611, dem_arcsec: float = 1.0):
+    """Resident SLCs for the serving workload: ``n_slc`` complex64 Gaussian
+    SLCs (seeded sizes in ``lines`` x ``samples``), each from its own pass
+    (orbit shifted in longitude), with a native-Doppler LUT2d (quadratic in
+    range, +-50 Hz) and a linear azimuth carrier, over one shared fBm DEM."""
+    import torch
+    rng = np.random.default_rng(seed)
+    prf, dr, r0, wvl = 1520.0, 6.25, 850e3, 0.24
+    slcs = []
+    lon_all, lat_all = [], []
+    for i in range(n_slc):
+        model = CircularOrbitModel(lat0_deg=35.0 + 0.05 * i, lon0_deg=-121.8 + 0.12 * i)
+        g = RadarGridParameters(100.0, wvl, prf, r0, dr, LookSide.Right, int(rng.integers(lines[0], lines[1] + 1)),
+                                int(rng.integers(samples[0], samples[1] + 1)), EPOCH)
+        orbit = model.orbit(g.sensing_mid, 21, 10.0)
+        lon, lat = _swath_bounds(model, g, 1500.0, n=5)
+        lon_all.append(lon)
+        lat_all.append(lat)
+        rr = np.linspace(g.starting_range - 200 * dr, g.end_range + 200 * dr, 32)
+        tt = np.linspace(g.sensing_start - 200 / prf, g.sensing_stop + 200 / prf, 32)
+        u = (rr - rr.mean()) / (rr.max() - rr.mean())
+        dop = LUT2d(rr, tt, np.tile(-50.0 + 100.0 * u ** 2, (32, 1)))
+        carrier = Poly2d([[0.0], [2 * np.pi * 300.0]], y_mean=g.sensing_mid)
+        slcs.append(SimpleNamespace(key=i, model=model, radar_grid=g, orbit=orbit, native_doppler=dop,
+                                    az_carrier=carrier, rg_carrier=Poly2d(np.zeros((1, 1))), lon=lon, lat=lat))
+    lon_all, lat_all = np.concatenate(lon_all), np.concatenate(lat_all)
+    d = dem_arcsec / 3600.0
+    x0, x1 = lon_all.min() - 0.25, lon_all.max() + 0.25
+    y0, y1 = lat_all.min() - 0.25, lat_all.max() + 0.25
+    nx, ny = int(np.ceil((x1 - x0) / d)), int(np.ceil((y1 - y0) / d))
+    dem = Raster(fbm_surface((ny, nx), 0.8, rng, 0.0, 3000.0), [x0, d, 0.0, y1, 0.0, -d], 4326)
+    if device is not None:
+        gen = torch.Generator(device=device)
+        gen.manual_seed(seed)
+        for s in slcs:
+            s.slc = torch.randn(s.radar_grid.shape, dtype=torch.complex64, device=device, generator=gen)
+    return SimpleNamespace(slcs=slcs, dem=dem, epsg=epsg, seed=seed)
+
+
+def serving_trace(scene, n_requests: int = 300, rate_hz: float = 200.0, side=(256, 4096), spacing=(10.0, 30.0),
+                  seed: int = 6):
+    """Poisson arrivals of geocode requests: each picks a resident SLC, a
+    square UTM geogrid of log-uniform side in ``side`` pixels and uniform
+    spacing in ``spacing`` metres, centred at a random point of the SLC's
+    footprint.  Returns (slc key, GeoGridParameters, arrival s) tuples."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate_hz, n_requests))
+    out = []
+    for k in range(n_requests):
+        s = scene.slcs[int(rng.integers(len(scene.slcs)))]
+        n = int(np.exp(rng.uniform(np.log(side[0]), np.log(side[1]))))
+        sp = float(np.round(rng.uniform(*spacing), 1))
+        f = rng.uniform(0.25, 0.75, 2)
+        lon_c = s.lon.min() + f[0] * (s.lon.max() - s.lon.min())
+        lat_c = s.lat.min() + f[1] * (s.lat.max() - s.lat.min())
+        out.append((s.key, _utm_grid_around(lon_c, lat_c, scene.epsg, n, n, sp), float(t[k] - t[0])))
+    return out

@@ -1,0 +1,51 @@
+"""Serving loop on the GPU: requests arriving while earlier batches run are
+admitted into later batches on other streams, and every result equals the
+same request geocoded alone."""
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from isce3_gb300 import synth  # noqa: E402
+from isce3_gb300.serve import GeocodeServer, ResidentStore, ServeRequest, serve_plain  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def served():
+    sc = synth.scene_serving(seed=8, n_slc=3, lines=(1024, 2048), samples=(1024, 2048), device="cuda")
+    store = ResidentStore(sc.dem)
+    for s in sc.slcs:
+        store.add(s.key, s.slc, s.radar_grid, s.orbit, native_doppler=s.native_doppler, az_carrier=s.az_carrier,
+                  rg_carrier=s.rg_carrier)
+    trace = synth.serving_trace(sc, n_requests=24, rate_hz=2000.0, side=(64, 512), spacing=(10.0, 30.0), seed=9)
+    return sc, store, trace
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+def test_served_results_equal_alone(served, precision):
+    sc, store, trace = served
+    mixed = [ServeRequest(k, g, t) for k, g, t in trace]
+    server = GeocodeServer(store, budget_bytes=2 * 10 ** 9, max_in_flight=3, max_batch=6,
+                           geo2rdr_precision=precision)
+    stats = server.serve(mixed, keep_outputs=True)
+    assert stats["completed"] == len(trace) and stats["batches"] >= 2
+    alone = [ServeRequest(k, g, 0.0) for k, g, _ in trace]
+    serve_plain(store, alone, geo2rdr_precision=precision, keep_outputs=True)
+    for a, b in zip(sorted(mixed, key=lambda r: r.arrival), alone):
+        assert torch.equal(a.mask, b.mask)
+        assert torch.equal(torch.view_as_real(a.geo), torch.view_as_real(b.geo))
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
+
+
+def test_budget_limits_concurrency(served):
+    sc, store, trace = served
+    reqs = [ServeRequest(k, g, 0.0) for k, g, _ in trace[:8]]
+    biggest = max(r.footprint for r in reqs)
+    server = GeocodeServer(store, budget_bytes=biggest, max_in_flight=3, max_batch=8)
+    stats = server.serve(reqs)
+    assert stats["completed"] == 8
+    assert stats["max_concurrent_batches"] >= 1
