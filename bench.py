@@ -557,6 +557,12 @@ def main():
     if not args.no_served:
         served = run_serving(args)
     hbm_peak, peak_kind = peaks()
+    traffic = None
+    prof = ROOT / "profiles" / "geocode_kernel_medium_v2.md"
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("dram_bytes_per_output_px:"):
+                traffic = float(line.split(":")[1]) * res["npx"]
     kernel_s = res["kernel_ms"] * 1e-3
     achieved = res["alg_bytes"] / kernel_s / 1e9
     value = res["npx"] * world / (res["ms"] * 1e-3)
@@ -567,7 +573,9 @@ def main():
         "config": workload_config(sc, args, world),
         "valid_px_per_s": res["n_valid"] * world / (res["ms"] * 1e-3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": f"{peak_kind} hbm_gbs",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": "ncu dram bytes/px of the medium capture (profiles/geocode_kernel_medium_v2.md)"
+                                       " x frame px", "peak_source": f"{peak_kind} hbm_gbs",
                      "kernel": "geocode_kernel (fused)", "kernel_ms": res["kernel_ms"],
                      "alg_bytes_per_launch": res["alg_bytes"],
                      "alg_bytes_terms": {"geo_out": 8 * res["npx"], "mask": res["npx"], "slc": 8 * res["n_slc"],

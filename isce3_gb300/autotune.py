@@ -71,7 +71,11 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
         return BatchTuning(c["tiles_per_pop"], c["blocks_per_sm"], True), {"cached": c["ms"]}
     occ = max(1, info["blocks"] // torch.cuda.get_device_properties(0).multi_processor_count)
     if candidates is None:
-        candidates = [BatchTuning(p, b) for p in (1, 2, 4, 8) for b in sorted({occ, max(1, occ - 1)})]
+        if info["tiles"] > 200_000:     # large batches: a short search, one timed launch each
+            candidates = [BatchTuning(p, occ) for p in (1, 2, 4)]
+            reps = 1
+        else:
+            candidates = [BatchTuning(p, b) for p in (1, 2, 4, 8) for b in sorted({occ, max(1, occ - 1)})]
     results = {}
     best, best_ms = None, float("inf")
     probe.close()
