@@ -471,11 +471,14 @@ def run_serving(args):
            "side_px": [256, 4096], "spacing_m": [10, 30], "budget_bytes": 150 * 10 ** 9,
            "slc_shapes": [list(s_.radar_grid.shape) for s_ in sc.slcs]}
     for prec in ("fp64", "ff"):
-        GeocodeServer(store, geo2rdr_precision=prec).serve([ServeRequest(k, g, t) for k, g, t in warm])
+        warm_server = GeocodeServer(store, geo2rdr_precision=prec)
+        warm_server.serve([ServeRequest(k, g, t) for k, g, t in warm])
+        warm_server.close()
         serve_plain(store, [ServeRequest(k, g, t) for k, g, t in warm], prec)
-        server = GeocodeServer(store, budget_bytes=150 * 10 ** 9, max_in_flight=4, max_batch=64,
-                               geo2rdr_precision=prec)
+        server = GeocodeServer(store, budget_bytes=150 * 10 ** 9, max_in_flight=3, max_batch=64,
+                               geo2rdr_precision=prec, per_request_completion=True)
         served = server.serve([ServeRequest(k, g, t) for k, g, t in trace])
+        server.close()
         plain = serve_plain(store, [ServeRequest(k, g, t) for k, g, t in trace], prec)
         out[prec] = {"served": served, "plain": plain,
                      "px_per_s_ratio": served["px_per_s"] / plain["px_per_s"] if plain["px_per_s"] else None}

@@ -229,6 +229,16 @@ typedef struct {
  * stream (or after it); destroy releases its buffers in that stream's order. */
 int gslc_batch_create(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
                       int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, void* stream, gslc_batch** out);
+/* As gslc_batch_create, with per-request completion: done_flags is
+ * n_requests words of mapped host memory (gslc_host_flags_create) that the
+ * kernel sets to 1 when the last tile of request i has been written, while
+ * the rest of the batch still runs.  The caller clears them before a launch. */
+int gslc_batch_create_signaled(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
+                               int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, void* stream,
+                               uint32_t* done_flags, gslc_batch** out);
+/* Mapped, device-visible host words for completion flags (cleared). */
+int gslc_host_flags_create(int32_t n, uint32_t** host);
+int gslc_host_flags_destroy(uint32_t* host);
 int gslc_batch_launch(gslc_batch* batch, void* stream);     /* enqueue only */
 int gslc_batch_status(gslc_batch* batch, void* stream);     /* synchronise the stream, report errors */
 int gslc_batch_info(const gslc_batch* batch, int64_t* n_tiles, int32_t* blocks, int32_t* tiles_per_pop,

@@ -157,6 +157,11 @@ _EXPORTS = {
     "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),
     "gslc_batch_create": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_int32, C.c_int32,
                                     C.POINTER(BatchTuning), C.c_void_p, C.POINTER(C.c_void_p)]),
+    "gslc_batch_create_signaled": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_int32, C.c_int32,
+                                             C.POINTER(BatchTuning), C.c_void_p, C.c_void_p,
+                                             C.POINTER(C.c_void_p)]),
+    "gslc_host_flags_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "gslc_host_flags_destroy": (C.c_int, [C.c_void_p]),
     "gslc_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gslc_batch_status": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gslc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),

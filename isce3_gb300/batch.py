@@ -20,6 +20,7 @@ import ctypes as C
 from dataclasses import dataclass, field
 from typing import Any
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -79,11 +80,50 @@ class BatchTuning:
         return t
 
 
+class HostFlags:
+    """Words of mapped host memory that a batch's kernel sets to 1 when the
+    last tile of a request has been written (``GeocodeBatch(done_flags=...)``).
+
+    ``array`` is a NumPy view over them; the host clears it before a launch
+    and polls it while the batch runs."""
+
+    def __init__(self, n: int):
+        if n < 1:
+            raise ValueError("HostFlags needs at least one word")
+        self.lib = L.lib()
+        p = C.c_void_p()
+        if self.lib.gslc_host_flags_create(int(n), C.byref(p)) != L.GSLC_OK:
+            raise RuntimeError("could not allocate mapped host memory for completion flags")
+        self.ptr = p.value
+        self.n = int(n)
+        self.array = np.ctypeslib.as_array((C.c_uint32 * self.n).from_address(self.ptr))
+
+    def clear(self) -> None:
+        self.array[:] = 0
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            self.array = None
+            self.lib.gslc_host_flags_destroy(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class GeocodeBatch:
-    """A bound batch of geocode requests; ``launch()`` runs them all at once."""
+    """A bound batch of geocode requests; ``launch()`` runs them all at once.
+
+    With ``done_flags`` (a ``HostFlags`` of at least ``len(requests)`` words)
+    word i turns 1 as soon as request i's outputs are written, while the rest
+    of the batch still runs; ``wait()`` still reports the batch's errors."""
 
     def __init__(self, requests: list[GeocodeRequest], geo2rdr_precision: str = "fp64",
-                 tuning: BatchTuning | None = None, device=None, stream: torch.cuda.Stream | None = None):
+                 tuning: BatchTuning | None = None, device=None, stream: torch.cuda.Stream | None = None,
+                 done_flags: HostFlags | None = None):
         self.dev = M.device_of(device)
         self.precision = geo2rdr_precision
         self.tuning = tuning or BatchTuning()
@@ -110,8 +150,15 @@ class GeocodeBatch:
             h = C.c_void_p()
             tc = self.tuning.to_c()
             prec = 1 if geo2rdr_precision in ("ff", "float-float") else 0
-            st = self.lib.gslc_batch_create(self.ctx, arr, n, prec, C.byref(tc), C.c_void_p(self.stream.cuda_stream),
-                                            C.byref(h))
+            if done_flags is None:
+                st = self.lib.gslc_batch_create(self.ctx, arr, n, prec, C.byref(tc),
+                                                C.c_void_p(self.stream.cuda_stream), C.byref(h))
+            else:
+                if done_flags.n < n:
+                    raise ValueError(f"done_flags holds {done_flags.n} words for {n} requests")
+                st = self.lib.gslc_batch_create_signaled(self.ctx, arr, n, prec, C.byref(tc),
+                                                         C.c_void_p(self.stream.cuda_stream),
+                                                         C.c_void_p(done_flags.ptr), C.byref(h))
             L.check(st, self.ctx, "gslc_batch_create")
         self.handle = h
         self._args = arr

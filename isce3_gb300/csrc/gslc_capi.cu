@@ -868,6 +868,12 @@ struct gslc_batch {
     GeoParams* d_items = nullptr;
     long long* d_tile_start = nullptr;
     long long* d_counter = nullptr;
+    int32_t* d_item_request = nullptr;
+    long long* d_request_tiles = nullptr;
+    unsigned long long* d_request_done = nullptr;
+    int32_t n_requests = 0;
+    uint32_t* h_flags = nullptr;        // per-request completion words (mapped host memory) or null
+    std::vector<int32_t> no_tiles;      // requests without tiles: flagged by the host at each launch
     double* d_orbit = nullptr;
     float2* d_scratch = nullptr;
     int32_t* d_err = nullptr;
@@ -884,6 +890,11 @@ struct gslc_batch {
 
 namespace {
 
+void flag_empty_requests(gslc_batch* b) {
+    if (b->h_flags)
+        for (int32_t i : b->no_tiles) b->h_flags[i] = 1;
+}
+
 int batch_fail(gslc_batch* b, gslc_ctx* c, int code, const std::string& m) {
     if (c) c->err = m;
     if (b) b->err = m;
@@ -893,6 +904,8 @@ int batch_fail(gslc_batch* b, gslc_ctx* c, int code, const std::string& m) {
 cudaError_t batch_enqueue(gslc_batch* b, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter, 0, sizeof(long long), s);
+    if (e == cudaSuccess && b->q.done_flags)
+        e = cudaMemsetAsync(b->d_request_done, 0, sizeof(unsigned long long) * b->n_requests, s);
     for (const DerampParams& dp : b->deramps) {
         if (e != cudaSuccess) break;
         e = launch_deramp(dp, s, nullptr);
@@ -905,6 +918,12 @@ cudaError_t batch_enqueue(gslc_batch* b, cudaStream_t s) {
 
 extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, int32_t n, int32_t precision,
                                  const gslc_batch_tuning* tuning, void* stream_, gslc_batch** out) {
+    return gslc_batch_create_signaled(c, items, n, precision, tuning, stream_, nullptr, out);
+}
+
+extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* items, int32_t n, int32_t precision,
+                                          const gslc_batch_tuning* tuning, void* stream_, uint32_t* done_flags,
+                                          gslc_batch** out) {
     if (!c || !out) return GSLC_EINVAL;
     *out = nullptr;
     c->err.clear();
@@ -952,7 +971,16 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
     }
     b->lonlat = any_ll;
     b->ff = precision == 1;
+    b->n_requests = n;
+    b->h_flags = done_flags;
+    {
+        std::vector<char> has(n, 0);
+        for (int i : owner) has[i] = 1;
+        for (int i = 0; i < n; ++i)
+            if (!has[i]) b->no_tiles.push_back(i);
+    }
     if (params.empty()) {
+        flag_empty_requests(b);
         *out = b;
         return GSLC_OK;
     }
@@ -963,6 +991,11 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_tile_start, (params.size() + 1) * sizeof(long long), st_);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_counter, sizeof(long long), st_);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_err, sizeof(int32_t) * 4, st_);
+    if (e == cudaSuccess && done_flags) {
+        e = cudaMallocAsync((void**)&b->d_item_request, params.size() * sizeof(int32_t), st_);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_request_tiles, n * sizeof(long long), st_);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->d_request_done, n * sizeof(unsigned long long), st_);
+    }
     if (e != cudaSuccess) {
         gslc_batch_destroy(b);
         return cuda_err(c, e, "batch allocation");
@@ -1034,6 +1067,29 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
         gslc_batch_destroy(b);
         return cuda_err(c, e, "batch upload");
     }
+    if (e == cudaSuccess && done_flags) {
+        std::vector<long long> req_tiles(n, 0);
+        for (size_t j = 0; j < params.size(); ++j) req_tiles[owner[j]] += tile_start[j + 1] - tile_start[j];
+        e = cudaMemcpyAsync(b->d_item_request, owner.data(), owner.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                            st_);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->d_request_tiles, req_tiles.data(), n * sizeof(long long), cudaMemcpyHostToDevice,
+                                st_);
+        if (e != cudaSuccess) {
+            gslc_batch_destroy(b);
+            return cuda_err(c, e, "batch upload");
+        }
+        unsigned int* dflags = nullptr;
+        e = cudaHostGetDevicePointer((void**)&dflags, done_flags, 0);
+        if (e != cudaSuccess) {
+            gslc_batch_destroy(b);
+            return cuda_err(c, e, "done flags are not mapped host memory");
+        }
+        b->q.item_request = b->d_item_request;
+        b->q.request_tiles = b->d_request_tiles;
+        b->q.request_done = b->d_request_done;
+        b->q.done_flags = dflags;
+    }
     b->n_tiles = tile_start.back();
     b->q.items = b->d_items;
     b->q.tile_start = b->d_tile_start;
@@ -1067,6 +1123,7 @@ extern "C" int gslc_batch_create(gslc_ctx* c, const gslc_geocode_args* items, in
 
 extern "C" int gslc_batch_launch(gslc_batch* b, void* stream) {
     if (!b) return GSLC_EINVAL;
+    flag_empty_requests(b);
     if (!b->q.n_items) return GSLC_OK;
     cudaError_t e = cudaSetDevice(b->device);
     if (e == cudaSuccess) e = b->exec ? cudaGraphLaunch(b->exec, (cudaStream_t)stream) : batch_enqueue(b, (cudaStream_t)stream);
@@ -1103,7 +1160,8 @@ extern "C" int gslc_batch_destroy(gslc_batch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     for (void* ptr : {(void*)b->d_items, (void*)b->d_tile_start, (void*)b->d_counter, (void*)b->d_orbit,
-                      (void*)b->d_scratch, (void*)b->d_err})
+                      (void*)b->d_scratch, (void*)b->d_err, (void*)b->d_item_request, (void*)b->d_request_tiles,
+                      (void*)b->d_request_done})
         if (ptr) cudaFreeAsync(ptr, b->stream);
     delete b;
     return GSLC_OK;
@@ -1137,4 +1195,17 @@ extern "C" int gslc_deramp_block(gslc_ctx* c, const gslc_radar_grid* rg, const g
     c->launches = 0;
     e = launch_deramp(dp, (cudaStream_t)stream, &c->launches);
     return e == cudaSuccess ? GSLC_OK : cuda_err(c, e, "deramp launch");
+}
+
+extern "C" int gslc_host_flags_create(int32_t n, uint32_t** host) {
+    if (!host || n < 1) return GSLC_EINVAL;
+    cudaError_t e = cudaHostAlloc((void**)host, sizeof(uint32_t) * n, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) return GSLC_ECUDA;
+    std::memset(*host, 0, sizeof(uint32_t) * n);
+    return GSLC_OK;
+}
+
+extern "C" int gslc_host_flags_destroy(uint32_t* host) {
+    if (host) cudaFreeHost(host);
+    return GSLC_OK;
 }

@@ -532,7 +532,17 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
             const long long local = tile - q.tile_start[lo];
             const int tiles_x = (p.gw + GBX - 1) / GBX;
             geocode_block<GEO_LONLAT, FF>(p, (int)(local % tiles_x), (int)(local / tiles_x));
+            if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
             __syncthreads();
+            if (q.done_flags && threadIdx.x == 0 && threadIdx.y == 0) {
+                // the block finishing a request's last tile raises its flag
+                const int r = q.item_request[lo];
+                const unsigned long long old = atomicAdd(q.request_done + r, 1ull);
+                if ((long long)old + 1 == q.request_tiles[r]) {
+                    __threadfence_system();
+                    *(volatile unsigned int*)(q.done_flags + r) = 1u;   // single writer
+                }
+            }
         }
     }
 }

@@ -76,6 +76,11 @@ struct BatchQueue {
     int32_t n_items, tiles_per_pop;
     long long n_tiles;
     long long* counter;          // zeroed before each launch
+    // per-request completion (optional: done_flags == nullptr disables it)
+    const int32_t* item_request;     // n_items: request of each items[] entry
+    const long long* request_tiles;  // n_requests: tiles over all its entries
+    unsigned long long* request_done;  // n_requests, zeroed before each launch
+    unsigned int* done_flags;        // n_requests, host-mapped: set to 1 when a request's last tile is written
 };
 
 // launchers (gslc_kernels.cu)

@@ -6,11 +6,19 @@
   HBM footprint (outputs + batch metadata) fits the budget and a batch slot
   is free; a request larger than the whole budget is rejected.
 - ``GeocodeServer.serve`` runs an arrival trace: each scheduling tick it
-  moves arrived requests into the queue, retires finished batches (CUDA
-  event polling, no device synchronisation), and launches the newly admitted
-  requests as ONE persistent-kernel batch on a free stream.  Requests that
-  arrive while earlier batches run join the next batch as soon as a slot and
-  memory free up, and batches on different streams overlap on the device.
+  moves arrived requests into the queue, marks finished requests, retires
+  finished batches (CUDA event polling, no device synchronisation), and
+  launches the newly admitted requests as ONE persistent-kernel batch on a
+  free stream.  Requests that arrive while earlier batches run join the next
+  batch as soon as a slot and memory free up, and batches on different
+  streams overlap on the device (the next batch's blocks start on the SMs
+  that the running batch's blocks leave at its tail).
+- Per-request completion: the persistent kernel counts the written tiles of
+  each request and the block that writes a request's last tile sets that
+  request's word in mapped host memory (``HostFlags``), so a request is done
+  as soon as its own tiles are, not when its whole batch is.  Tiles are
+  handed out in admission order, so the first-admitted requests of a batch
+  finish first.
 - ``serve_plain`` runs the same trace one synchronous ``geocode_slc`` call
   per request, first-in first-out: the baseline.
 
@@ -31,7 +39,7 @@ import torch
 
 from . import _lib as L
 from . import _marshal as M
-from .batch import BatchTuning, GeocodeBatch, GeocodeRequest
+from .batch import BatchTuning, GeocodeBatch, GeocodeRequest, HostFlags
 from .core import LUT2d, Poly2d
 from .geocode import geocode_slc
 
@@ -150,22 +158,33 @@ class AdmissionPolicy:
 
 
 class _InFlight:
-    def __init__(self, batch, requests, event, stream, nbytes):
-        self.batch, self.requests, self.event, self.stream, self.nbytes = batch, requests, event, stream, nbytes
+    def __init__(self, batch, requests, event, slot, nbytes):
+        self.batch, self.requests, self.event, self.slot, self.nbytes = batch, requests, event, slot, nbytes
+        self.open = list(range(len(requests)))     # requests not yet seen complete
+
+
+class _Slot:
+    """A stream and, with per-request completion, its batch's flag words."""
+
+    def __init__(self, dev, max_batch: int, signaled: bool):
+        self.stream = torch.cuda.Stream(dev)
+        self.flags = HostFlags(max_batch) if signaled else None
 
 
 class GeocodeServer:
     """Continuous-batching geocode server over a ``ResidentStore``."""
 
-    def __init__(self, store: ResidentStore, budget_bytes: int = 150 * 10 ** 9, max_in_flight: int = 4,
-                 max_batch: int = 64, geo2rdr_precision: str = "fp64", tuning: BatchTuning | None = None):
+    def __init__(self, store: ResidentStore, budget_bytes: int = 150 * 10 ** 9, max_in_flight: int = 3,
+                 max_batch: int = 64, geo2rdr_precision: str = "fp64", tuning: BatchTuning | None = None,
+                 per_request_completion: bool = True):
         self.store = store
         self.dev = store.dev
         self.policy = AdmissionPolicy(budget_bytes, max_in_flight, max_batch)
         self.precision = geo2rdr_precision
         self.tuning = tuning or BatchTuning(use_graph=False)
-        self.streams = [torch.cuda.Stream(self.dev) for _ in range(max_in_flight)]
-        self.free_streams = list(self.streams)
+        self.signaled = bool(per_request_completion)
+        self.slots = [_Slot(self.dev, max_batch, self.signaled) for _ in range(max_in_flight)]
+        self.free_slots = list(self.slots)
         self.pending: collections.deque = collections.deque()
         self.in_flight: list[_InFlight] = []
         self.used = 0
@@ -188,26 +207,40 @@ class GeocodeServer:
         done = 0
         still = []
         for f in self.in_flight:
-            if f.event.query():
+            finished = f.event.query()
+            if f.slot.flags is not None and f.open:
+                flags = f.slot.flags.array
+                t = None
+                keep = []
+                for i in f.open:
+                    if flags[i]:
+                        t = now_fn() if t is None else t
+                        f.requests[i].t_done = t
+                        done += 1
+                    else:
+                        keep.append(i)
+                f.open = keep
+            if finished:
                 try:
-                    f.batch.wait(f.stream)
+                    f.batch.wait(f.slot.stream)
                 except Exception as e:     # report per request, keep serving
                     for r in f.requests:
                         r.error = str(e)
                 t = now_fn()
-                for r in f.requests:
-                    r.t_done = t
+                for i in f.open:
+                    f.requests[i].t_done = t
+                done += len(f.open)
+                f.open = []
                 f.batch.close()
                 self.used -= f.nbytes
-                self.free_streams.append(f.stream)
-                done += len(f.requests)
+                self.free_slots.append(f.slot)
             else:
                 still.append(f)
         self.in_flight = still
         return done
 
     def _admit(self, now_fn, finished: list) -> int:
-        if not self.free_streams or not self.pending:
+        if not self.free_slots or not self.pending:
             return 0
         admitted, rejected = self.policy.select(self.pending, self.used, len(self.in_flight))
         for r in rejected:
@@ -215,20 +248,23 @@ class GeocodeServer:
             finished.append(r)
         if not admitted:
             return 0
-        stream = self.free_streams.pop()
+        slot = self.free_slots.pop(0)
+        stream = slot.stream
         t = now_fn()
         with torch.cuda.stream(stream):
             reqs = []
             for r in admitted:
                 r.t_admit = t
                 reqs.append(self._request(r))
-            batch = GeocodeBatch(reqs, self.precision, self.tuning, self.dev, stream)
+            if slot.flags is not None:
+                slot.flags.clear()         # the slot's previous batch has retired
+            batch = GeocodeBatch(reqs, self.precision, self.tuning, self.dev, stream, done_flags=slot.flags)
             batch.launch(stream)
             ev = torch.cuda.Event()
             ev.record(stream)
         nbytes = sum(r.footprint for r in admitted)
         self.used += nbytes
-        self.in_flight.append(_InFlight(batch, admitted, ev, stream, nbytes))
+        self.in_flight.append(_InFlight(batch, admitted, ev, slot, nbytes))
         self.batches += 1
         self.batch_sizes.append(len(admitted))
         self.max_concurrent = max(self.max_concurrent, len(self.in_flight))
@@ -254,14 +290,20 @@ class GeocodeServer:
             self._admit(now, finished)
             if not self.in_flight and not self.pending and nxt < len(order):
                 time.sleep(max(0.0, order[nxt].arrival - now()))
-            elif self.in_flight and (not self.free_streams or not self.pending):
+            elif self.in_flight and (not self.free_slots or not self.pending):
                 time.sleep(5e-5)
         if not keep_outputs:
             for r in order:
                 r.geo = r.mask = None
         out = summarize(order, self.batches, self.batch_sizes)
         out["max_concurrent_batches"] = self.max_concurrent
+        out["per_request_completion"] = self.signaled
         return out
+
+    def close(self) -> None:
+        for s in self.slots:
+            if s.flags is not None:
+                s.flags.close()
 
 
 def _default_ellipsoid():

@@ -6,7 +6,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from isce3_gb300 import synth  # noqa: E402
-from isce3_gb300.batch import BatchTuning, GeocodeBatch, GeocodeRequest  # noqa: E402
+from isce3_gb300.batch import BatchTuning, GeocodeBatch, GeocodeRequest, HostFlags  # noqa: E402
 from isce3_gb300.geocode import geocode_slc  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -68,6 +68,29 @@ def test_batch_equals_plain_calls(bursts, precision, graph, pop):
     valid = sum(int((m == 1).sum()) for _, m in outs)
     assert valid > 0.2 * sum(m.numel() for _, m in outs)
     batch.close()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_request_flags(bursts, graph):
+    """Per-request completion words: every request's word is 1 once the
+    batch has run, cleared words are set again by a replay, and the outputs
+    are those of the plain calls."""
+    ref = _plain(bursts, "fp64")
+    outs = _outputs(bursts)
+    n = len(bursts.bursts)
+    flags = HostFlags(n + 3)
+    batch = GeocodeBatch(_requests(bursts, outs), "fp64", BatchTuning(tiles_per_pop=1, use_graph=graph),
+                         done_flags=flags)
+    for _ in range(2):
+        flags.clear()
+        batch.run()
+        assert flags.array[:n].tolist() == [1] * n
+        assert flags.array[n:].tolist() == [0, 0, 0]      # words past the batch untouched
+        _same(ref, outs)
+    batch.close()
+    with pytest.raises(ValueError):
+        GeocodeBatch(_requests(bursts, outs), "fp64", done_flags=HostFlags(n - 1))
+    flags.close()
 
 
 def test_batch_rejects_host_arrays(bursts):

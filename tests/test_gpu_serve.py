@@ -25,14 +25,17 @@ def served():
     return sc, store, trace
 
 
-@pytest.mark.parametrize("precision", ["fp64", "ff"])
-def test_served_results_equal_alone(served, precision):
+@pytest.mark.parametrize("precision,signaled", [("fp64", True), ("ff", True), ("fp64", False)])
+def test_served_results_equal_alone(served, precision, signaled):
     sc, store, trace = served
     mixed = [ServeRequest(k, g, t) for k, g, t in trace]
     server = GeocodeServer(store, budget_bytes=2 * 10 ** 9, max_in_flight=3, max_batch=6,
-                           geo2rdr_precision=precision)
+                           geo2rdr_precision=precision, per_request_completion=signaled)
     stats = server.serve(mixed, keep_outputs=True)
+    server.close()
     assert stats["completed"] == len(trace) and stats["batches"] >= 2
+    assert stats["per_request_completion"] is signaled
+    assert all(r.t_admit <= r.t_done for r in mixed)
     alone = [ServeRequest(k, g, 0.0) for k, g, _ in trace]
     serve_plain(store, alone, geo2rdr_precision=precision, keep_outputs=True)
     for a, b in zip(sorted(mixed, key=lambda r: r.arrival), alone):
