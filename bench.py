@@ -54,6 +54,9 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the burst (batched vs plain) measurement")
     p.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
+    p.add_argument("--precision-study", action="store_true",
+                   help="instead of timing: fp64 and float-float geo2rdr against the oracle over the whole "
+                        "workload (error histograms, Newton iteration counts); writes one JSON line")
     return p.parse_args()
 
 
@@ -499,6 +502,80 @@ def parity_sample(res, row0, rows, box, out):
     return r
 
 
+def _abs_stats(x: np.ndarray) -> dict:
+    """Quantiles and a decade histogram of |x| (zeros counted apart)."""
+    x = np.abs(x[np.isfinite(x)])
+    if x.size == 0:
+        return {"n": 0}
+    q = np.quantile(x, [0.5, 0.9, 0.99, 0.999, 0.9999])
+    nz = x[x > 0]
+    edges = np.arange(-18, 2)
+    hist = np.histogram(np.log10(nz), bins=edges)[0] if nz.size else np.zeros(len(edges) - 1, int)
+    return {"n": int(x.size), "zeros": int(x.size - nz.size), "p50": float(q[0]), "p90": float(q[1]),
+            "p99": float(q[2]), "p999": float(q[3]), "p9999": float(q[4]), "max": float(x.max()),
+            "log10_hist": {f"[1e{int(a)},1e{int(a) + 1})": int(c) for a, c in zip(edges[:-1], hist) if c}}
+
+
+def run_precision_study(args):
+    """fp64 and float-float geo2rdr against the oracle over the whole
+    workload: histograms of the azimuth-time, slant-range and phase
+    differences and of the relative complex error, and the oracle's Newton
+    iteration counts."""
+    import torch
+    from isce3_gb300.geocode import geocode_slc
+    from oracle import oracle
+    from oracle.compare import compare
+    oracle.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    sc = make_scene(args.workload)
+    g = sc.geogrid
+    rgd = sc.radar_grid
+    common = (sc.dem, rgd, g, sc.orbit, sc.native_doppler, sc.image_grid_doppler, sc.ellipsoid, sc.threshold,
+              sc.maxiter)
+    kw = dict(az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    slc_d = torch.from_numpy(sc.slc).to(dev)
+    gpu = {}
+    for prec in ("fp64", "ff"):
+        geo = torch.empty((g.length, g.width), dtype=torch.complex64, device=dev)
+        mask = torch.empty((g.length, g.width), dtype=torch.uint8, device=dev)
+        az = torch.empty((g.length, g.width), dtype=torch.float64, device=dev)
+        rg = torch.empty_like(az)
+        geocode_slc(geo, slc_d, *common, mask_block=mask, az_index_block=az, rg_index_block=rg,
+                    geo2rdr_precision=prec, **kw)
+        torch.cuda.synchronize()
+        gpu[prec] = {k: v.cpu().numpy() for k, v in dict(geo=geo, mask=mask, az=az, rg=rg).items()}
+        del geo, mask, az, rg
+    del slc_d
+    torch.cuda.empty_cache()
+    o = {"geo": np.zeros((g.length, g.width), np.complex64), "mask": np.zeros((g.length, g.width), np.uint8),
+         "az": np.zeros((g.length, g.width)), "rg": np.zeros((g.length, g.width)),
+         "niter": np.zeros((g.length, g.width), np.uint8)}
+    t0 = time.perf_counter()
+    oracle.geocode_slc(o["geo"], np.array(sc.slc, copy=True), *common, mask_block=o["mask"],
+                       az_index_block=o["az"], rg_index_block=o["rg"], niter_block=o["niter"],
+                       inplace_deramp=True, **kw)
+    t_oracle = time.perf_counter() - t0
+    it = o["niter"][o["niter"] > 0]
+    out = {"study": "geo2rdr precision vs oracle", "config": workload_config(sc, args, 1),
+           "oracle_seconds": t_oracle, "oracle_cores": oracle.ncores(),
+           "newton_iterations": {str(int(k)): int(c) for k, c in zip(*np.unique(it, return_counts=True))},
+           "mean_newton_iterations": float(it.mean()) if it.size else None}
+    for prec, r in gpu.items():
+        both = np.isfinite(r["az"]) & np.isfinite(o["az"])
+        dt = (r["az"][both] - o["az"][both]) / rgd.prf
+        dr = (r["rg"][both] - o["rg"][both]) * rgd.range_pixel_spacing
+        gg, go = r["geo"], o["geo"]
+        fin = np.isfinite(gg) & np.isfinite(go) & (np.abs(go) > 0)
+        dphi = np.angle(gg[fin] * np.conj(go[fin]))
+        rel = np.abs(gg[fin] - go[fin]) / np.abs(go[fin])
+        summary = compare(gg, go, r["az"], o["az"], r["rg"], o["rg"], r["mask"], o["mask"])
+        out[prec] = {"delta_aztime_s": _abs_stats(dt), "delta_srange_m": _abs_stats(dr),
+                     "delta_phase_rad": _abs_stats(dphi), "rel_complex_err": _abs_stats(rel),
+                     "parity": {k: v for k, v in summary.items() if not isinstance(v, np.ndarray)}}
+    print(json.dumps(out, default=float), flush=True)
+
+
 def run_reference(args, rank, world):
     """The reference's CPU algorithm (the oracle restatement, OpenMP, all host
     cores) on the same workload: each step one bounded sample of geogrid rows."""
@@ -544,6 +621,9 @@ def main():
         sys.exit(1)
     from isce3_gb300 import _lib as L
     L.build()
+    if args.precision_study:
+        run_precision_study(args)
+        return
     sc, res = run_gpu(args, rank, world)
     if rank != 0:
         return

@@ -189,6 +189,46 @@ int gslc_deramp_block(gslc_ctx* ctx, const gslc_radar_grid* radar_grid, const gs
                       const gslc_azrg_func* rg_carrier, int64_t first_line, int64_t first_sample,
                       const void* src, void* dst, int64_t length, int64_t width, void* stream);
 
+/* Host-only: the DEM window of geogrid lines [line_start, line_start +
+ * block_length) x [0, block_width) (the block form of
+ * DEMRasterToInterpolator, geometry/loadDem.cpp:22-133). */
+int gslc_compute_dem_window_block(const gslc_dem_raster* dem, const gslc_geo_grid* geo_grid, int32_t line_start,
+                                  int32_t block_length, int32_t block_width, int32_t margin, gslc_dem_window* out);
+
+/* Arguments of isce3::cuda::geocode::Geocode (constructor + geocodeRasters,
+ * cxx/isce3/cuda/geocode/Geocode.h:70-128): complex64 rasters on the radar
+ * grid of a RadarGeometry, sinc-interpolated onto one geogrid. */
+typedef struct {
+    gslc_radar_grid radar_grid;     /* RadarGeometry::radarGrid() */
+    gslc_geo_grid geo_grid;
+    gslc_orbit orbit;               /* RadarGeometry::orbit() */
+    gslc_lut2d doppler;             /* RadarGeometry::doppler(): the geo2rdr Doppler */
+    gslc_lut2d native_doppler, az_time_correction, srange_correction;
+    gslc_dem_raster dem;
+    const gslc_subswaths* subswaths;  /* host pointer to descriptor, or NULL */
+    double ellipsoid_a, ellipsoid_e2;
+    double threshold, delta_range;  /* reference defaults 1e-8, 10 */
+    int32_t maxiter;                /* reference default 50 */
+    int32_t lines_per_block;        /* reference default 1000 */
+    int32_t n_rasters;
+    int32_t geo2rdr_precision;      /* 0 FP64, 1 float-float */
+    const void* const* input_rasters;   /* host array of device pointers (complex64, radar length*width) */
+    void* const* output_rasters;        /* host array of device pointers (complex64, geo length*width) */
+    const double* invalid_values;       /* host, n_rasters: output is (v, v) where invalid */
+    double* az_index;               /* device or NULL: radar line coordinate per geo pixel (NaN if masked) */
+    double* rg_index;               /* device or NULL */
+    int32_t dem_margin;             /* DEM pixels of margin per block (reference: 50) */
+    int32_t _pad;
+} gslc_raster_geocode_args;
+
+/* Geocode rasters block by block with the CUDA geocoder's rules
+ * (Geocode::geocodeRasters, cxx/isce3/cuda/geocode/Geocode.cu:652-864, for
+ * SINC_METHOD and GDT_CFloat32; bound to Python as
+ * isce3.cuda.geocode.Geocode.geocode_rasters,
+ * python/extensions/pybind_isce3/cuda/geocode/cuGeocode.cpp:17-90).  Each
+ * geogrid block of lines_per_block lines has its own DEM window, as there. */
+int gslc_geocode_rasters(gslc_ctx* ctx, const gslc_raster_geocode_args* args, void* stream);
+
 /* Number of the library's own kernels launched by the last call on ctx. */
 int64_t gslc_last_launch_count(const gslc_ctx* ctx);
 

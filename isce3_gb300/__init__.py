@@ -3,10 +3,11 @@
 Modules mirror the reference's Python packages on this path:
 ``core`` (Orbit, LUT2d, Poly2d, Ellipsoid, DateTime, StateVector, LookSide),
 ``product`` (RadarGridParameters, GeoGridParameters, SubSwaths), ``io``
-(Raster), ``geocode`` (geocode_slc) and ``cuda`` (Geocode).  The compute is
+(Raster), ``container`` (RadarGeometry), ``geocode`` (geocode_slc) and
+``cuda.geocode`` (Geocode, the block raster geocoder).  The compute is
 one CUDA library, libgslc.so, reached through the C ABI in include/gslc.h.
 """
-from . import core, product, io  # noqa: F401
+from . import core, product, io, container  # noqa: F401
 from .core import (DataInterpMethod, DateTime, Ellipsoid, LookSide, LUT2d, Orbit, OrbitInterpMethod,  # noqa: F401
                    Poly2d, StateVector)
 from .product import GeoGridParameters, RadarGridParameters, SubSwaths  # noqa: F401

@@ -134,6 +134,18 @@ class GeocodeArgs(C.Structure):
                 ("subswaths", C.POINTER(SubSwathsDesc)), ("rdr_deramped", C.c_int32), ("_pad2", C.c_int32)]
 
 
+class RasterGeocodeArgs(C.Structure):
+    _fields_ = [("radar_grid", RadarGrid), ("geo_grid", GeoGrid), ("orbit", OrbitDesc), ("doppler", Lut2d),
+                ("native_doppler", Lut2d), ("az_time_correction", Lut2d), ("srange_correction", Lut2d),
+                ("dem", DemRaster), ("subswaths", C.POINTER(SubSwathsDesc)),
+                ("ellipsoid_a", C.c_double), ("ellipsoid_e2", C.c_double), ("threshold", C.c_double),
+                ("delta_range", C.c_double), ("maxiter", C.c_int32), ("lines_per_block", C.c_int32),
+                ("n_rasters", C.c_int32), ("geo2rdr_precision", C.c_int32),
+                ("input_rasters", C.POINTER(C.c_void_p)), ("output_rasters", C.POINTER(C.c_void_p)),
+                ("invalid_values", C.POINTER(C.c_double)), ("az_index", C.c_void_p), ("rg_index", C.c_void_p),
+                ("dem_margin", C.c_int32), ("_pad", C.c_int32)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("tiles_per_pop", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
                 ("_pad", C.c_int32)]
@@ -146,7 +158,10 @@ _EXPORTS = {
     "gslc_version": (C.c_char_p, []),
     "gslc_compute_dem_window": (C.c_int, [C.POINTER(DemRaster), C.POINTER(GeoGrid), C.c_int32,
                                           C.POINTER(DemWindow)]),
+    "gslc_compute_dem_window_block": (C.c_int, [C.POINTER(DemRaster), C.POINTER(GeoGrid), C.c_int32, C.c_int32,
+                                                C.c_int32, C.c_int32, C.POINTER(DemWindow)]),
     "gslc_geocode_slc": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_void_p]),
+    "gslc_geocode_rasters": (C.c_int, [C.c_void_p, C.POINTER(RasterGeocodeArgs), C.c_void_p]),
     "gslc_last_launch_count": (C.c_int64, [C.c_void_p]),
     "gslc_orbit_interpolate": (C.c_int, [C.POINTER(OrbitDesc), C.c_double, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]),

@@ -140,6 +140,60 @@ def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.
     return d, t
 
 
+def dem_raster_desc_blocks(raster, geogrid: GeoGridParameters, lines_per_block: int, margin: int,
+                           dev: torch.device):
+    """Descriptor whose device samples cover the DEM window of every block of
+    ``lines_per_block`` geogrid lines (each block loads its own window, as
+    cuda/geocode/Geocode.cu:402-407 does): the union of those windows is
+    uploaded once, or the resident raster is used."""
+    res = getattr(raster, "resident", None)
+    if res is not None and res.device == dev:
+        return dem_raster_desc_resident(res, raster.get_geotransform(), raster.get_epsg()), res
+    d = L.DemRaster()
+    d.width, d.length = raster.width, raster.length
+    gt = raster.get_geotransform()
+    for i in range(6):
+        d.gt[i] = gt[i]
+    d.epsg = raster.get_epsg()
+    g = geo_grid_desc(geogrid)
+    lib = L.lib()
+    x0 = y0 = None
+    x1 = y1 = None
+    for line_start in range(0, geogrid.length, lines_per_block):
+        w = L.DemWindow()
+        n = min(lines_per_block, geogrid.length - line_start)
+        st = lib.gslc_compute_dem_window_block(C.byref(d), C.byref(g), int(line_start), int(n), int(geogrid.width),
+                                               int(margin), C.byref(w))
+        if st == L.GSLC_EPROJ:
+            raise ValueError("projection transformation between geogrid and DEM failed")
+        if st == L.GSLC_EUNSUPPORTED:
+            raise NotImplementedError("DEM and geogrid EPSG must be 4326 or UTM, without rotation")
+        if st != L.GSLC_OK:
+            raise ValueError(f"invalid DEM raster (status {st})")
+        if w.wraps:
+            raise NotImplementedError("DEM window crossing the DEM file discontinuity")
+        if not w.have_raster:
+            continue
+        x0 = w.x_off if x0 is None else min(x0, w.x_off)
+        y0 = w.y_off if y0 is None else min(y0, w.y_off)
+        x1 = w.x_off + w.width if x1 is None else max(x1, w.x_off + w.width)
+        y1 = w.y_off + w.length if y1 is None else max(y1, w.y_off + w.length)
+    if x0 is None:
+        d.data = None
+        return d, None
+    key = (str(dev), "win", x0, y0, x1 - x0, y1 - y0)
+
+    def make():
+        sub = np.ascontiguousarray(raster.data[y0:y1, x0:x1])
+        return torch.from_numpy(sub).to(dev)
+
+    t = _cached_device(raster, key, make)
+    d.data = t.data_ptr()
+    d.data_x_off, d.data_y_off = x0, y0
+    d.data_width, d.data_length, d.data_stride = x1 - x0, y1 - y0, x1 - x0
+    return d, t
+
+
 def dem_raster_desc_resident(raster_tensor: torch.Tensor, geotransform, epsg: int) -> L.DemRaster:
     """Descriptor of a whole DEM raster already resident on the device."""
     d = L.DemRaster()

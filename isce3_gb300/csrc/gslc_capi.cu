@@ -80,6 +80,18 @@ SplineConst make_spline_const() {
         q_prev = k.q[i];
     }
     k.p[0] = k.q[0] = 0.0f;
+    // the CUDA interpolator's recurrence: p = 1.0 / (0.5 * Q + 2.0) in FP64,
+    // Q = -0.5 * p stored to FP32 (cuda/core/gpuSpline2dInterpolator.cu:89-92)
+    float qd_prev = 0.0f;
+    for (int i = 1; i < 5; ++i) {
+        volatile double half_q = 0.5 * (double)qd_prev;
+        const double p = 1.0 / (half_q + 2.0);
+        k.pd[i] = p;
+        k.qd[i] = (float)(-0.5 * p);
+        qd_prev = k.qd[i];
+    }
+    k.pd[0] = 0.0;
+    k.qd[0] = 0.0f;
     return k;
 }
 
@@ -281,10 +293,17 @@ int to_azrg(gslc_ctx* c, const gslc_azrg_func& f, AzRg& o, const char* name) {
 // ---- DEM window: geometry/loadDem.cpp:22-133 + DEMInterpolator.cpp:29-455 --
 extern "C" int gslc_compute_dem_window(const gslc_dem_raster* r, const gslc_geo_grid* g, int32_t margin, gslc_dem_window* out) {
     if (!r || !g || !out) return GSLC_EINVAL;
+    return gslc_compute_dem_window_block(r, g, 0, g->length, g->width, margin, out);
+}
+
+extern "C" int gslc_compute_dem_window_block(const gslc_dem_raster* r, const gslc_geo_grid* g, int32_t line_start,
+                                             int32_t block_length, int32_t block_width, int32_t margin,
+                                             gslc_dem_window* out) {
+    if (!r || !g || !out) return GSLC_EINVAL;
     std::memset(out, 0, sizeof(*out));
     if (!is_lonlat_or_utm(r->epsg) || !is_lonlat_or_utm(g->epsg)) return GSLC_EUNSUPPORTED;
     if (r->gt[2] != 0.0 || r->gt[4] != 0.0) return GSLC_EUNSUPPORTED;
-    const int lineStart = 0, blockLength = g->length, blockWidth = g->width;
+    const int lineStart = line_start, blockLength = block_length, blockWidth = block_width;
     double minX = std::numeric_limits<double>::max(), maxX = std::numeric_limits<double>::lowest();
     double minY = std::numeric_limits<double>::max(), maxY = std::numeric_limits<double>::lowest();
     if (r->epsg != g->epsg) {
@@ -442,6 +461,27 @@ double grid_end(const gslc_radar_grid& g) { return g.starting_range + (g.width -
 
 namespace {
 
+// The kernel's view of a DEM window: samples, size and pixel-centre start
+// (DEMInterpolator fields after loadDEM), checked against the samples given.
+int bind_dem_window(gslc_ctx* c, const gslc_dem_raster& d, const gslc_dem_window& w, Dem& dem) {
+    dem.have_raster = w.have_raster && d.data != nullptr;
+    dem.epsg_is_lonlat = d.epsg == 4326;
+    if (!dem.epsg_is_lonlat) utm_setup(d.epsg, dem.utm);
+    if (dem.have_raster) {
+        if (w.x_off < d.data_x_off || w.y_off < d.data_y_off || w.x_off + w.width > d.data_x_off + d.data_width ||
+            w.y_off + w.length > d.data_y_off + d.data_length || d.data_stride < d.data_width)
+            return set_err(c, GSLC_EINVAL, "DEM samples provided do not cover the DEM window of the geogrid");
+        dem.data = d.data + (w.y_off - d.data_y_off) * d.data_stride + (w.x_off - d.data_x_off);
+        dem.stride = d.data_stride;
+        dem.width = (int32_t)w.width;
+        dem.length = (int32_t)w.length;
+        dem.x_start = w.x_start; dem.y_start = w.y_start;
+        dem.dx = w.dx; dem.dy = w.dy;
+    }
+    dem.sc = make_spline_const();
+    return GSLC_OK;
+}
+
 // Validation and launch parameters of one geocode call: everything except
 // the device addresses of the orbit polynomials (bind_orbit), the sinc table
 // and the error word.  GSLC_EMPTY_GRID means there is nothing to do.
@@ -472,6 +512,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
         if (int st = check_lut(c, *l, "LUT2d")) return st;
 
     std::memset(&p, 0, sizeof(p));
+    p.dop_dr = 1.0e-8;      // geocodeSlc.cpp:120-123
     p.gx0 = gg.start_x; p.gy0 = gg.start_y; p.gdx = gg.spacing_x; p.gdy = gg.spacing_y;
     p.gw = gg.width; p.gl = gg.length;
     p.geo_is_lonlat = gg.epsg == 4326;
@@ -483,22 +524,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     if (st == GSLC_EPROJ) return set_err(c, GSLC_EINVAL, "projection transformation between geogrid and DEM failed");
     if (st != GSLC_OK) return set_err(c, st, "unsupported or invalid DEM raster");
     if (w.wraps) return set_err(c, GSLC_EUNSUPPORTED, "DEM window crossing the DEM file discontinuity");
-    p.dem.have_raster = w.have_raster && a->dem.data != nullptr;
-    p.dem.epsg_is_lonlat = a->dem.epsg == 4326;
-    if (!p.dem.epsg_is_lonlat) utm_setup(a->dem.epsg, p.dem.utm);
-    if (p.dem.have_raster) {
-        const gslc_dem_raster& d = a->dem;
-        if (w.x_off < d.data_x_off || w.y_off < d.data_y_off || w.x_off + w.width > d.data_x_off + d.data_width ||
-            w.y_off + w.length > d.data_y_off + d.data_length || d.data_stride < d.data_width)
-            return set_err(c, GSLC_EINVAL, "DEM samples provided do not cover the DEM window of the geogrid");
-        p.dem.data = d.data + (w.y_off - d.data_y_off) * d.data_stride + (w.x_off - d.data_x_off);
-        p.dem.stride = d.data_stride;
-        p.dem.width = (int32_t)w.width;
-        p.dem.length = (int32_t)w.length;
-        p.dem.x_start = w.x_start; p.dem.y_start = w.y_start;
-        p.dem.dx = w.dx; p.dem.dy = w.dy;
-    }
-    p.dem.sc = make_spline_const();
+    if ((st = bind_dem_window(c, a->dem, w, p.dem))) return st;
     p.ell_a = a->ellipsoid_a;
     p.ell_e2 = a->ellipsoid_e2;
 
@@ -672,6 +698,111 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
         cudaEventElapsedTime(&c->ms_deramp, c->ev[2], c->ev[3]);
     }
     if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    return GSLC_OK;
+}
+
+// ---- raster geocoder (cuda/geocode/Geocode.cu:652-864) --------------------
+extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args* r, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (!r) return set_err(c, GSLC_EINVAL, "null arguments");
+    if (r->n_rasters < 1 || !r->input_rasters || !r->output_rasters || !r->invalid_values)
+        return set_err(c, GSLC_EINVAL, "number of input and output rasters not equal");
+    if (r->lines_per_block < 1) return set_err(c, GSLC_EINVAL, "lines_per_block must be positive");
+    if (r->maxiter < 0) return set_err(c, GSLC_EINVAL, "maxiter must be non-negative");
+    if (!(r->delta_range != 0.0)) return set_err(c, GSLC_EINVAL, "delta_range must be non-zero");
+    for (int i = 0; i < r->n_rasters; ++i)
+        if (std::fabs(r->invalid_values[i]) > 3.4028234663852886e38)   // Geocode.cu:332-337 (NaN passes)
+            return set_err(c, GSLC_EINVAL, "float32-type datatype invalid value exceeds type max");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    // the shared geometry through the geocodeSlc preparation: no slicing,
+    // carriers or flattening
+    gslc_geocode_args a;
+    std::memset(&a, 0, sizeof(a));
+    a.radar_grid = a.sliced_radar_grid = r->radar_grid;
+    a.geo_grid = r->geo_grid;
+    a.orbit = r->orbit;
+    a.native_doppler = r->native_doppler;
+    a.image_grid_doppler = r->doppler;
+    a.az_time_correction = r->az_time_correction;
+    a.srange_correction = r->srange_correction;
+    a.az_carrier.kind = a.rg_carrier.kind = 0;      // default LUT2d: zero
+    a.ellipsoid_a = r->ellipsoid_a;
+    a.ellipsoid_e2 = r->ellipsoid_e2;
+    a.threshold_geo2rdr = r->threshold;
+    a.numiter_geo2rdr = r->maxiter;
+    a.n_blocks = r->n_rasters;
+    a.rdr_length = r->radar_grid.length;
+    a.rdr_width = r->radar_grid.width;
+    a.rdr_blocks = r->input_rasters;
+    a.geo_blocks = r->output_rasters;
+    a.dem = r->dem;
+    a.dem_margin = r->dem_margin;
+    a.geo2rdr_precision = r->geo2rdr_precision;
+    a.subswaths = r->subswaths;
+    GeoParams p;
+    std::vector<double> coef;
+    int st = prepare_geocode(c, &a, p, coef);
+    if (st == GSLC_EMPTY_GRID) return GSLC_OK;
+    if (st != GSLC_OK) return st;
+    p.raster = 1;
+    p.dop_dr = r->delta_range;
+    p.mask = nullptr;
+    p.az_out = r->az_index;
+    p.rg_out = r->rg_index;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    if (coef.size() > c->orbit_cap) {
+        if (c->d_orbit) cudaFree(c->d_orbit);
+        c->d_orbit = nullptr;
+        e = cudaMalloc(&c->d_orbit, coef.size() * sizeof(double));
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc orbit");
+        c->orbit_cap = coef.size();
+    }
+    e = cudaMemcpyAsync(c->d_orbit, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "orbit upload");
+    bind_orbit(p, c->d_orbit);
+    p.sinc = c->d_sinc;
+    p.err = c->d_err;
+    if (c->timing) cudaEventRecord(c->ev[0], stream);
+    const gslc_geo_grid& gg = r->geo_grid;
+    const int lpb = r->lines_per_block;
+    const int n_geo_blocks = (gg.length + lpb - 1) / lpb;
+    for (int gb = 0; gb < n_geo_blocks; ++gb) {
+        // Geocode.cu:393-418: block extent and its own DEM window
+        const int line_start = gb * lpb;
+        const int block_length = std::min(lpb, gg.length - line_start);
+        gslc_dem_window w;
+        st = gslc_compute_dem_window_block(&r->dem, &gg, line_start, block_length, gg.width, r->dem_margin, &w);
+        if (st == GSLC_EPROJ) return set_err(c, GSLC_EINVAL, "projection transformation between geogrid and DEM failed");
+        if (st != GSLC_OK) return set_err(c, st, "unsupported or invalid DEM raster");
+        if (w.wraps) return set_err(c, GSLC_EUNSUPPORTED, "DEM window crossing the DEM file discontinuity");
+        if ((st = bind_dem_window(c, r->dem, w, p.dem))) return st;
+        p.geo_row0 = line_start;
+        p.gl = block_length;
+        const int64_t off = (int64_t)line_start * gg.width;
+        p.az_out = r->az_index ? r->az_index + off : nullptr;
+        p.rg_out = r->rg_index ? r->rg_index + off : nullptr;
+        for (int b0 = 0; b0 < r->n_rasters; b0 += MAX_BLOCKS) {
+            p.nblk = std::min(MAX_BLOCKS, r->n_rasters - b0);
+            for (int b = 0; b < p.nblk; ++b) {
+                p.rdr[b] = (const float2*)r->input_rasters[b0 + b];
+                p.geo[b] = (float2*)r->output_rasters[b0 + b] + off;
+                const double v = r->invalid_values[b0 + b];
+                p.inv_blk[b] = std::isnan(v) ? NAN : (float)v;   // Geocode.cu:700-712
+            }
+            e = launch_geocode(p, r->geo2rdr_precision, stream, &c->launches);
+            if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
+        }
+    }
+    if (c->timing) cudaEventRecord(c->ev[1], stream);
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "geocode");
+    if (c->timing) {
+        cudaEventElapsedTime(&c->ms_geocode, c->ev[0], c->ev[1]);
+        c->ms_deramp = 0.f;
+    }
     return GSLC_OK;
 }
 

@@ -57,6 +57,13 @@ __device__ __forceinline__ double dem_row_lonlat(const Dem& d, double lat) {
     return (((lat * 180.0) / PI) - d.y_start) / d.dy;
 }
 
+// The CUDA DEM interpolator: LonLat::forward then the column, without the
+// +-360 wrap of the CPU one (cuda/geometry/gpuDEMInterpolator.cu:149-204,
+// cuda/core/gpuProjections.cu:108-117).
+__device__ __forceinline__ double dem_col_lonlat_nowrap(const Dem& d, double lon) {
+    return ((lon * 180.0) / PI - d.x_start) / d.dx;
+}
+
 // Both coordinates for a UTM DEM (forward projection per pixel).
 __device__ __forceinline__ bool dem_coords_utm(const Dem& d, double lon, double lat, double& row, double& col) {
     double X, Y;
@@ -94,6 +101,38 @@ __device__ double dem_spline(const Dem& d, double row, double col) {
     return (double)spline6_at(yy, HC, R);
 }
 
+// The same bounds and window with the CUDA interpolator's mixed-precision
+// spline (cuda/core/gpuSpline2dInterpolator.cu:119-145; the DEM reference
+// height is 0).
+__device__ double dem_spline_gpu(const Dem& d, double row, double col) {
+    const int irow = (int)floor(row), icol = (int)floor(col);
+    if (irow < 2 || irow >= d.length - 1) return 0.0;
+    if (icol < 2 || icol >= d.width - 1) return 0.0;
+    const int i0 = (int)row - 2, j0 = (int)col - 2;
+    const double xs = dsub(col, (double)j0), ys = dsub(row, (double)i0);
+    int cidx[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) cidx[j] = min(max(j0 + j, 0), d.width - 2) + 1;
+    float HC[6], A[6], R[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const int indi = min(max(i0 + i, 0), d.length - 2) + 1;
+        const float* rowp = d.data + (int64_t)indi * d.stride;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) A[j] = __ldg(rowp + cidx[j]);
+        init_spline6_gpu(A, R, d.sc);
+        HC[i] = spline6_at_gpu(xs, A, R);
+    }
+    init_spline6_gpu(HC, R, d.sc);
+    return (double)spline6_at_gpu(ys, HC, R);
+}
+
+template <bool RASTER>
+__device__ __forceinline__ double dem_height(const Dem& d, double row, double col) {
+    return RASTER ? dem_spline_gpu(d, row, col) : dem_spline(d, row, col);
+}
+
+
 // geometry/detail/Geo2Rdr.icc:50-112 (coarse search when the initial guess is
 // outside the orbit)
 __device__ bool update_aztime(const GeoParams& p, V3 xyz, double& t) {
@@ -115,11 +154,12 @@ __device__ bool update_aztime(const GeoParams& p, V3 xyz, double& t) {
 }
 
 // geometry/detail/Geo2Rdr.icc:114-179 with geometry/geometry.cpp:241-251
-// (deltaRange = 1e-8 as passed by geocodeSlc.cpp:120-123).  With a
+// (deltaRange = 1e-8 as passed by geocodeSlc.cpp:120-123; the raster
+// geocoder passes its delta_range argument).  With a
 // zero image-grid Doppler the slant range enters only the returned iterate,
 // so it is formed once, after convergence.
 __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
-    constexpr double dr = 1.0e-8;
+    const double dr = p.dop_dr;
     t = p.t_mid;
     const bool first_shared = p.t_mid_in_orbit;
     if (!p.t_mid_in_orbit && !update_aztime(p, xyz, t)) return false;
@@ -323,13 +363,29 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
     return cval;
 }
 
+// cuda/product/SubSwaths.h:177-205 (ViewSubSwaths::contains): no subswaths
+// means everything is contained, tested before the bounds.
+__device__ bool subswath_contains_gpu(const GeoParams& p, int az, int rg) {
+    if (p.subsw_n == 0) return true;
+    if (az < 0 || az >= p.subsw_len || rg < 0 || rg >= p.subsw_wid) return false;
+    for (int s = 0; s < p.subsw_n; ++s) {
+        const int32_t* v = p.subsw + ((int64_t)s * p.subsw_len + az) * 2;
+        if (rg >= __ldg(v) && rg < __ldg(v + 1)) return true;
+    }
+    return false;
+}
+
 // Block shape: 32 geogrid columns x 8 lines.  Terms that depend only on the
 // column (easting/longitude) or only on the line (northing/latitude) are
 // evaluated once per block column/line into shared memory.
 constexpr int GBX = 32, GBY = 8;
 
 // One GBX x GBY tile (tile column bx, tile line by) of one geocode request.
-template <bool GEO_LONLAT, bool FF>
+// RASTER selects the generic CUDA raster geocoder's per-pixel rules
+// (cuda/geocode/Geocode.cu:87-172 and :203-287): DEM through the CUDA
+// interpolator, corrections and native Doppler that do not contain the
+// point mask it, no Doppler demodulation, carrier or flattening.
+template <bool GEO_LONLAT, bool FF, bool RASTER>
 __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by) {
     __shared__ double s_col[4][GBX];
     __shared__ double s_row[5][GBY];
@@ -348,7 +404,12 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
             double sl, cl;
             sincos(lon, &sl, &cl);
             double col = 0.0;
-            s_colok[tx] = dem_ll ? (dem_col_lonlat(p.dem, lon, col) ? 1 : 0) : 1;
+            if (RASTER) {
+                s_colok[tx] = 1;
+                if (dem_ll) col = dem_col_lonlat_nowrap(p.dem, lon);
+            } else {
+                s_colok[tx] = dem_ll ? (dem_col_lonlat(p.dem, lon, col) ? 1 : 0) : 1;
+            }
             s_col[0][tx] = lon;
             s_col[1][tx] = sl;
             s_col[2][tx] = cl;
@@ -361,7 +422,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
             s_colok[tx] = c.ok;
         }
     } else if (ty == 1 && tx < GBY) {
-        const int lr = min(by * GBY + tx, p.gl - 1);
+        const int lr = min(by * GBY + tx, p.gl - 1) + p.geo_row0;
         const double y = dadd(p.gy0, dmul(p.gdy, (double)lr + 0.5));   // geocodeSlc.cpp:100
         if (GEO_LONLAT) {
             const double lat = (y * PI) / 180.0;
@@ -394,10 +455,11 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
         double h = 0.0;
         if (p.dem.have_raster) {
             if (dem_ll) {
-                if (s_colok[tx]) h = dem_spline(p.dem, s_row[4][ty], s_col[3][tx]);
+                if (s_colok[tx]) h = dem_height<RASTER>(p.dem, s_row[4][ty], s_col[3][tx]);
             } else {
                 double row, col;
-                if (dem_coords_utm(p.dem, s_col[0][tx], s_row[0][ty], row, col)) h = dem_spline(p.dem, row, col);
+                if (dem_coords_utm(p.dem, s_col[0][tx], s_row[0][ty], row, col))
+                    h = dem_height<RASTER>(p.dem, row, col);
             }
         }
         // lonLatToXyz (Ellipsoid.h:177-190) with the line's rEast and the sines/cosines above
@@ -407,7 +469,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     } else {
         ok = s_colok[tx];
         if (!ok) {
-            atomicOr(p.err, 1);
+            if (!RASTER) atomicOr(p.err, 1);   // the raster geocoder does not check the inverse
         } else {
             UtmCol c;
             c.Ce = s_col[0][tx]; c.shi = s_col[1][tx]; c.chi = s_col[2][tx]; c.ok = 1;
@@ -418,9 +480,12 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
             if (p.dem.have_raster) {
                 double row, col;
                 if (dem_ll) {
-                    if (dem_col_lonlat(p.dem, ll.lon, col)) h = dem_spline(p.dem, dem_row_lonlat(p.dem, ll.lat), col);
+                    if (RASTER)
+                        h = dem_height<true>(p.dem, dem_row_lonlat(p.dem, ll.lat), dem_col_lonlat_nowrap(p.dem, ll.lon));
+                    else if (dem_col_lonlat(p.dem, ll.lon, col))
+                        h = dem_spline(p.dem, dem_row_lonlat(p.dem, ll.lat), col);
                 } else if (dem_coords_utm(p.dem, ll.lon, ll.lat, row, col)) {
-                    h = dem_spline(p.dem, row, col);
+                    h = dem_height<RASTER>(p.dem, row, col);
                 }
             }
             xyz = lonlat_to_xyz_sc(p.ell_a, p.ell_e2, ll.slon, ll.clon, ll.slat, ll.clat, h);
@@ -431,7 +496,29 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
         bool conv;
         if (FF) conv = geo2rdr_ff(p, xyz, t, R);
         else conv = geo2rdr(p, xyz, t, R);
-        if (conv) {
+        if (RASTER) {
+            // Geocode.cu:126-171: corrections and native Doppler that do not
+            // contain the point mask it; floor indices inside the radar grid
+            bool masked = !conv;
+            if (conv) {
+                if (lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
+                else masked = true;
+                if (lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
+                else masked = true;
+                if (!lut_contains(p.nat_dop, t, R)) masked = true;
+            }
+            const double yv = (t - p.rg_t0) * p.rg_prf;
+            const double xv = (R - p.rg_r0) / p.rg_dr;
+            const int yi = (int)floor(yv), xi = (int)floor(xv);
+            if (!masked && p.have_subsw && !subswath_contains_gpu(p, yi, xi)) masked = true;
+            const bool outside = yi < 0 || yi >= p.rg_len || xi < 0 || xi >= p.rg_wid;
+            if (!masked && !outside) {
+                valid = true;
+                azc = yv;
+                rgc = xv;
+                mval = 1;
+            }
+        } else if (conv) {
             if (!p.use_corr) R_uncorr = R;
             if (lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
             if (lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
@@ -460,6 +547,21 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     if (p.az_out) p.az_out[k] = azc;
     if (p.rg_out) p.rg_out[k] = rgc;
 
+    if (RASTER) {
+        // Geocode.cu:232-287: the sinc chip must lie 4 samples inside the
+        // radar raster (the reference's block bounding box +-5 lines/samples
+        // reduces to this), then Sinc2d over the undemodulated chip
+        const bool inside = valid && !(rgc < 4.0 || azc < 4.0 || rgc >= (double)p.inW - 4.0 ||
+                                       azc >= (double)p.inL - 4.0);
+        if (!inside) {
+            for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = make_float2(p.inv_blk[b], p.inv_blk[b]);
+            return;
+        }
+        const int xi = (int)floor(rgc), yi = (int)floor(azc);
+        const double fx = rgc - (double)xi, fy = azc - (double)yi;
+        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = sinc_pixel(p, p.rdr[b], yi, xi, fy, fx, 0.0);
+        return;
+    }
     const float2 invalid = make_float2(p.inv_re, p.inv_im);
     if (!valid) {
         for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
@@ -500,9 +602,9 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     }
 }
 
-template <bool GEO_LONLAT, bool FF>
+template <bool GEO_LONLAT, bool FF, bool RASTER>
 __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
-    geocode_block<GEO_LONLAT, FF>(p, blockIdx.x, blockIdx.y);
+    geocode_block<GEO_LONLAT, FF, RASTER>(p, blockIdx.x, blockIdx.y);
 }
 
 // Persistent form: blocks pop runs of tiles of any request in the batch from
@@ -531,7 +633,7 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
             const GeoParams& p = q.items[lo];
             const long long local = tile - q.tile_start[lo];
             const int tiles_x = (p.gw + GBX - 1) / GBX;
-            geocode_block<GEO_LONLAT, FF>(p, (int)(local % tiles_x), (int)(local / tiles_x));
+            geocode_block<GEO_LONLAT, FF, false>(p, (int)(local % tiles_x), (int)(local / tiles_x));
             if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
             __syncthreads();
             if (q.done_flags && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -547,48 +649,49 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
     }
 }
 
-// A carrier on one radar line: Poly2d collapses to a polynomial in the
-// normalised range, d_j = sum_i c_ij yval^i (core/Poly2d.cpp:8-24 regrouped).
-constexpr int LINE_POLY_MAX = 8;
-struct LinePoly {
-    int n;                       // x_order + 1, or 0 when evaluated per sample
-    double d[LINE_POLY_MAX];
+// The carrier on one radar line, in the reference's operation order
+// (core/Poly2d.cpp:8-24, core/LUT2d.cpp:124-158): a Poly2d of range order 0
+// is constant along the line; otherwise it is evaluated per sample.
+struct CarrierLine {
+    int mode;          // 0 zero, 1 constant on the line, 2 Poly2d per sample, 3 LUT2d per sample
+    double val, yval;
 };
 
-__device__ __forceinline__ void line_poly(const AzRg& f, double az, LinePoly& lp) {
-    lp.n = 0;
-    if (f.is_zero || f.kind != 1 || f.poly.x_order + 1 > LINE_POLY_MAX) return;
-    const Poly& q = f.poly;
-    const double yval = (az - q.y_mean) * q.inv_y_norm;
-    lp.n = q.x_order + 1;
-#pragma unroll
-    for (int j = 0; j < LINE_POLY_MAX; ++j) {
-        if (j >= lp.n) break;
-        double acc = 0.0, sy = 1.0;
-        for (int i = 0; i <= q.y_order; ++i, sy *= yval) acc += sy * q.c[i * lp.n + j];
-        lp.d[j] = acc;
+__device__ __forceinline__ CarrierLine carrier_line(const AzRg& f, double az) {
+    CarrierLine c{0, 0.0, 0.0};
+    if (f.is_zero) return c;
+    if (f.kind != 1) {
+        c.mode = 3;
+        return c;
     }
+    c.yval = ddiv(dsub(az, f.poly.y_mean), f.poly.y_norm);
+    if (f.poly.x_order == 0) {
+        c.mode = 1;
+        c.val = poly_eval_exact(f.poly, c.yval, 0.0);
+    } else {
+        c.mode = 2;
+    }
+    return c;
 }
 
-__device__ __noinline__ double carrier_general(const AzRg& f, double az, double rg) { return azrg_eval(f, az, rg); }
-
-__device__ __forceinline__ double carrier_at(const AzRg& f, const LinePoly& lp, double az, double rg) {
-    if (f.is_zero) return 0.0;
-    if (lp.n == 0) return carrier_general(f, az, rg);
-    const double xval = (rg - f.poly.x_mean) * f.poly.inv_x_norm;
-    double acc = lp.d[lp.n - 1];
-    for (int j = lp.n - 2; j >= 0; --j) acc = acc * xval + lp.d[j];
-    return acc;
+__device__ __noinline__ double carrier_sample(const AzRg& f, const CarrierLine& c, double az, double rg) {
+    return c.mode == 2 ? poly_eval_exact(f.poly, c.yval, rg) : lut_eval_exact(f.lut, az, rg);
 }
 
-// geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier)).
-// Grid: x covers a line in chunks of 4 * blockDim.x samples, y the lines.
+__device__ __forceinline__ double carrier_at(const AzRg& f, const CarrierLine& c, double az, double rg) {
+    if (c.mode == 0) return 0.0;
+    if (c.mode == 1) return c.val;
+    return carrier_sample(f, c, az, rg);
+}
+
+// geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier)),
+// the FP64 phase bit-for-bit in the reference's order, so that its float
+// rounding agrees.  Grid: x covers a line in chunks of 4 * blockDim.x
+// samples, y the lines.
 __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ DerampParams p) {
     for (int64_t i = blockIdx.y; i < p.inL; i += gridDim.y) {
-        const double az = p.rg_t0 + (double)(i + p.az_first) * p.inv_prf;
-        LinePoly lr, la;
-        line_poly(p.rg_car, az, lr);
-        line_poly(p.az_car, az, la);
+        const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
+        const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
         const float2* src = p.src + i * p.inW;
         float2* dst = p.dst + i * p.inW;
         const int64_t j0 = (int64_t)blockIdx.x * blockDim.x * 4 + threadIdx.x;
@@ -598,12 +701,26 @@ __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ Der
             const int64_t j = j0 + (int64_t)u * blockDim.x;
             v[u] = j < p.inW ? __ldg(src + j) : make_float2(0.f, 0.f);
         }
+        if (lr.mode <= 1 && la.mode <= 1) {
+            // carriers constant along the line (azimuth polynomials): the
+            // same phase as per sample, formed once
+            const float phase = (float)dadd(lr.mode ? lr.val : 0.0, la.mode ? la.val : 0.0);
+            float sn, cs;
+            sincosf(phase, &sn, &cs);
+            const float2 rot = make_float2(cs, -sn);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t j = j0 + (int64_t)u * blockDim.x;
+                if (j < p.inW) dst[j] = cmul(v[u], rot);
+            }
+            continue;
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int64_t j = j0 + (int64_t)u * blockDim.x;
             if (j >= p.inW) break;
             const double rg = dadd(p.rg_r0, dmul((double)(j + p.rg_first), p.rg_dr));
-            const float phase = (float)(carrier_at(p.rg_car, lr, az, rg) + carrier_at(p.az_car, la, az, rg));
+            const float phase = (float)dadd(carrier_at(p.rg_car, lr, az, rg), carrier_at(p.az_car, la, az, rg));
             float sn, cs;
             sincosf(phase, &sn, &cs);
             dst[j] = cmul(v[u], make_float2(cs, -sn));
@@ -639,12 +756,20 @@ cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, in
     // the float-float path covers zero image-grid Doppler with the first
     // iterate at sensingMid; anything else runs in FP64
     const bool ff = precision == 1 && p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0;
-    if (p.geo_is_lonlat) {
-        if (ff) geocode_kernel<true, true><<<grid, block, 0, s>>>(p);
-        else geocode_kernel<true, false><<<grid, block, 0, s>>>(p);
+    if (p.raster) {
+        if (p.geo_is_lonlat) {
+            if (ff) geocode_kernel<true, true, true><<<grid, block, 0, s>>>(p);
+            else geocode_kernel<true, false, true><<<grid, block, 0, s>>>(p);
+        } else {
+            if (ff) geocode_kernel<false, true, true><<<grid, block, 0, s>>>(p);
+            else geocode_kernel<false, false, true><<<grid, block, 0, s>>>(p);
+        }
+    } else if (p.geo_is_lonlat) {
+        if (ff) geocode_kernel<true, true, false><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<true, false, false><<<grid, block, 0, s>>>(p);
     } else {
-        if (ff) geocode_kernel<false, true><<<grid, block, 0, s>>>(p);
-        else geocode_kernel<false, false><<<grid, block, 0, s>>>(p);
+        if (ff) geocode_kernel<false, true, false><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<false, false, false><<<grid, block, 0, s>>>(p);
     }
     if (launches) ++*launches;
     return cudaGetLastError();

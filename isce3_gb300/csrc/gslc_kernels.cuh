@@ -58,6 +58,13 @@ struct GeoParams {
     int32_t subsw_n, have_subsw;
     int64_t subsw_len, subsw_wid;
     int32_t* err;               // device error word: bit 0 projection inverse failed
+    // geo2rdr Doppler derivative step (geocodeSlc passes 1e-8; the raster
+    // geocoder's default is 10)
+    double dop_dr;
+    // raster mode (cuda/geocode/Geocode.cu semantics): first geogrid line of
+    // this launch and the invalid value of each raster
+    int32_t raster, geo_row0;
+    float inv_blk[MAX_BLOCKS];
 };
 
 struct DerampParams {

@@ -25,14 +25,18 @@ GSLC_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
 GSLC_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
 GSLC_HD float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 GSLC_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+GSLC_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
 GSLC_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+GSLC_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 #else
 GSLC_HD float fadd(float a, float b) { return a + b; }
 GSLC_HD float fsub(float a, float b) { return a - b; }
 GSLC_HD float fmul(float a, float b) { return a * b; }
 GSLC_HD float fdiv(float a, float b) { return a / b; }
 GSLC_HD double dadd(double a, double b) { return a + b; }
+GSLC_HD double dsub(double a, double b) { return a - b; }
 GSLC_HD double dmul(double a, double b) { return a * b; }
+GSLC_HD double ddiv(double a, double b) { return a / b; }
 #endif
 
 constexpr double PI = 3.14159265358979323846;
@@ -114,6 +118,45 @@ GSLC_HD double poly_eval(const Poly& p, double y, double x) {
     for (int i = 0; i <= p.y_order; i++, scaley *= yval) {
         double scalex = 1.;
         for (int j = 0; j <= p.x_order; j++, scalex *= xval) val += scalex * scaley * p.c[i * (p.x_order + 1) + j];
+    }
+    return val;
+}
+
+// Exact-order forms (no contraction, divisions as the reference writes
+// them): the deramp rounds the carrier phase to float, so an ulp of FP64
+// difference there can move the float phase by one float ulp.
+// core/LUT2d.cpp:124-158 + core/BilinearInterpolator.cpp:12-49 (den == 1).
+GSLC_HD double lut_eval_exact(const Lut& l, double y, double x) {
+    if (!l.have_data) return l.ref_value;
+    double xi = ddiv(dsub(x, l.x0), l.dx);
+    double yi = ddiv(dsub(y, l.y0), l.dy);
+    xi = fmin(fmax(xi, 0.0), l.nx - 1.0);
+    yi = fmin(fmax(yi, 0.0), l.ny - 1.0);
+    if (l.method == 3) {
+        long r = (long)round(yi), c = (long)round(xi);
+        return ld_ro(l.data + r * l.nx + c);
+    }
+    const int x1 = (int)floor(xi), x2 = (int)ceil(xi);
+    const int y1 = (int)floor(yi), y2 = (int)ceil(yi);
+    const double q11 = ld_ro(l.data + (long)y1 * l.nx + x1), q12 = ld_ro(l.data + (long)y2 * l.nx + x1);
+    const double q21 = ld_ro(l.data + (long)y1 * l.nx + x2), q22 = ld_ro(l.data + (long)y2 * l.nx + x2);
+    if (y1 == y2 && x1 == x2) return q11;
+    if (y1 == y2) return dadd(dmul(dsub(x2, xi), q11), dmul(dsub(xi, x1), q21));
+    if (x1 == x2) return dadd(dmul(dsub(y2, yi), q11), dmul(dsub(yi, y1), q12));
+    double v = dmul(q11, dmul(dsub(x2, xi), dsub(y2, yi)));
+    v = dadd(v, dmul(q21, dmul(dsub(xi, x1), dsub(y2, yi))));
+    v = dadd(v, dmul(q12, dmul(dsub(x2, xi), dsub(yi, y1))));
+    return dadd(v, dmul(q22, dmul(dsub(xi, x1), dsub(yi, y1))));
+}
+
+// core/Poly2d.cpp:8-24 with yval = (y - y_mean) / y_norm given
+GSLC_HD double poly_eval_exact(const Poly& p, double yval, double x) {
+    const double xval = p.x_order > 0 ? ddiv(dsub(x, p.x_mean), p.x_norm) : 0.0;  // unused at order 0
+    double scaley = 1., val = 0.;
+    for (int i = 0; i <= p.y_order; i++, scaley = dmul(scaley, yval)) {
+        double scalex = 1.;
+        for (int j = 0; j <= p.x_order; j++, scalex = dmul(scalex, xval))
+            val = dadd(val, dmul(dmul(scalex, scaley), p.c[i * (p.x_order + 1) + j]));
     }
     return val;
 }
@@ -406,7 +449,11 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {                   // DWDivDW 
 // ---- Biquintic spline, FP32, exact reference order -------------------------
 // core/Spline2dInterpolator.cpp:89-108 (_initSpline) for n = 6.  p[i], q[i]
 // depend on nothing but n; the host computes them with the same FP32 ops.
-struct SplineConst { float p[5], q[5]; };
+struct SplineConst {
+    float p[5], q[5];       // FP32 recurrence (core/Spline2dInterpolator.cpp)
+    double pd[5];           // FP64 p of the CUDA interpolator (cuda/core/gpuSpline2dInterpolator.cu)
+    float qd[5];            // its Q, stored to FP32
+};
 
 GSLC_HD void init_spline6(const float Y[6], float R[6], const SplineConst& k) {
     R[0] = 0.0f;
@@ -418,6 +465,31 @@ GSLC_HD void init_spline6(const float Y[6], float R[6], const SplineConst& k) {
     R[5] = 0.0f;
 #pragma unroll
     for (int i = 4; i > 0; --i) R[i] = fadd(fmul(k.q[i], R[i + 1]), R[i]);
+}
+
+// cuda/core/gpuSpline2dInterpolator.cu:85-101 (_initSpline) for T = float
+// and n = 6: the double literals promote parts of each expression to FP64,
+// and the results are stored back to FP32; every operation rounds once.
+GSLC_HD void init_spline6_gpu(const float Y[6], float R[6], const SplineConst& k) {
+    R[0] = 0.0f;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) {
+        const float s = fmul(3.0f, fadd(fsub(Y[i + 1], fmul(2.0f, Y[i])), Y[i - 1]));
+        R[i] = (float)dmul(dsub((double)s, dmul(0.5, (double)R[i - 1])), k.pd[i]);
+    }
+    R[5] = 0.0f;
+#pragma unroll
+    for (int i = 4; i > 0; --i) R[i] = fadd(fmul(k.qd[i], R[i + 1]), R[i]);
+}
+
+// cuda/core/gpuSpline2dInterpolator.cu:103-117 (_spline) on its in-range
+// branch (x in [2, 3), j = 2), mixed precision as written there.
+GSLC_HD float spline6_at_gpu(double x, const float Y[6], const float R[6]) {
+    const double xx = dsub(x, 2.0);
+    const double t0 = dsub(dsub((double)fsub(Y[2], Y[1]), ddiv((double)R[1], 3.0)), ddiv((double)R[2], 6.0));
+    const float d6 = fdiv(fsub(R[2], R[1]), 6.0f);
+    const double t1 = dmul(xx, dadd(ddiv((double)R[1], 2.0), dmul(xx, (double)d6)));
+    return (float)dadd((double)Y[1], dmul(xx, dadd(t0, t1)));
 }
 
 // core/Spline2dInterpolator.cpp:69-87 (_spline) on the branch every in-range

@@ -673,6 +673,72 @@ double dem_interp_lonlat(const DEM& d, double lon, double lat) {
     return dem_interp_xy(d, xyz.x, xyz.y);
 }
 
+// cuda/core/gpuSpline2dInterpolator.cu:85-101 for T = float: the double
+// literals promote parts of each expression to double.
+void init_spline_gpu(const float* Y, int n, float* R, float* Q) {
+    Q[0] = 0.0f;
+    R[0] = 0.0f;
+    for (int i = 1; i < n - 1; ++i) {
+        const double p = 1.0 / (0.5 * Q[i - 1] + 2.0);
+        Q[i] = (float)(-0.5 * p);
+        R[i] = (float)((3 * (Y[i + 1] - 2 * Y[i] + Y[i - 1]) - 0.5 * R[i - 1]) * p);
+    }
+    R[n - 1] = 0.0f;
+    for (int i = (n - 2); i > 0; --i) R[i] = Q[i] * R[i + 1] + R[i];
+}
+
+// cuda/core/gpuSpline2dInterpolator.cu:103-117
+float spline_gpu(double x, const float* Y, int n, const float* R) {
+    if (x < 1.0) {
+        return (float)(Y[0] + (x - 1.0) * (Y[1] - Y[0] - (R[1] / 6.0)));
+    } else if (x > n) {
+        return (float)(Y[n - 1] + ((x - n) * (Y[n - 1] - Y[n - 2] + (R[n - 2] / 6.))));
+    } else {
+        int j = int(std::floor(x));
+        double xx = x - j;
+        double t0 = Y[j] - Y[j - 1] - (R[j - 1] / 3.0) - (R[j] / 6.0);
+        double t1 = xx * ((R[j - 1] / 2.0) + (xx * ((R[j] - R[j - 1]) / 6)));
+        return (float)(Y[j - 1] + (xx * (t0 + t1)));
+    }
+}
+
+// cuda/core/gpuSpline2dInterpolator.cu:119-145 (order 6; MAX_ORDER arrays
+// zero-initialised as there)
+float spline2d_gpu(const float* z, int ny, int nx, double x, double y) {
+    const int order = 6;
+    int i0 = (int)y, j0 = (int)x;
+    i0 = i0 - (order / 2) + 1;
+    j0 = j0 - (order / 2) + 1;
+    float A[20] = {0}, R[20] = {0}, Q[20] = {0}, HC[20] = {0};
+    for (int i = 0; i < order; ++i) {
+        const int indi = std::min(std::max(i0 + i, 0), ny - 2);
+        for (int j = 0; j < order; ++j) {
+            const int indj = std::min(std::max(j0 + j, 0), nx - 2);
+            A[j] = z[(size_t)(indi + 1) * nx + indj + 1];
+        }
+        init_spline_gpu(A, order, R, Q);
+        HC[i] = spline_gpu(x - j0, A, order, R);
+    }
+    init_spline_gpu(HC, order, R, Q);
+    return spline_gpu(y - i0, HC, order, R);
+}
+
+// cuda/geometry/gpuDEMInterpolator.cu:149-204: projection forward, no +-360
+// wrap, float result
+float dem_interp_lonlat_gpu(const DEM& d, double lon, double lat) {
+    float value = (float)d.ref_height;
+    if (!d.have_raster) return value;
+    V3 xyz{0, 0, 0};
+    d.proj.forward({lon, lat, 0.0}, xyz);
+    const double row = (xyz.y - d.ystart) / d.deltay;
+    const double col = (xyz.x - d.xstart) / d.deltax;
+    const int irow = int(std::floor(row));
+    const int icol = int(std::floor(col));
+    if (irow < 2 || irow >= int(d.length - 1)) return (float)d.ref_height;
+    if (icol < 2 || icol >= int(d.width - 1)) return (float)d.ref_height;
+    return spline2d_gpu(d.dem.data(), (int)d.length, (int)d.width, col, row);
+}
+
 // ---------------------------------------------------------------- geo2rdr
 enum { G_OK = 0, G_OOB = 1, G_LOOK = 2, G_NOCONV = 3 };
 
@@ -718,7 +784,7 @@ int update_aztime(double* t, const orc_orbit* o, V3 xyz, int side) {
 // geometry/detail/Geo2Rdr.icc:114-179
 int geo2rdr_detail(double* t, double* r, V3 llh, double a, double e2, const orc_orbit* o,
                    const orc_lut2d* dop, double wvl, int side, double t0, double thr, int maxiter,
-                   double dr) {
+                   double dr, int* iters = nullptr) {
     const V3 xyz = lonlat_to_xyz(a, e2, llh);
     if (t0 >= o->t0 && t0 <= orb_time(o, o->n - 1)) {
         *t = t0;
@@ -738,6 +804,7 @@ int geo2rdr_detail(double* t, double* r, V3 llh, double a, double e2, const orc_
         }
         int st = doppler_aztime_diff(&dt, *t, *r, rvec, vel, dop, wvl, dr);
         if (st != G_OK) return st;
+        if (iters) *iters = i + 1;
         if (std::abs(dt) < thr) return G_OK;
     }
     return G_NOCONV;
@@ -830,9 +897,11 @@ extern "C" int orc_geocode_slc(orc_geocode_args* a) {
                 continue;
             }
             llh.z = dem_interp_lonlat(dem, llh.x, llh.y);
+            int niter = 0;
             int st = geo2rdr_detail(&aztime, &srange, llh, a->ell_a, a->ell_e2, &a->orbit,
                                     &a->image_grid_doppler, rg.wavelength, rg.look_side, aztime,
-                                    a->threshold_geo2rdr, a->numiter_geo2rdr, 1.0e-8);
+                                    a->threshold_geo2rdr, a->numiter_geo2rdr, 1.0e-8, &niter);
+            if (a->out_niter) a->out_niter[k] = st == G_OK ? (uint8_t)std::min(niter, 255) : 0;
             if (st != G_OK) continue;
             if (!useCorr) uncorr[k] = srange;
             if (lut_contains(&a->az_time_correction, aztime, srange))
@@ -954,6 +1023,154 @@ extern "C" int orc_geocode_slc(orc_geocode_args* a) {
 }
 
 extern "C" const char* orc_last_error(void) { return g_err.c_str(); }
+
+// ================================================================ raster geocode
+namespace {
+
+// cuda/product/SubSwaths.h:177-205 (ViewSubSwaths::contains)
+bool subswath_contains_gpu(const orc_subswaths* s, int az, int rg) {
+    if (!s || s->n == 0) return true;
+    if (az < 0 || az >= s->length || rg < 0 || rg >= s->width) return false;
+    for (int k = 0; k < s->n; ++k) {
+        const int32_t* v = s->valid + (size_t)k * s->length * 2;
+        if (rg >= v[(size_t)az * 2] && rg < v[(size_t)az * 2 + 1]) return true;
+    }
+    return false;
+}
+
+}  // namespace
+
+extern "C" int orc_geocode_rasters(orc_raster_args* a) {
+    g_err.clear();
+    const orc_radar_grid& rg = a->radar_grid;
+    const orc_geo_grid& gg = a->geo_grid;
+    if (a->lines_per_block < 1) return fail("lines_per_block must be positive");
+    if (a->n_rasters < 1) return fail("number of input and output rasters not equal");
+#ifdef _OPENMP
+    if (a->nthreads > 0) omp_set_num_threads(a->nthreads);
+#endif
+    Proj proj;
+    if (!proj.init(gg.epsg)) return fail("unsupported geogrid EPSG");
+    const long W = gg.width, Lg = gg.length;
+    const long lpb = a->lines_per_block;
+    const long n_blocks = (Lg + lpb - 1) / lpb;     // Geocode.cu:343
+    const double t_mid = rg_sensing_mid(rg);
+    const size_t rW = (size_t)rg.width, rL = (size_t)rg.length;
+    for (long blk = 0; blk < n_blocks; ++blk) {
+        // Geocode.cu:378-400: block extent
+        const long line_start = blk * lpb;
+        const long block_length = (blk == n_blocks - 1) ? Lg - line_start : lpb;
+        const size_t n = (size_t)block_length * W;
+        // Geocode.cu:402-407: the block's own DEM window
+        DEM dem;
+        if (dem_raster_to_interp(dem, &a->dem, &gg, (int)line_start, (int)block_length, (int)W, a->dem_margin))
+            return 1;
+        std::vector<double> rx(n), ry(n);
+        std::vector<char> mask(n);
+        // geoToRdrIndices, Geocode.cu:87-172
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (long tid = 0; tid < (long)n; ++tid) {
+            const long block_line = tid / W, pixel = tid % W;
+            const long line = line_start + block_line;
+            const V3 xyz{gg.start_x + gg.spacing_x * (0.5 + pixel), gg.start_y + gg.spacing_y * (0.5 + line), 0.0};
+            V3 llh{0, 0, 0};
+            // the CUDA kernel ignores the inverse's status; a failed inverse is masked here
+            const bool proj_ok = proj.inverse(xyz, llh) == 0;
+            llh.z = dem_interp_lonlat_gpu(dem, llh.x, llh.y);
+            double srange = 0.0, aztime = t_mid;
+            bool converged = false;
+            if (proj_ok)
+                converged = geo2rdr_detail(&aztime, &srange, llh, a->ell_a, a->ell_e2, &a->orbit, &a->doppler,
+                                           rg.wavelength, rg.look_side, aztime, a->threshold, a->maxiter,
+                                           a->delta_range) == G_OK;
+            bool masked = false;
+            if (converged) {
+                if (lut_contains(&a->az_time_correction, aztime, srange))
+                    aztime += lut_eval(&a->az_time_correction, aztime, srange);
+                else
+                    masked = true;
+                if (lut_contains(&a->srange_correction, aztime, srange))
+                    srange += lut_eval(&a->srange_correction, aztime, srange);
+                else
+                    masked = true;
+                if (!lut_contains(&a->native_doppler, aztime, srange)) masked = true;
+            }
+            bool invalid = !converged || masked;
+            double y = 0.0, x = 0.0;
+            if (!invalid) {
+                y = (aztime - rg.sensing_start) * rg.prf;
+                x = (srange - rg.starting_range) / rg.range_pixel_spacing;
+                const int y_int = (int)std::floor(y), x_int = (int)std::floor(x);
+                if (!subswath_contains_gpu(a->subswaths, y_int, x_int)) invalid = true;
+                const bool not_in_rdr_grid = y_int < 0 || (size_t)y_int >= rL || x_int < 0 || (size_t)x_int >= rW;
+                invalid = invalid || not_in_rdr_grid;
+            }
+            ry[tid] = invalid ? 0.0 : y;
+            rx[tid] = invalid ? 0.0 : x;
+            mask[tid] = invalid;
+        }
+        // Geocode.cu:418-460: masked min/max and the radar block (+-5)
+        double xmin = NAN, xmax = NAN, ymin = NAN, ymax = NAN;
+        for (size_t k = 0; k < n; ++k) {
+            if (mask[k]) continue;
+            if (std::isnan(xmin) || rx[k] < xmin) xmin = rx[k];
+            if (std::isnan(xmax) || rx[k] > xmax) xmax = rx[k];
+            if (std::isnan(ymin) || ry[k] < ymin) ymin = ry[k];
+            if (std::isnan(ymax) || ry[k] > ymax) ymax = ry[k];
+        }
+        const bool all_masked = std::isnan(ymin);
+        size_t rg_first = 0, rg_last = 0, az_first = 0, az_last = 0, bw = 0, bl = 0;
+        if (!all_masked) {
+            rg_first = std::min(rW - 1, (size_t)std::floor(xmin));
+            rg_last = (size_t)std::max(0.0, std::ceil(xmax) - 1);
+            az_first = std::min(rL - 1, (size_t)std::floor(ymin));
+            az_last = (size_t)std::max(0.0, std::ceil(ymax) - 1);
+            const size_t margin = 5;
+            rg_first = margin > rg_first ? 0 : rg_first - margin;
+            rg_last = std::min(rW - 1, rg_last + margin);
+            az_first = margin > az_first ? 0 : az_first - margin;
+            az_last = std::min(rL - 1, az_last + margin);
+            bw = rg_last - rg_first + 1;
+            bl = az_last - az_first + 1;
+        }
+        for (long k = 0; k < (long)n; ++k) {
+            const size_t o = (size_t)line_start * W + k;
+            if (a->out_az_index) a->out_az_index[o] = mask[k] ? NAN : ry[k];
+            if (a->out_rg_index) a->out_rg_index[o] = mask[k] ? NAN : rx[k];
+        }
+        for (int r = 0; r < a->n_rasters; ++r) {
+            const double iv = a->invalid_values[r];
+            const float inv = std::isnan(iv) ? std::numeric_limits<float>::quiet_NaN() : (float)iv;
+            const cf* in = reinterpret_cast<const cf*>(a->input_rasters[r]);
+            cf* out = reinterpret_cast<cf*>(a->output_rasters[r]) + (size_t)line_start * W;
+            // interpolate, Geocode.cu:203-287, over the radar block read at
+            // (rg_first, az_first) (Geocode.cu:586-600)
+#pragma omp parallel for schedule(dynamic, 1024)
+            for (long k = 0; k < (long)n; ++k) {
+                cf val{inv, inv};
+                if (bw > 0 && !mask[k]) {
+                    const double rdry = ry[k] - (double)az_first;
+                    const double rdrx = rx[k] - (double)rg_first;
+                    const bool oob = rdrx < 4.0 || rdry < 4.0 || rdrx >= (double)bw - 4.0 || rdry >= (double)bl - 4.0;
+                    if (!oob) {
+                        const int xi = (int)std::floor(rdrx), yi = (int)std::floor(rdry);
+                        const double fx = rdrx - (double)xi, fy = rdry - (double)yi;
+                        cf chip[81];
+                        for (int i = 0; i < 9; ++i)
+                            for (int j = 0; j < 9; ++j) {
+                                const size_t row = az_first + (size_t)(yi + i - 4);
+                                const size_t col = rg_first + (size_t)(xi + j - 4);
+                                chip[i * 9 + j] = in[row * rW + col];
+                            }
+                        val = sinc2d_chip(chip, 9, 9, 4.0 + fx, 4.0 + fy);
+                    }
+                }
+                out[k] = val;
+            }
+        }
+    }
+    return 0;
+}
 
 // ================================================================ components
 extern "C" int orc_orbit_interpolate(const orc_orbit* o, double t, double* pos, double* vel) {

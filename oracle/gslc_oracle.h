@@ -110,10 +110,36 @@ typedef struct {
     int32_t dem_margin;         /* DEMRasterToInterpolator default: 50 */
     int32_t nthreads;           /* 0: OpenMP default */
     double phase_seconds[4];    /* out: index pass, deramp, interpolate, reramp */
+    uint8_t* out_niter;         /* optional: geo2rdr iterations per geo pixel (0 = not solved) */
 } orc_geocode_args;
 
 /* Returns 0 on success; >0 argument error (message via orc_last_error). */
 int orc_geocode_slc(orc_geocode_args* a);
+
+/* isce3::cuda::geocode::Geocode::geocodeRasters for SINC_METHOD and
+ * GDT_CFloat32 (cxx/isce3/cuda/geocode/Geocode.cu:87-287, 378-864), restated
+ * on the CPU block by block, bounding boxes included. */
+typedef struct {
+    orc_radar_grid radar_grid;
+    orc_geo_grid geo_grid;
+    orc_orbit orbit;
+    orc_lut2d doppler;          /* RadarGeometry::doppler(): the geo2rdr Doppler */
+    orc_lut2d native_doppler, az_time_correction, srange_correction;
+    double ell_a, ell_e2;
+    double threshold, delta_range;
+    int32_t maxiter, lines_per_block;
+    int32_t n_rasters, dem_margin;
+    const float* const* input_rasters;  /* complex64 interleaved, radar length*width */
+    float* const* output_rasters;       /* complex64 interleaved, geo length*width */
+    const double* invalid_values;       /* n_rasters */
+    orc_dem_raster dem;
+    const orc_subswaths* subswaths;     /* may be NULL */
+    double* out_az_index;               /* optional: y index per geo pixel, NaN where masked */
+    double* out_rg_index;               /* optional: x index per geo pixel, NaN where masked */
+    int32_t nthreads;
+} orc_raster_args;
+
+int orc_geocode_rasters(orc_raster_args* a);
 const char* orc_last_error(void);
 
 /* ---- component entry points used by the pinning tests ---- */

@@ -82,7 +82,18 @@ class Args(C.Structure):
                 ("flatten_phase", C.c_void_p), ("dem", DemRaster), ("subswaths", C.POINTER(SubSw)),
                 ("out_az_index", C.c_void_p), ("out_rg_index", C.c_void_p),
                 ("out_uncorrected_srange", C.c_void_p), ("dem_margin", C.c_int32), ("nthreads", C.c_int32),
-                ("phase_seconds", C.c_double * 4)]
+                ("phase_seconds", C.c_double * 4), ("out_niter", C.c_void_p)]
+
+
+class RasterArgs(C.Structure):
+    _fields_ = [("radar_grid", RadarGrid), ("geo_grid", GeoGrid), ("orbit", OrbitS), ("doppler", Lut),
+                ("native_doppler", Lut), ("az_time_correction", Lut), ("srange_correction", Lut),
+                ("ell_a", C.c_double), ("ell_e2", C.c_double), ("threshold", C.c_double),
+                ("delta_range", C.c_double), ("maxiter", C.c_int32), ("lines_per_block", C.c_int32),
+                ("n_rasters", C.c_int32), ("dem_margin", C.c_int32), ("input_rasters", C.POINTER(C.c_void_p)),
+                ("output_rasters", C.POINTER(C.c_void_p)), ("invalid_values", C.POINTER(C.c_double)),
+                ("dem", DemRaster), ("subswaths", C.POINTER(SubSw)), ("out_az_index", C.c_void_p),
+                ("out_rg_index", C.c_void_p), ("nthreads", C.c_int32)]
 
 
 _lib = None
@@ -95,6 +106,8 @@ def lib() -> C.CDLL:
         _lib = C.CDLL(str(LIB))
         _lib.orc_geocode_slc.restype = C.c_int
         _lib.orc_geocode_slc.argtypes = [C.POINTER(Args)]
+        _lib.orc_geocode_rasters.restype = C.c_int
+        _lib.orc_geocode_rasters.argtypes = [C.POINTER(RasterArgs)]
         _lib.orc_last_error.restype = C.c_char_p
         _lib.orc_orbit_interpolate.argtypes = [C.POINTER(OrbitS), C.c_double, C.c_void_p, C.c_void_p]
         _lib.orc_interp2d_double.restype = C.c_double
@@ -202,7 +215,7 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid
                 reramp=True, az_carrier=None, rg_carrier=None, az_time_correction=None, srange_correction=None,
                 flatten_with_corrected_srange=False, invalid_value=np.nan + np.nan * 1j,
                 carrier_phase_block=None, flatten_phase_block=None, *, az_index_block=None, rg_index_block=None,
-                uncorrected_srange_block=None, dem_margin=50, nthreads=0, inplace_deramp=False):
+                uncorrected_srange_block=None, dem_margin=50, nthreads=0, inplace_deramp=False, niter_block=None):
     """Run the oracle with geocode_slc's arguments; outputs are written in place.
 
     Radar blocks are deramped on copies unless ``inplace_deramp``.  Returns
@@ -251,6 +264,7 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid
     a.out_az_index = opt(az_index_block)
     a.out_rg_index = opt(rg_index_block)
     a.out_uncorrected_srange = opt(uncorrected_srange_block)
+    a.out_niter = opt(niter_block)
     a.dem = dem_struct(dem_raster, keep)
     a.dem_margin = dem_margin
     a.nthreads = nthreads
@@ -265,6 +279,56 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid
     if st != 0:
         raise ValueError(lib().orc_last_error().decode())
     return list(a.phase_seconds)
+
+
+def geocode_rasters(output_rasters, input_rasters, radar_geometry, geogrid, dem_raster, lines_per_block=1000,
+                    invalid_values=None, native_doppler=None, az_time_correction=None, srange_correction=None,
+                    subswaths=None, threshold=1e-8, maxiter=50, delta_range=10.0, *, ellipsoid=None,
+                    az_index_block=None, rg_index_block=None, dem_margin=50, nthreads=0):
+    """The reference CUDA raster geocoder (Geocode::geocodeRasters, SINC on
+    complex64) restated on the CPU; outputs are written in place."""
+    from isce3_gb300.core import Ellipsoid, LUT2d
+    ellipsoid = ellipsoid or Ellipsoid()
+    keep = _Keep()
+    n = len(input_rasters)
+    ins = [np.ascontiguousarray(r, dtype=np.complex64) for r in input_rasters]
+    keep.extend(ins)
+    for o in output_rasters:
+        if o.dtype != np.complex64 or not o.flags.c_contiguous:
+            raise ValueError("outputs must be C-contiguous complex64 arrays")
+    a = RasterArgs()
+    a.radar_grid = radar_struct(radar_geometry.radar_grid)
+    a.geo_grid = geo_struct(geogrid)
+    a.orbit = orbit_struct(radar_geometry.orbit, keep)
+    a.doppler = lut_struct(radar_geometry.doppler, keep)
+    a.native_doppler = lut_struct(native_doppler or LUT2d(), keep)
+    a.az_time_correction = lut_struct(az_time_correction or LUT2d(), keep)
+    a.srange_correction = lut_struct(srange_correction or LUT2d(), keep)
+    a.ell_a, a.ell_e2 = ellipsoid.a, ellipsoid.e2
+    a.threshold, a.delta_range = threshold, delta_range
+    a.maxiter, a.lines_per_block = maxiter, lines_per_block
+    a.n_rasters, a.dem_margin = n, dem_margin
+    ip = (C.c_void_p * n)(*[_ptr(r) for r in ins])
+    op = (C.c_void_p * n)(*[_ptr(r) for r in output_rasters])
+    iv = (C.c_double * n)(*([np.nan] * n if invalid_values is None else [float(v) for v in invalid_values]))
+    keep.extend([ip, op, iv])
+    a.input_rasters = C.cast(ip, C.POINTER(C.c_void_p))
+    a.output_rasters = C.cast(op, C.POINTER(C.c_void_p))
+    a.invalid_values = C.cast(iv, C.POINTER(C.c_double))
+    a.dem = dem_struct(dem_raster, keep)
+    a.out_az_index = _ptr(az_index_block) if az_index_block is not None else None
+    a.out_rg_index = _ptr(rg_index_block) if rg_index_block is not None else None
+    a.nthreads = nthreads
+    if subswaths is not None:
+        ss = SubSw()
+        ss.n, ss.length, ss.width = subswaths.num_sub_swaths, subswaths.length, subswaths.width
+        packed = keep.arr(subswaths.packed(), np.int32)
+        ss.valid = _ptr(packed)
+        keep.append(ss)
+        a.subswaths = C.pointer(ss)
+    st = lib().orc_geocode_rasters(C.byref(a))
+    if st != 0:
+        raise ValueError(lib().orc_last_error().decode())
 
 
 def orbit_interpolate(orbit, t):

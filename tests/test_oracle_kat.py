@@ -84,3 +84,20 @@ def test_correction_cancels_shift(oracle_mod, scene, mode):
     assert v.sum() > 0.3 * v.size
     err = np.angle(geo[v] * np.exp(-1j * _truth(g, "x")[v]))
     assert np.abs(err).max() < 1e-6
+
+
+def test_newton_iteration_counts(oracle_mod, scene):
+    """The oracle's per-pixel geo2rdr iteration count: set for every pixel
+    it solved, within the iteration limit, and unchanged by the data."""
+    g = scene.geogrid
+    slc = synth.kat_slc(scene, "x", 0.0)
+    geo = np.zeros((g.length, g.width), np.complex64)
+    az = np.zeros((g.length, g.width))
+    it = np.zeros((g.length, g.width), np.uint8)
+    oracle_mod.geocode_slc(geo, slc, scene.dem, scene.radar_grid, g, scene.orbit, LUT2d(), LUT2d(),
+                           scene.ellipsoid, 1e-8, 25, az_index_block=az, niter_block=it)
+    solved = np.isfinite(az)
+    assert solved.sum() > 0.4 * solved.size
+    assert (it[solved] >= 1).all() and (it <= 25).all()
+    # linear convergence from mid-swath: a few iterations at least
+    assert 2 <= it[solved].mean() <= 25
