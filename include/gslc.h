@@ -169,6 +169,15 @@ int gslc_compute_dem_window(const gslc_dem_raster* dem, const gslc_geo_grid* geo
  * Returns GSLC_EINVAL outside the orbit's time span. */
 int gslc_orbit_interpolate(const gslc_orbit* orbit, double t, double* pos, double* vel);
 
+/* Host-only: zero-Doppler geo2rdr of one ECEF point (isce3::geometry::geo2rdr,
+ * geometry/geometry.cpp:241-251 with geometry/detail/Geo2Rdr.icc:114-179, image
+ * grid Doppler zero): the Newton iterations the kernels run, from t_guess.
+ * converged = 0 (aztime, slant_range NaN) where the reference returns no
+ * convergence, including the look-side check and iterates leaving the orbit. */
+int gslc_geo2rdr_zero_doppler(const gslc_orbit* orbit, const double* xyz, double t_guess, int32_t look_side,
+                              double threshold, int32_t maxiter, double* aztime, double* slant_range,
+                              int32_t* converged);
+
 /* Host-only: the float sinc kernel table (SINC_SUB=8192 phases x 8 taps) the
  * kernels use (core/Sinc2dInterpolator.cpp:12-40, cast to float at use). */
 int gslc_sinc_table(float* out);

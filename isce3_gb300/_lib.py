@@ -165,6 +165,9 @@ _EXPORTS = {
     "gslc_last_launch_count": (C.c_int64, [C.c_void_p]),
     "gslc_orbit_interpolate": (C.c_int, [C.POINTER(OrbitDesc), C.c_double, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]),
+    "gslc_geo2rdr_zero_doppler": (C.c_int, [C.POINTER(OrbitDesc), C.c_void_p, C.c_double, C.c_int32, C.c_double,
+                                            C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_int32)]),
     "gslc_sinc_table": (C.c_int, [C.c_void_p]),
     "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),

@@ -185,6 +185,146 @@ void make_orbit_coeffs(const gslc_orbit& o, std::vector<double>& out) {
     }
 }
 
+dd dd_mul(dd a, dd b) {
+    const double p = a.hi * b.hi;
+    const double e = std::fma(a.hi, b.hi, -p);
+    return two_sum(p, e + (a.hi * b.lo + a.lo * b.hi));
+}
+dd dd_recip(dd a) {
+    const double q1 = 1.0 / a.hi;
+    const dd r = dd_add({1.0, 0.0}, dd_mul(a, {-q1, 0.0}));
+    return two_sum(q1, r.hi / a.hi);
+}
+double dd_round(dd a) { return a.hi + a.lo; }
+
+// r(w) = q(w + c) for an integer c in {-1, 0, 1}, in double-double
+void shift_poly_dd(const double* q, int n, int c, dd* r) {
+    double binom[8][8] = {};
+    for (int k = 0; k < 8; ++k) {
+        binom[k][0] = binom[k][k] = 1.0;
+        for (int m = 1; m < k; ++m) binom[k][m] = binom[k - 1][m - 1] + binom[k - 1][m];
+    }
+    for (int m = 0; m < n; ++m) r[m] = {0.0, 0.0};
+    for (int k = 0; k < n; ++k)
+        for (int m = 0; m <= k; ++m) {
+            double cp = 1.0;                        // c^(k - m), with 0^0 = 1
+            for (int i = 0; i < k - m; ++i) cp *= c;
+            if (cp != 0.0) r[m] = dd_add(r[m], dd_mul_d({q[k], 0.0}, binom[k][m] * cp));
+        }
+}
+
+// Newton tables of every segment (SEG_STRIDE layout, gslc_math.cuh) from the
+// piece coefficients of make_orbit_coeffs.  H = a . b and W = |b|^2 are
+// formed in double-double from the rounded a, b the kernel evaluates;
+// G = 1/W is W's reciprocal power series.  Returns the highest H and G
+// degree needed over the segments, and div = 1 where G would need more
+// than 12 terms (the kernel then divides).
+void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, int& nh_max, int& ng_max, int& div) {
+    const int nseg = o.n - 1;
+    nh_max = 0;
+    ng_max = 0;
+    div = 0;
+    for (int j = 0; j < nseg; ++j) {
+        const int idx = std::min(std::max(j - 1, 0), o.n - 4);
+        const int c = j - idx - 1;                 // u = w + c
+        const double* pc = piece + (size_t)idx * ORB_STRIDE;
+        double* s = out + (size_t)j * SEG_STRIDE;
+        std::fill(s, s + SEG_STRIDE, 0.0);
+        for (int d = 0; d < 3; ++d) s[d] = pc[d];
+        double a[3][8], b[3][7];
+        for (int d = 0; d < 3; ++d) {
+            dd ta[8], tb[7];
+            shift_poly_dd(pc + 3 + d * 8, 8, c, ta);
+            shift_poly_dd(pc + 27 + d * 7, 7, c, tb);
+            for (int k = 0; k < 8; ++k) s[SEG_A + d * 8 + k] = a[d][k] = dd_round(ta[k]);
+            for (int k = 0; k < 7; ++k) s[SEG_B + d * 7 + k] = b[d][k] = dd_round(tb[k]);
+        }
+        dd H[SEG_NH], W[SEG_NG], G[SEG_NG];
+        for (int k = 0; k < SEG_NH; ++k) H[k] = {0.0, 0.0};
+        for (int k = 0; k < SEG_NG; ++k) W[k] = {0.0, 0.0};
+        for (int d = 0; d < 3; ++d)
+            for (int i = 0; i < 7; ++i) {
+                for (int k = 0; k < 8; ++k) H[i + k] = dd_add(H[i + k], dd_mul({a[d][k], 0.0}, {b[d][i], 0.0}));
+                for (int k = 0; k < 7; ++k) W[i + k] = dd_add(W[i + k], dd_mul({b[d][k], 0.0}, {b[d][i], 0.0}));
+            }
+        const dd g0 = dd_recip(W[0]);
+        G[0] = g0;
+        for (int k = 1; k < SEG_NG; ++k) {
+            dd acc{0.0, 0.0};
+            for (int m = 1; m <= k; ++m) acc = dd_add(acc, dd_mul(W[m], G[k - m]));
+            G[k] = dd_mul(acc, {-g0.hi, -g0.lo});
+        }
+        for (int k = 0; k < SEG_NH; ++k) s[SEG_H + k] = dd_round(H[k]);
+        for (int k = 0; k < SEG_NG; ++k) s[SEG_G + k] = dd_round(G[k]);
+        // H degree: the tail over |w| <= 1/2 moves the Newton step by < 1e-17 s
+        int nh = SEG_NH - 1;
+        {
+            double tail = 0.0;
+            const double lim = 1e-17 * std::fabs(W[0].hi);
+            while (nh > 0) {
+                const double t = tail + std::fabs(s[SEG_H + nh]) * std::ldexp(1.0, -nh);
+                if (t > lim) break;
+                tail = t;
+                --nh;
+            }
+        }
+        // G degree: the lowest whose truncated, rounded series times W is
+        // within 2^-52 of 1 on 65 points of the segment
+        int ng = -1;
+        for (int K = 1; K < SEG_NG && ng < 0; ++K) {
+            double worst = 0.0;
+            for (int q = 0; q <= 64; ++q) {
+                const double w = -0.5 + q / 64.0;
+                dd gv{s[SEG_G + K], 0.0}, wv = W[SEG_NG - 1];
+                for (int k = K - 1; k >= 0; --k) gv = dd_add(dd_mul_d(gv, w), {s[SEG_G + k], 0.0});
+                for (int k = SEG_NG - 2; k >= 0; --k) wv = dd_add(dd_mul_d(wv, w), W[k]);
+                const dd e = dd_add(dd_mul(gv, wv), {-1.0, 0.0});
+                worst = std::max(worst, std::fabs(e.hi));
+            }
+            if (worst <= std::ldexp(1.0, -52)) ng = K;
+        }
+        if (ng < 0) {
+            div = 1;
+            ng = SEG_NG - 1;
+        }
+        nh_max = std::max(nh_max, nh);
+        ng_max = std::max(ng_max, ng);
+    }
+}
+
+// The device orbit table of o (pieces, their float pairs, the Newton
+// segments; orbit_table_doubles) and the Orbit descriptor, its table
+// pointers left null for bind_orbit.
+void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
+    make_orbit_coeffs(o, coef);
+    // float-pair copy of the polynomial coefficients for the float-float geo2rdr,
+    // stored after the doubles (ORB_FF_STRIDE float2 per piece = 45 doubles' room)
+    const int np = o.n - 3;
+    const size_t nd = coef.size();
+    coef.resize(nd + (size_t)np * ORB_FF_STRIDE, 0.0);
+    float2* ffc = reinterpret_cast<float2*>(coef.data() + nd);
+    for (int idx = 0; idx < np; ++idx)
+        for (int k = 0; k < ORB_FF_STRIDE; ++k) {
+            const double v = coef[(size_t)idx * ORB_STRIDE + 3 + k];
+            const float hi = (float)v;
+            ffc[(size_t)idx * ORB_FF_STRIDE + k] = make_float2(hi, (float)(v - (double)hi));
+        }
+    // Newton segment tables after them (orbit_seg_offset, 16-byte aligned)
+    int seg_nh = 0, seg_ng = 0, seg_div = 0;
+    coef.resize(orbit_table_doubles(o.n), 0.0);
+    make_orbit_segments(o, coef.data(), coef.data() + orbit_seg_offset(o.n), seg_nh, seg_ng, seg_div);
+    ob = Orbit{};
+    ob.t0 = o.t0;
+    ob.spacing = o.spacing;
+    ob.inv_spacing = 1.0 / o.spacing;
+    ob.t_end = o.t0 + (o.n - 1) * o.spacing;
+    ob.n = o.n;
+    ob.n_pieces = o.n - 3;
+    ob.seg_nh = seg_nh;
+    ob.seg_ng = seg_ng;
+    ob.seg_div = seg_div;
+}
+
 bool utm_setup(int code, Utm& u) {
     // core/Projections.cpp:80-170
     int zone;
@@ -405,6 +545,46 @@ extern "C" int gslc_orbit_interpolate(const gslc_orbit* o, double t, double* pos
     return GSLC_OK;
 }
 
+extern "C" int gslc_geo2rdr_zero_doppler(const gslc_orbit* o, const double* xyz, double t_guess, int32_t look_side,
+                                         double threshold, int32_t maxiter, double* aztime, double* slant_range,
+                                         int32_t* converged) {
+    if (!o || !xyz || !aztime || !slant_range || !converged || o->n < 4 || !(o->spacing > 0) || o->method != 0 ||
+        !o->pos || !o->vel || (look_side != -1 && look_side != 1))
+        return GSLC_EINVAL;
+    std::vector<double> coef;
+    Orbit ob;
+    build_orbit_table(*o, coef, ob);
+    ob.coef = coef.data();
+    ob.coef_ff = reinterpret_cast<const float2*>(coef.data() + (size_t)ob.n_pieces * ORB_STRIDE);
+    ob.seg = coef.data() + orbit_seg_offset(o->n);
+    *converged = 0;
+    *aztime = *slant_range = std::nan("");
+    // iteration 0 (geometry/detail/Geo2Rdr.icc:114-179): look side and first step at t_guess
+    if (!(t_guess >= ob.t0 && t_guess <= ob.t_end)) return GSLC_OK;
+    if (maxiter < 1) return GSLC_OK;
+    const V3 x{xyz[0], xyz[1], xyz[2]};
+    V3 pos, vel;
+    orbit_eval(ob, t_guess, pos, vel);
+    const V3 rvec = vsub(x, pos);
+    // the kernels' form of iteration 0 (look side and step from per-launch constants)
+    if ((look_side == -1) != (vdot(rvec, vcross(vel, pos)) > 0.)) return GSLC_OK;
+    double t = t_guess, R = 0.0;
+    const double dt = -vdot(rvec, vel) * (1.0 / vdot(vel, vel));
+    bool ok;
+    if (std::fabs(dt) < threshold) {
+        R = vnorm(rvec);
+        ok = true;
+    } else {
+        ok = geo2rdr_zero_doppler_seg(ob, x, threshold, maxiter, t, dt, R);
+    }
+    if (ok) {
+        *aztime = t;
+        *slant_range = R;
+        *converged = 1;
+    }
+    return GSLC_OK;
+}
+
 extern "C" int gslc_sinc_table(float* out) {
     if (!out) return GSLC_EINVAL;
     const std::vector<float> t = make_sinc_table();
@@ -528,31 +708,9 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.ell_a = a->ellipsoid_a;
     p.ell_e2 = a->ellipsoid_e2;
 
-    // orbit polynomials
-    make_orbit_coeffs(a->orbit, coef);
-    // float-pair copy of the polynomial coefficients for the float-float geo2rdr,
-    // stored after the doubles (ORB_FF_STRIDE float2 per piece = 45 doubles' room)
-    {
-        const int np = a->orbit.n - 3;
-        const size_t nd = coef.size();
-        coef.resize(nd + (size_t)np * ORB_FF_STRIDE, 0.0);
-        float2* ffc = reinterpret_cast<float2*>(coef.data() + nd);
-        for (int idx = 0; idx < np; ++idx)
-            for (int k = 0; k < ORB_FF_STRIDE; ++k) {
-                const double v = coef[(size_t)idx * ORB_STRIDE + 3 + k];
-                const float hi = (float)v;
-                ffc[(size_t)idx * ORB_FF_STRIDE + k] = make_float2(hi, (float)(v - (double)hi));
-            }
-    }
-    Orbit& ob = p.orbit;
-    ob.t0 = a->orbit.t0;
-    ob.spacing = a->orbit.spacing;
-    ob.inv_spacing = 1.0 / a->orbit.spacing;
-    ob.t_end = a->orbit.t0 + (a->orbit.n - 1) * a->orbit.spacing;
-    ob.n = a->orbit.n;
-    ob.n_pieces = a->orbit.n - 3;
-    ob.coef = nullptr;      // bound to device memory by bind_orbit
-    ob.coef_ff = nullptr;
+    // orbit polynomials and Newton tables
+    build_orbit_table(a->orbit, coef, p.orbit);
+    const Orbit& ob = p.orbit;
 
     // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)
     p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
@@ -561,6 +719,8 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
         Orbit host_ob = ob;
         host_ob.coef = coef.data();
         orbit_eval(host_ob, p.t_mid, p.pos0, p.vel0);
+        p.n0 = vcross(p.vel0, p.pos0);
+        p.inv_vv0 = 1.0 / vdot(p.vel0, p.vel0);
     }
     p.thr = a->threshold_geo2rdr;
     p.maxiter = a->numiter_geo2rdr;
@@ -609,6 +769,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
 void bind_orbit(GeoParams& p, const double* d_coef) {
     p.orbit.coef = d_coef;
     p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+    p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
 }
 
 }  // namespace
@@ -881,7 +1042,7 @@ static __device__ __align__(256) float2 g_noalloc_deramp[NOALLOC_MAX_DERAMP];
 // sinc kernel table, SINC_SUB x SINC_LEN
 static __device__ __align__(256) float g_noalloc_sinc[SINC_SUB * SINC_LEN];
 // orbit polynomial pieces
-static __device__ __align__(256) double g_noalloc_orbit[(NOALLOC_MAX_STATE_VECTORS - 3) * (ORB_STRIDE + ORB_FF_STRIDE)];
+static __device__ __align__(256) double g_noalloc_orbit[orbit_table_doubles(NOALLOC_MAX_STATE_VECTORS)];
 // error word (bit 0: projection inverse failed); cleared at every call
 static __device__ __align__(256) int32_t g_noalloc_err[4];
 
@@ -952,7 +1113,7 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     static thread_local int32_t h_err[4];
     c.h_err = h_err;
     c.d_orbit = d.orbit;
-    c.orbit_cap = (size_t)(NOALLOC_MAX_STATE_VECTORS - 3) * (ORB_STRIDE + ORB_FF_STRIDE);
+    c.orbit_cap = orbit_table_doubles(NOALLOC_MAX_STATE_VECTORS);
 
     gslc_geocode_args args = *a;
     std::vector<const void*> blocks(a->rdr_blocks, a->rdr_blocks + a->n_blocks);

@@ -165,6 +165,20 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
     if (!p.t_mid_in_orbit && !update_aztime(p, xyz, t)) return false;
     const bool dop_data = p.img_dop.have_data;
     const bool dop_const = !dop_data && p.img_dop.ref_value == 0.0;
+    if (p.maxiter < 1) return false;
+    if (dop_const && first_shared) {
+        // iteration 0 at sensingMid with the shared state: the look-side
+        // test (rvec x vel) . pos > 0 as rvec . (vel x pos), the step with
+        // 1/|vel|^2 (within an ulp of the quotient)
+        const V3 rvec = vsub(xyz, p.pos0);
+        if ((p.look_side == -1) != (vdot(rvec, p.n0) > 0.)) return false;
+        const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
+        if (fabs(dt) < p.thr) {
+            R = vnorm(rvec);
+            return true;
+        }
+        return p.maxiter > 1 && geo2rdr_zero_doppler_seg(p.orbit, xyz, p.thr, p.maxiter, t, dt, R);
+    }
     const double half_wvl = 0.5 * p.rg_wvl;
     double dt = 0.0;
     for (int i = 0; i < p.maxiter; ++i) {
@@ -180,13 +194,14 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
         const V3 rvec = vsub(xyz, pos);
         if (i == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
         if (dop_const) {
-            // fdop == 0 and fdopder == 0 exactly: fn = rvec.vel, fn' = -vel.vel
+            // fdop == 0 and fdopder == 0 exactly: fn = rvec.vel, fn' = -vel.vel;
+            // iterations after this one run on the segment tables
             dt = vdot(rvec, vel) / (-vdot(vel, vel));
             if (fabs(dt) < p.thr) {
                 R = vnorm(rvec);
                 return true;
             }
-            continue;
+            return geo2rdr_zero_doppler_seg(p.orbit, xyz, p.thr, p.maxiter, t, dt, R);
         }
         R = vnorm(rvec);
         if (dop_data && p.img_dop.bounds_error &&
@@ -242,8 +257,8 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
     t = p.t_mid;
     {
         const V3 rvec = vsub(xyz, p.pos0);
-        if ((p.look_side == -1) != (vdot(vcross(rvec, p.vel0), p.pos0) > 0.)) return false;
-        const double dt = vdot(rvec, p.vel0) / (-vdot(p.vel0, p.vel0));
+        if ((p.look_side == -1) != (vdot(rvec, p.n0) > 0.)) return false;
+        const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
         if (fabs(dt) < p.thr) {
             R = vnorm(rvec);
             return true;

@@ -31,6 +31,8 @@ struct GeoParams {
     int32_t t_mid_in_orbit, maxiter;
     double thr;
     V3 pos0, vel0;              // orbit at t_mid (first Newton iterate is shared)
+    V3 n0;                      // vel0 x pos0: look side of rvec is sign(rvec . n0)
+    double inv_vv0;             // 1 / |vel0|^2
     // radar grid (full) and sliced grid
     double rg_t0, rg_prf, rg_r0, rg_dr, rg_wvl;
     int64_t rg_len, rg_wid;

@@ -7,6 +7,7 @@
 // 1e-4 rad parity tolerance.  FP64 geometry may contract to FMA; its
 // differences stay ~1e-16 relative.
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 #include <math.h>
 
@@ -360,12 +361,33 @@ GSLC_HD bool utm_forward(const Utm& u, double lon, double lat, double& x, double
 constexpr int ORB_STRIDE = 48;   // pref[3], a[3][8], b[3][7] (b = d/dt coefficients)
 constexpr int ORB_FF_STRIDE = 45;  // a[3][8], b[3][7] split into float pairs
 
+// Newton tables per state-vector interval ("segment" j = 0..n-2, the time
+// span [t_j, t_j+1]).  Segment j uses the Hermite piece
+// idx = clamp(j - 1, 0, n - 4), re-expanded in w = u - (j - idx - 1) so that
+// w lies in [-0.5, 0.5] on the segment (w = u for interior segments).  With
+// D = xyz - P_ref, the zero-Doppler residual of geo2rdr is
+//   (xyz - pos(w)) . vel(w) = D . vel(w) - H(w),   H(w) = a(w) . vel(w),
+// and the Newton step divides by -|vel(w)|^2 = -1 / G(w).  H is a degree-13
+// polynomial (truncated where its tail is below 1e-9 m^2/s), G a truncated
+// power series of 1/|vel|^2 accurate to about one ulp on the segment.
+constexpr int SEG_NH = 14, SEG_NG = 13;
+constexpr int SEG_STRIDE = 76;   // pref[3], a[3][8], b[3][7], h[14], g[13], pad
+constexpr int SEG_A = 3, SEG_B = 27, SEG_H = 48, SEG_G = 62;
+
 struct Orbit {
     double t0, spacing, inv_spacing, t_end;
     int32_t n, n_pieces;
     const double* coef;          // n_pieces * ORB_STRIDE
     const float2* coef_ff;       // n_pieces * ORB_FF_STRIDE: a[3][8], b[3][7] as (hi, lo)
+    const double* seg;           // (n - 1) * SEG_STRIDE
+    int32_t seg_nh, seg_ng;      // highest H and G degree used over all segments
+    int32_t seg_div, _pad;       // 1: G did not converge, divide by -|vel|^2 instead
 };
+
+// Orbit table layout in doubles: the pieces, their float pairs, then the
+// segments (16-byte aligned).
+constexpr size_t orbit_seg_offset(int n) { return ((size_t)(n - 3) * (ORB_STRIDE + ORB_FF_STRIDE) + 1) & ~(size_t)1; }
+constexpr size_t orbit_table_doubles(int n) { return orbit_seg_offset(n) + (size_t)(n - 1) * SEG_STRIDE; }
 
 GSLC_HD int orbit_piece(const Orbit& o, double t) {
     // core/Linspace.icc:77-89 search(t) - 2, clamped (InterpolateOrbit.icc:18-19)
@@ -396,6 +418,83 @@ GSLC_HD void orbit_eval(const Orbit& o, double t, V3& pos, V3& vel) {
     }
     pos = {p[0], p[1], p[2]};
     vel = {v[0], v[1], v[2]};
+}
+
+// Segment of orbit_piece(t) = pc at piece coordinate u; u becomes the
+// segment coordinate w (exact: u + 1 and u - 1 on these ranges).
+GSLC_HD int orbit_segment(const Orbit& o, int pc, double& u) {
+    if (pc == 0 && u < -0.5) { u += 1.0; return 0; }
+    if (pc == o.n - 4 && u >= 0.5) { u -= 1.0; return o.n - 2; }
+    return pc + 1;
+}
+
+GSLC_HD double seg_poly(const double* c, int deg, double w) {
+    double acc = ld_ro(c + deg);
+    for (int k = deg - 1; k >= 0; --k) acc = fma(acc, w, ld_ro(c + k));
+    return acc;
+}
+
+// Iterations 1.. of geo2rdr's zero-Doppler Newton solve
+// (geometry/detail/Geo2Rdr.icc:114-179 with fdop = fdopder = 0): the same
+// iterates t <- t - fn/fn', fn = (xyz - pos).vel, fn' = -|vel|^2, with fn
+// formed as D.vel - H(w) on the segment tables (Orbit::seg) instead of
+// subtracting the interpolated position, and 1/|vel|^2 as G(w).  Rounding
+// differs from the direct form by ~1e-13 s in azimuth time, below the
+// reference's own orbit interpolation noise (~1e-11 s).
+GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, V3 xyz, double thr, int maxiter, double& t, double dt,
+                                       double& R) {
+    int seg = -1;
+    double D[3] = {0.0, 0.0, 0.0};
+    double w = 0.0;
+    const double* c = o.seg;
+    for (int i = 1; i < maxiter; ++i) {
+        t -= dt;
+        // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
+        // from the exact coordinate); entering a segment, leaving it, and on
+        // the first and last segment (the orbit's time span) w, the piece
+        // and the span check come from t exactly as orbit interpolation does.
+        w -= dt * o.inv_spacing;
+        if (seg <= 0 || seg >= o.n - 2 || !(w >= -0.5 && w < 0.5)) {
+            if (!(t >= o.t0 && t <= o.t_end)) return false;  // FillNaN -> no convergence
+            const int pc = orbit_piece(o, t);
+            const double tidx = o.t0 + pc * o.spacing;
+            w = (t - tidx) * o.inv_spacing - 1.5;
+            const int j = orbit_segment(o, pc, w);
+            c = o.seg + (int64_t)j * SEG_STRIDE;
+            if (j != seg) {
+                seg = j;
+                D[0] = xyz.x - ld_ro(c + 0);
+                D[1] = xyz.y - ld_ro(c + 1);
+                D[2] = xyz.z - ld_ro(c + 2);
+            }
+        }
+        double v[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double* b = c + SEG_B + d * 7;
+            double acc = ld_ro(b + 6);
+#pragma unroll
+            for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_ro(b + k));
+            v[d] = acc;
+        }
+        const double fn = fma(D[0], v[0], fma(D[1], v[1], D[2] * v[2])) - seg_poly(c + SEG_H, o.seg_nh, w);
+        if (o.seg_div) dt = fn / (-(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+        else dt = -fn * seg_poly(c + SEG_G, o.seg_ng, w);
+        if (fabs(dt) < thr) {
+            double r[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double* a = c + SEG_A + d * 8;
+                double acc = ld_ro(a + 7);
+#pragma unroll
+                for (int k = 6; k >= 0; --k) acc = fma(acc, w, ld_ro(a + k));
+                r[d] = D[d] - acc;
+            }
+            R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            return true;
+        }
+    }
+    return false;
 }
 
 // ---- float-float (double-word FP32) arithmetic ------------------------------

@@ -40,6 +40,48 @@ def test_orbit_polynomial_matches_reference_hermite(lib, oracle_mod):
     assert lib.gslc_orbit_interpolate(C.byref(d), o.end_time + 1.0, p, v) == L.GSLC_EINVAL
 
 
+@pytest.mark.parametrize("which", ["c1", "c2"])
+def test_zero_doppler_newton_matches_oracle(lib, oracle_mod, which):
+    """The kernels' Newton iterations (segment tables: residual D.vel - H,
+    step times G = 1/|vel|^2) against the oracle's geo2rdr
+    (geometry/detail/Geo2Rdr.icc:114-179) from sensingMid, on random geogrid
+    points at random heights: same convergence everywhere, and the same
+    iterate except where the last step sits at the threshold."""
+    sc = synth.scene_c2(slc=False) if which == "c2" else synth.scene_c1(slc=False)
+    o, rg, g, ell = sc.orbit, sc.radar_grid, sc.geogrid, sc.ellipsoid
+    d = M.orbit_desc(o)
+    t_mid = rg.sensing_start + 0.5 * (rg.length - 1) / rg.prf
+    rng = np.random.default_rng(7)
+    n, splits, dts, drs = 1500, 0, [], []
+    for _ in range(n):
+        x = g.start_x + g.spacing_x * rng.uniform(-0.1, 1.1) * g.width
+        y = g.start_y + g.spacing_y * rng.uniform(-0.1, 1.1) * g.length
+        lon, lat, _h = oracle_mod.proj_inverse(g.epsg, x, y)
+        llh = np.array([lon, lat, rng.uniform(0.0, 3000.0)])
+        xyz = np.zeros(3)
+        oracle_mod.lib().orc_lonlat_to_xyz(ell.a, ell.e2, llh.ctypes.data, xyz.ctypes.data)
+        t0, r0, ok0 = oracle_mod.geo2rdr(llh, ell, o, LUT2d(), rg.wavelength, rg.lookside, t_mid, 1e-8, 50, 1e-8)
+        t, r, cv = C.c_double(), C.c_double(), C.c_int32()
+        assert lib.gslc_geo2rdr_zero_doppler(C.byref(d), xyz.ctypes.data, t_mid, int(rg.lookside), 1e-8, 50,
+                                             C.byref(t), C.byref(r), C.byref(cv)) == 0
+        assert bool(cv.value) == bool(ok0)
+        if not ok0:
+            assert np.isnan(t.value) and np.isnan(r.value)
+            continue
+        if abs(t.value - t0) > 1e-9:      # stopped one iterate apart (|dt| at the threshold)
+            splits += 1
+            assert abs(t.value - t0) < 1e-8
+            continue
+        dts.append(abs(t.value - t0))
+        drs.append(abs(r.value - r0))
+    assert splits <= 0.01 * n
+    # the oracle's Hermite formula carries ~1e-11 s / ~4e-9 m of rounding noise
+    assert max(dts) < 5e-11 and max(drs) < 2e-8
+    t, r, cv = C.c_double(), C.c_double(), C.c_int32()
+    assert lib.gslc_geo2rdr_zero_doppler(C.byref(d), np.zeros(3).ctypes.data, t_mid, 0, 1e-8, 50,
+                                         C.byref(t), C.byref(r), C.byref(cv)) == L.GSLC_EINVAL
+
+
 def test_sinc_table_identical_to_oracle(lib, oracle_mod):
     tab = np.zeros((8192, 8), np.float32)
     assert lib.gslc_sinc_table(tab.ctypes.data) == 0
