@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBPATH = BUILD / "libgslc.so"
 HEADER = ROOT / "include" / "gslc.h"
-SOURCES = ["gslc_kernels.cu", "gslc_capi.cu", "gslc_batch.cu"]
+SOURCES = ["gslc_kernels.cu", "gslc_persistent.cu", "gslc_capi.cu", "gslc_batch.cu"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(ROOT / "include")]
@@ -38,7 +38,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile libgslc.so for sm_103a (translation units in parallel)."""
     BUILD.mkdir(exist_ok=True)
     srcs = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
-    deps = srcs + list(CSRC.glob("*.cuh")) + [HEADER]
+    deps = srcs + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.cu")) + [HEADER]
     if not force and LIBPATH.exists():
         newest = max(p.stat().st_mtime for p in deps)
         if LIBPATH.stat().st_mtime >= newest:
@@ -148,7 +148,7 @@ class RasterGeocodeArgs(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("tiles_per_pop", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
-                ("_pad", C.c_int32)]
+                ("rows_per_thread", C.c_int32)]
 
 
 _EXPORTS = {

@@ -1,11 +1,13 @@
 """Launch-shape autotuner for the batched geocode.
 
-For a batch it times a small set of persistent-kernel shapes — tiles taken
-per counter pop, persistent blocks per SM — with CUDA events on the real
-requests, keeps the fastest, and caches the choice in JSON keyed by GPU name
-and a hash of the batch's shape (request count, tile count bucket, geogrid
-projection, geo2rdr precision), so later batches of the same kind skip the
-search.  The tile itself is 32 x 8 output pixels, one per thread.
+For a batch it times a small set of persistent-kernel shapes — the tile
+shape (32 x 8, 32 x 16 or 32 x 32 output pixels, i.e. 1, 2 or 4 geogrid
+lines per thread; on UTM grids the tile is also the unit of the fitted
+projection inverse), tiles taken per counter pop, persistent blocks per SM —
+with CUDA events on the real requests, keeps the fastest, and caches the
+choice in JSON keyed by GPU name and a hash of the batch's shape (request
+count, tile count bucket, geogrid projection, geo2rdr precision), so later
+batches of the same kind skip the search.
 """
 from __future__ import annotations
 
@@ -68,14 +70,16 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
     if key in cache:
         c = cache[key]
         probe.close()
-        return BatchTuning(c["tiles_per_pop"], c["blocks_per_sm"], True), {"cached": c["ms"]}
+        return (BatchTuning(c["tiles_per_pop"], c["blocks_per_sm"], True, c.get("rows_per_thread", 4)),
+                {"cached": c["ms"]})
     occ = max(1, info["blocks"] // torch.cuda.get_device_properties(0).multi_processor_count)
     if candidates is None:
-        if info["tiles"] > 200_000:     # large batches: a short search, one timed launch each
-            candidates = [BatchTuning(p, occ) for p in (1, 2, 4)]
+        if info["tiles"] > 50_000:      # large batches: a short search, one timed launch each
+            candidates = [BatchTuning(p, occ, True, r) for r in (1, 2, 4) for p in (1, 2)]
             reps = 1
         else:
-            candidates = [BatchTuning(p, b) for p in (1, 2, 4, 8) for b in sorted({occ, max(1, occ - 1)})]
+            candidates = [BatchTuning(p, b, True, r) for r in (1, 2, 4) for p in (1, 2, 4)
+                          for b in sorted({occ, max(1, occ - 1)})]
     results = {}
     best, best_ms = None, float("inf")
     probe.close()
@@ -83,13 +87,14 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
         b = GeocodeBatch(requests, precision, t)
         ms = time_batch(b, reps)
         b.close()
-        results[(t.tiles_per_pop, t.blocks_per_sm)] = ms
+        results[(t.rows_per_thread, t.tiles_per_pop, t.blocks_per_sm)] = ms
         if ms < best_ms:
             best, best_ms = t, ms
     if use_cache:
         with _lock:
             cache = _load()
-            cache[key] = {"tiles_per_pop": best.tiles_per_pop, "blocks_per_sm": best.blocks_per_sm, "ms": best_ms,
+            cache[key] = {"tiles_per_pop": best.tiles_per_pop, "blocks_per_sm": best.blocks_per_sm,
+                          "rows_per_thread": best.rows_per_thread, "ms": best_ms,
                           "gpu": torch.cuda.get_device_name(), "precision": precision, "requests": len(requests)}
             _store(cache)
     return best, results

@@ -697,6 +697,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.gw = gg.width; p.gl = gg.length;
     p.geo_is_lonlat = gg.epsg == 4326;
     if (!p.geo_is_lonlat) utm_setup(gg.epsg, p.utm);
+    p.tile_fit = p.geo_is_lonlat ? 0 : 1;
 
     // DEM window the reference would load (loadDem.cpp:22-133)
     gslc_dem_window w;
@@ -1229,6 +1230,8 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
     b->stream = (cudaStream_t)stream_;
     const cudaStream_t st_ = b->stream;
 
+    const int rpt = tuning ? tuning->rows_per_thread : 0;
+    const int ppt = (rpt == 1 || rpt == 2 || rpt == 4) ? rpt : 4;
     std::vector<GeoParams> params;
     std::vector<std::vector<double>> coefs;
     std::vector<int> owner;                 // item index of each params entry
@@ -1346,7 +1349,7 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
             p.rdr[k] = use;
             p.geo[k] = (float2*)a.geo_blocks[block_base + k];
         }
-        const long long tiles = (long long)((p.gw + TILE_X - 1) / TILE_X) * ((p.gl + TILE_Y - 1) / TILE_Y);
+        const long long tiles = (long long)((p.gw + TILE_X - 1) / TILE_X) * ((p.gl + TILE_Y * ppt - 1) / (TILE_Y * ppt));
         tile_start[j + 1] = tile_start[j] + tiles;
     }
     if (e == cudaSuccess)
@@ -1391,7 +1394,8 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
     b->q.tiles_per_pop = (tuning && tuning->tiles_per_pop > 0) ? tuning->tiles_per_pop : 2;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int occ = std::max(1, persistent_blocks_per_sm(b->lonlat, b->ff));
+    b->q.ppt = ppt;
+    const int occ = std::max(1, persistent_blocks_per_sm(b->lonlat, b->ff, ppt));
     const int per_sm = (tuning && tuning->blocks_per_sm > 0) ? std::min(tuning->blocks_per_sm, occ) : occ;
     b->blocks = sms * per_sm;
     b->launches_per_run = (int64_t)b->deramps.size() + 1;

@@ -10,6 +10,9 @@
 //      then carrier reramp and flattening (geocodeSlc.cpp:298-394).
 // Nothing here is a dense contraction, so no tensor cores; the kernel is
 // bound by the FP64 pipe (geometry) and latency, not by HBM.
+// Built twice: as is (plain launch, deramp, probe) and with
+// GSLC_PERSISTENT_TU defined by gslc_persistent.cu (the persistent batched
+// kernel), so that the two sets of kernel instances compile in parallel.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include "gslc_kernels.cuh"
@@ -390,122 +393,282 @@ __device__ bool subswath_contains_gpu(const GeoParams& p, int az, int rg) {
     return false;
 }
 
-// Block shape: 32 geogrid columns x 8 lines.  Terms that depend only on the
-// column (easting/longitude) or only on the line (northing/latitude) are
-// evaluated once per block column/line into shared memory.
+// Block shape: 32 x 8 threads.  A tile is 32 geogrid columns x 8*PPT
+// lines; thread (tx, ty) geocodes lines ty, ty + 8, ... of column tx, so a
+// warp stores 32 consecutive pixels of one line.
 constexpr int GBX = 32, GBY = 8;
 
-// One GBX x GBY tile (tile column bx, tile line by) of one geocode request.
+// ---- tile fit of the projection inverse (UTM geogrids) --------------------
+// Over one tile (at most 1 km on a side) the map from (column, line) to the
+// DEM coordinates of the point, to lonLatToXyz(lon, lat, 0) and to the
+// ellipsoid normal is smooth to far below the rounding of its exact
+// evaluation: a bicubic Lagrange interpolant through 4 x 4 node pixels has a
+// truncation error below 1e-16 rad (3e-10 m) there, so it stands in for the
+// per-pixel UTM inverse (core/Projections.cpp:200-232), the DEM coordinate
+// arithmetic (geometry/DEMInterpolator.cpp:593-646) and the trigonometry of
+// Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190).  The nodes are evaluated
+// exactly; the interpolation adds a few ulps of rounding (coordinates) and
+// ~3e-9 m (positions).  Tiles where a node fails the inverse, or where nodes
+// disagree on the DEM branch (west edge, 360-degree wrap, DEM forward
+// projection), take the exact per-pixel path.
+constexpr int FIT_Q = 8;   // dem row, dem col, xyz0[3], normal[3]
+
+template <int N>
+struct FitNodes {
+    int v[4];
+    constexpr FitNodes() : v{0, (N - 1 + 1) / 3, (2 * (N - 1) + 1) / 3, N - 1} {}
+};
+
+struct FitWeights {
+    double x[GBX][4];          // Lagrange weights of the column nodes
+    double y8[8][4], y16[16][4], y32[32][4];
+};
+
+template <int N>
+constexpr void fit_weights(double (&w)[N][4]) {
+    const FitNodes<N> nd;
+    for (int t = 0; t < N; ++t)
+        for (int i = 0; i < 4; ++i) {
+            double v = 1.0;
+            for (int k = 0; k < 4; ++k)
+                if (k != i) v = v * (double)(t - nd.v[k]) / (double)(nd.v[i] - nd.v[k]);
+            w[t][i] = v;
+        }
+}
+
+constexpr FitWeights make_fit_weights() {
+    FitWeights f{};
+    fit_weights<GBX>(f.x);
+    fit_weights<8>(f.y8);
+    fit_weights<16>(f.y16);
+    fit_weights<32>(f.y32);
+    return f;
+}
+
+__constant__ FitWeights c_fit = make_fit_weights();
+
+template <int TY>
+__device__ __forceinline__ double fit_wy(int r, int j) {
+    if (TY == 8) return c_fit.y8[r][j];
+    if (TY == 16) return c_fit.y16[r][j];
+    return c_fit.y32[r][j];
+}
+
+// DEM column for an EPSG:4326 DEM as dem_col_lonlat, with the branch taken:
+// 0 none, 1 -360, 2 +360, 3 west of the DEM (reference height), +4 if the
+// 360-degree fmod applied.
+__device__ __forceinline__ int dem_col_lonlat_branch(const Dem& d, double lon, double& col) {
+    double X = (lon * 180.0) / PI;
+    int br = 0;
+    if (X > 360 || X < -360) { X = fmod(X, 360.0); br = 4; }
+    if (X < -180) X += 360;
+    if (X - 360 >= d.x_start) { X -= 360; br += 1; }
+    else if (X < d.x_start && X + 360 >= d.x_start) { X += 360; br += 2; }
+    else if (X < d.x_start) return br + 3;
+    col = (X - d.x_start) / d.dx;
+    return br;
+}
+
+// Exact values of the fitted quantities at one node pixel; the DEM branch,
+// or -1 where the UTM inverse fails.
+template <bool RASTER>
+__device__ int fit_node(const GeoParams& p, int pixel, int line, double* F) {
+    const double x = dadd(p.gx0, dmul(p.gdx, (double)pixel + 0.5));
+    const double y = dadd(p.gy0, dmul(p.gdy, (double)(line + p.geo_row0) + 0.5));
+    const UtmCol c = utm_inverse_col(p.utm, x);
+    if (!c.ok) return -1;
+    const UtmRow r = utm_inverse_row(p.utm, y);
+    const LonLatSC ll = utm_inverse_px(p.utm, r, c);
+    double row = 0.0, col = 0.0;
+    int br = 0;
+    if (p.dem.have_raster) {
+        if (p.dem.epsg_is_lonlat) {
+            row = dem_row_lonlat(p.dem, ll.lat);
+            if (RASTER) col = dem_col_lonlat_nowrap(p.dem, ll.lon);
+            else br = dem_col_lonlat_branch(p.dem, ll.lon, col);
+        } else {
+            br = dem_coords_utm(p.dem, ll.lon, ll.lat, row, col) ? 0 : 3;
+        }
+    }
+    const double re = p.ell_a / sqrt(1.0 - p.ell_e2 * (ll.slat * ll.slat));
+    F[0] = row;
+    F[1] = col;
+    F[2] = re * ll.clat * ll.clon;
+    F[3] = re * ll.clat * ll.slon;
+    F[4] = (re * (1.0 - p.ell_e2)) * ll.slat;
+    F[5] = ll.clat * ll.clon;
+    F[6] = ll.clat * ll.slon;
+    F[7] = ll.slat;
+    return br;
+}
+
+template <bool FF, bool RASTER>
+__device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, bool ok, V3 xyz);
+
+// One tile (tile column bx, tile line by) of one geocode request.
 // RASTER selects the generic CUDA raster geocoder's per-pixel rules
 // (cuda/geocode/Geocode.cu:87-172 and :203-287): DEM through the CUDA
 // interpolator, corrections and native Doppler that do not contain the
 // point mask it, no Doppler demodulation, carrier or flattening.
-template <bool GEO_LONLAT, bool FF, bool RASTER>
+template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
 __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by) {
+    constexpr int TY = GBY * PPT;
     __shared__ double s_col[4][GBX];
-    __shared__ double s_row[5][GBY];
+    __shared__ double s_row[5][TY];
     __shared__ int s_colok[GBX];
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    __shared__ double s_F[16][FIT_Q];
+    __shared__ int s_nb[16];
+    __shared__ double s_G[TY][FIT_Q][4];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * GBX + tx;
     const int pixel = bx * GBX + tx;
-    const int line = by * GBY + ty;
+    const int line0 = by * TY;
     const bool dem_ll = p.dem.have_raster && p.dem.epsg_is_lonlat;
 
-    if (ty == 0) {
-        // pixel centre easting/longitude (geocodeSlc.cpp:103), same rounding as the reference
-        const int pc = min(pixel, p.gw - 1);
-        const double x = dadd(p.gx0, dmul(p.gdx, (double)pc + 0.5));
-        if (GEO_LONLAT) {
-            const double lon = (x * PI) / 180.0;          // LonLat::inverse (Projections.h:136-140)
-            double sl, cl;
-            sincos(lon, &sl, &cl);
-            double col = 0.0;
-            if (RASTER) {
-                s_colok[tx] = 1;
-                if (dem_ll) col = dem_col_lonlat_nowrap(p.dem, lon);
-            } else {
-                s_colok[tx] = dem_ll ? (dem_col_lonlat(p.dem, lon, col) ? 1 : 0) : 1;
+    bool fit = false;
+    if (!GEO_LONLAT && p.tile_fit && fabs(p.gdx) * (GBX - 1) <= 1000.0 && fabs(p.gdy) * (TY - 1) <= 1000.0) {
+        constexpr FitNodes<GBX> nx;
+        constexpr FitNodes<TY> ny;
+        if (tid < 16) s_nb[tid] = fit_node<RASTER>(p, bx * GBX + nx.v[tid & 3], line0 + ny.v[tid >> 2], s_F[tid]);
+        __syncthreads();
+        fit = s_nb[0] >= 0;
+#pragma unroll
+        for (int n = 1; n < 16; ++n) fit = fit && s_nb[n] == s_nb[0];
+        if (fit) {
+            // the node values reduced over the line nodes, per tile line:
+            // G[r][q][i] = sum_j F[j][i][q] * wy[r][j]
+            for (int idx = tid; idx < TY * FIT_Q * 4; idx += GBX * GBY) {
+                const int r = idx / (FIT_Q * 4), q = (idx >> 2) % FIT_Q, i = idx & 3;
+                double g = 0.0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) g = fma(s_F[j * 4 + i][q], fit_wy<TY>(r, j), g);
+                s_G[r][q][i] = g;
             }
-            s_col[0][tx] = lon;
-            s_col[1][tx] = sl;
-            s_col[2][tx] = cl;
-            s_col[3][tx] = col;
-        } else {
-            const UtmCol c = utm_inverse_col(p.utm, x);
-            s_col[0][tx] = c.Ce;
-            s_col[1][tx] = c.shi;
-            s_col[2][tx] = c.chi;
-            s_colok[tx] = c.ok;
-        }
-    } else if (ty == 1 && tx < GBY) {
-        const int lr = min(by * GBY + tx, p.gl - 1) + p.geo_row0;
-        const double y = dadd(p.gy0, dmul(p.gdy, (double)lr + 0.5));   // geocodeSlc.cpp:100
-        if (GEO_LONLAT) {
-            const double lat = (y * PI) / 180.0;
-            double sl, cl;
-            sincos(lat, &sl, &cl);
-            s_row[0][tx] = lat;
-            s_row[1][tx] = sl;
-            s_row[2][tx] = cl;
-            s_row[3][tx] = p.ell_a / sqrt(1.0 - p.ell_e2 * (sl * sl));    // rEast (Ellipsoid.h:117-120)
-            s_row[4][tx] = dem_ll ? dem_row_lonlat(p.dem, lat) : 0.0;
-        } else {
-            const UtmRow r = utm_inverse_row(p.utm, y);
-            s_row[0][tx] = r.Cn;
-            s_row[1][tx] = r.sr;
-            s_row[2][tx] = r.cr;
+            __syncthreads();
         }
     }
-    __syncthreads();
-    if (pixel >= p.gw || line >= p.gl) return;
-    const int64_t k = (int64_t)line * p.gw + pixel;
+    if (!fit) {
+        if (ty == 0) {
+            // pixel centre easting/longitude (geocodeSlc.cpp:103), same rounding as the reference
+            const int pc = min(pixel, p.gw - 1);
+            const double x = dadd(p.gx0, dmul(p.gdx, (double)pc + 0.5));
+            if (GEO_LONLAT) {
+                const double lon = (x * PI) / 180.0;          // LonLat::inverse (Projections.h:136-140)
+                double sl, cl;
+                sincos(lon, &sl, &cl);
+                double col = 0.0;
+                if (RASTER) {
+                    s_colok[tx] = 1;
+                    if (dem_ll) col = dem_col_lonlat_nowrap(p.dem, lon);
+                } else {
+                    s_colok[tx] = dem_ll ? (dem_col_lonlat(p.dem, lon, col) ? 1 : 0) : 1;
+                }
+                s_col[0][tx] = lon;
+                s_col[1][tx] = sl;
+                s_col[2][tx] = cl;
+                s_col[3][tx] = col;
+            } else {
+                const UtmCol c = utm_inverse_col(p.utm, x);
+                s_col[0][tx] = c.Ce;
+                s_col[1][tx] = c.shi;
+                s_col[2][tx] = c.chi;
+                s_colok[tx] = c.ok;
+            }
+        } else if (ty == 1 && tx < TY) {
+            const int lr = min(line0 + tx, p.gl - 1) + p.geo_row0;
+            const double y = dadd(p.gy0, dmul(p.gdy, (double)lr + 0.5));   // geocodeSlc.cpp:100
+            if (GEO_LONLAT) {
+                const double lat = (y * PI) / 180.0;
+                double sl, cl;
+                sincos(lat, &sl, &cl);
+                s_row[0][tx] = lat;
+                s_row[1][tx] = sl;
+                s_row[2][tx] = cl;
+                s_row[3][tx] = p.ell_a / sqrt(1.0 - p.ell_e2 * (sl * sl));    // rEast (Ellipsoid.h:117-120)
+                s_row[4][tx] = dem_ll ? dem_row_lonlat(p.dem, lat) : 0.0;
+            } else {
+                const UtmRow r = utm_inverse_row(p.utm, y);
+                s_row[0][tx] = r.Cn;
+                s_row[1][tx] = r.sr;
+                s_row[2][tx] = r.cr;
+            }
+        }
+        __syncthreads();
+    }
+    if (pixel >= p.gw) return;
+    double wx[4];
+    if (fit) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) wx[i] = c_fit.x[tx][i];
+    }
+#pragma unroll 1
+    for (int kk = 0; kk < PPT; ++kk) {
+        const int r = ty + GBY * kk;       // tile line
+        const int line = line0 + r;
+        if (line >= p.gl) break;
+        const int64_t k = (int64_t)line * p.gw + pixel;
+        bool ok = true;
+        V3 xyz;
+        if (fit) {
+            double f[FIT_Q];
+#pragma unroll
+            for (int q = 0; q < FIT_Q; ++q)
+                f[q] = fma(s_G[r][q][0], wx[0], fma(s_G[r][q][1], wx[1], fma(s_G[r][q][2], wx[2], s_G[r][q][3] * wx[3])));
+            double h = 0.0;
+            if (p.dem.have_raster && (s_nb[0] & 3) != 3) h = dem_height<RASTER>(p.dem, f[0], f[1]);
+            xyz = {fma(h, f[5], f[2]), fma(h, f[6], f[3]), fma(h, f[7], f[4])};
+        } else if (GEO_LONLAT) {
+            double h = 0.0;
+            if (p.dem.have_raster) {
+                if (dem_ll) {
+                    if (s_colok[tx]) h = dem_height<RASTER>(p.dem, s_row[4][r], s_col[3][tx]);
+                } else {
+                    double row, col;
+                    if (dem_coords_utm(p.dem, s_col[0][tx], s_row[0][r], row, col))
+                        h = dem_height<RASTER>(p.dem, row, col);
+                }
+            }
+            // lonLatToXyz (Ellipsoid.h:177-190) with the line's rEast and the sines/cosines above
+            const double re = s_row[3][r], slat = s_row[1][r], clat = s_row[2][r];
+            xyz = {(re + h) * clat * s_col[2][tx], (re + h) * clat * s_col[1][tx],
+                   ((re * (1.0 - p.ell_e2)) + h) * slat};
+        } else {
+            ok = s_colok[tx];
+            if (!ok) {
+                if (!RASTER) atomicOr(p.err, 1);   // the raster geocoder does not check the inverse
+            } else {
+                UtmCol c;
+                c.Ce = s_col[0][tx]; c.shi = s_col[1][tx]; c.chi = s_col[2][tx]; c.ok = 1;
+                UtmRow rr;
+                rr.Cn = s_row[0][r]; rr.sr = s_row[1][r]; rr.cr = s_row[2][r];
+                const LonLatSC ll = utm_inverse_px(p.utm, rr, c);
+                double h = 0.0;
+                if (p.dem.have_raster) {
+                    double row, col;
+                    if (dem_ll) {
+                        if (RASTER)
+                            h = dem_height<true>(p.dem, dem_row_lonlat(p.dem, ll.lat), dem_col_lonlat_nowrap(p.dem, ll.lon));
+                        else if (dem_col_lonlat(p.dem, ll.lon, col))
+                            h = dem_spline(p.dem, dem_row_lonlat(p.dem, ll.lat), col);
+                    } else if (dem_coords_utm(p.dem, ll.lon, ll.lat, row, col)) {
+                        h = dem_height<RASTER>(p.dem, row, col);
+                    }
+                }
+                xyz = lonlat_to_xyz_sc(p.ell_a, p.ell_e2, ll.slon, ll.clon, ll.slat, ll.clat, h);
+            }
+        }
+        geocode_pixel<FF, RASTER>(p, k, ok, xyz);
+    }
+}
 
+// Everything after the ground point: geo2rdr, corrections, masks, the
+// radar-coordinate outputs, the sinc interpolation of every block, reramp
+// and flattening, for output pixel k.
+template <bool FF, bool RASTER>
+__device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, bool ok, V3 xyz) {
     bool valid = false;
     uint8_t mval = 255;
     double azc = CUDART_NAN, rgc = CUDART_NAN;
     double R_uncorr = (double)p.inv_re;
-
-    bool ok = true;
-    V3 xyz;
-    if (GEO_LONLAT) {
-        double h = 0.0;
-        if (p.dem.have_raster) {
-            if (dem_ll) {
-                if (s_colok[tx]) h = dem_height<RASTER>(p.dem, s_row[4][ty], s_col[3][tx]);
-            } else {
-                double row, col;
-                if (dem_coords_utm(p.dem, s_col[0][tx], s_row[0][ty], row, col))
-                    h = dem_height<RASTER>(p.dem, row, col);
-            }
-        }
-        // lonLatToXyz (Ellipsoid.h:177-190) with the line's rEast and the sines/cosines above
-        const double re = s_row[3][ty], slat = s_row[1][ty], clat = s_row[2][ty];
-        xyz = {(re + h) * clat * s_col[2][tx], (re + h) * clat * s_col[1][tx],
-               ((re * (1.0 - p.ell_e2)) + h) * slat};
-    } else {
-        ok = s_colok[tx];
-        if (!ok) {
-            if (!RASTER) atomicOr(p.err, 1);   // the raster geocoder does not check the inverse
-        } else {
-            UtmCol c;
-            c.Ce = s_col[0][tx]; c.shi = s_col[1][tx]; c.chi = s_col[2][tx]; c.ok = 1;
-            UtmRow r;
-            r.Cn = s_row[0][ty]; r.sr = s_row[1][ty]; r.cr = s_row[2][ty];
-            const LonLatSC ll = utm_inverse_px(p.utm, r, c);
-            double h = 0.0;
-            if (p.dem.have_raster) {
-                double row, col;
-                if (dem_ll) {
-                    if (RASTER)
-                        h = dem_height<true>(p.dem, dem_row_lonlat(p.dem, ll.lat), dem_col_lonlat_nowrap(p.dem, ll.lon));
-                    else if (dem_col_lonlat(p.dem, ll.lon, col))
-                        h = dem_spline(p.dem, dem_row_lonlat(p.dem, ll.lat), col);
-                } else if (dem_coords_utm(p.dem, ll.lon, ll.lat, row, col)) {
-                    h = dem_height<RASTER>(p.dem, row, col);
-                }
-            }
-            xyz = lonlat_to_xyz_sc(p.ell_a, p.ell_e2, ll.slon, ll.clon, ll.slat, ll.clat, h);
-        }
-    }
     if (ok) {
         double t, R;
         bool conv;
@@ -617,15 +780,15 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     }
 }
 
-template <bool GEO_LONLAT, bool FF, bool RASTER>
+template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
 __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
-    geocode_block<GEO_LONLAT, FF, RASTER>(p, blockIdx.x, blockIdx.y);
+    geocode_block<GEO_LONLAT, FF, RASTER, PPT>(p, blockIdx.x, blockIdx.y);
 }
 
 // Persistent form: blocks pop runs of tiles of any request in the batch from
 // one counter until the batch is exhausted.  Requests keep their own
 // parameters, so each request's output equals its plain call.
-template <bool GEO_LONLAT, bool FF>
+template <bool GEO_LONLAT, bool FF, int PPT>
 __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_constant__ BatchQueue q) {
     __shared__ long long s_base;
     for (;;) {
@@ -648,7 +811,7 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
             const GeoParams& p = q.items[lo];
             const long long local = tile - q.tile_start[lo];
             const int tiles_x = (p.gw + GBX - 1) / GBX;
-            geocode_block<GEO_LONLAT, FF, false>(p, (int)(local % tiles_x), (int)(local / tiles_x));
+            geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x));
             if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
             __syncthreads();
             if (q.done_flags && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -664,6 +827,7 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
     }
 }
 
+#ifndef GSLC_PERSISTENT_TU
 // The carrier on one radar line, in the reference's operation order
 // (core/Poly2d.cpp:8-24, core/LUT2d.cpp:124-158): a Poly2d of range order 0
 // is constant along the line; otherwise it is evaluated per sample.
@@ -758,58 +922,44 @@ __global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, int iters,
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+#endif  // GSLC_PERSISTENT_TU
+
 }  // namespace
 
+#ifndef GSLC_PERSISTENT_TU
 cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s) {
     dfma_probe_kernel<<<blocks, 256, 0, s>>>(out, iters, 0.9999999, 1e-7);
     return cudaGetLastError();
 }
 
-cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
+template <int PPT>
+void launch_geocode_ppt(const GeoParams& p, bool ff, cudaStream_t s) {
     const dim3 block(GBX, GBY);
-    const dim3 grid((p.gw + GBX - 1) / GBX, (p.gl + GBY - 1) / GBY);
+    const dim3 grid((p.gw + GBX - 1) / GBX, (p.gl + GBY * PPT - 1) / (GBY * PPT));
+    if (p.raster) {
+        if (p.geo_is_lonlat) {
+            if (ff) geocode_kernel<true, true, true, PPT><<<grid, block, 0, s>>>(p);
+            else geocode_kernel<true, false, true, PPT><<<grid, block, 0, s>>>(p);
+        } else {
+            if (ff) geocode_kernel<false, true, true, PPT><<<grid, block, 0, s>>>(p);
+            else geocode_kernel<false, false, true, PPT><<<grid, block, 0, s>>>(p);
+        }
+    } else if (p.geo_is_lonlat) {
+        if (ff) geocode_kernel<true, true, false, PPT><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<true, false, false, PPT><<<grid, block, 0, s>>>(p);
+    } else {
+        if (ff) geocode_kernel<false, true, false, PPT><<<grid, block, 0, s>>>(p);
+        else geocode_kernel<false, false, false, PPT><<<grid, block, 0, s>>>(p);
+    }
+}
+
+cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
     // the float-float path covers zero image-grid Doppler with the first
     // iterate at sensingMid; anything else runs in FP64
     const bool ff = precision == 1 && p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0;
-    if (p.raster) {
-        if (p.geo_is_lonlat) {
-            if (ff) geocode_kernel<true, true, true><<<grid, block, 0, s>>>(p);
-            else geocode_kernel<true, false, true><<<grid, block, 0, s>>>(p);
-        } else {
-            if (ff) geocode_kernel<false, true, true><<<grid, block, 0, s>>>(p);
-            else geocode_kernel<false, false, true><<<grid, block, 0, s>>>(p);
-        }
-    } else if (p.geo_is_lonlat) {
-        if (ff) geocode_kernel<true, true, false><<<grid, block, 0, s>>>(p);
-        else geocode_kernel<true, false, false><<<grid, block, 0, s>>>(p);
-    } else {
-        if (ff) geocode_kernel<false, true, false><<<grid, block, 0, s>>>(p);
-        else geocode_kernel<false, false, false><<<grid, block, 0, s>>>(p);
-    }
+    launch_geocode_ppt<4>(p, ff, s);     // the plain form uses 32 x 32-pixel tiles
     if (launches) ++*launches;
     return cudaGetLastError();
-}
-
-cudaError_t launch_geocode_persistent(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s,
-                                      int64_t* launches) {
-    const dim3 block(GBX, GBY);
-    if (lonlat) {
-        if (ff) geocode_persistent<true, true><<<blocks, block, 0, s>>>(q);
-        else geocode_persistent<true, false><<<blocks, block, 0, s>>>(q);
-    } else {
-        if (ff) geocode_persistent<false, true><<<blocks, block, 0, s>>>(q);
-        else geocode_persistent<false, false><<<blocks, block, 0, s>>>(q);
-    }
-    if (launches) ++*launches;
-    return cudaGetLastError();
-}
-
-int persistent_blocks_per_sm(bool lonlat, bool ff) {
-    int n = 0;
-    const void* f = lonlat ? (ff ? (const void*)geocode_persistent<true, true> : (const void*)geocode_persistent<true, false>)
-                           : (ff ? (const void*)geocode_persistent<false, true> : (const void*)geocode_persistent<false, false>);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, GBX * GBY, 0);
-    return n;
 }
 
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches) {
@@ -820,5 +970,44 @@ cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launch
     if (launches) ++*launches;
     return cudaGetLastError();
 }
+
+#else
+template <int PPT>
+void launch_persistent_ppt(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s) {
+    const dim3 block(GBX, GBY);
+    if (lonlat) {
+        if (ff) geocode_persistent<true, true, PPT><<<blocks, block, 0, s>>>(q);
+        else geocode_persistent<true, false, PPT><<<blocks, block, 0, s>>>(q);
+    } else {
+        if (ff) geocode_persistent<false, true, PPT><<<blocks, block, 0, s>>>(q);
+        else geocode_persistent<false, false, PPT><<<blocks, block, 0, s>>>(q);
+    }
+}
+
+cudaError_t launch_geocode_persistent(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s,
+                                      int64_t* launches) {
+    switch (q.ppt) {
+        case 1: launch_persistent_ppt<1>(q, lonlat, ff, blocks, s); break;
+        case 2: launch_persistent_ppt<2>(q, lonlat, ff, blocks, s); break;
+        default: launch_persistent_ppt<4>(q, lonlat, ff, blocks, s); break;
+    }
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+template <int PPT>
+const void* persistent_fn(bool lonlat, bool ff) {
+    return lonlat ? (ff ? (const void*)geocode_persistent<true, true, PPT> : (const void*)geocode_persistent<true, false, PPT>)
+                  : (ff ? (const void*)geocode_persistent<false, true, PPT> : (const void*)geocode_persistent<false, false, PPT>);
+}
+
+int persistent_blocks_per_sm(bool lonlat, bool ff, int ppt) {
+    int n = 0;
+    const void* f = ppt == 1 ? persistent_fn<1>(lonlat, ff) : ppt == 2 ? persistent_fn<2>(lonlat, ff) : persistent_fn<4>(lonlat, ff);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, GBX * GBY, 0);
+    return n;
+}
+
+#endif  // GSLC_PERSISTENT_TU
 
 }  // namespace gslc

@@ -67,6 +67,8 @@ struct GeoParams {
     // this launch and the invalid value of each raster
     int32_t raster, geo_row0;
     float inv_blk[MAX_BLOCKS];
+    // 1: UTM tiles may use the fitted projection inverse
+    int32_t tile_fit, _pad3;
 };
 
 struct DerampParams {
@@ -84,6 +86,7 @@ struct BatchQueue {
     const long long* tile_start; // n_items + 1, tile_start[0] = 0
     int32_t n_items, tiles_per_pop;
     long long n_tiles;
+    int32_t ppt, _pad;               // geogrid lines per thread of every request's tiles
     long long* counter;          // zeroed before each launch
     // per-request completion (optional: done_flags == nullptr disables it)
     const int32_t* item_request;     // n_items: request of each items[] entry
@@ -98,7 +101,7 @@ cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launch
 cudaError_t probe_fp64(double* out, int blocks, int iters, cudaStream_t s);
 cudaError_t launch_geocode_persistent(const BatchQueue& q, bool lonlat, bool ff, int blocks, cudaStream_t s,
                                       int64_t* launches);
-int persistent_blocks_per_sm(bool lonlat, bool ff);
-constexpr int TILE_X = 32, TILE_Y = 8;   // geogrid pixels per tile
+int persistent_blocks_per_sm(bool lonlat, bool ff, int ppt);
+constexpr int TILE_X = 32, TILE_Y = 8;   // geogrid pixels per tile at one line per thread
 
 }  // namespace gslc
