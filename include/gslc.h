@@ -151,6 +151,14 @@ typedef struct {
     int32_t rdr_deramped;           /* 1: blocks already carry the deramp of these carriers (resident
                                        stores deramp once); the reramp still applies */
     int32_t _pad2;
+    /* Sample formats (the GSLC workflow's codecs, nisar/workflows/gslc.py:185-226,
+     * isce3/core/types.py:38-165), applied inside the kernel's loads and stores:
+     * rdr_format 0 complex64, 1 complex32 (float16 pairs, decoded exactly);
+     * geo_format 0 complex64, 1 complex32 (float32 -> float16 round to nearest
+     * even, as numpy's astype), 2 complex64 with all but mantissa_bits mantissa
+     * bits zeroed (truncate_mantissa). */
+    int32_t rdr_format, geo_format;
+    int32_t mantissa_bits, _pad3;
 } gslc_geocode_args;
 
 int gslc_ctx_create(int device, gslc_ctx** out);

@@ -131,7 +131,9 @@ class GeocodeArgs(C.Structure):
                 ("mask", C.c_void_p), ("carrier_phase", C.c_void_p), ("flatten_phase", C.c_void_p),
                 ("az_index", C.c_void_p), ("rg_index", C.c_void_p), ("dem", DemRaster),
                 ("dem_margin", C.c_int32), ("geo2rdr_precision", C.c_int32),
-                ("subswaths", C.POINTER(SubSwathsDesc)), ("rdr_deramped", C.c_int32), ("_pad2", C.c_int32)]
+                ("subswaths", C.POINTER(SubSwathsDesc)), ("rdr_deramped", C.c_int32), ("_pad2", C.c_int32),
+                ("rdr_format", C.c_int32), ("geo_format", C.c_int32), ("mantissa_bits", C.c_int32),
+                ("_pad3", C.c_int32)]
 
 
 class RasterGeocodeArgs(C.Structure):

@@ -575,7 +575,7 @@ extern "C" int gslc_geo2rdr_zero_doppler(const gslc_orbit* o, const double* xyz,
         R = vnorm(rvec);
         ok = true;
     } else {
-        ok = geo2rdr_zero_doppler_seg(ob, x, threshold, maxiter, t, dt, R);
+        ok = geo2rdr_zero_doppler_seg(ob, ob.seg, x, threshold, maxiter, t, dt, R);
     }
     if (ok) {
         *aztime = t;
@@ -687,6 +687,12 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
         return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
     if (a->rdr_length < 0 || a->rdr_width < 0) return set_err(c, GSLC_EINVAL, "invalid radar block shape");
+    if (a->rdr_format != 0 && a->rdr_format != 1) return set_err(c, GSLC_EINVAL, "rdr_format must be 0 (complex64) or 1 (complex32)");
+    if (a->geo_format < 0 || a->geo_format > 2) return set_err(c, GSLC_EINVAL, "geo_format must be 0, 1 or 2");
+    if (a->geo_format == 2 && !(a->mantissa_bits > 0 && a->mantissa_bits <= 23))
+        return set_err(c, GSLC_EINVAL, "Require 0 < significant_bits <= 23");
+    if (a->rdr_format == 1 && a->inplace_deramp)
+        return set_err(c, GSLC_EINVAL, "in-place deramp needs complex64 radar blocks");
     if (gg.width == 0 || gg.length == 0) return GSLC_EMPTY_GRID;
     for (const gslc_lut2d* l : {&a->native_doppler, &a->image_grid_doppler, &a->az_time_correction, &a->srange_correction})
         if (int st = check_lut(c, *l, "LUT2d")) return st;
@@ -698,6 +704,9 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.geo_is_lonlat = gg.epsg == 4326;
     if (!p.geo_is_lonlat) utm_setup(gg.epsg, p.utm);
     p.tile_fit = p.geo_is_lonlat ? 0 : 1;
+    p.rdr_c32 = a->rdr_format == 1 ? 1 : 0;
+    p.geo_fmt = a->geo_format;
+    p.mant_bits = a->geo_format == 2 ? a->mantissa_bits : 23;
 
     // DEM window the reference would load (loadDem.cpp:22-133)
     gslc_dem_window w;
@@ -827,6 +836,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
             DerampParams dp;
             std::memset(&dp, 0, sizeof(dp));
             dp.src = rdr[b]; dp.dst = dst;
+            dp.src_c32 = p.rdr_c32;
             dp.inL = a->rdr_length; dp.inW = a->rdr_width;
             dp.az_first = a->first_azimuth_line; dp.rg_first = a->first_range_sample;
             dp.rg_t0 = rg.sensing_start; dp.rg_prf = rg.prf; dp.rg_r0 = rg.starting_range; dp.rg_dr = rg.range_pixel_spacing;
@@ -836,6 +846,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
             if (e != cudaSuccess) return cuda_err(c, e, "deramp launch");
             rdr[b] = dst;
         }
+        p.rdr_c32 = 0;      // the deramped copies are complex64
     }
     if (c->timing) {
         cudaEventRecord(c->ev[3], stream);
@@ -860,6 +871,7 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
         cudaEventElapsedTime(&c->ms_deramp, c->ev[2], c->ev[3]);
     }
     if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    if (c->h_err[0] & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
     return GSLC_OK;
 }
 
@@ -927,6 +939,8 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
     bind_orbit(p, c->d_orbit);
     p.sinc = c->d_sinc;
     p.err = c->d_err;
+    e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "memset");
     if (c->timing) cudaEventRecord(c->ev[0], stream);
     const gslc_geo_grid& gg = r->geo_grid;
     const int lpb = r->lines_per_block;
@@ -959,12 +973,14 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
         }
     }
     if (c->timing) cudaEventRecord(c->ev[1], stream);
-    e = cudaStreamSynchronize(stream);
+    e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return cuda_err(c, e, "geocode");
     if (c->timing) {
         cudaEventElapsedTime(&c->ms_geocode, c->ev[0], c->ev[1]);
         c->ms_deramp = 0.f;
     }
+    if (c->h_err[0] & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
     return GSLC_OK;
 }
 
@@ -1123,6 +1139,9 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     if (!to_azrg(&c, a->az_carrier, az, "az_carrier") && !to_azrg(&c, a->rg_carrier, rg, "rg_carrier"))
         carriers = !(az.is_zero && rg.is_zero);
     const int64_t nrdr = a->rdr_length * a->rdr_width;
+    if (carriers && !a->rdr_deramped && nrdr > 0 && a->rdr_format == 1)
+        return noalloc_fail(errbuf, errbuf_len, GSLC_EUNSUPPORTED,
+                            "complex32 radar blocks with carriers need the deramp scratch of gslc_geocode_slc");
     if (carriers && !a->inplace_deramp && !a->rdr_deramped && nrdr > 0) {
         // deramp works on a copy in the static scratch; the caller's blocks stay as given
         if (nrdr * a->n_blocks > NOALLOC_MAX_DERAMP)
@@ -1337,6 +1356,7 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
                 DerampParams dp;
                 std::memset(&dp, 0, sizeof(dp));
                 dp.src = src; dp.dst = dst;
+                dp.src_c32 = params[j].rdr_c32;
                 dp.inL = a.rdr_length; dp.inW = a.rdr_width;
                 dp.az_first = a.first_azimuth_line; dp.rg_first = a.first_range_sample;
                 const gslc_radar_grid& rg = a.radar_grid;
@@ -1349,6 +1369,7 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
             p.rdr[k] = use;
             p.geo[k] = (float2*)a.geo_blocks[block_base + k];
         }
+        if (!p.carriers_zero && nrdr > 0 && !a.rdr_deramped) p.rdr_c32 = 0;   // deramped copies are complex64
         const long long tiles = (long long)((p.gw + TILE_X - 1) / TILE_X) * ((p.gl + TILE_Y * ppt - 1) / (TILE_Y * ppt));
         tile_start[j + 1] = tile_start[j] + tiles;
     }
@@ -1436,6 +1457,8 @@ extern "C" int gslc_batch_status(gslc_batch* b, void* stream) {
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return batch_fail(b, b->ctx, GSLC_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
     if (b->h_err[0] & 1) return batch_fail(b, b->ctx, GSLC_EPROJ, "Inverse projection transformation failed");
+    if (b->h_err[0] & 2)
+        return batch_fail(b, b->ctx, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
     return GSLC_OK;
 }
 

@@ -15,6 +15,7 @@
 // kernel), so that the two sets of kernel instances compile in parallel.
 #include <cuda_runtime.h>
 #include <math_constants.h>
+#include <cuda_fp16.h>
 #include "gslc_kernels.cuh"
 
 namespace gslc {
@@ -161,7 +162,7 @@ __device__ bool update_aztime(const GeoParams& p, V3 xyz, double& t) {
 // geocoder passes its delta_range argument).  With a
 // zero image-grid Doppler the slant range enters only the returned iterate,
 // so it is formed once, after convergence.
-__device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
+__device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t, double& R) {
     const double dr = p.dop_dr;
     t = p.t_mid;
     const bool first_shared = p.t_mid_in_orbit;
@@ -180,7 +181,7 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
             R = vnorm(rvec);
             return true;
         }
-        return p.maxiter > 1 && geo2rdr_zero_doppler_seg(p.orbit, xyz, p.thr, p.maxiter, t, dt, R);
+        return p.maxiter > 1 && geo2rdr_zero_doppler_seg(p.orbit, seg, xyz, p.thr, p.maxiter, t, dt, R);
     }
     const double half_wvl = 0.5 * p.rg_wvl;
     double dt = 0.0;
@@ -204,7 +205,7 @@ __device__ bool geo2rdr(const GeoParams& p, V3 xyz, double& t, double& R) {
                 R = vnorm(rvec);
                 return true;
             }
-            return geo2rdr_zero_doppler_seg(p.orbit, xyz, p.thr, p.maxiter, t, dt, R);
+            return geo2rdr_zero_doppler_seg(p.orbit, seg, xyz, p.thr, p.maxiter, t, dt, R);
         }
         R = vnorm(rvec);
         if (dop_data && p.img_dop.bounds_error &&
@@ -325,7 +326,14 @@ __device__ int subswath_of(const GeoParams& p, int az, int rg) {
 // geocodeSlc.cpp:409-511 for one pixel and one block: 9x9 chip demodulated
 // by the native Doppler, Sinc2d over it (Sinc2dInterpolator.cpp:45-96), then
 // the Doppler added back.  Sum order is the reference's (i outer, j inner).
-__device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr, int intAz, int intRg,
+__device__ __forceinline__ float2 ld_sample(const float2* q) { return __ldg(q); }
+__device__ __forceinline__ float2 ld_sample(const __half2* q) {
+    // complex32: float16 -> float32 is exact, as numpy's astype
+    return __half22float2(__ldg(q));
+}
+
+template <typename S>
+__device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg,
                              double fracAz, double fracRg, double doppFreq) {
     const double x = 4.0 + fracRg, y = 4.0 + fracAz;
     const int ix = (int)floor(x), iy = (int)floor(y);
@@ -349,11 +357,11 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
         for (int m = 0; m < 5; ++m) sincosf((float)(doppFreq * m), &ds[m], &dc[m]);
     }
     // chip row r9 = iy + 4 - i maps to radar row intAz + iy - i; col c9 = ix + 4 - j
-    const float2* base = rdr + (int64_t)(intAz + iy) * p.inW + (intRg + ix);
+    const S* base = rdr + (int64_t)(intAz + iy) * p.inW + (intRg + ix);
     float sre = 0.f, sim = 0.f;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const float2* rowp = base - (int64_t)i * p.inW;
+        const S* rowp = base - (int64_t)i * p.inW;
         float2 dv = make_float2(1.f, 0.f);
         if (demod) {
             const int m = iy - i;
@@ -363,7 +371,7 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            float2 a = __ldg(rowp - j);
+            float2 a = ld_sample(rowp - j);
             if (demod) a = cmul(a, dv);
             sre = fadd(sre, fmul(fmul(a.x, ky[i]), kx[j]));
             sim = fadd(sim, fmul(fmul(a.y, ky[i]), kx[j]));
@@ -379,6 +387,40 @@ __device__ float2 sinc_pixel(const GeoParams& p, const float2* __restrict__ rdr,
         cval = cmul(cval, make_float2(c, s));
     }
     return cval;
+}
+
+// block b of the request, in its sample format
+__device__ __forceinline__ float2 sinc_block(const GeoParams& p, int b, int intAz, int intRg, double fracAz,
+                                             double fracRg, double doppFreq) {
+    if (p.rdr_c32) return sinc_pixel(p, reinterpret_cast<const __half2*>(p.rdr[b]), intAz, intRg, fracAz, fracRg, doppFreq);
+    return sinc_pixel(p, p.rdr[b], intAz, intRg, fracAz, fracRg, doppFreq);
+}
+
+// float32 -> float16 bits as numpy's astype(float16): round to nearest even
+// (overflow to infinity), and NaN as sign | 0x7c00 | the top mantissa bits
+// (never the infinity pattern)
+__device__ __forceinline__ unsigned short f32_to_f16_bits(float x) {
+    if (isnan(x)) {
+        const unsigned int u = __float_as_uint(x);
+        unsigned short h = (unsigned short)(((u >> 16) & 0x8000u) | 0x7c00u | ((u & 0x7fffffu) >> 13));
+        if ((h & 0x3ffu) == 0) h |= 1u;
+        return h;
+    }
+    return __half_as_ushort(__float2half_rn(x));
+}
+
+// output pixel k of block b in the request's output format
+__device__ __forceinline__ void store_geo(const GeoParams& p, int b, int64_t k, float2 v) {
+    if (p.geo_fmt == 0) {
+        p.geo[b][k] = v;
+    } else if (p.geo_fmt == 1) {
+        const unsigned int w = (unsigned int)f32_to_f16_bits(v.x) | ((unsigned int)f32_to_f16_bits(v.y) << 16);
+        reinterpret_cast<unsigned int*>(p.geo[b])[k] = w;
+    } else {
+        // truncate_mantissa: keep the sign, exponent and mant_bits mantissa bits
+        const unsigned int m = 0xffffffffu << (23 - p.mant_bits);
+        p.geo[b][k] = make_float2(__uint_as_float(__float_as_uint(v.x) & m), __uint_as_float(__float_as_uint(v.y) & m));
+    }
 }
 
 // cuda/product/SubSwaths.h:177-205 (ViewSubSwaths::contains): no subswaths
@@ -397,6 +439,85 @@ __device__ bool subswath_contains_gpu(const GeoParams& p, int az, int rg) {
 // lines; thread (tx, ty) geocodes lines ty, ty + 8, ... of column tx, so a
 // warp stores 32 consecutive pixels of one line.
 constexpr int GBX = 32, GBY = 8;
+
+// ---- orbit tables in shared memory ----------------------------------------
+// The Newton segment tables of the request (Orbit::seg, 608 B per
+// state-vector interval) are brought into shared memory by one bulk
+// asynchronous copy (cp.async.bulk, completion counted in bytes on an
+// mbarrier) issued by one thread when the tile starts; it overlaps the
+// tile's ground-point work and is waited for before the first Newton
+// iteration.  Orbits whose tables exceed SEG_SMEM read them from global
+// memory.  The wait is bounded: if it runs out the block reads the global
+// tables, raises error bit 1 (GSLC_ETIMEOUT on the host) and stages nothing
+// more.
+constexpr int SEG_SMEM = 4096;   // doubles (32 KiB): orbits of up to 54 state vectors
+
+struct OrbitStage {
+    double* buf;          // shared, 16-byte aligned
+    uint64_t* bar;        // shared mbarrier
+    int* off;             // shared flag: a wait ran out, stage nothing more
+    uint32_t phase;       // parity of the copy to wait for
+    int issued;           // a copy of this request's tables was issued
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+    return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+
+__device__ __forceinline__ uint32_t seg_bytes(const GeoParams& p) {
+    return (uint32_t)((p.orbit.n - 1) * SEG_STRIDE * sizeof(double));
+}
+
+__device__ __forceinline__ bool seg_fits(const GeoParams& p) {
+    return p.orbit.n - 1 <= SEG_SMEM / SEG_STRIDE;
+}
+
+// one thread, once per block
+__device__ __forceinline__ void stage_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// one thread: the copy of p's segment tables into buf (the caller checked
+// seg_fits; source and size are multiples of 16 bytes)
+__device__ __forceinline__ void stage_issue(const GeoParams& p, double* buf, uint64_t* bar) {
+    const uint32_t bytes = seg_bytes(p);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(buf)), "l"(p.orbit.seg), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred P;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// wait for a copy, at most ~2^31 SM clocks (about a second)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1ll << 31)) return false;
+    return true;
+}
+
+// every thread: true when the staged tables can be read
+__device__ __forceinline__ bool stage_ready(const OrbitStage& st, const GeoParams& p) {
+    if (!st.issued) return false;
+    if (mbar_wait_bounded(st.bar, st.phase)) return true;
+    atomicOr(p.err, 2);
+    *st.off = 1;
+    return false;
+}
 
 // ---- tile fit of the projection inverse (UTM geogrids) --------------------
 // Over one tile (at most 1 km on a side) the map from (column, line) to the
@@ -503,7 +624,7 @@ __device__ int fit_node(const GeoParams& p, int pixel, int line, double* F) {
 }
 
 template <bool FF, bool RASTER>
-__device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, bool ok, V3 xyz);
+__device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* seg, int64_t k, bool ok, V3 xyz);
 
 // One tile (tile column bx, tile line by) of one geocode request.
 // RASTER selects the generic CUDA raster geocoder's per-pixel rules
@@ -511,7 +632,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, boo
 // interpolator, corrections and native Doppler that do not contain the
 // point mask it, no Doppler demodulation, carrier or flattening.
 template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
-__device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by) {
+__device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by, const OrbitStage& st) {
     constexpr int TY = GBY * PPT;
     __shared__ double s_col[4][GBX];
     __shared__ double s_row[5][TY];
@@ -595,6 +716,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
         __syncthreads();
     }
     if (pixel >= p.gw) return;
+    const double* seg = stage_ready(st, p) ? st.buf : p.orbit.seg;
     double wx[4];
     if (fit) {
 #pragma unroll
@@ -656,7 +778,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
                 xyz = lonlat_to_xyz_sc(p.ell_a, p.ell_e2, ll.slon, ll.clon, ll.slat, ll.clat, h);
             }
         }
-        geocode_pixel<FF, RASTER>(p, k, ok, xyz);
+        geocode_pixel<FF, RASTER>(p, seg, k, ok, xyz);
     }
 }
 
@@ -664,7 +786,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
 // radar-coordinate outputs, the sinc interpolation of every block, reramp
 // and flattening, for output pixel k.
 template <bool FF, bool RASTER>
-__device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, bool ok, V3 xyz) {
+__device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* seg, int64_t k, bool ok, V3 xyz) {
     bool valid = false;
     uint8_t mval = 255;
     double azc = CUDART_NAN, rgc = CUDART_NAN;
@@ -673,7 +795,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, boo
         double t, R;
         bool conv;
         if (FF) conv = geo2rdr_ff(p, xyz, t, R);
-        else conv = geo2rdr(p, xyz, t, R);
+        else conv = geo2rdr(p, seg, xyz, t, R);
         if (RASTER) {
             // Geocode.cu:126-171: corrections and native Doppler that do not
             // contain the point mask it; floor indices inside the radar grid
@@ -732,17 +854,17 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, boo
         const bool inside = valid && !(rgc < 4.0 || azc < 4.0 || rgc >= (double)p.inW - 4.0 ||
                                        azc >= (double)p.inL - 4.0);
         if (!inside) {
-            for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = make_float2(p.inv_blk[b], p.inv_blk[b]);
+            for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, make_float2(p.inv_blk[b], p.inv_blk[b]));
             return;
         }
         const int xi = (int)floor(rgc), yi = (int)floor(azc);
         const double fx = rgc - (double)xi, fy = azc - (double)yi;
-        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = sinc_pixel(p, p.rdr[b], yi, xi, fy, fx, 0.0);
+        for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, sinc_block(p, b, yi, xi, fy, fx, 0.0));
         return;
     }
     const float2 invalid = make_float2(p.inv_re, p.inv_im);
     if (!valid) {
-        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
+        for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);
         return;
     }
     // block-relative chip position (geocodeSlc.cpp:440-458, 335-348)
@@ -757,7 +879,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, boo
         interp = lut_contains(p.nat_dop, az, rng);
     }
     if (!interp) {
-        for (int b = 0; b < p.nblk; ++b) p.geo[b][k] = invalid;
+        for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);
         return;
     }
     // Doppler in radians per line: eval * 2 * pi / prf (geocodeSlc.cpp:473-474)
@@ -774,15 +896,26 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, int64_t k, boo
     float2 ph = make_float2(1.f, 0.f);
     if (rot) ph = expi_fp64(total);
     for (int b = 0; b < p.nblk; ++b) {
-        float2 v = sinc_pixel(p, p.rdr[b], intAzB, intRgB, fracAz, fracRg, doppFreq);
+        float2 v = sinc_block(p, b, intAzB, intRgB, fracAz, fracRg, doppFreq);
         if (rot) v = cmul(v, ph);
-        p.geo[b][k] = v;
+        store_geo(p, b, k, v);
     }
 }
 
 template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
 __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
-    geocode_block<GEO_LONLAT, FF, RASTER, PPT>(p, blockIdx.x, blockIdx.y);
+    __shared__ __align__(128) double s_seg[SEG_SMEM];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_off;
+    // the float-float path reads only the piece tables
+    const bool stage = !FF && seg_fits(p);
+    if (stage && threadIdx.x == 0 && threadIdx.y == 0) {
+        stage_init(&s_bar);
+        stage_issue(p, s_seg, &s_bar);
+    }
+    // geocode_block synchronises the block before any thread waits
+    const OrbitStage st{s_seg, &s_bar, &s_off, 0u, stage ? 1 : 0};
+    geocode_block<GEO_LONLAT, FF, RASTER, PPT>(p, blockIdx.x, blockIdx.y, st);
 }
 
 // Persistent form: blocks pop runs of tiles of any request in the batch from
@@ -791,6 +924,17 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constan
 template <bool GEO_LONLAT, bool FF, int PPT>
 __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_constant__ BatchQueue q) {
     __shared__ long long s_base;
+    __shared__ __align__(128) double s_seg[SEG_SMEM];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_off;
+    const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+    if (lead) {
+        s_off = 0;
+        if (!FF) stage_init(&s_bar);
+    }
+    int staged = -1;            // items[] entry whose tables are in s_seg
+    uint32_t phase = 0;         // parity of the next copy
+    OrbitStage st{s_seg, &s_bar, &s_off, 0u, 0};
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0)
             s_base = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(q.counter),
@@ -811,7 +955,18 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_con
             const GeoParams& p = q.items[lo];
             const long long local = tile - q.tile_start[lo];
             const int tiles_x = (p.gw + GBX - 1) / GBX;
-            geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x));
+            // every thread finished the previous tile (barrier below), so
+            // the tables of a new request may overwrite s_seg
+            if (!FF && lo != staged && !s_off) {
+                staged = lo;
+                st.issued = seg_fits(p) ? 1 : 0;
+                if (st.issued) {
+                    if (lead) stage_issue(p, s_seg, &s_bar);
+                    st.phase = phase;
+                    phase ^= 1u;
+                }
+            }
+            geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x), st);
             if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
             __syncthreads();
             if (q.done_flags && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -872,13 +1027,14 @@ __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ Der
         const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
         const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
         const float2* src = p.src + i * p.inW;
+        const __half2* src16 = reinterpret_cast<const __half2*>(p.src) + i * p.inW;
         float2* dst = p.dst + i * p.inW;
         const int64_t j0 = (int64_t)blockIdx.x * blockDim.x * 4 + threadIdx.x;
         float2 v[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {     // loads first: four samples in flight per thread
             const int64_t j = j0 + (int64_t)u * blockDim.x;
-            v[u] = j < p.inW ? __ldg(src + j) : make_float2(0.f, 0.f);
+            v[u] = j < p.inW ? (p.src_c32 ? ld_sample(src16 + j) : __ldg(src + j)) : make_float2(0.f, 0.f);
         }
         if (lr.mode <= 1 && la.mode <= 1) {
             // carriers constant along the line (azimuth polynomials): the

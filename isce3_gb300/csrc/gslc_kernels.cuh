@@ -68,12 +68,16 @@ struct GeoParams {
     int32_t raster, geo_row0;
     float inv_blk[MAX_BLOCKS];
     // 1: UTM tiles may use the fitted projection inverse
-    int32_t tile_fit, _pad3;
+    int32_t tile_fit;
+    // sample formats: rdr 0 complex64, 1 complex32; geo 0 complex64,
+    // 1 complex32, 2 complex64 keeping mant_bits mantissa bits
+    int32_t rdr_c32, geo_fmt, mant_bits;
 };
 
 struct DerampParams {
-    const float2* src;
-    float2* dst;
+    const float2* src;          // complex64, or complex32 when src_c32
+    float2* dst;                // complex64
+    int32_t src_c32, _pad;
     int64_t inL, inW, az_first, rg_first;
     double rg_t0, rg_prf, rg_r0, rg_dr, inv_prf;
     AzRg az_car, rg_car;

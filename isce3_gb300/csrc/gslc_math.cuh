@@ -69,6 +69,12 @@ GSLC_HD bool lut_contains(const Lut& l, double y, double x) {
     return (i >= 0.0 && i <= l.nx - 1.0) && (j >= 0.0 && j <= l.ny - 1.0);
 }
 
+// a load through a pointer that may address shared memory
+template <typename T>
+GSLC_HD T ld_gen(const T* p) {
+    return *p;
+}
+
 template <typename T>
 GSLC_HD T ld_ro(const T* p) {
 #if defined(__CUDA_ARCH__)
@@ -429,8 +435,8 @@ GSLC_HD int orbit_segment(const Orbit& o, int pc, double& u) {
 }
 
 GSLC_HD double seg_poly(const double* c, int deg, double w) {
-    double acc = ld_ro(c + deg);
-    for (int k = deg - 1; k >= 0; --k) acc = fma(acc, w, ld_ro(c + k));
+    double acc = ld_gen(c + deg);
+    for (int k = deg - 1; k >= 0; --k) acc = fma(acc, w, ld_gen(c + k));
     return acc;
 }
 
@@ -441,12 +447,13 @@ GSLC_HD double seg_poly(const double* c, int deg, double w) {
 // subtracting the interpolated position, and 1/|vel|^2 as G(w).  Rounding
 // differs from the direct form by ~1e-13 s in azimuth time, below the
 // reference's own orbit interpolation noise (~1e-11 s).
-GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, V3 xyz, double thr, int maxiter, double& t, double dt,
-                                       double& R) {
-    int seg = -1;
+// seg: the segment tables (Orbit::seg, or a copy of them in shared memory).
+GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz, double thr, int maxiter, double& t,
+                                       double dt, double& R) {
+    int cur = -1;
     double D[3] = {0.0, 0.0, 0.0};
     double w = 0.0;
-    const double* c = o.seg;
+    const double* c = seg;
     for (int i = 1; i < maxiter; ++i) {
         t -= dt;
         // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
@@ -454,27 +461,27 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, V3 xyz, double thr, int ma
         // the first and last segment (the orbit's time span) w, the piece
         // and the span check come from t exactly as orbit interpolation does.
         w -= dt * o.inv_spacing;
-        if (seg <= 0 || seg >= o.n - 2 || !(w >= -0.5 && w < 0.5)) {
+        if (cur <= 0 || cur >= o.n - 2 || !(w >= -0.5 && w < 0.5)) {
             if (!(t >= o.t0 && t <= o.t_end)) return false;  // FillNaN -> no convergence
             const int pc = orbit_piece(o, t);
             const double tidx = o.t0 + pc * o.spacing;
             w = (t - tidx) * o.inv_spacing - 1.5;
             const int j = orbit_segment(o, pc, w);
-            c = o.seg + (int64_t)j * SEG_STRIDE;
-            if (j != seg) {
-                seg = j;
-                D[0] = xyz.x - ld_ro(c + 0);
-                D[1] = xyz.y - ld_ro(c + 1);
-                D[2] = xyz.z - ld_ro(c + 2);
+            c = seg + (int64_t)j * SEG_STRIDE;
+            if (j != cur) {
+                cur = j;
+                D[0] = xyz.x - ld_gen(c + 0);
+                D[1] = xyz.y - ld_gen(c + 1);
+                D[2] = xyz.z - ld_gen(c + 2);
             }
         }
         double v[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const double* b = c + SEG_B + d * 7;
-            double acc = ld_ro(b + 6);
+            double acc = ld_gen(b + 6);
 #pragma unroll
-            for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_ro(b + k));
+            for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_gen(b + k));
             v[d] = acc;
         }
         const double fn = fma(D[0], v[0], fma(D[1], v[1], D[2] * v[2])) - seg_poly(c + SEG_H, o.seg_nh, w);
@@ -485,9 +492,9 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, V3 xyz, double thr, int ma
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const double* a = c + SEG_A + d * 8;
-                double acc = ld_ro(a + 7);
+                double acc = ld_gen(a + 7);
 #pragma unroll
-                for (int k = 6; k >= 0; --k) acc = fma(acc, w, ld_ro(a + k));
+                for (int k = 6; k >= 0; --k) acc = fma(acc, w, ld_gen(a + k));
                 r[d] = D[d] - acc;
             }
             R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);

@@ -158,6 +158,35 @@ def test_utm_geogrid_and_lut_doppler(oracle_mod, precision):
     assert r["n_valid"] > 10000
 
 
+@pytest.mark.parametrize("case", ["coarse_exact", "dem_west_edge", "utm_dem"])
+def test_utm_tile_fit_and_exact_paths(oracle_mod, case):
+    """UTM geogrids through both ground-point paths of the kernel: the tile
+    fit of the projection inverse (tiles up to 1 km), the exact per-pixel
+    inverse (40 m spacing: 1.2 km tiles), tiles straddling the DEM's west
+    edge (nodes disagree on the reference-height branch, so those tiles fall
+    back to the exact path), and a UTM DEM (forward projection at the
+    nodes)."""
+    from isce3_gb300.io import Raster
+    spacing = 40.0 if case == "coarse_exact" else 12.0
+    sc = synth.scene_c2(length=2048, width=1024, geo=200 if case == "coarse_exact" else 600, spacing=spacing)
+    g, dem = sc.geogrid, sc.dem
+    if case == "dem_west_edge":
+        gt = list(dem.get_geotransform())
+        lon_c, _lat, _h = oracle_mod.proj_inverse(g.epsg, g.start_x + 0.5 * g.width * g.spacing_x,
+                                                  g.start_y + 0.5 * g.length * g.spacing_y)
+        k = int((np.degrees(lon_c) - gt[0]) / gt[1])
+        dem = Raster(np.ascontiguousarray(dem.data[:, k:]), [gt[0] + k * gt[1]] + gt[1:], 4326)
+    elif case == "utm_dem":
+        rng = np.random.default_rng(11)
+        n = 400
+        x0 = g.start_x - 0.25 * g.width * g.spacing_x
+        y0 = g.start_y + 0.25 * g.length * abs(g.spacing_y)
+        dem = Raster(synth.fbm_surface((n, n), 0.8, rng, 0.0, 2000.0), [x0, 30.0, 0.0, y0, 0.0, -30.0], g.epsg)
+    gpu, ora = _run_both(oracle_mod, sc, [sc.slc], dem=dem, az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 10000
+
+
 def test_known_answer_lonlat_phase_gpu(c1):
     """The lon-as-phase KAT run through the GPU path (1e-6 rad)."""
     g = c1.geogrid
