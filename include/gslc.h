@@ -206,6 +206,17 @@ int gslc_deramp_block(gslc_ctx* ctx, const gslc_radar_grid* radar_grid, const gs
                       const gslc_azrg_func* rg_carrier, int64_t first_line, int64_t first_sample,
                       const void* src, void* dst, int64_t length, int64_t width, void* stream);
 
+/* The GSLC workflow's sample codecs on device arrays of n complex samples
+ * (python/packages/isce3/core/types.py:38-72, used by
+ * nisar/workflows/gslc.py:185-226): complex64 -> complex32 with numpy's
+ * float32 -> float16 rounding (to_complex32), complex32 -> complex64
+ * (read_c4_dataset_as_c8, exact), and truncate_mantissa (types.py:116-165)
+ * on n_words float16, float32 or float64 words (word_bytes 2, 4, 8) in place. */
+int gslc_complex64_to_complex32(gslc_ctx* ctx, const void* src, void* dst, int64_t n, void* stream);
+int gslc_complex32_to_complex64(gslc_ctx* ctx, const void* src, void* dst, int64_t n, void* stream);
+int gslc_truncate_mantissa(gslc_ctx* ctx, void* data, int64_t n_words, int32_t word_bytes, int32_t significant_bits,
+                           void* stream);
+
 /* Host-only: the DEM window of geogrid lines [line_start, line_start +
  * block_length) x [0, block_width) (the block form of
  * DEMRasterToInterpolator, geometry/loadDem.cpp:22-133). */

@@ -170,6 +170,9 @@ _EXPORTS = {
     "gslc_geo2rdr_zero_doppler": (C.c_int, [C.POINTER(OrbitDesc), C.c_void_p, C.c_double, C.c_int32, C.c_double,
                                             C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int32)]),
+    "gslc_complex64_to_complex32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "gslc_complex32_to_complex64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "gslc_truncate_mantissa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p]),
     "gslc_sinc_table": (C.c_int, [C.c_void_p]),
     "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),

@@ -50,7 +50,7 @@ class GeocodeRequest:
                   az_time_correction=None, srange_correction=None, flatten_with_corrected_srange=False,
                   invalid_value=complex(float("nan"), float("nan")), carrier_phase_block=None,
                   flatten_phase_block=None, inplace_deramp=False, az_index_block=None, rg_index_block=None,
-                  dem_margin=50, rdr_deramped=False)
+                  dem_margin=50, rdr_deramped=False, output_nonzero_mantissa_bits=None)
         unknown = set(self.kwargs) - set(kw)
         if unknown:
             raise TypeError(f"unknown geocode_slc arguments {sorted(unknown)}")
@@ -64,7 +64,7 @@ class GeocodeRequest:
                                kw["flatten_with_corrected_srange"], kw["invalid_value"],
                                kw["carrier_phase_block"], kw["flatten_phase_block"], precision,
                                kw["inplace_deramp"], kw["az_index_block"], kw["rg_index_block"], kw["dem_margin"],
-                               kw["rdr_deramped"])
+                               kw["rdr_deramped"], kw["output_nonzero_mantissa_bits"])
 
 
 @dataclass

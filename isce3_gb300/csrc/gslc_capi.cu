@@ -1486,6 +1486,47 @@ extern "C" int gslc_batch_destroy(gslc_batch* b) {
     return GSLC_OK;
 }
 
+// ---- GSLC sample codecs (isce3/core/types.py:38-165) ------------------------
+namespace {
+int codec_call(gslc_ctx* c, int op, const void* src, void* dst, int64_t n, int bits, int word_bytes, void* stream) {
+    c->err.clear();
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    c->launches = 0;
+    e = launch_codec(op, src, dst, n, bits, word_bytes, (cudaStream_t)stream, &c->launches);
+    return e == cudaSuccess ? GSLC_OK : cuda_err(c, e, "codec launch");
+}
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+}  // namespace
+
+extern "C" int gslc_complex64_to_complex32(gslc_ctx* c, const void* src, void* dst, int64_t n, void* stream) {
+    if (!c) return GSLC_EINVAL;
+    if (n < 0 || (n > 0 && (!src || !dst || !aligned(src, 8) || !aligned(dst, 4))))
+        return set_err(c, GSLC_EINVAL, "complex64 -> complex32: invalid arrays");
+    return codec_call(c, 0, src, dst, n, 0, 0, stream);
+}
+
+extern "C" int gslc_complex32_to_complex64(gslc_ctx* c, const void* src, void* dst, int64_t n, void* stream) {
+    if (!c) return GSLC_EINVAL;
+    if (n < 0 || (n > 0 && (!src || !dst || !aligned(src, 4) || !aligned(dst, 8))))
+        return set_err(c, GSLC_EINVAL, "complex32 -> complex64: invalid arrays");
+    return codec_call(c, 1, src, dst, n, 0, 0, stream);
+}
+
+extern "C" int gslc_truncate_mantissa(gslc_ctx* c, void* data, int64_t n_words, int32_t word_bytes,
+                                      int32_t significant_bits, void* stream) {
+    if (!c) return GSLC_EINVAL;
+    if (word_bytes != 2 && word_bytes != 4 && word_bytes != 8)
+        return set_err(c, GSLC_EINVAL, "argument z is not complex float or float type");
+    const int mant = word_bytes == 2 ? 10 : word_bytes == 4 ? 23 : 52;
+    if (!(significant_bits > 0 && significant_bits <= mant))
+        return set_err(c, GSLC_EINVAL, "Require 0 < significant_bits <= " + std::to_string(mant));
+    if (n_words < 0 || (n_words > 0 && (!data || !aligned(data, (size_t)word_bytes))))
+        return set_err(c, GSLC_EINVAL, "truncate_mantissa: invalid array");
+    if (significant_bits == mant) return GSLC_OK;
+    return codec_call(c, 2, nullptr, data, n_words, significant_bits, word_bytes, stream);
+}
+
 // geocodeSlc.cpp:240-274 (carrierPhaseDeramp) as a call of its own: dst =
 // src * exp(-i float(rg_carrier + az_carrier)) for a block whose first sample
 // is (first_line, first_sample) of radar_grid.  src == dst deramps in place.

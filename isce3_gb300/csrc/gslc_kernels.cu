@@ -13,6 +13,7 @@
 // Built twice: as is (plain launch, deramp, probe) and with
 // GSLC_PERSISTENT_TU defined by gslc_persistent.cu (the persistent batched
 // kernel), so that the two sets of kernel instances compile in parallel.
+#include <algorithm>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cuda_fp16.h>
@@ -1078,6 +1079,79 @@ __global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, int iters,
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// ---- sample codecs (HBM-bound byte work) -----------------------------------
+// complex64 -> complex32 (isce3/core/types.py:38-42 to_complex32: numpy's
+// float32 -> float16 rounding), complex32 -> complex64 (types.py:45-72,
+// exact), and truncate_mantissa (types.py:116-165: AND with a mask keeping
+// sign, exponent and the leading mantissa bits).  Grid-stride loops, four
+// samples in flight per thread, coalesced 8-byte (and 4-byte) accesses.
+__global__ void __launch_bounds__(256) c64_to_c32_kernel(const float2* __restrict__ src, unsigned int* __restrict__ dst,
+                                                         int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            v[u] = i < n ? __ldg(src + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) dst[i] = (unsigned int)f32_to_f16_bits(v[u].x) | ((unsigned int)f32_to_f16_bits(v[u].y) << 16);
+        }
+    }
+}
+
+// float16 -> float32 bits as numpy's astype(float32): exact, and a NaN keeps
+// its sign and its mantissa bits shifted into the top of the float32 mantissa
+__device__ __forceinline__ float f16_bits_to_f32(unsigned short h) {
+    if ((h & 0x7c00u) == 0x7c00u && (h & 0x3ffu))
+        return __uint_as_float(((unsigned int)(h & 0x8000u) << 16) | 0x7f800000u | ((unsigned int)(h & 0x3ffu) << 13));
+    return __half2float(__ushort_as_half(h));
+}
+
+__global__ void __launch_bounds__(256) c32_to_c64_kernel(const unsigned int* __restrict__ src,
+                                                         float2* __restrict__ dst, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) {
+                const unsigned int w = __ldg(src + i);
+                v[u] = make_float2(f16_bits_to_f32((unsigned short)(w & 0xffffu)), f16_bits_to_f32((unsigned short)(w >> 16)));
+            } else {
+                v[u] = make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) dst[i] = v[u];
+        }
+    }
+}
+
+template <typename W>
+__global__ void __launch_bounds__(256) mask_words_kernel(W* __restrict__ data, int64_t n, W mask) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        W v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            v[u] = i < n ? data[i] : W(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) data[i] = v[u] & mask;
+        }
+    }
+}
+
 #endif  // GSLC_PERSISTENT_TU
 
 }  // namespace
@@ -1114,6 +1188,43 @@ cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, in
     // iterate at sensingMid; anything else runs in FP64
     const bool ff = precision == 1 && p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0;
     launch_geocode_ppt<4>(p, ff, s);     // the plain form uses 32 x 32-pixel tiles
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+// grid for the codec kernels: a multiple of the SM count, enough for 4
+// samples per thread per pass
+static unsigned codec_grid(int64_t n) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const int64_t want = (n + 1023) / 1024;
+    const int64_t cap = (int64_t)sms * 8;
+    return (unsigned)std::max<int64_t>(1, std::min(want, cap));
+}
+
+cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits, int word_bytes, cudaStream_t s,
+                         int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    const unsigned g = codec_grid(n);
+    if (op == 0) {
+        c64_to_c32_kernel<<<g, 256, 0, s>>>((const float2*)src, (unsigned int*)dst, n);
+    } else if (op == 1) {
+        c32_to_c64_kernel<<<g, 256, 0, s>>>((const unsigned int*)src, (float2*)dst, n);
+    } else if (word_bytes == 2) {
+        const unsigned short m = (unsigned short)(0xffffu << (10 - bits));
+        mask_words_kernel<unsigned short><<<g, 256, 0, s>>>((unsigned short*)dst, n, m);
+    } else if (word_bytes == 4) {
+        const unsigned int m = 0xffffffffu << (23 - bits);
+        mask_words_kernel<unsigned int><<<g, 256, 0, s>>>((unsigned int*)dst, n, m);
+    } else {
+        const unsigned long long m = ~0ull << (52 - bits);
+        mask_words_kernel<unsigned long long><<<g, 256, 0, s>>>((unsigned long long*)dst, n, m);
+    }
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -32,6 +32,30 @@ log = logging.getLogger("isce3_gb300.geocode.geocode_slc")
 
 ArrayLike = Union[np.ndarray, torch.Tensor]
 
+# complex32 as isce3.core.types.complex32 (python/packages/isce3/core/types.py:12):
+# pairs of float16; torch.complex32 tensors are the device-side equivalent
+COMPLEX32 = np.dtype([("r", np.float16), ("i", np.float16)])
+
+
+def sample_format(x) -> int | None:
+    """0 for complex64, 1 for complex32 (NumPy pairs of float16 or
+    torch.complex32), None otherwise."""
+    if isinstance(x, torch.Tensor):
+        return {torch.complex64: 0, torch.complex32: 1}.get(x.dtype)
+    if x.dtype == np.complex64:
+        return 0
+    if x.dtype == COMPLEX32:
+        return 1
+    return None
+
+
+def _raw(x):
+    """A NumPy complex32 array as its 32-bit words (torch has no structured
+    dtypes); everything else unchanged."""
+    if isinstance(x, np.ndarray) and x.dtype == COMPLEX32:
+        return x.view(np.int32)
+    return x
+
 
 def _is_array(x) -> bool:
     return isinstance(x, (np.ndarray, torch.Tensor))
@@ -126,7 +150,7 @@ class _Staged:
         if upload:
             self.dev = host.to(dev, non_blocking=host.is_pinned())
         else:
-            self.dev = torch.empty(tuple(host.shape), dtype=torch_dtype, device=dev)
+            self.dev = torch.empty(tuple(host.shape), dtype=host.dtype, device=dev)
 
     def ptr(self) -> int:
         return self.dev.data_ptr()
@@ -147,6 +171,7 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
                 carrier_phase_block=None, flatten_phase_block=None, *,
                 geo2rdr_precision: str = "fp64", inplace_deramp: bool = False,
                 az_index_block=None, rg_index_block=None, dem_margin: int = 50, rdr_deramped: bool = False,
+                output_nonzero_mantissa_bits: int | None = None,
                 device=None, stream: torch.cuda.Stream | None = None) -> None:
     """Geocode radar SLC arrays sharing one radar grid onto one geogrid.
 
@@ -157,7 +182,14 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
     reference), ``az_index_block``/``rg_index_block`` (f64 outputs of the radar
     coordinates per geo pixel), ``dem_margin``, ``rdr_deramped`` (the radar
     blocks already carry the carrier deramp, as resident stores keep them),
+    ``output_nonzero_mantissa_bits`` (complex64 outputs keep only this many
+    mantissa bits, as isce3.core.types.truncate_mantissa after the call),
     ``device`` and ``stream``.
+
+    Radar blocks may be complex32 (NumPy arrays of isce3's complex32 dtype, or
+    torch.complex32 tensors): the kernel decodes them exactly as
+    read_c4_dataset_as_c8 would.  Geo blocks of complex32 receive the
+    float16 encoding of the result (isce3.core.types.to_complex32).
     """
     call = _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
                            image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
@@ -165,7 +197,7 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
                            az_carrier, rg_carrier, az_time_correction, srange_correction,
                            flatten_with_corrected_srange, invalid_value, carrier_phase_block, flatten_phase_block,
                            geo2rdr_precision, inplace_deramp, az_index_block, rg_index_block, dem_margin,
-                           rdr_deramped)
+                           rdr_deramped, output_nonzero_mantissa_bits)
     dev = M.device_of(device)
     lib = L.lib()
     ctx = L.context(dev.index)
@@ -180,7 +212,8 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
                     sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
                     az_carrier, rg_carrier, az_time_correction, srange_correction, flatten_with_corrected_srange,
                     invalid_value, carrier_phase_block, flatten_phase_block, geo2rdr_precision, inplace_deramp,
-                    az_index_block, rg_index_block, dem_margin, rdr_deramped=False):
+                    az_index_block, rg_index_block, dem_margin, rdr_deramped=False,
+                    output_nonzero_mantissa_bits=None):
     """Defaults and validation of geocode_slc (geocode_slc.py:192-213); the
     arguments of _build_args in its order."""
     az_carrier = LUT2d() if az_carrier is None else az_carrier
@@ -208,11 +241,29 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
     if not isinstance(az_carrier, (LUT2d, Poly2d)):
         raise TypeError("carriers must be LUT2d or Poly2d")
     for g in geo_data_blocks:
-        _check_dtype(g, np.complex64, torch.complex64, "geo_data_blocks")
+        if sample_format(g) is None:
+            raise TypeError(f"geo_data_blocks must be complex64 or complex32, got {g.dtype}")
         if tuple(g.shape) != (geogrid.length, geogrid.width):
             raise ValueError("geo_data_blocks shape does not match the geogrid")
     for r in rdr_data_blocks:
-        _check_dtype(r, np.complex64, torch.complex64, "rdr_data_blocks")
+        if sample_format(r) is None:
+            raise TypeError(f"rdr_data_blocks must be complex64 or complex32, got {r.dtype}")
+    rdr_format = sample_format(rdr_data_blocks[0])
+    geo_format = sample_format(geo_data_blocks[0])
+    if any(sample_format(r) != rdr_format for r in rdr_data_blocks) or \
+            any(sample_format(g) != geo_format for g in geo_data_blocks):
+        raise TypeError("all radar blocks, and all geo blocks, must share one sample type")
+    mantissa_bits = 23
+    if output_nonzero_mantissa_bits is not None:
+        if geo_format != 0:
+            raise ValueError("output_nonzero_mantissa_bits applies to complex64 geo blocks")
+        mantissa_bits = int(output_nonzero_mantissa_bits)
+        if not 0 < mantissa_bits <= 23:
+            raise ValueError(f"Require 0 < significant_bits={mantissa_bits} <= 23")
+        if mantissa_bits < 23:
+            geo_format = 2
+    if rdr_format == 1 and inplace_deramp:
+        raise ValueError("inplace_deramp needs complex64 radar blocks")
     if mask_block is not None:
         _check_dtype(mask_block, np.uint8, torch.uint8, "mask_block")
     precision = {"fp64": 0, "ff": 1, "float-float": 1}.get(geo2rdr_precision)
@@ -224,7 +275,7 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
             subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
             az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
             carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
-            rg_index_block, dem_margin, rdr_deramped)
+            rg_index_block, dem_margin, rdr_deramped, rdr_format, geo_format, mantissa_bits)
 
 
 def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sliced_radargrid, geogrid, orbit,
@@ -232,14 +283,15 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
                 subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
                 az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
                 carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
-                rg_index_block, dem_margin, rdr_deramped=False):
+                rg_index_block, dem_margin, rdr_deramped=False, rdr_format=0, geo_format=0, mantissa_bits=23):
     """Stage arrays on ``dev`` and fill a gslc_geocode_args.
 
     Returns (args, outputs to copy back, objects to keep alive)."""
-    rdr = [_Staged(r, dev, True, torch.complex64) for r in rdr_data_blocks]
+    rdr = [_Staged(_raw(r), dev, True, torch.complex64) for r in rdr_data_blocks]
     if any(r.host is not None for r in rdr) and inplace_deramp:
         raise ValueError("inplace_deramp needs device-resident radar tensors")
-    geo = [_Staged(g, dev, False, torch.complex64) for g in geo_data_blocks]
+    geo_t = torch.complex64 if geo_format != 1 else torch.int32
+    geo = [_Staged(_raw(g), dev, False, geo_t) for g in geo_data_blocks]
     outs = list(geo)
 
     def opt_out(arr, np_dtype, t_dtype, what, upload):
@@ -294,6 +346,7 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
     a.dem_margin = int(dem_margin)
     a.geo2rdr_precision = precision
+    a.rdr_format, a.geo_format, a.mantissa_bits = int(rdr_format), int(geo_format), int(mantissa_bits)
     ss = None
     if subswaths is not None:
         ss = M.subswaths_desc(subswaths, dev)
