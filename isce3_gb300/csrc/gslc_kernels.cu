@@ -903,8 +903,10 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
     }
 }
 
+// Two blocks per SM: the UTM variants fit 128 registers without spills
+// (190 unbounded), doubling the warps that hide FP64 and float-float latency.
 template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
-__global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constant__ GeoParams p) {
+__global__ void __launch_bounds__(GBX * GBY, 2) geocode_kernel(const __grid_constant__ GeoParams p) {
     __shared__ __align__(128) double s_seg[SEG_SMEM];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ int s_off;
@@ -923,7 +925,7 @@ __global__ void __launch_bounds__(GBX * GBY) geocode_kernel(const __grid_constan
 // one counter until the batch is exhausted.  Requests keep their own
 // parameters, so each request's output equals its plain call.
 template <bool GEO_LONLAT, bool FF, int PPT>
-__global__ void __launch_bounds__(GBX * GBY) geocode_persistent(const __grid_constant__ BatchQueue q) {
+__global__ void __launch_bounds__(GBX * GBY, 2) geocode_persistent(const __grid_constant__ BatchQueue q) {
     __shared__ long long s_base;
     __shared__ __align__(128) double s_seg[SEG_SMEM];
     __shared__ __align__(8) uint64_t s_bar;
