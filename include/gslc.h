@@ -313,6 +313,67 @@ int gslc_batch_info(const gslc_batch* batch, int64_t* n_tiles, int32_t* blocks, 
                     int64_t* launches);
 int gslc_batch_destroy(gslc_batch* batch);
 
+/* Block planning.  One geogrid block of a geogrid (its own start, same
+ * spacing and EPSG), as python/packages/isce3/core/rdr_geo_block_generator.py
+ * builds it for each block. */
+typedef struct {
+    double start_x, start_y, spacing_x, spacing_y;
+    int32_t width, length;
+} gslc_geo_block;
+
+/* isce3::geometry::RadarGridBoundingBox (geometry/boundingbox.h:18-23) plus
+ * the outcome: status 0 ok; 1 geo2rdr did not converge at the corners in
+ * `detail` (bit 0 top-left/north-west, 1 top-right, 2 bottom-left, 3
+ * bottom-right; the reference's RuntimeError "did not converge"); 2 the box
+ * does not overlap the radar grid (bit 0 azimuth first and last <= 0, 1
+ * both >= max azimuth, 2 range <= 0, 3 range >= max range; RuntimeError
+ * "does not overlap"); 3 a projection inverse failed (RuntimeError
+ * "Inverse projection transformation failed"). */
+typedef struct {
+    int32_t first_azimuth_line, last_azimuth_line, first_range_sample, last_range_sample;
+    int32_t status, detail;
+} gslc_radar_bbox;
+
+/* Arguments of isce3::geometry::getRadarBoundingBox with min/max heights
+ * (geometry/boundingbox.h:152-161). */
+typedef struct {
+    gslc_radar_grid radar_grid;
+    gslc_orbit orbit;
+    gslc_lut2d doppler;             /* radar image grid Doppler; default LUT2d: zero */
+    int32_t epsg;                   /* of every block: 4326 or UTM */
+    int32_t n_blocks;
+    const gslc_geo_block* blocks;   /* host, n_blocks */
+    float min_height, max_height;
+    int32_t margin;                 /* >= 0 */
+    int32_t geogrid_expansion_threshold;
+    double threshold;               /* Geo2RdrParams: 1e-8 */
+    int32_t maxiter, _pad;          /* 50 */
+    double delta_range;             /* 10 */
+} gslc_bbox_args;
+
+/* The radar bounding box of every block in ONE launch (8 geo2rdr sequences per
+ * block, one thread each).  Replaces isce3::geometry::getRadarBoundingBox
+ * (geometry/boundingbox.cpp:434-641; bound as
+ * isce3.geometry.get_radar_bbox in
+ * python/extensions/pybind_isce3/geometry/boundingbox.cpp:82-131) called once
+ * per block by block_generator (rdr_geo_block_generator.py:55-117).  `out` is
+ * host memory for n_blocks results; the call returns when they are there.
+ * Argument errors (max_height < min_height, margin < 0) return GSLC_EINVAL
+ * like the reference's InvalidArgument / OutOfRange; per-block failures are
+ * statuses, never call errors.  geogrid_expansion_threshold is limited to
+ * [0, 10000] and maxiter to [0, 1000] (GSLC_EINVAL beyond), which bounds the
+ * work of one thread; the reference has no limit. */
+int gslc_radar_bbox_blocks(gslc_ctx* ctx, const gslc_bbox_args* args, gslc_radar_bbox* out, void* stream);
+
+/* DEM statistics over a device float raster (length x width, row stride in
+ * floats): min, max and mean of the non-NaN samples and their count.
+ * Replaces isce3::geometry::DEMInterpolator::computeMinMaxMeanHeight
+ * (geometry/DEMInterpolator.cpp:515-560).  The mean's sum is folded in a
+ * fixed order, so it is the same on every call; with no valid sample min is
+ * FLT_MAX, max -FLT_MAX and mean NaN, as there. */
+int gslc_dem_stats(gslc_ctx* ctx, const float* data, int64_t length, int64_t width, int64_t row_stride,
+                   float* min_height, float* max_height, double* mean_height, int64_t* n_valid, void* stream);
+
 /* Allocation-free plain form.  No counterpart in the reference: an addition
  * for callers that must not allocate device memory while they run (serving
  * loops that reserve HBM up front under a fixed budget, hosts that forbid

@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBPATH = BUILD / "libgslc.so"
 HEADER = ROOT / "include" / "gslc.h"
-SOURCES = ["gslc_kernels.cu", "gslc_persistent.cu", "gslc_capi.cu", "gslc_batch.cu"]
+SOURCES = ["gslc_kernels.cu", "gslc_persistent.cu", "gslc_capi.cu", "gslc_plan.cu"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(ROOT / "include")]
@@ -153,6 +153,25 @@ class BatchTuning(C.Structure):
                 ("rows_per_thread", C.c_int32)]
 
 
+class GeoBlock(C.Structure):
+    _fields_ = [("start_x", C.c_double), ("start_y", C.c_double), ("spacing_x", C.c_double),
+                ("spacing_y", C.c_double), ("width", C.c_int32), ("length", C.c_int32)]
+
+
+class RadarBBox(C.Structure):
+    _fields_ = [("first_azimuth_line", C.c_int32), ("last_azimuth_line", C.c_int32),
+                ("first_range_sample", C.c_int32), ("last_range_sample", C.c_int32),
+                ("status", C.c_int32), ("detail", C.c_int32)]
+
+
+class BBoxArgs(C.Structure):
+    _fields_ = [("radar_grid", RadarGrid), ("orbit", OrbitDesc), ("doppler", Lut2d), ("epsg", C.c_int32),
+                ("n_blocks", C.c_int32), ("blocks", C.c_void_p), ("min_height", C.c_float),
+                ("max_height", C.c_float), ("margin", C.c_int32), ("geogrid_expansion_threshold", C.c_int32),
+                ("threshold", C.c_double), ("maxiter", C.c_int32), ("_pad", C.c_int32),
+                ("delta_range", C.c_double)]
+
+
 _EXPORTS = {
     "gslc_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "gslc_ctx_destroy": (C.c_int, [C.c_void_p]),
@@ -190,6 +209,9 @@ _EXPORTS = {
     "gslc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int64)]),
     "gslc_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gslc_radar_bbox_blocks": (C.c_int, [C.c_void_p, C.POINTER(BBoxArgs), C.c_void_p, C.c_void_p]),
+    "gslc_dem_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_float),
+                                 C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "gslc_deramp_block": (C.c_int, [C.c_void_p, C.POINTER(RadarGrid), C.POINTER(AzRgFunc), C.POINTER(AzRgFunc),
                                     C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                     C.c_void_p]),

@@ -1033,6 +1033,139 @@ extern "C" int gslc_probe_fp64_gflops(gslc_ctx* c, double* gflops) {
     return GSLC_OK;
 }
 
+// ---- block planning (geometry/boundingbox.cpp:434-641) --------------------
+extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc_radar_bbox* out, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (!a || (a->n_blocks > 0 && (!a->blocks || !out))) return set_err(c, GSLC_EINVAL, "null arguments");
+    // boundingbox.cpp:444-454
+    if (a->max_height < a->min_height) return set_err(c, GSLC_EINVAL, "max_height <  min_height");
+    if (a->margin < 0)
+        return set_err(c, GSLC_EINVAL,
+                       "Margin should be a nonnegative number. " + std::to_string(a->margin) + " requested.");
+    if (a->n_blocks < 0 || a->n_blocks > (1 << 24)) return set_err(c, GSLC_EINVAL, "n_blocks out of range");
+    // bounds on the work of one thread (the reference has none): a sequence
+    // runs at most expansion x maxiter Newton iterations
+    if (a->geogrid_expansion_threshold < 0 || a->geogrid_expansion_threshold > 10000 || a->maxiter < 0 ||
+        a->maxiter > 1000)
+        return set_err(c, GSLC_EINVAL, "geogrid_expansion_threshold must be in [0, 10000] and maxiter in [0, 1000]");
+    if (!grid_ok(a->radar_grid)) return set_err(c, GSLC_EINVAL, "invalid radar grid");
+    if (!is_lonlat_or_utm(a->epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
+    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
+    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
+        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (int st = check_lut(c, a->doppler, "doppler")) return st;
+    if (a->n_blocks == 0) return GSLC_OK;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+
+    PlanParams p;
+    std::memset(&p, 0, sizeof(p));
+    std::vector<double> coef;
+    build_orbit_table(a->orbit, coef, p.orbit);
+    const gslc_radar_grid& rg = a->radar_grid;
+    p.n_blocks = a->n_blocks;
+    p.geo_is_lonlat = a->epsg == 4326;
+    if (!p.geo_is_lonlat) utm_setup(a->epsg, p.utm);
+    p.dop = to_lut(a->doppler);
+    p.ell_a = WGS84_A;
+    p.ell_e2 = WGS84_E2;
+    p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));     // RadarGridParameters::sensingMid
+    p.t0 = rg.sensing_start;
+    p.prf = rg.prf;
+    p.r0 = rg.starting_range;
+    p.dr = rg.range_pixel_spacing;
+    p.wvl = rg.wavelength;
+    p.look_side = rg.look_side;
+    p.maxiter = a->maxiter;
+    p.thr = a->threshold;
+    p.delta_range = a->delta_range;
+    p.hmin = a->min_height;
+    p.hmax = a->max_height;
+    p.margin = a->margin;
+    p.expansion = a->geogrid_expansion_threshold;
+    p.length = rg.length;
+    p.width = rg.width;
+
+    // one stream-ordered scratch: orbit table, block list, results
+    const size_t n = (size_t)a->n_blocks;
+    const size_t orb_b = coef.size() * sizeof(double);
+    const size_t blk_off = (orb_b + 255) & ~(size_t)255, blk_b = n * 6 * sizeof(double);
+    const size_t out_off = (blk_off + blk_b + 255) & ~(size_t)255, out_b = n * 6 * sizeof(int32_t);
+    std::vector<double> blocks(n * 6);
+    for (size_t i = 0; i < n; ++i) {
+        const gslc_geo_block& b = a->blocks[i];
+        double* d = &blocks[i * 6];
+        d[0] = b.start_x; d[1] = b.start_y; d[2] = b.spacing_x; d[3] = b.spacing_y;
+        d[4] = (double)b.width; d[5] = (double)b.length;
+    }
+    char* buf = nullptr;
+    e = cudaMallocAsync((void**)&buf, out_off + out_b, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMallocAsync planner scratch");
+    e = cudaMemcpyAsync(buf, coef.data(), orb_b, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf + blk_off, blocks.data(), blk_b, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) {
+        const double* d_coef = reinterpret_cast<const double*>(buf);
+        p.orbit.coef = d_coef;
+        p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+        p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
+        p.blocks = reinterpret_cast<const double*>(buf + blk_off);
+        p.out = reinterpret_cast<int32_t*>(buf + out_off);
+        e = launch_radar_bbox(p, stream, &c->launches);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, buf + out_off, out_b, cudaMemcpyDeviceToHost, stream);
+    cudaFreeAsync(buf, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "radar bbox");
+    return GSLC_OK;
+}
+
+extern "C" int gslc_dem_stats(gslc_ctx* c, const float* data, int64_t length, int64_t width, int64_t row_stride,
+                              float* mn, float* mx, double* mean, int64_t* n_valid, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (!mn || !mx || !mean || !n_valid || length < 0 || width < 0 || (length * width > 0 && !data) ||
+        (length > 1 && row_stride < width))
+        return set_err(c, GSLC_EINVAL, "invalid DEM raster arguments");
+    if (length * width == 0) {
+        *mn = std::numeric_limits<float>::max();
+        *mx = -std::numeric_limits<float>::max();
+        *mean = std::nan("");
+        *n_valid = 0;
+        return GSLC_OK;
+    }
+    cudaStream_t stream = (cudaStream_t)stream_;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    void* scratch = nullptr;
+    e = cudaMallocAsync(&scratch, dem_stats_scratch_bytes(), stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMallocAsync DEM stats scratch");
+    DemStats* h = nullptr;
+    e = cudaMallocHost((void**)&h, sizeof(DemStats));
+    if (e != cudaSuccess) {
+        cudaFreeAsync(scratch, stream);
+        return cuda_err(c, e, "cudaMallocHost");
+    }
+    e = launch_dem_stats(data, length, width, row_stride, scratch, h, stream, &c->launches);
+    cudaFreeAsync(scratch, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        cudaFreeHost(h);
+        return cuda_err(c, e, "DEM stats");
+    }
+    const long long nv = (long long)(length * width) - h->nan;
+    *mn = h->mn;
+    *mx = h->mx;
+    *mean = h->sum / (double)nv;     // 0 / 0 -> NaN as the reference
+    *n_valid = nv;
+    cudaFreeHost(h);
+    return GSLC_OK;
+}
+
 #include <mutex>
 
 // ===========================================================================

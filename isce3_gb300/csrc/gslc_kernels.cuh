@@ -99,6 +99,35 @@ struct BatchQueue {
     unsigned int* done_flags;        // n_requests, host-mapped: set to 1 when a request's last tile is written
 };
 
+// Radar bounding boxes of geogrid blocks (gslc_plan.cu): 8 geo2rdr
+// sequences per block, geometry/boundingbox.cpp:434-641.
+struct PlanParams {
+    const double* blocks;        // n_blocks x (start x, start y, spacing x, spacing y, width, length)
+    int32_t n_blocks, geo_is_lonlat;
+    Utm utm;
+    Orbit orbit;
+    Lut dop;                     // image-grid Doppler of geo2rdr
+    double ell_a, ell_e2;        // the projection's ellipsoid (WGS84)
+    double t_mid, t0, prf, r0, dr, wvl;   // radar grid: sensingMid, sensingStart, ...
+    int32_t look_side, maxiter;
+    double thr, delta_range;
+    float hmin, hmax;
+    int32_t margin, expansion;
+    int64_t length, width;       // radar grid size
+    int32_t* out;                // n_blocks x (first az, last az, first rg, last rg, status, detail)
+};
+
+// DEM statistics (geometry/DEMInterpolator.cpp:515-560): min, max, sum of
+// the non-NaN samples and the NaN count.
+struct DemStats { float mn, mx; double sum; long long nan; };
+constexpr int DEM_STATS_BLOCKS = 304;   // fixed: the fold order, hence the sum, does not depend on the GPU
+
+// launchers (gslc_plan.cu)
+cudaError_t launch_radar_bbox(const PlanParams& p, cudaStream_t s, int64_t* launches);
+size_t dem_stats_scratch_bytes();
+cudaError_t launch_dem_stats(const float* z, int64_t length, int64_t width, int64_t stride, void* scratch,
+                             DemStats* host_out, cudaStream_t s, int64_t* launches);
+
 // launchers (gslc_kernels.cu)
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);

@@ -1249,3 +1249,92 @@ extern "C" int orc_dem_subset(const orc_dem_raster* dem, const orc_geo_grid* g, 
     *x_start = d.xstart; *y_start = d.ystart;
     return 0;
 }
+
+// ---------------------------------------------------------------- block planning
+// geometry/boundingbox.cpp:434-641 (getRadarBoundingBox with min/max heights):
+// the four geogrid corners at the two heights, each corner pushed outwards by
+// one geogrid pixel per retry until geo2rdr converges; floor/ceil of the
+// radar coordinates, the overlap checks, then the margin, clamped.
+extern "C" int orc_radar_bbox(const orc_geo_grid* g, const orc_radar_grid* rg, const orc_orbit* orbit,
+                              const orc_lut2d* doppler, float min_height, float max_height, int margin,
+                              double threshold, int maxiter, double delta_range, int expansion_threshold,
+                              int32_t* out) {
+    if (max_height < min_height) return fail("max_height <  min_height");
+    if (margin < 0) return fail("Margin should be a nonnegative number.");
+    Proj proj;
+    if (!proj.init(g->epsg)) return fail("unsupported EPSG");
+    const float height_range[2] = {min_height, max_height};
+    int first_az = (int)(rg->length - 1), last_az = 0;
+    int first_rg = (int)(rg->width - 1), last_rg = 0;
+    const int ex[2][2] = {{-1, 1}, {-1, 1}}, ey[2][2] = {{-1, -1}, {1, 1}};
+    int bad = 0;
+    for (size_t line = 0; line < 2; ++line) {
+        const double y0 = g->start_y + g->spacing_y * line * g->length;
+        for (size_t pixel = 0; pixel < 2; ++pixel) {
+            const double x0 = g->start_x + g->spacing_x * pixel * g->width;
+            bool corner_converge = false;
+            for (int ih = 0; ih < 2; ++ih) {
+                const float height = height_range[ih];
+                double aztime = rg_sensing_mid(*rg);
+                double srange = rg->starting_range;
+                int iters = 0, geostat = 0;
+                while (geostat == 0 && iters < expansion_threshold) {
+                    const double x = x0 + iters * ex[line][pixel] * g->spacing_x;
+                    const double y = y0 + iters * ey[line][pixel] * g->spacing_y;
+                    V3 llh{0, 0, 0};
+                    if (proj.inverse({x, y, 0.0}, llh) != 0) {
+                        out[4] = 3; out[5] = 0;
+                        return 0;   // RuntimeError: Inverse projection transformation failed
+                    }
+                    llh.z = height;
+                    const double t0 = aztime;
+                    geostat = geo2rdr_detail(&aztime, &srange, llh, WGS84_A, WGS84_E2, orbit, doppler,
+                                             rg->wavelength, rg->look_side, t0, threshold, maxiter,
+                                             delta_range) == G_OK;
+                    iters += 1;
+                }
+                if (geostat == 0) continue;
+                corner_converge = true;
+                const double az = (aztime - rg->sensing_start) * rg->prf;
+                const double r = (srange - rg->starting_range) / rg->range_pixel_spacing;
+                first_az = std::min(first_az, (int)std::floor(az));
+                last_az = std::max(last_az, (int)std::ceil(az));
+                first_rg = std::min(first_rg, (int)std::floor(r));
+                last_rg = std::max(last_rg, (int)std::ceil(r));
+            }
+            if (!corner_converge) bad |= 1 << (2 * line + pixel);
+        }
+    }
+    out[0] = first_az; out[1] = last_az; out[2] = first_rg; out[3] = last_rg;
+    if (bad) { out[4] = 1; out[5] = bad; return 0; }
+    const int max_az = (int)(rg->length - 1), max_rg = (int)(rg->width - 1);
+    int why = 0;
+    if (first_az <= 0 && last_az <= 0) why |= 1;
+    if (first_az >= max_az && last_az >= max_az) why |= 2;
+    if (first_rg <= 0 && last_rg <= 0) why |= 4;
+    if (first_rg >= max_rg && last_rg >= max_rg) why |= 8;
+    if (why) { out[4] = 2; out[5] = why; return 0; }
+    out[0] = std::max(first_az - margin, 0);
+    out[2] = std::max(first_rg - margin, 0);
+    out[1] = std::min(last_az + margin, max_az);
+    out[3] = std::min(last_rg + margin, max_rg);
+    out[4] = 0; out[5] = 0;
+    return 0;
+}
+
+// geometry/DEMInterpolator.cpp:515-560 (computeMinMaxMeanHeight): NaN samples
+// are skipped and leave the mean's denominator.
+extern "C" void orc_dem_stats(const float* z, int64_t length, int64_t width, float* mn, float* mx, double* mean,
+                              int64_t* n_valid) {
+    float lo = std::numeric_limits<float>::max(), hi = -std::numeric_limits<float>::max();
+    double sum = 0.0;
+    int64_t n = length * width;
+    for (int64_t i = 0; i < length * width; ++i) {
+        const float v = z[i];
+        if (std::isnan(v)) { --n; continue; }
+        hi = std::max(v, hi);
+        lo = std::min(v, lo);
+        sum += v;
+    }
+    *mn = lo; *mx = hi; *mean = sum / n; *n_valid = n;
+}

@@ -168,6 +168,19 @@ int orc_dem_subset(const orc_dem_raster* dem, const orc_geo_grid* g, int margin,
                    int64_t* x_off, int64_t* y_off, int64_t* width, int64_t* length,
                    double* x_start, double* y_start);
 
+/* radar bounding box of a geogrid (geometry/boundingbox.cpp:434-641).  out:
+ * first/last azimuth line, first/last range sample, status (0 ok, 1 geo2rdr
+ * failed at the corners in bits of out[5], 2 no overlap with the reasons in
+ * out[5], 3 projection inverse failed), detail.  Returns >0 on an argument
+ * error (the reference throws InvalidArgument / OutOfRange). */
+int orc_radar_bbox(const orc_geo_grid* g, const orc_radar_grid* rg, const orc_orbit* orbit,
+                   const orc_lut2d* doppler, float min_height, float max_height, int margin,
+                   double threshold, int maxiter, double delta_range, int expansion_threshold,
+                   int32_t* out);
+/* DEM statistics (geometry/DEMInterpolator.cpp:515-560) */
+void orc_dem_stats(const float* z, int64_t length, int64_t width, float* mn, float* mx, double* mean,
+                   int64_t* n_valid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,11 @@ def lib() -> C.CDLL:
                                      C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double]
         _lib.orc_sinc_table.argtypes = [C.c_void_p]
         _lib.orc_dem_subset.argtypes = [C.POINTER(DemRaster), C.POINTER(GeoGrid), C.c_int] + [C.c_void_p] * 6
+        _lib.orc_radar_bbox.argtypes = [C.POINTER(GeoGrid), C.POINTER(RadarGrid), C.POINTER(OrbitS), C.POINTER(Lut),
+                                        C.c_float, C.c_float, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
+                                        C.c_void_p]
+        _lib.orc_dem_stats.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]
     return _lib
 
 
@@ -382,6 +387,37 @@ def geo2rdr(llh, ellipsoid, orbit, doppler, wavelength, side, t0, threshold=1e-8
     ok = lib().orc_geo2rdr(_ptr(llh), ellipsoid.a, ellipsoid.e2, C.byref(o), C.byref(d), _ptr(t), _ptr(r),
                            wavelength, int(side), threshold, maxiter, delta_range)
     return t[0], r[0], ok
+
+
+def radar_bbox(geo_grid, radar_grid, orbit, min_height=-500.0, max_height=9000.0, doppler=None, margin=50,
+               threshold=1e-8, maxiter=50, delta_range=10.0, geogrid_expansion_threshold=100):
+    """geometry/boundingbox.cpp:434-641 on the CPU: (first_az, last_az,
+    first_rg, last_rg, status, detail) as gslc_radar_bbox reports them."""
+    keep = _Keep()
+    g = geo_struct(geo_grid)
+    rg = radar_struct(radar_grid)
+    o = orbit_struct(orbit, keep)
+    if doppler is None:
+        d = Lut()
+        d.have_data, d.bounds_error, d.method, d.dx, d.dy = 0, 1, 1, 1.0, 1.0
+    else:
+        d = lut_struct(doppler, keep)
+    out = np.zeros(6, dtype=np.int32)
+    st = lib().orc_radar_bbox(C.byref(g), C.byref(rg), C.byref(o), C.byref(d), float(min_height), float(max_height),
+                              int(margin), threshold, int(maxiter), delta_range, int(geogrid_expansion_threshold),
+                              _ptr(out))
+    if st:
+        raise ValueError(lib().orc_last_error().decode())
+    return tuple(int(v) for v in out)
+
+
+def dem_stats(z: np.ndarray):
+    """DEMInterpolator::computeMinMaxMeanHeight (DEMInterpolator.cpp:515-560)."""
+    z = np.ascontiguousarray(z, dtype=np.float32)
+    mn, mx = np.zeros(1, np.float32), np.zeros(1, np.float32)
+    mean, n = np.zeros(1, np.float64), np.zeros(1, np.int64)
+    lib().orc_dem_stats(_ptr(z), z.shape[0], z.shape[1], _ptr(mn), _ptr(mx), _ptr(mean), _ptr(n))
+    return mn[0], mx[0], mean[0], int(n[0])
 
 
 def sinc_table() -> np.ndarray:
