@@ -320,6 +320,38 @@ def run_gpu(args, rank, world):
     return sc, res
 
 
+PROFILE = ROOT / "profiles" / "geocode_kernel_medium.md"
+
+
+def profile_per_px() -> dict:
+    """Per-output-pixel figures of the committed ncu capture of the fused
+    kernel on the medium workload (lines "name: value" at its end)."""
+    vals = {}
+    if PROFILE.exists():
+        for line in PROFILE.read_text().splitlines():
+            k, _, v = line.partition(":")
+            if k.endswith("_per_output_px") and v.strip():
+                try:
+                    vals[k.strip()] = float(v)
+                except ValueError:
+                    pass
+    return vals
+
+
+def fp64_roofline(prof_vals: dict, variant: str, npx: int, kernel_ms: float, peak_gflops: float) -> dict:
+    """FP64 roofline of the fused kernel: FP64 FLOP per output pixel counted
+    by ncu (2 x DFMA + DADD + DMUL thread instructions of the medium capture)
+    times the frame's pixels over the kernel time measured in this run,
+    against the DFMA-loop peak measured in this run."""
+    out = {"peak_gflops_measured": peak_gflops, "probe": "gslc_probe_fp64_gflops DFMA loop", "unit": "GFLOP/s"}
+    f = prof_vals.get(f"fp64_flop_{variant}_per_output_px")
+    if f is not None and kernel_ms > 0:
+        ach = f * npx / (kernel_ms * 1e-3) / 1e9
+        out.update({"achieved": ach, "peak": peak_gflops, "frac": ach / peak_gflops, "flop_per_output_px": f,
+                    "flop_source": f"ncu 2*dfma+dadd+dmul of the medium capture ({PROFILE.name})"})
+    return out
+
+
 def C_double():
     import ctypes
     return ctypes.c_double()
@@ -642,12 +674,8 @@ def main():
     if not args.no_served:
         served = run_serving(args)
     hbm_peak, peak_kind = peaks()
-    traffic = None
-    prof = ROOT / "profiles" / "geocode_kernel_medium_v2.md"
-    if prof.exists():
-        for line in prof.read_text().splitlines():
-            if line.startswith("dram_bytes_per_output_px:"):
-                traffic = float(line.split(":")[1]) * res["npx"]
+    prof_vals = profile_per_px()
+    traffic = prof_vals["dram_bytes_per_output_px"] * res["npx"] if "dram_bytes_per_output_px" in prof_vals else None
     kernel_s = res["kernel_ms"] * 1e-3
     achieved = res["alg_bytes"] / kernel_s / 1e9
     value = res["npx"] * world / (res["ms"] * 1e-3)
@@ -659,17 +687,18 @@ def main():
         "valid_px_per_s": res["n_valid"] * world / (res["ms"] * 1e-3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": "ncu dram bytes/px of the medium capture (profiles/geocode_kernel_medium_v2.md)"
-                                       " x frame px", "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic_source": f"ncu dram bytes/px of the medium capture ({PROFILE.name}) x frame px", "peak_source": f"{peak_kind} hbm_gbs",
                      "kernel": "geocode_kernel (fused)", "kernel_ms": res["kernel_ms"],
                      "alg_bytes_per_launch": res["alg_bytes"],
                      "alg_bytes_terms": {"geo_out": 8 * res["npx"], "mask": res["npx"], "slc": 8 * res["n_slc"],
                                          "dem_window": res["dem_bytes"]},
                      "binding": "fp64 pipe (geo2rdr); see fp64"},
-        "fp64": {"peak_gflops_measured": res["fp64_peak_gflops"], "probe": "gslc_probe_fp64_gflops DFMA loop"},
+        "fp64": fp64_roofline(prof_vals, "fp64", res["npx"], res["kernel_ms"], res["fp64_peak_gflops"]),
         "deramp_ms": res["deramp_ms"],
         "geo2rdr_ff": {"value": res["ff"]["value"], "unit": UNIT, "ms_per_step": res["ff"]["ms"],
                        "kernel_ms": res["ff"]["kernel_ms"], "parity_sample": par_ff,
+                       "fp64": fp64_roofline(prof_vals, "ff", res["npx"], res["ff"]["kernel_ms"],
+                                             res["fp64_peak_gflops"]),
                        "note": "float-float (double-word FP32) Newton iterations, FP64 first iterate and range"},
         "batched": batched,
         "served": served,
