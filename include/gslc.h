@@ -374,6 +374,48 @@ int gslc_radar_bbox_blocks(gslc_ctx* ctx, const gslc_bbox_args* args, gslc_radar
 int gslc_dem_stats(gslc_ctx* ctx, const float* data, int64_t length, int64_t width, int64_t row_stride,
                    float* min_height, float* max_height, double* mean_height, int64_t* n_valid, void* stream);
 
+/* Arguments of isce3::geometry::makeRadarGridCubes
+ * (geometry/metadataCubes.cpp:276-489) for the outputs the GSLC workflow
+ * writes (nisar/workflows/h5_prep.py:869-978).  Each output is device memory
+ * of n_heights x length x width elements (height-major) or NULL. */
+typedef struct {
+    gslc_radar_grid radar_grid;
+    gslc_geo_grid geo_grid;         /* EPSG 4326 or UTM */
+    const double* heights;          /* host, n_heights */
+    int32_t n_heights;
+    int32_t maxiter;                /* numiter_geo2rdr, [0, 1000] */
+    gslc_orbit orbit;
+    gslc_lut2d native_doppler;      /* device data */
+    gslc_lut2d grid_doppler;        /* device data */
+    double threshold;               /* threshold_geo2rdr */
+    double delta_range;
+    double* slant_range;            /* f64, m */
+    double* azimuth_time;           /* f64, s since the orbit's epoch */
+    float* incidence_angle;         /* f32, degrees */
+    float* los_unit_vector_x;       /* f32, east component, target to sensor */
+    float* los_unit_vector_y;       /* f32, north component */
+    float* along_track_unit_vector_x;
+    float* along_track_unit_vector_y;
+    float* elevation_angle;         /* f32, degrees */
+    double* ground_track_velocity;  /* f64, m/s */
+} gslc_cube_args;
+
+/* Radar grid metadata cubes in one launch, one thread per (height, line,
+ * column) point: geo2rdr with the grid Doppler (slant range, azimuth time),
+ * geo2rdr with the native Doppler and the vectors of writeVectorDerivedCubes
+ * (metadataCubes.cpp:74-274).  Replaces isce3::geometry::makeRadarGridCubes
+ * (bound as isce3.geometry.make_radar_grid_cubes,
+ * python/extensions/pybind_isce3/geometry/metadataCubes.cpp:16-35).  Points
+ * that do not converge are NaN.  The reference starts each point's solves
+ * from the previous point's results (a chain through each height layer in
+ * row-major order); this call reproduces that chain by passes: each launch
+ * solves every point from the starts implied by the previous pass, until no
+ * convergence status changes and no iterate moves by 1e-13 s (at most 16
+ * passes; gslc_last_cube_passes reports them).  The call synchronises the
+ * stream.  A failed projection inverse returns GSLC_EPROJ. */
+int gslc_make_radar_grid_cubes(gslc_ctx* ctx, const gslc_cube_args* args, void* stream);
+int gslc_last_cube_passes(const gslc_ctx* ctx);
+
 /* Allocation-free plain form.  No counterpart in the reference: an addition
  * for callers that must not allocate device memory while they run (serving
  * loops that reserve HBM up front under a fixed budget, hosts that forbid

@@ -172,6 +172,16 @@ class BBoxArgs(C.Structure):
                 ("delta_range", C.c_double)]
 
 
+class CubeArgs(C.Structure):
+    _fields_ = [("radar_grid", RadarGrid), ("geo_grid", GeoGrid), ("heights", C.c_void_p), ("n_heights", C.c_int32),
+                ("maxiter", C.c_int32), ("orbit", OrbitDesc), ("native_doppler", Lut2d), ("grid_doppler", Lut2d),
+                ("threshold", C.c_double), ("delta_range", C.c_double), ("slant_range", C.c_void_p),
+                ("azimuth_time", C.c_void_p), ("incidence_angle", C.c_void_p), ("los_unit_vector_x", C.c_void_p),
+                ("los_unit_vector_y", C.c_void_p), ("along_track_unit_vector_x", C.c_void_p),
+                ("along_track_unit_vector_y", C.c_void_p), ("elevation_angle", C.c_void_p),
+                ("ground_track_velocity", C.c_void_p)]
+
+
 _EXPORTS = {
     "gslc_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "gslc_ctx_destroy": (C.c_int, [C.c_void_p]),
@@ -210,6 +220,8 @@ _EXPORTS = {
                                   C.POINTER(C.c_int64)]),
     "gslc_batch_destroy": (C.c_int, [C.c_void_p]),
     "gslc_radar_bbox_blocks": (C.c_int, [C.c_void_p, C.POINTER(BBoxArgs), C.c_void_p, C.c_void_p]),
+    "gslc_make_radar_grid_cubes": (C.c_int, [C.c_void_p, C.POINTER(CubeArgs), C.c_void_p]),
+    "gslc_last_cube_passes": (C.c_int, [C.c_void_p]),
     "gslc_dem_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_float),
                                  C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "gslc_deramp_block": (C.c_int, [C.c_void_p, C.POINTER(RadarGrid), C.POINTER(AzRgFunc), C.POINTER(AzRgFunc),

@@ -26,6 +26,7 @@ struct gslc_ctx {
     int timing = 0;                 // record CUDA events around the kernels
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float ms_geocode = 0.f, ms_deramp = 0.f;
+    int cube_passes = 0;            // passes of the last gslc_make_radar_grid_cubes
     std::string err;
 };
 
@@ -1122,6 +1123,140 @@ extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc
     if (e != cudaSuccess) return cuda_err(c, e, "radar bbox");
     return GSLC_OK;
 }
+
+// ---- radar grid metadata cubes (geometry/metadataCubes.cpp:276-489) --------
+extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (!a) return set_err(c, GSLC_EINVAL, "null arguments");
+    const gslc_geo_grid& gg = a->geo_grid;
+    if (a->n_heights < 0 || (a->n_heights > 0 && !a->heights) || gg.width < 0 || gg.length < 0)
+        return set_err(c, GSLC_EINVAL, "invalid cube shape");
+    if ((int64_t)a->n_heights * gg.length * gg.width > (int64_t)1 << 34)
+        return set_err(c, GSLC_EINVAL, "cube larger than 2^34 points");
+    if (a->maxiter < 0 || a->maxiter > 1000) return set_err(c, GSLC_EINVAL, "numiter_geo2rdr must be in [0, 1000]");
+    if (!grid_ok(a->radar_grid)) return set_err(c, GSLC_EINVAL, "invalid radar grid");
+    if (!is_lonlat_or_utm(gg.epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
+    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
+    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
+        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (int st = check_lut(c, a->native_doppler, "native_doppler")) return st;
+    if (int st = check_lut(c, a->grid_doppler, "grid_doppler")) return st;
+    const int64_t npts = (int64_t)a->n_heights * gg.length * gg.width;
+    if (npts == 0) return GSLC_OK;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+
+    CubeParams p;
+    std::memset(&p, 0, sizeof(p));
+    std::vector<double> coef;
+    build_orbit_table(a->orbit, coef, p.orbit);
+    const gslc_radar_grid& rg = a->radar_grid;
+    p.gx0 = gg.start_x; p.gy0 = gg.start_y; p.gdx = gg.spacing_x; p.gdy = gg.spacing_y;
+    p.width = gg.width; p.length = gg.length; p.n_heights = a->n_heights;
+    p.geo_is_lonlat = gg.epsg == 4326;
+    if (!p.geo_is_lonlat) utm_setup(gg.epsg, p.utm);
+    p.grid_dop = to_lut(a->grid_doppler);
+    p.nat_dop = to_lut(a->native_doppler);
+    p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
+    p.mid_range = 0.5 * (rg.starting_range + grid_end(rg));      // RadarGridParameters::midRange
+    p.wvl = rg.wavelength;
+    p.thr = a->threshold;
+    p.delta_range = a->delta_range;
+    p.look_side = rg.look_side;
+    p.maxiter = a->maxiter;
+    p.slant_range = a->slant_range; p.azimuth_time = a->azimuth_time;
+    p.incidence = a->incidence_angle; p.los_x = a->los_unit_vector_x; p.los_y = a->los_unit_vector_y;
+    p.along_x = a->along_track_unit_vector_x; p.along_y = a->along_track_unit_vector_y;
+    p.elevation = a->elevation_angle; p.ground_velocity = a->ground_track_velocity;
+    p.want_vectors = (p.incidence || p.los_x || p.los_y || p.along_x || p.along_y || p.elevation ||
+                      p.ground_velocity) ? 1 : 0;
+
+    // device scratch: orbit table, heights, chain starts / iterates / statuses
+    const size_t orb_b = coef.size() * sizeof(double);
+    auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t h_off = up(orb_b), h_b = (size_t)a->n_heights * sizeof(double);
+    const size_t sg_off = up(h_off + h_b), pt_b = (size_t)npts * sizeof(double);
+    const size_t sn_off = up(sg_off + pt_b), tg_off = up(sn_off + pt_b), tn_off = up(tg_off + pt_b);
+    const size_t st_off = up(tn_off + pt_b), total = st_off + (size_t)npts;
+    std::vector<double> start_g((size_t)npts, p.t_mid), start_n((size_t)npts, p.t_mid);
+    std::vector<double> tg((size_t)npts), tn((size_t)npts), prev_tg, prev_tn;
+    std::vector<uint8_t> stat((size_t)npts), prev_stat;
+    char* buf = nullptr;
+    e = cudaMallocAsync((void**)&buf, total, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMallocAsync cube scratch");
+    e = cudaMemcpyAsync(buf, coef.data(), orb_b, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf + h_off, a->heights, h_b, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
+    const double* d_coef = reinterpret_cast<const double*>(buf);
+    p.orbit.coef = d_coef;
+    p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+    p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
+    p.heights = reinterpret_cast<const double*>(buf + h_off);
+    p.start_grid = reinterpret_cast<const double*>(buf + sg_off);
+    p.start_native = reinterpret_cast<const double*>(buf + sn_off);
+    p.t_grid = reinterpret_cast<double*>(buf + tg_off);
+    p.t_native = reinterpret_cast<double*>(buf + tn_off);
+    p.status = reinterpret_cast<uint8_t*>(buf + st_off);
+    p.err = c->d_err;
+    // The reference chains each height layer through its points in row-major
+    // order (metadataCubes.cpp:311-413): a point's grid-Doppler solve starts
+    // from the previous point's result, or sensingMid after a failure; its
+    // native-Doppler solve from the native state of the last point whose grid
+    // solve converged (reset to sensingMid after a native failure).  Each
+    // pass solves every point from the starts the previous pass implies; the
+    // first k points of a chain are exact after k passes and, since a start
+    // moves the converged iterate by far less than it moves the start, the
+    // passes stop once no status changes and no iterate moves by 1e-13 s.
+    const int64_t plane = (int64_t)gg.length * gg.width;
+    constexpr int MAX_PASSES = 16;
+    int passes = 0;
+    bool settled = false;
+    while (e == cudaSuccess && !settled && passes < MAX_PASSES) {
+        e = cudaMemcpyAsync(buf + sg_off, start_g.data(), pt_b, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(buf + sn_off, start_n.data(), pt_b, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = launch_radar_grid_cubes(p, stream, &c->launches);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tg.data(), p.t_grid, pt_b, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tn.data(), p.t_native, pt_b, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(stat.data(), p.status, (size_t)npts, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) break;
+        ++passes;
+        if (passes > 1 && stat == prev_stat) {
+            double moved = 0.0;
+            for (int64_t k = 0; k < npts; ++k) {
+                if (stat[k] & 1) moved = std::max(moved, std::fabs(tg[k] - prev_tg[k]));
+                if (stat[k] & 2) moved = std::max(moved, std::fabs(tn[k] - prev_tn[k]));
+            }
+            settled = moved < 1e-13;
+        }
+        if (settled) break;
+        for (int hc = 0; hc < a->n_heights; ++hc) {
+            double sg = p.t_mid, sn = p.t_mid;
+            for (int64_t q = 0; q < plane; ++q) {
+                const int64_t k = hc * plane + q;
+                start_g[k] = sg;
+                start_n[k] = sn;
+                sg = (stat[k] & 1) ? tg[k] : p.t_mid;
+                if ((stat[k] & 1) && p.want_vectors) sn = (stat[k] & 2) ? tn[k] : p.t_mid;
+            }
+        }
+        prev_stat = stat;
+        prev_tg = tg;
+        prev_tn = tn;
+    }
+    c->cube_passes = passes;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaFreeAsync(buf, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "radar grid cubes");
+    if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    return GSLC_OK;
+}
+
+extern "C" int gslc_last_cube_passes(const gslc_ctx* c) { return c ? c->cube_passes : -1; }
 
 extern "C" int gslc_dem_stats(gslc_ctx* c, const float* data, int64_t length, int64_t width, int64_t row_stride,
                               float* mn, float* mx, double* mean, int64_t* n_valid, void* stream_) {

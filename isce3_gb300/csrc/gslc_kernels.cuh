@@ -117,6 +117,37 @@ struct PlanParams {
     int32_t* out;                // n_blocks x (first az, last az, first rg, last rg, status, detail)
 };
 
+// Radar grid metadata cubes (gslc_plan.cu, geometry/metadataCubes.cpp:276-489):
+// n_heights x length x width points; NULL outputs are skipped.
+struct CubeParams {
+    double gx0, gy0, gdx, gdy;
+    int32_t width, length, n_heights, geo_is_lonlat;
+    Utm utm;
+    const double* heights;       // device, n_heights
+    Orbit orbit;
+    Lut grid_dop, nat_dop;
+    double t_mid, mid_range, wvl, thr, delta_range;
+    int32_t look_side, maxiter, want_vectors, _pad;
+    double* slant_range;
+    double* azimuth_time;
+    float* incidence;
+    float* los_x;
+    float* los_y;
+    float* along_x;
+    float* along_y;
+    float* elevation;
+    double* ground_velocity;
+    // chain state: starts of this pass, final iterates and statuses out
+    // (bit 0 grid-Doppler solve converged, bit 1 native-Doppler solve converged)
+    const double* start_grid;
+    const double* start_native;
+    double* t_grid;
+    double* t_native;
+    uint8_t* status;
+    int32_t* err;                // bit 0: a projection inverse failed
+};
+cudaError_t launch_radar_grid_cubes(const CubeParams& p, cudaStream_t s, int64_t* launches);
+
 // DEM statistics (geometry/DEMInterpolator.cpp:515-560): min, max, sum of
 // the non-NaN samples and the NaN count.
 struct DemStats { float mn, mx; double sum; long long nan; };

@@ -17,18 +17,18 @@ namespace {
 
 // geometry/detail/Geo2Rdr.icc:50-112 (updateAztime): 15-point coarse search
 // over the orbit span for the closest approach.
-__device__ bool plan_update_aztime(const PlanParams& p, V3 xyz, double& t) {
+__device__ bool coarse_aztime(const Orbit& o, int look_side, V3 xyz, double& t) {
     constexpr int num = 15;
-    const double tstart = p.orbit.t0, tend = p.orbit.t_end;
+    const double tstart = o.t0, tend = o.t_end;
     const double dt = (tend - tstart) / (num - 1);
     double r_closest = 1e16, t_closest = -1000.;
     for (int k = 0; k < num; ++k) {
         const double tt = tstart + k * dt;
         if (tt < tstart || tt > tend) continue;
         V3 pos, vel;
-        orbit_eval(p.orbit, tt, pos, vel);
+        orbit_eval(o, tt, pos, vel);
         const V3 rvec = vsub(xyz, pos);
-        if (k == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
+        if (k == 0 && ((look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
         const double r = vnorm(rvec);
         if (r < r_closest) { r_closest = r; t_closest = tt; }
     }
@@ -36,36 +36,40 @@ __device__ bool plan_update_aztime(const PlanParams& p, V3 xyz, double& t) {
     return true;
 }
 
-// geometry/geometry.cpp:241-251 over geometry/detail/Geo2Rdr.icc:114-179:
-// t is the initial guess on entry (used when inside the orbit span) and the
-// last iterate on return, converged or not, so that a retry starts where the
-// reference's does.  An iterate outside the span ends the solve (the
-// reference's FillNaN orbit makes every later step NaN).
-__device__ bool plan_geo2rdr(const PlanParams& p, V3 xyz, double& t, double& R) {
-    const Orbit& o = p.orbit;
-    if (!(t >= o.t0 && t <= o.t_end) && !plan_update_aztime(p, xyz, t)) return false;
-    const double half_wvl = 0.5 * p.wvl, dr = p.delta_range;
+// geometry/geometry.cpp:241-251 over geometry/detail/Geo2Rdr.icc:114-179,
+// with a LUT2d Doppler: t is the initial guess on entry (used when inside the
+// orbit span) and the last iterate on return, converged or not, so that a
+// retry starts where the reference's does.  An iterate outside the span ends
+// the solve (the reference's FillNaN orbit makes every later step NaN).
+__device__ bool geo2rdr_lut(const Orbit& o, const Lut& dop, int look_side, double wvl, double thr, int maxiter,
+                            double dr, V3 xyz, double& t, double& R) {
+    if (!(t >= o.t0 && t <= o.t_end) && !coarse_aztime(o, look_side, xyz, t)) return false;
+    const double half_wvl = 0.5 * wvl;
     double dt = 0.0;
-    for (int i = 0; i < p.maxiter; ++i) {
+    for (int i = 0; i < maxiter; ++i) {
         t -= dt;
         if (!(t >= o.t0 && t <= o.t_end)) return false;
         V3 pos, vel;
         orbit_eval(o, t, pos, vel);
         const V3 rvec = vsub(xyz, pos);
         R = vnorm(rvec);
-        if (i == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
-        if (p.dop.have_data && p.dop.bounds_error && !(lut_contains(p.dop, t, R) && lut_contains(p.dop, t, R + dr)))
+        if (i == 0 && ((look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
+        if (dop.have_data && dop.bounds_error && !(lut_contains(dop, t, R) && lut_contains(dop, t, R + dr)))
             return false;
         const double dopfact = vdot(rvec, vel);
-        const double fdop = half_wvl * lut_eval(p.dop, t, R);
-        const double fdopder = (half_wvl * lut_eval(p.dop, t, R + dr) - fdop) / dr;
+        const double fdop = half_wvl * lut_eval(dop, t, R);
+        const double fdopder = (half_wvl * lut_eval(dop, t, R + dr) - fdop) / dr;
         const double fn = dopfact - fdop * R;
         const double c1 = -vdot(vel, vel);
         const double c2 = (fdop / R) + fdopder;
         dt = fn / (c1 + c2 * dopfact);
-        if (fabs(dt) < p.thr) return true;
+        if (fabs(dt) < thr) return true;
     }
     return false;
+}
+
+__device__ __forceinline__ bool plan_geo2rdr(const PlanParams& p, V3 xyz, double& t, double& R) {
+    return geo2rdr_lut(p.orbit, p.dop, p.look_side, p.wvl, p.thr, p.maxiter, p.delta_range, xyz, t, R);
 }
 
 __device__ __forceinline__ int shfl_min8(int v) {
@@ -168,6 +172,125 @@ __global__ void __launch_bounds__(256) radar_bbox_kernel(const __grid_constant__
     out[5] = 0;
 }
 
+// ---- radar grid metadata cubes (geometry/metadataCubes.cpp:276-489) --------
+// One thread per (height, line, column) point: geo2rdr with the grid Doppler
+// (slant range, azimuth time), then with the native Doppler for the platform
+// state, and the vectors of writeVectorDerivedCubes (:74-274).  The reference
+// starts each point's solves from the previous point's results (a chain
+// through each height layer); one launch here is one pass that solves every
+// point from the starts the host derived from the previous pass, and writes
+// every output (NaN where a solve failed), the final iterates and the
+// statuses for the next derivation.
+__device__ __forceinline__ V3 vunit(V3 v) {
+    const double n = vnorm(v);
+    return {v.x / n, v.y / n, v.z / n};
+}
+
+// core/DenseMatrix.h:73-79 (xyzToEnu) applied to v
+__device__ __forceinline__ V3 to_enu(double slat, double clat, double slon, double clon, V3 v) {
+    return {-slon * v.x + clon * v.y, -slat * clon * v.x - slat * slon * v.y + clat * v.z,
+            clat * clon * v.x + clat * slon * v.y + slat * v.z};
+}
+
+// core/Ellipsoid.h:197-231 (Vermeille 2002): latitude and longitude of an
+// ECEF point (the height is not needed here)
+__device__ void xyz_to_latlon(double a, double e2, V3 x, double& lat, double& lon) {
+    const double e4 = e2 * e2, a2 = a * a;
+    const double p = (x.x * x.x + x.y * x.y) / a2;
+    const double q = ((1. - e2) * (x.z * x.z)) / a2;
+    const double r = (p + q - e4) / 6.;
+    const double s = (e4 * p * q) / (4. * (r * r * r));
+    const double t = pow(1. + s + sqrt(s * (2. + s)), 1. / 3.);
+    const double u = r * (1. + t + (1. / t));
+    const double rv = sqrt(u * u + (e4 * q));
+    const double w = (e2 * (u + rv - q)) / (2. * rv);
+    const double k = sqrt(u + rv + w * w) - w;
+    const double d = (k * sqrt(x.x * x.x + x.y * x.y)) / (k + e2);
+    lat = atan2(x.z, d);
+    lon = atan2(x.y, x.x);
+}
+
+__global__ void __launch_bounds__(256) radar_grid_cubes_kernel(const __grid_constant__ CubeParams p) {
+    const int64_t plane = (int64_t)p.length * p.width;
+    const int64_t n = plane * p.n_heights;
+    const double dnan = __longlong_as_double(0x7ff8000000000000LL);
+    const float fnan = __int_as_float(0x7fc00000);
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int hc = (int)(k / plane);
+        const int64_t r = k - hc * plane;
+        const int i = (int)(r / p.width), j = (int)(r - (int64_t)i * p.width);
+        const double h = p.heights[hc];
+        double sr = dnan, at = dnan, gv = dnan;
+        float inc = fnan, lx = fnan, ly = fnan, ax = fnan, ay = fnan, el = fnan;
+        unsigned char st = 0;
+        double t = p.start_grid[k], tn = p.start_native[k];
+        // pixel centre (metadataCubes.cpp:341-345), reference rounding
+        const double y = dadd(p.gy0, dmul(0.5 + (double)i, p.gdy));
+        const double x = dadd(p.gx0, dmul(0.5 + (double)j, p.gdx));
+        double lon, lat;
+        bool proj_ok = true;
+        if (p.geo_is_lonlat) {
+            lon = ddiv(dmul(x, PI), 180.0);
+            lat = ddiv(dmul(y, PI), 180.0);
+        } else if (!utm_inverse(p.utm, x, y, lon, lat)) {
+            atomicOr(p.err, 1);
+            proj_ok = false;
+        }
+        if (proj_ok) {
+            double slon, clon, slat, clat;
+            sincos(lon, &slon, &clon);
+            sincos(lat, &slat, &clat);
+            const V3 target = lonlat_to_xyz_sc(WGS84_A, WGS84_E2, slon, clon, slat, clat, h);
+            double R = p.mid_range;
+            if (geo2rdr_lut(p.orbit, p.grid_dop, p.look_side, p.wvl, p.thr, p.maxiter, p.delta_range, target, t, R)) {
+                st = 1;
+                sr = R;
+                at = t;
+                double Rn = p.mid_range;
+                if (p.want_vectors && geo2rdr_lut(p.orbit, p.nat_dop, p.look_side, p.wvl, p.thr, p.maxiter,
+                                                  p.delta_range, target, tn, Rn)) {
+                    st |= 2;
+                    V3 sat, vel;
+                    orbit_eval(p.orbit, tn, sat, vel);
+                    // law of cosines (metadataCubes.cpp:118-132)
+                    const double slant = vnorm(vsub(target, sat));
+                    const double rt = vnorm(target), rp = vnorm(sat);
+                    const double cos_alpha = ((rt * rt + rp * rp - slant * slant) / (2 * rt * rp));
+                    gv = cos_alpha * rt * vnorm(vel) / rp;
+                    const V3 look = vunit(vsub(sat, target));
+                    if (p.elevation) {
+                        double sl, so, ss, cs, sso, cso;
+                        xyz_to_latlon(WGS84_A, WGS84_E2, sat, sl, so);
+                        sincos(sl, &ss, &cs);
+                        sincos(so, &sso, &cso);
+                        const V3 les = vunit(to_enu(ss, cs, sso, cso, look));
+                        el = (float)(acos(les.z) * 180.0 / PI);
+                    }
+                    const V3 le = vunit(to_enu(slat, clat, slon, clon, look));
+                    inc = (float)(acos(fabs(le.z)) * 180.0 / PI);
+                    lx = (float)le.x;
+                    ly = (float)le.y;
+                    const V3 atv = vunit(to_enu(slat, clat, slon, clon, vel));
+                    ax = (float)atv.x;
+                    ay = (float)atv.y;
+                }
+            }
+        }
+        p.t_grid[k] = t;
+        p.t_native[k] = tn;
+        p.status[k] = st;
+        if (p.slant_range) p.slant_range[k] = sr;
+        if (p.azimuth_time) p.azimuth_time[k] = at;
+        if (p.incidence) p.incidence[k] = inc;
+        if (p.los_x) p.los_x[k] = lx;
+        if (p.los_y) p.los_y[k] = ly;
+        if (p.along_x) p.along_x[k] = ax;
+        if (p.along_y) p.along_y[k] = ay;
+        if (p.elevation) p.elevation[k] = el;
+        if (p.ground_velocity) p.ground_velocity[k] = gv;
+    }
+}
+
 // DEM statistics, pass 1: per-block min, max, sum and NaN count over a
 // strided float raster (coalesced along rows, grid-stride over lines).
 // Starting values are the reference's +-FLT_MAX.
@@ -228,6 +351,19 @@ cudaError_t launch_radar_bbox(const PlanParams& p, cudaStream_t s, int64_t* laun
     const int threads = 256;
     const int64_t n = (int64_t)p.n_blocks * 8;
     radar_bbox_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(p);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_radar_grid_cubes(const CubeParams& p, cudaStream_t s, int64_t* launches) {
+    const int64_t n = (int64_t)p.length * p.width * p.n_heights;
+    if (n <= 0) return cudaSuccess;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (n + 255) / 256;
+    const unsigned grid = (unsigned)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
+    radar_grid_cubes_kernel<<<grid, 256, 0, s>>>(p);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -222,3 +222,92 @@ def get_radar_bbox(geo_grid: GeoGridParameters, radar_grid: RadarGridParameters,
     if isinstance(r, Exception):
         raise r
     return r
+
+
+_CUBE_OUTPUTS = [("slant_range_raster", "slant_range", np.float64),
+                 ("azimuth_time_raster", "azimuth_time", np.float64),
+                 ("incidence_angle_raster", "incidence_angle", np.float32),
+                 ("los_unit_vector_x_raster", "los_unit_vector_x", np.float32),
+                 ("los_unit_vector_y_raster", "los_unit_vector_y", np.float32),
+                 ("along_track_unit_vector_x_raster", "along_track_unit_vector_x", np.float32),
+                 ("along_track_unit_vector_y_raster", "along_track_unit_vector_y", np.float32),
+                 ("elevation_angle_raster", "elevation_angle", np.float32),
+                 ("ground_track_velocity_raster", "ground_track_velocity", np.float64)]
+_TORCH = {np.float64: torch.float64, np.float32: torch.float32}
+
+
+def make_radar_grid_cubes(radar_grid: RadarGridParameters, geogrid: GeoGridParameters, heights, orbit: Orbit,
+                          native_doppler: LUT2d, grid_doppler: LUT2d, slant_range_raster=None,
+                          azimuth_time_raster=None, incidence_angle_raster=None, los_unit_vector_x_raster=None,
+                          los_unit_vector_y_raster=None, along_track_unit_vector_x_raster=None,
+                          along_track_unit_vector_y_raster=None, elevation_angle_raster=None,
+                          ground_track_velocity_raster=None, threshold_geo2rdr: float = 1e-8,
+                          numiter_geo2rdr: int = 50, delta_range: float = 10.0,
+                          flag_set_output_rasters_geolocation: bool = False, *, device=None,
+                          lo_unit_vector_x_raster=None) -> None:
+    """``isce3.geometry.make_radar_grid_cubes`` on the GPU, one launch.
+
+    Argument order and defaults follow the pybind binding
+    (python/extensions/pybind_isce3/geometry/metadataCubes.cpp:16-35, whose
+    keyword for the LOS x cube is ``lo_unit_vector_x_raster``; both names are
+    accepted).  Each output is an array of shape (len(heights), length,
+    width) — NumPy (host) or a CUDA torch tensor — of float64 (slant range,
+    azimuth time, ground-track velocity) or float32 (the angles and unit
+    vectors), or None to skip it.  Band k of the reference's rasters is
+    plane k here.  Points where geo2rdr does not converge are NaN.
+    ``flag_set_output_rasters_geolocation`` only tags GDAL rasters in the
+    reference and has nothing to tag here.
+    """
+    if lo_unit_vector_x_raster is not None:
+        if los_unit_vector_x_raster is not None:
+            raise ValueError("give one of lo_unit_vector_x_raster and los_unit_vector_x_raster")
+        los_unit_vector_x_raster = lo_unit_vector_x_raster
+    given = dict(slant_range_raster=slant_range_raster, azimuth_time_raster=azimuth_time_raster,
+                 incidence_angle_raster=incidence_angle_raster, los_unit_vector_x_raster=los_unit_vector_x_raster,
+                 los_unit_vector_y_raster=los_unit_vector_y_raster,
+                 along_track_unit_vector_x_raster=along_track_unit_vector_x_raster,
+                 along_track_unit_vector_y_raster=along_track_unit_vector_y_raster,
+                 elevation_angle_raster=elevation_angle_raster,
+                 ground_track_velocity_raster=ground_track_velocity_raster)
+    h = np.ascontiguousarray(np.asarray(heights, dtype=np.float64).ravel())
+    shape = (h.size, geogrid.length, geogrid.width)
+    dev = M.device_of(device)
+    a = L.CubeArgs()
+    a.radar_grid = M.radar_grid_desc(radar_grid)
+    a.geo_grid = M.geo_grid_desc(geogrid)
+    a.heights = h.ctypes.data
+    a.n_heights = h.size
+    a.maxiter = int(numiter_geo2rdr)
+    a.orbit = M.orbit_desc(orbit)
+    a.native_doppler = M.lut_desc(native_doppler if native_doppler is not None else LUT2d(), dev)
+    a.grid_doppler = M.lut_desc(grid_doppler if grid_doppler is not None else LUT2d(), dev)
+    a.threshold, a.delta_range = float(threshold_geo2rdr), float(delta_range)
+    copies = []
+    keep = [h]
+    for name, field, dt in _CUBE_OUTPUTS:
+        arr = given[name]
+        if arr is None:
+            continue
+        if tuple(arr.shape) != shape:
+            raise ValueError(f"{name}: shape {tuple(arr.shape)} != (heights, length, width) {shape}")
+        if isinstance(arr, torch.Tensor) and arr.device.type == "cuda":
+            if arr.dtype != _TORCH[dt] or not arr.is_contiguous():
+                raise ValueError(f"{name}: must be a C-contiguous {np.dtype(dt).name} tensor")
+            t = arr
+        else:
+            if np.asarray(arr).dtype != dt:
+                raise ValueError(f"{name}: dtype must be {np.dtype(dt).name}")
+            t = torch.empty(shape, dtype=_TORCH[dt], device=dev)
+            copies.append((arr, t))
+        keep.append(t)
+        setattr(a, field, t.data_ptr())
+    lib = L.lib()
+    ctx = L.context(dev.index)
+    s = torch.cuda.current_stream(dev)
+    L.check(lib.gslc_make_radar_grid_cubes(ctx, C.byref(a), C.c_void_p(s.cuda_stream)), ctx,
+            "make_radar_grid_cubes")
+    for host, t in copies:
+        if isinstance(host, torch.Tensor):
+            host.copy_(t)
+        else:
+            host[...] = t.cpu().numpy()

@@ -1338,3 +1338,123 @@ extern "C" void orc_dem_stats(const float* z, int64_t length, int64_t width, flo
     }
     *mn = lo; *mx = hi; *mean = sum / n; *n_valid = n;
 }
+
+// ---------------------------------------------------------------- metadata cubes
+namespace {
+// core/Ellipsoid.h:197-231 (Vermeille 2002)
+V3 xyz_to_lonlat(double a, double e2, V3 x) {
+    const double e4 = e2 * e2, a2 = a * a;
+    const double p = (std::pow(x.x, 2) + std::pow(x.y, 2)) / a2;
+    const double q = ((1. - e2) * std::pow(x.z, 2)) / a2;
+    const double r = (p + q - e4) / 6.;
+    const double s = (e4 * p * q) / (4. * std::pow(r, 3));
+    const double t = std::pow(1. + s + std::sqrt(s * (2. + s)), (1. / 3.));
+    const double u = r * (1. + t + (1. / t));
+    const double rv = std::sqrt(std::pow(u, 2) + (e4 * q));
+    const double w = (e2 * (u + rv - q)) / (2. * rv);
+    const double k = std::sqrt(u + rv + std::pow(w, 2)) - w;
+    const double d = (k * std::sqrt(std::pow(x.x, 2) + std::pow(x.y, 2))) / (k + e2);
+    V3 llh;
+    llh.y = std::atan2(x.z, d);
+    llh.x = std::atan2(x.y, x.x);
+    llh.z = ((k + e2 - 1.) * std::sqrt(std::pow(d, 2) + std::pow(x.z, 2))) / k;
+    return llh;
+}
+
+// core/DenseMatrix.h:73-79 (xyzToEnu) applied to v
+V3 xyz_to_enu(double lat, double lon, V3 v) {
+    return {-std::sin(lon) * v.x + std::cos(lon) * v.y + 0. * v.z,
+            -std::sin(lat) * std::cos(lon) * v.x + -std::sin(lat) * std::sin(lon) * v.y + std::cos(lat) * v.z,
+            std::cos(lat) * std::cos(lon) * v.x + std::cos(lat) * std::sin(lon) * v.y + std::sin(lat) * v.z};
+}
+
+V3 normalized(V3 v) {
+    const double n = norm(v);
+    return {v.x / n, v.y / n, v.z / n};
+}
+}  // namespace
+
+// geometry/metadataCubes.cpp:276-489 (makeRadarGridCubes) with
+// writeVectorDerivedCubes (:74-274) for the outputs isce3 writes in the GSLC
+// workflow: per height layer, every geogrid point solves geo2rdr with the
+// grid Doppler from the previous point's result (sensingMid at the start and
+// after a failure), then with the native Doppler for the platform position.
+// Outputs are n_heights x length x width, NaN where not solved; NULL skips one.
+extern "C" int orc_radar_grid_cubes(const orc_radar_grid* rg, const orc_geo_grid* g, const double* heights,
+                                    int n_heights, const orc_orbit* orbit, const orc_lut2d* native_doppler,
+                                    const orc_lut2d* grid_doppler, double threshold, int maxiter,
+                                    double delta_range, double* slant_range, double* azimuth_time,
+                                    float* incidence, float* los_x, float* los_y, float* along_x,
+                                    float* along_y, float* elevation, double* ground_velocity, int nthreads) {
+    Proj proj;
+    if (!proj.init(g->epsg)) return fail("unsupported EPSG");
+    const int64_t L = g->length, W = g->width, plane = L * W;
+    const double fnan = std::numeric_limits<float>::quiet_NaN();
+    auto fill = [&](auto* p, double v) {
+        if (p) for (int64_t i = 0; i < plane * n_heights; ++i) p[i] = (std::remove_reference_t<decltype(*p)>)v;
+    };
+    fill(slant_range, NaN); fill(azimuth_time, NaN); fill(incidence, fnan); fill(los_x, fnan); fill(los_y, fnan);
+    fill(along_x, fnan); fill(along_y, fnan); fill(elevation, fnan); fill(ground_velocity, NaN);
+    const bool vec = incidence || los_x || los_y || along_x || along_y || elevation || ground_velocity;
+    const double mid_range = 0.5 * (rg->starting_range + rg_ending_range(*rg));
+    int proj_fail = 0;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : proj_fail)
+    for (int hc = 0; hc < n_heights; ++hc) {
+        double az_t = rg_sensing_mid(*rg), nat_t = rg_sensing_mid(*rg);
+        double sr = mid_range, nat_sr = mid_range;
+        const double height = heights[hc];
+        for (int64_t i = 0; i < L; ++i) {
+            const double pos_y = g->start_y + (0.5 + i) * g->spacing_y;
+            for (int64_t j = 0; j < W; ++j) {
+                const double pos_x = g->start_x + (0.5 + j) * g->spacing_x;
+                V3 llh{0, 0, 0};
+                if (proj.inverse({pos_x, pos_y, height}, llh) != 0) { proj_fail = 1; continue; }
+                const int64_t k = hc * plane + i * W + j;
+                double t0 = az_t;
+                if (geo2rdr_detail(&az_t, &sr, llh, WGS84_A, WGS84_E2, orbit, grid_doppler, rg->wavelength,
+                                   rg->look_side, t0, threshold, maxiter, delta_range) != G_OK) {
+                    az_t = rg_sensing_mid(*rg);
+                    sr = mid_range;
+                    continue;
+                }
+                if (slant_range) slant_range[k] = sr;
+                if (azimuth_time) azimuth_time[k] = az_t;
+                if (!vec) continue;
+                t0 = nat_t;
+                if (geo2rdr_detail(&nat_t, &nat_sr, llh, WGS84_A, WGS84_E2, orbit, native_doppler, rg->wavelength,
+                                   rg->look_side, t0, threshold, maxiter, delta_range) != G_OK) {
+                    nat_t = rg_sensing_mid(*rg);
+                    nat_sr = mid_range;
+                    continue;
+                }
+                V3 sat, vel;
+                if (orbit_interp(orbit, nat_t, &sat, &vel) != 0) continue;
+                const V3 target = lonlat_to_xyz(WGS84_A, WGS84_E2, llh);
+                if (ground_velocity) {
+                    const double slant = norm(sub(target, sat));
+                    const double rt = norm(target), rp = norm(sat);
+                    const double cos_alpha = ((rt * rt + rp * rp - slant * slant) / (2 * rt * rp));
+                    ground_velocity[k] = cos_alpha * rt * norm(vel) / rp;
+                }
+                const V3 look = normalized(sub(sat, target));
+                if (elevation) {
+                    const V3 sat_llh = xyz_to_lonlat(WGS84_A, WGS84_E2, sat);
+                    const V3 le = normalized(xyz_to_enu(sat_llh.y, sat_llh.x, look));
+                    elevation[k] = (float)(std::acos(le.z) * 180.0 / M_PI);
+                }
+                const V3 le = normalized(xyz_to_enu(llh.y, llh.x, look));
+                if (incidence) incidence[k] = (float)(std::acos(std::abs(le.z)) * 180.0 / M_PI);
+                if (los_x) los_x[k] = (float)le.x;
+                if (los_y) los_y[k] = (float)le.y;
+                if (along_x || along_y) {
+                    const V3 at = normalized(xyz_to_enu(llh.y, llh.x, vel));
+                    if (along_x) along_x[k] = (float)at.x;
+                    if (along_y) along_y[k] = (float)at.y;
+                }
+            }
+        }
+    }
+    if (proj_fail) return fail("Inverse projection transformation failed");
+    return 0;
+}

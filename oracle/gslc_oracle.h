@@ -177,6 +177,14 @@ int orc_radar_bbox(const orc_geo_grid* g, const orc_radar_grid* rg, const orc_or
                    const orc_lut2d* doppler, float min_height, float max_height, int margin,
                    double threshold, int maxiter, double delta_range, int expansion_threshold,
                    int32_t* out);
+/* radar grid metadata cubes (geometry/metadataCubes.cpp:276-489): arrays of
+ * n_heights x length x width, NaN where geo2rdr did not converge; NULL skips
+ * an output.  Returns >0 if a projection inverse failed. */
+int orc_radar_grid_cubes(const orc_radar_grid* rg, const orc_geo_grid* g, const double* heights, int n_heights,
+                         const orc_orbit* orbit, const orc_lut2d* native_doppler, const orc_lut2d* grid_doppler,
+                         double threshold, int maxiter, double delta_range, double* slant_range,
+                         double* azimuth_time, float* incidence, float* los_x, float* los_y, float* along_x,
+                         float* along_y, float* elevation, double* ground_velocity, int nthreads);
 /* DEM statistics (geometry/DEMInterpolator.cpp:515-560) */
 void orc_dem_stats(const float* z, int64_t length, int64_t width, float* mn, float* mx, double* mean,
                    int64_t* n_valid);

@@ -129,6 +129,9 @@ def lib() -> C.CDLL:
         _lib.orc_radar_bbox.argtypes = [C.POINTER(GeoGrid), C.POINTER(RadarGrid), C.POINTER(OrbitS), C.POINTER(Lut),
                                         C.c_float, C.c_float, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
                                         C.c_void_p]
+        _lib.orc_radar_grid_cubes.argtypes = [C.POINTER(RadarGrid), C.POINTER(GeoGrid), C.c_void_p, C.c_int,
+                                              C.POINTER(OrbitS), C.POINTER(Lut), C.POINTER(Lut), C.c_double, C.c_int,
+                                              C.c_double] + [C.c_void_p] * 9 + [C.c_int]
         _lib.orc_dem_stats.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]
     return _lib
@@ -409,6 +412,32 @@ def radar_bbox(geo_grid, radar_grid, orbit, min_height=-500.0, max_height=9000.0
     if st:
         raise ValueError(lib().orc_last_error().decode())
     return tuple(int(v) for v in out)
+
+
+CUBE_NAMES = [("slant_range", np.float64), ("azimuth_time", np.float64), ("incidence_angle", np.float32),
+              ("los_unit_vector_x", np.float32), ("los_unit_vector_y", np.float32),
+              ("along_track_unit_vector_x", np.float32), ("along_track_unit_vector_y", np.float32),
+              ("elevation_angle", np.float32), ("ground_track_velocity", np.float64)]
+
+
+def radar_grid_cubes(radar_grid, geogrid, heights, orbit, native_doppler, grid_doppler, threshold=1e-8,
+                     maxiter=50, delta_range=10.0, outputs=None, nthreads=0):
+    """geometry/metadataCubes.cpp:276-489 on the CPU; returns {name: array of
+    (heights, length, width)} for the names in ``outputs`` (default: all)."""
+    keep = _Keep()
+    rg, g = radar_struct(radar_grid), geo_struct(geogrid)
+    o = orbit_struct(orbit, keep)
+    nd, gd = lut_struct(native_doppler, keep), lut_struct(grid_doppler, keep)
+    h = np.ascontiguousarray(np.asarray(heights, dtype=np.float64).ravel())
+    shape = (h.size, geogrid.length, geogrid.width)
+    want = [n for n, _ in CUBE_NAMES] if outputs is None else list(outputs)
+    arrs = {n: np.empty(shape, dt) for n, dt in CUBE_NAMES if n in want}
+    ptrs = [(_ptr(arrs[n]) if n in arrs else None) for n, _ in CUBE_NAMES]
+    st = lib().orc_radar_grid_cubes(C.byref(rg), C.byref(g), _ptr(h), h.size, C.byref(o), C.byref(nd), C.byref(gd),
+                                    threshold, int(maxiter), delta_range, *ptrs, int(nthreads))
+    if st:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return arrs
 
 
 def dem_stats(z: np.ndarray):
