@@ -54,6 +54,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the burst (batched vs plain) measurement")
     p.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
+    p.add_argument("--no-geometry", action="store_true", help="skip the block-planner and metadata-cube legs")
     p.add_argument("--precision-study", action="store_true",
                    help="instead of timing: fp64 and float-float geo2rdr against the oracle over the whole "
                         "workload (error histograms, Newton iteration counts); writes one JSON line")
@@ -384,7 +385,7 @@ def run_e2e(args, sc, dev, common, kw):
         step()
     torch.cuda.synchronize()
     t = []
-    for _ in range(args.steps):
+    for _ in range(max(args.steps, 10)):     # at least 10 drop-in calls: single outliers weigh less
         t0 = time.perf_counter()
         step()
         torch.cuda.synchronize()
@@ -396,6 +397,7 @@ def run_e2e(args, sc, dev, common, kw):
     sec = float(np.mean(t))
     return {"value": g.length * g.width / sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": sec * 1e3, "p50_ms": float(np.median(t)) * 1e3,
+            "ms_steps": [round(x * 1e3, 2) for x in t],
             "timing": "host wall clock around the drop-in call, synchronized"}
 
 
@@ -519,6 +521,80 @@ def run_serving(args):
         plain = serve_plain(store, [ServeRequest(k, g, t) for k, g, t in trace], prec)
         out[prec] = {"served": served, "plain": plain,
                      "px_per_s_ratio": served["px_per_s"] / plain["px_per_s"] if plain["px_per_s"] else None}
+    return out
+
+
+def run_geometry(args, sc):
+    """Block planning and metadata cubes around the frame: the GPU call (one
+    launch of bounding boxes, the cube passes) against the oracle on the host
+    cores, with their agreement."""
+    import torch
+    from oracle import oracle
+    from isce3_gb300 import geometry
+    from isce3_gb300.product import GeoGridParameters
+    from isce3_gb300.rdr_geo_block_generator import plan_blocks
+    oracle.build()
+    g = sc.geogrid
+    out = {}
+    # planner: the frame's geogrid in 500 x 500 blocks (256 blocks), DEM heights
+    blocks = [b for _, _, b in plan_blocks(g, 500, 500)]
+    dem = geometry.DEMInterpolator(sc.dem)
+    mn, mx, _ = dem.compute_min_max_mean_height()
+    for _ in range(2):
+        geometry.get_radar_bboxes(blocks, sc.radar_grid, sc.orbit, float(mn), float(mx))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        gpu = geometry.get_radar_bboxes(blocks, sc.radar_grid, sc.orbit, float(mn), float(mx))
+    gpu_s = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    ref = [oracle.radar_bbox(b, sc.radar_grid, sc.orbit, float(mn), float(mx)) for b in blocks]
+    cpu_s = time.perf_counter() - t0
+    same = sum(1 for a, r in zip(gpu, ref)
+               if (r[4] != 0 and isinstance(a, Exception)) or
+               (r[4] == 0 and not isinstance(a, Exception) and
+                (a.first_azimuth_line, a.last_azimuth_line, a.first_range_sample, a.last_range_sample) == r[:4]))
+    out["planner"] = {"blocks": len(blocks), "block_px": [500, 500], "gpu_ms_per_plan": gpu_s * 1e3,
+                      "cpu_ms_per_plan": cpu_s * 1e3, "cpu_threads": 1, "equal_to_oracle": same,
+                      "timing": "host wall clock around the synchronous call (H2D, launch, D2H)"}
+    # cubes: 20 heights x 200 x 200 at 500 m over the frame (the GSLC workflow's cube)
+    h = np.arange(-500.0, 9001.0, 500.0)
+    n = 200
+    cx, cy = g.start_x + g.spacing_x * g.width / 2, g.start_y + g.spacing_y * g.length / 2
+    cube = GeoGridParameters(cx - 250.0 * n, cy + 250.0 * n, 500.0, -500.0, n, n, g.epsg)
+    shape = (h.size, n, n)
+    names = [k for k, _ in oracle.CUBE_NAMES]
+    dts = dict(oracle.CUBE_NAMES)
+    arrs = {k: torch.empty(shape, dtype=torch.float64 if dts[k] == np.float64 else torch.float32, device="cuda")
+            for k in names}
+    kw = {f"{k}_raster": v for k, v in arrs.items()}
+    geometry.make_radar_grid_cubes(sc.radar_grid, cube, h, sc.orbit, sc.native_doppler, sc.image_grid_doppler,
+                                   numiter_geo2rdr=100, delta_range=1e-8, **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        geometry.make_radar_grid_cubes(sc.radar_grid, cube, h, sc.orbit, sc.native_doppler,
+                                       sc.image_grid_doppler, numiter_geo2rdr=100, delta_range=1e-8, **kw)
+    gpu_s = (time.perf_counter() - t0) / 3
+    from isce3_gb300 import _lib as L
+    passes = int(L.lib().gslc_last_cube_passes(L.context(torch.cuda.current_device())))
+    ncpu = oracle.ncores()
+    t0 = time.perf_counter()
+    ref = oracle.radar_grid_cubes(sc.radar_grid, cube, h, sc.orbit, sc.native_doppler, sc.image_grid_doppler,
+                                  maxiter=100, delta_range=1e-8, nthreads=ncpu)
+    cpu_s = time.perf_counter() - t0
+    par = {}
+    for k in names:
+        a, r = arrs[k].cpu().numpy(), ref[k]
+        v = np.isfinite(r)
+        par[k] = {"mask_mismatch": int((np.isfinite(a) != v).sum()),
+                  "max_abs_diff": float(np.max(np.abs(a[v].astype(np.float64) - r[v]))) if v.any() else 0.0}
+    npts = int(np.prod(shape))
+    out["cubes"] = {"points": npts, "shape": list(shape), "spacing_m": 500.0, "gpu_ms": gpu_s * 1e3,
+                    "points_per_s": npts / gpu_s, "passes": passes, "cpu_ms": cpu_s * 1e3,
+                    "cpu_points_per_s": npts / cpu_s, "cpu_threads": ncpu, "parity": par,
+                    "timing": "host wall clock around the synchronous call"}
     return out
 
 
@@ -670,6 +746,9 @@ def main():
     batched = None
     if not args.no_batched:
         batched = run_bursts(args)
+    geometry_leg = None
+    if not args.no_geometry:
+        geometry_leg = run_geometry(args, sc)
     served = None
     if not args.no_served:
         served = run_serving(args)
@@ -702,6 +781,7 @@ def main():
                        "note": "float-float (double-word FP32) Newton iterations, FP64 first iterate and range"},
         "batched": batched,
         "served": served,
+        "geometry": geometry_leg,
         "e2e": res["e2e"], "gpu_launches": res["launches"], "clocks": res["clocks"],
         "cpu_baseline": cpu, "parity_sample": par,
     }

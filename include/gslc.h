@@ -161,6 +161,10 @@ typedef struct {
     int32_t mantissa_bits, _pad3;
 } gslc_geocode_args;
 
+/* A context: the sinc table and error words on `device`.  Creating one also
+ * lets the device's default memory pool (which the calls' stream-ordered
+ * scratch comes from) keep up to 16 GiB cached between synchronisations
+ * (cudaMemPoolAttrReleaseThreshold, process-local; a higher value is kept). */
 int gslc_ctx_create(int device, gslc_ctx** out);
 int gslc_ctx_destroy(gslc_ctx* ctx);
 const char* gslc_last_error(const gslc_ctx* ctx);
@@ -408,11 +412,15 @@ typedef struct {
  * python/extensions/pybind_isce3/geometry/metadataCubes.cpp:16-35).  Points
  * that do not converge are NaN.  The reference starts each point's solves
  * from the previous point's results (a chain through each height layer in
- * row-major order); this call reproduces that chain by passes: each launch
+ * row-major order); this call follows that chain by passes: each launch
  * solves every point from the starts implied by the previous pass, until no
- * convergence status changes and no iterate moves by 1e-13 s (at most 16
- * passes; gslc_last_cube_passes reports them).  The call synchronises the
- * stream.  A failed projection inverse returns GSLC_EPROJ. */
+ * convergence status changes (at least 2, at most 16 passes;
+ * gslc_last_cube_passes reports them), so the validity masks are the
+ * reference's.  Where neighbouring points share an azimuth time the
+ * reference's solve can stop at its start, so its own times depend on the
+ * visiting order by up to the geo2rdr threshold; times here agree with it
+ * to that threshold.  The call synchronises the stream.  A failed
+ * projection inverse returns GSLC_EPROJ. */
 int gslc_make_radar_grid_cubes(gslc_ctx* ctx, const gslc_cube_args* args, void* stream);
 int gslc_last_cube_passes(const gslc_ctx* ctx);
 

@@ -609,6 +609,18 @@ extern "C" int gslc_ctx_create(int device, gslc_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int32_t) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(int32_t) * 4);
     if (e != cudaSuccess) { gslc_ctx_destroy(c); return GSLC_ECUDA; }
+    // The calls' scratch (deramped copies, batch buffers, planner and cube
+    // scratch) is stream-ordered memory of the device's default pool.  With
+    // the pool's default release threshold of 0 every synchronisation hands
+    // it back to the driver and the next call maps it again; keep up to
+    // 16 GiB cached instead (process-local; a higher threshold is kept).
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t cur = 0, keep = 16ull << 30;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur) == cudaSuccess && cur < keep)
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
     *out = c;
     return GSLC_OK;
 }
@@ -1182,7 +1194,7 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     const size_t sn_off = up(sg_off + pt_b), tg_off = up(sn_off + pt_b), tn_off = up(tg_off + pt_b);
     const size_t st_off = up(tn_off + pt_b), total = st_off + (size_t)npts;
     std::vector<double> start_g((size_t)npts, p.t_mid), start_n((size_t)npts, p.t_mid);
-    std::vector<double> tg((size_t)npts), tn((size_t)npts), prev_tg, prev_tn;
+    std::vector<double> tg((size_t)npts), tn((size_t)npts);
     std::vector<uint8_t> stat((size_t)npts), prev_stat;
     char* buf = nullptr;
     e = cudaMallocAsync((void**)&buf, total, stream);
@@ -1207,9 +1219,11 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     // native-Doppler solve from the native state of the last point whose grid
     // solve converged (reset to sensingMid after a native failure).  Each
     // pass solves every point from the starts the previous pass implies; the
-    // first k points of a chain are exact after k passes and, since a start
-    // moves the converged iterate by far less than it moves the start, the
-    // passes stop once no status changes and no iterate moves by 1e-13 s.
+    // first k points of a chain are exact after k passes.  Where neighbouring
+    // points share an azimuth time the reference's solve can stop at its
+    // start, so its returned times depend on the visiting order by up to the
+    // threshold; the passes stop once no convergence status changes (at least
+    // two, so that every point starts warm as in the reference).
     const int64_t plane = (int64_t)gg.length * gg.width;
     constexpr int MAX_PASSES = 16;
     int passes = 0;
@@ -1224,14 +1238,7 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) break;
         ++passes;
-        if (passes > 1 && stat == prev_stat) {
-            double moved = 0.0;
-            for (int64_t k = 0; k < npts; ++k) {
-                if (stat[k] & 1) moved = std::max(moved, std::fabs(tg[k] - prev_tg[k]));
-                if (stat[k] & 2) moved = std::max(moved, std::fabs(tn[k] - prev_tn[k]));
-            }
-            settled = moved < 1e-13;
-        }
+        settled = passes > 1 && stat == prev_stat;
         if (settled) break;
         for (int hc = 0; hc < a->n_heights; ++hc) {
             double sg = p.t_mid, sn = p.t_mid;
@@ -1244,8 +1251,6 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
             }
         }
         prev_stat = stat;
-        prev_tg = tg;
-        prev_tn = tn;
     }
     c->cube_passes = passes;
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);

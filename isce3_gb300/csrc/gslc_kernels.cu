@@ -1025,10 +1025,17 @@ __device__ __forceinline__ double carrier_at(const AzRg& f, const CarrierLine& c
 // the FP64 phase bit-for-bit in the reference's order, so that its float
 // rounding agrees.  Grid: x covers a line in chunks of 4 * blockDim.x
 // samples, y the lines.
+__device__ __forceinline__ bool carrier_line_constant(const AzRg& f) {
+    return f.is_zero || (f.kind == 1 && f.poly.x_order == 0);
+}
+
 __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ DerampParams p) {
+    __shared__ float2 s_rot;
+    // carriers constant along each line (zero, or azimuth-only polynomials):
+    // the line's phasor is formed once per block and line, the same value the
+    // per-sample form gives, so the pass streams at HBM rate
+    const bool line_const = carrier_line_constant(p.rg_car) && carrier_line_constant(p.az_car);
     for (int64_t i = blockIdx.y; i < p.inL; i += gridDim.y) {
-        const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
-        const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
         const float2* src = p.src + i * p.inW;
         const __half2* src16 = reinterpret_cast<const __half2*>(p.src) + i * p.inW;
         float2* dst = p.dst + i * p.inW;
@@ -1039,20 +1046,27 @@ __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ Der
             const int64_t j = j0 + (int64_t)u * blockDim.x;
             v[u] = j < p.inW ? (p.src_c32 ? ld_sample(src16 + j) : __ldg(src + j)) : make_float2(0.f, 0.f);
         }
-        if (lr.mode <= 1 && la.mode <= 1) {
-            // carriers constant along the line (azimuth polynomials): the
-            // same phase as per sample, formed once
-            const float phase = (float)dadd(lr.mode ? lr.val : 0.0, la.mode ? la.val : 0.0);
-            float sn, cs;
-            sincosf(phase, &sn, &cs);
-            const float2 rot = make_float2(cs, -sn);
+        if (line_const) {
+            if (threadIdx.x == 0) {
+                const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
+                const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
+                const float phase = (float)dadd(lr.mode ? lr.val : 0.0, la.mode ? la.val : 0.0);
+                float sn, cs;
+                sincosf(phase, &sn, &cs);
+                s_rot = make_float2(cs, -sn);
+            }
+            __syncthreads();
+            const float2 rot = s_rot;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int64_t j = j0 + (int64_t)u * blockDim.x;
                 if (j < p.inW) dst[j] = cmul(v[u], rot);
             }
+            __syncthreads();              // s_rot is rewritten for the next line
             continue;
         }
+        const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
+        const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int64_t j = j0 + (int64_t)u * blockDim.x;

@@ -287,6 +287,18 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     """Stage arrays on ``dev`` and fill a gslc_geocode_args.
 
     Returns (args, outputs to copy back, objects to keep alive)."""
+    # Small inputs first: the DEM window and LUT samples come from pageable
+    # host memory with synchronous copies, which would otherwise queue behind
+    # the radar blocks' asynchronous (pinned) upload on the same stream.
+    holder = M.AzRgHolder()
+    a = L.GeocodeArgs()
+    a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
+    a.native_doppler = M.lut_desc(native_doppler, dev)
+    a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
+    a.az_time_correction = M.lut_desc(az_time_correction, dev)
+    a.srange_correction = M.lut_desc(srange_correction, dev)
+    a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
+    a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
     rdr = [_Staged(_raw(r), dev, True, torch.complex64) for r in rdr_data_blocks]
     if any(r.host is not None for r in rdr) and inplace_deramp:
         raise ValueError("inplace_deramp needs device-resident radar tensors")
@@ -310,18 +322,10 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     azi = opt_out(az_index_block, np.float64, torch.float64, "az_index_block", False)
     rgi = opt_out(rg_index_block, np.float64, torch.float64, "rg_index_block", False)
 
-    holder = M.AzRgHolder()
-    a = L.GeocodeArgs()
     a.radar_grid = M.radar_grid_desc(radargrid)
     a.sliced_radar_grid = M.radar_grid_desc(sliced_radargrid)
     a.geo_grid = M.geo_grid_desc(geogrid)
     a.orbit = M.orbit_desc(orbit)
-    a.native_doppler = M.lut_desc(native_doppler, dev)
-    a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
-    a.az_time_correction = M.lut_desc(az_time_correction, dev)
-    a.srange_correction = M.lut_desc(srange_correction, dev)
-    a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
-    a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
     a.ellipsoid_a, a.ellipsoid_e2 = ellipsoid.a, ellipsoid.e2
     a.threshold_geo2rdr = float(threshold_geo2rdr)
     a.numiter_geo2rdr = int(num_iter_geo2rdr)
@@ -343,7 +347,6 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     a.flatten_phase = flat.ptr() if flat else None
     a.az_index = azi.ptr() if azi else None
     a.rg_index = rgi.ptr() if rgi else None
-    a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
     a.dem_margin = int(dem_margin)
     a.geo2rdr_precision = precision
     a.rdr_format, a.geo_format, a.mantissa_bits = int(rdr_format), int(geo_format), int(mantissa_bits)

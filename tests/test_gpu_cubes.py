@@ -2,11 +2,13 @@
 makeRadarGridCubes (geometry/metadataCubes.cpp:276-489), which chains each
 height layer's geo2rdr solves point to point as the reference does.
 
-Validity (NaN) masks must be identical in every cube; azimuth time within
-1e-9 s and slant range within 1e-6 m (the two sides' orbit interpolants
-differ by ~1e-11 s in the converged iterate); float32 angles and unit
-vectors within 2 float ulps of the value; ground-track velocity within
-1e-9 relative."""
+Validity (NaN) masks must be identical in every cube.  Azimuth time within
+2e-8 s, twice the geo2rdr threshold: where neighbouring points share an
+azimuth time the reference's warm-started solve can stop at its start, so
+its own times depend on the visiting order by up to the threshold.  Slant
+range within 1e-6 m (|dR/dt| is at most a few m/s at these Doppler
+centroids), float32 angles and unit vectors within 2 float ulps of the
+value, ground-track velocity within 1e-9 relative."""
 import numpy as np
 import pytest
 
@@ -42,7 +44,7 @@ def _compare(got, ref):
             continue
         d = np.abs(g[v].astype(np.float64) - r[v].astype(np.float64))
         if n == "azimuth_time":
-            assert d.max() <= 1e-9, (n, d.max())
+            assert d.max() <= 2e-8, (n, d.max())
         elif n == "slant_range":
             assert d.max() <= 1e-6, (n, d.max())
         elif n == "ground_track_velocity":
@@ -65,7 +67,7 @@ def test_cubes_utm_native_doppler(oracle_mod):
     _compare(got, ref)
     v = np.isfinite(ref["incidence_angle"])
     assert 0.02 < v.mean() < 0.98                 # both outcomes occur
-    assert 1 <= passes <= 16
+    assert 2 <= passes <= 16
 
 
 def test_cubes_grid_doppler_equals_native(oracle_mod):
