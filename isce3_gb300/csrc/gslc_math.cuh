@@ -443,17 +443,21 @@ GSLC_HD double seg_poly(const double* c, int deg, double w) {
 // Iterations 1.. of geo2rdr's zero-Doppler Newton solve
 // (geometry/detail/Geo2Rdr.icc:114-179 with fdop = fdopder = 0): the same
 // iterates t <- t - fn/fn', fn = (xyz - pos).vel, fn' = -|vel|^2, with fn
-// formed as D.vel - H(w) on the segment tables (Orbit::seg) instead of
-// subtracting the interpolated position, and 1/|vel|^2 as G(w).  Rounding
-// differs from the direct form by ~1e-13 s in azimuth time, below the
-// reference's own orbit interpolation noise (~1e-11 s).
+// formed on the segment tables (Orbit::seg) instead of subtracting the
+// interpolated position: fn(w) = D.v(w) - H(w) with D = xyz - P_ref is one
+// degree-13 polynomial whose coefficients k <= 6 are D.b_k - h_k (formed
+// when the iterate enters a segment) and whose others are -h_k; 1/|vel|^2 is
+// G(w).  Rounding differs from the direct form by ~1e-13 s in azimuth time,
+// below the reference's own orbit interpolation noise (~1e-11 s).
 // seg: the segment tables (Orbit::seg, or a copy of them in shared memory).
 GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz, double thr, int maxiter, double& t,
                                        double dt, double& R) {
     int cur = -1;
     double D[3] = {0.0, 0.0, 0.0};
+    double cf[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // fn(w) coefficients 0..6
     double w = 0.0;
     const double* c = seg;
+    const int nh = o.seg_nh;
     for (int i = 1; i < maxiter; ++i) {
         t -= dt;
         // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
@@ -473,20 +477,40 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
                 D[0] = xyz.x - ld_gen(c + 0);
                 D[1] = xyz.y - ld_gen(c + 1);
                 D[2] = xyz.z - ld_gen(c + 2);
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    const double dv = fma(D[0], ld_gen(c + SEG_B + k), fma(D[1], ld_gen(c + SEG_B + 7 + k),
+                                                                         D[2] * ld_gen(c + SEG_B + 14 + k)));
+                    cf[k] = k <= nh ? dv - ld_gen(c + SEG_H + k) : dv;
+                }
             }
         }
-        double v[3];
+        double fn;
+        if (o.seg_div) {
+            // G did not converge on some segment: the direct form, dividing by -|vel|^2
+            double v[3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double* b = c + SEG_B + d * 7;
-            double acc = ld_gen(b + 6);
+            for (int d = 0; d < 3; ++d) {
+                const double* b = c + SEG_B + d * 7;
+                double acc = ld_gen(b + 6);
 #pragma unroll
-            for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_gen(b + k));
-            v[d] = acc;
+                for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_gen(b + k));
+                v[d] = acc;
+            }
+            fn = fma(D[0], v[0], fma(D[1], v[1], D[2] * v[2])) - seg_poly(c + SEG_H, nh, w);
+            dt = fn / (-(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+        } else {
+            double acc = cf[6];
+            if (nh > 6) {
+                acc = -ld_gen(c + SEG_H + nh);
+                for (int k = nh - 1; k >= 7; --k) acc = fma(acc, w, -ld_gen(c + SEG_H + k));
+                acc = fma(acc, w, cf[6]);
+            }
+#pragma unroll
+            for (int k = 5; k >= 0; --k) acc = fma(acc, w, cf[k]);
+            fn = acc;
+            dt = -fn * seg_poly(c + SEG_G, o.seg_ng, w);
         }
-        const double fn = fma(D[0], v[0], fma(D[1], v[1], D[2] * v[2])) - seg_poly(c + SEG_H, o.seg_nh, w);
-        if (o.seg_div) dt = fn / (-(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
-        else dt = -fn * seg_poly(c + SEG_G, o.seg_ng, w);
         if (fabs(dt) < thr) {
             double r[3];
 #pragma unroll
