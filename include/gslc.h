@@ -146,7 +146,9 @@ typedef struct {
     double* rg_index;               /* device or NULL: radar sample coordinate per geo pixel */
     gslc_dem_raster dem;
     int32_t dem_margin;             /* DEM pixels of margin (reference default 50) */
-    int32_t geo2rdr_precision;      /* 0 FP64 (reference numerics), 1 float-float */
+    int32_t geo2rdr_precision;      /* 0 FP64 (reference numerics), 1 float-float where it applies (zero
+                                       image-grid Doppler, sensingMid in the orbit span), else FP64; a batch
+                                       runs float-float only if every request qualifies */
     const gslc_subswaths* subswaths;  /* host pointer to descriptor, or NULL */
     int32_t rdr_deramped;           /* 1: blocks already carry the deramp of these carriers (resident
                                        stores deramp once); the reramp still applies */

@@ -298,22 +298,25 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
 // pointers left null for bind_orbit.
 void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
     make_orbit_coeffs(o, coef);
-    // float-pair copy of the polynomial coefficients for the float-float geo2rdr,
-    // stored after the doubles (ORB_FF_STRIDE float2 per piece = 45 doubles' room)
-    const int np = o.n - 3;
-    const size_t nd = coef.size();
-    coef.resize(nd + (size_t)np * ORB_FF_STRIDE, 0.0);
-    float2* ffc = reinterpret_cast<float2*>(coef.data() + nd);
-    for (int idx = 0; idx < np; ++idx)
-        for (int k = 0; k < ORB_FF_STRIDE; ++k) {
-            const double v = coef[(size_t)idx * ORB_STRIDE + 3 + k];
-            const float hi = (float)v;
-            ffc[(size_t)idx * ORB_FF_STRIDE + k] = make_float2(hi, (float)(v - (double)hi));
-        }
-    // Newton segment tables after them (orbit_seg_offset, 16-byte aligned)
+    // Newton segment tables after the pieces (orbit_seg_offset, 16-byte aligned)
     int seg_nh = 0, seg_ng = 0, seg_div = 0;
     coef.resize(orbit_table_doubles(o.n), 0.0);
-    make_orbit_segments(o, coef.data(), coef.data() + orbit_seg_offset(o.n), seg_nh, seg_ng, seg_div);
+    double* seg = coef.data() + orbit_seg_offset(o.n);
+    make_orbit_segments(o, coef.data(), seg, seg_nh, seg_ng, seg_div);
+    // their float pairs for the float-float Newton: b, h, g, a of each segment
+    float2* ffs = reinterpret_cast<float2*>(coef.data() + orbit_segff_offset(o.n));
+    auto split = [](double v) {
+        const float hi = (float)v;
+        return make_float2(hi, (float)(v - (double)hi));
+    };
+    for (int j = 0; j < o.n - 1; ++j) {
+        const double* sj = seg + (size_t)j * SEG_STRIDE;
+        float2* fj = ffs + (size_t)j * SEGFF_STRIDE;
+        for (int k = 0; k < 21; ++k) fj[SEGFF_B + k] = split(sj[SEG_B + k]);
+        for (int k = 0; k < SEG_NH; ++k) fj[SEGFF_H + k] = split(sj[SEG_H + k]);
+        for (int k = 0; k < SEG_NG; ++k) fj[SEGFF_G + k] = split(sj[SEG_G + k]);
+        for (int k = 0; k < 24; ++k) fj[SEGFF_A + k] = split(sj[SEG_A + k]);
+    }
     ob = Orbit{};
     ob.t0 = o.t0;
     ob.spacing = o.spacing;
@@ -556,7 +559,7 @@ extern "C" int gslc_geo2rdr_zero_doppler(const gslc_orbit* o, const double* xyz,
     Orbit ob;
     build_orbit_table(*o, coef, ob);
     ob.coef = coef.data();
-    ob.coef_ff = reinterpret_cast<const float2*>(coef.data() + (size_t)ob.n_pieces * ORB_STRIDE);
+    ob.seg_ff = reinterpret_cast<const float2*>(coef.data() + orbit_segff_offset(ob.n));
     ob.seg = coef.data() + orbit_seg_offset(o->n);
     *converged = 0;
     *aztime = *slant_range = std::nan("");
@@ -791,7 +794,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
 // (doubles, then the float pairs, as make_orbit_coeffs + prepare lay them out).
 void bind_orbit(GeoParams& p, const double* d_coef) {
     p.orbit.coef = d_coef;
-    p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+    p.orbit.seg_ff = reinterpret_cast<const float2*>(d_coef + orbit_segff_offset(p.orbit.n));
     p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
 }
 
@@ -1122,7 +1125,7 @@ extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc
     if (e == cudaSuccess) {
         const double* d_coef = reinterpret_cast<const double*>(buf);
         p.orbit.coef = d_coef;
-        p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+        p.orbit.seg_ff = reinterpret_cast<const float2*>(d_coef + orbit_segff_offset(p.orbit.n));
         p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
         p.blocks = reinterpret_cast<const double*>(buf + blk_off);
         p.out = reinterpret_cast<int32_t*>(buf + out_off);
@@ -1204,7 +1207,7 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
     const double* d_coef = reinterpret_cast<const double*>(buf);
     p.orbit.coef = d_coef;
-    p.orbit.coef_ff = reinterpret_cast<const float2*>(d_coef + (size_t)p.orbit.n_pieces * ORB_STRIDE);
+    p.orbit.seg_ff = reinterpret_cast<const float2*>(d_coef + orbit_segff_offset(p.orbit.n));
     p.orbit.seg = d_coef + orbit_seg_offset(p.orbit.n);
     p.heights = reinterpret_cast<const double*>(buf + h_off);
     p.start_grid = reinterpret_cast<const double*>(buf + sg_off);
@@ -1557,7 +1560,9 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
         return set_err(c, GSLC_EUNSUPPORTED, "a batch mixes EPSG:4326 and UTM geogrids");
     }
     b->lonlat = any_ll;
+    // float-float only where every request qualifies (one kernel variant per batch)
     b->ff = precision == 1;
+    for (const GeoParams& q : params) b->ff = b->ff && ff_eligible(q);
     b->n_requests = n;
     b->h_flags = done_flags;
     {

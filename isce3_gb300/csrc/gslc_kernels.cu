@@ -226,34 +226,17 @@ __device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t
 }
 
 // The same Newton path in float-float.  Iteration 0 uses the shared FP64
-// state at sensingMid; later iterations evaluate the orbit polynomial, the
-// range vector relative to the interval's reference position, the Doppler
-// residual and the step in double-word FP32 (~2^-44 relative), keeping the
-// azimuth time as a double-word offset s from the interval's first node.
-// The FP64 pipe then carries only the first iterate, interval changes and
-// the final slant range.  Used when the image-grid Doppler is zero (the
-// NISAR GSLC convention); otherwise the FP64 path runs.
-__device__ __forceinline__ void orbit_eval_ff(const Orbit& o, int idx, ff u, ff pr[3], ff v[3]) {
-    const float2* c = o.coef_ff + (int64_t)idx * ORB_FF_STRIDE;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        float2 q = __ldg(c + d * 8 + 7);
-        ff acc = {q.x, q.y};
-#pragma unroll
-        for (int k = 6; k >= 0; --k) {
-            q = __ldg(c + d * 8 + k);
-            acc = ff_fma(acc, u, {q.x, q.y});
-        }
-        pr[d] = acc;
-        q = __ldg(c + 24 + d * 7 + 6);
-        ff vacc = {q.x, q.y};
-#pragma unroll
-        for (int k = 5; k >= 0; --k) {
-            q = __ldg(c + 24 + d * 7 + k);
-            vacc = ff_fma(vacc, u, {q.x, q.y});
-        }
-        v[d] = vacc;
-    }
+// state at sensingMid; later iterations run on the float-pair segment tables
+// (Orbit::seg_ff) in double-word FP32 (~2^-44 relative): the residual is the
+// pixel's degree-13 polynomial fn(w) (coefficients D.b_k - h_k for k <= 6,
+// D = xyz - P_ref formed in FP64 on segment entry, -h_k above), the step is
+// -fn.G(w), and the segment coordinate w is tracked as a double word.  The
+// FP64 pipe carries only the first iterate, segment entries and the final
+// time and slant range.  Used when the image-grid Doppler is zero (the NISAR
+// GSLC convention); otherwise the FP64 path runs.
+__device__ __forceinline__ ff ld_ff(const float2* q) {
+    const float2 v = __ldg(q);
+    return {v.x, v.y};
 }
 
 __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
@@ -272,43 +255,64 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
     }
     const float thr = (float)p.thr;
     const ff inv_sp = ff_from_double(o.inv_spacing);
-    int piece = -1;
-    double tidx = 0.0;
-    ff s = {0.f, 0.f}, D[3];
-    float s_lo = 0.f, s_hi = 0.f;              // s range of the current piece
+    const int nh = o.seg_nh, ng = o.seg_ng;
+    int j = -1;
+    double tj = 0.0;                    // start time of segment j: t = tj + (w + 0.5) spacing
+    ff w = {0.f, 0.f}, D[3], cf[7];
+    const float2* c = o.seg_ff;
     for (int i = 1; i < p.maxiter; ++i) {
-        const float sf = s.hi + s.lo;
-        if (piece < 0 || !(sf >= s_lo && sf < s_hi)) {
-            // (re)enter an orbit interval: FP64 time, range check, reference position
-            if (piece >= 0) t = tidx + ((double)s.hi + (double)s.lo);
-            if (!(t >= o.t0 && t <= o.t_end)) return false;   // FillNaN -> no convergence
-            piece = orbit_piece(o, t);
-            tidx = o.t0 + piece * o.spacing;
-            const double* pref = o.coef + (int64_t)piece * ORB_STRIDE;
-            D[0] = ff_from_double(xyz.x - __ldg(pref + 0));
-            D[1] = ff_from_double(xyz.y - __ldg(pref + 1));
-            D[2] = ff_from_double(xyz.z - __ldg(pref + 2));
-            s = ff_from_double(t - tidx);
-            // the piece serves u in [-1.5, 1.5] (first/last) or [-0.5, 0.5)
-            const float sp = (float)o.spacing;
-            s_lo = piece == 0 ? 0.f : sp;
-            s_hi = piece == o.n - 4 ? 3.f * sp : 2.f * sp;
-            if (piece == o.n - 4) s_hi = (float)(o.t_end - tidx);
+        const float wf = w.hi + w.lo;
+        // entering or leaving a segment, and on the first and last segment
+        // (the orbit's time span): time, span check and w from FP64
+        if (j <= 0 || j >= o.n - 2 || !(wf >= -0.5f && wf < 0.5f)) {
+            if (j >= 0) t = tj + ((double)w.hi + (double)w.lo + 0.5) * o.spacing;
+            if (!(t >= o.t0 && t <= o.t_end)) return false;    // FillNaN -> no convergence
+            const int pc = orbit_piece(o, t);
+            const double tidx = o.t0 + pc * o.spacing;
+            double w64 = (t - tidx) * o.inv_spacing - 1.5;
+            const int jn = orbit_segment(o, pc, w64);
+            w = ff_from_double(w64);
+            if (jn != j) {
+                j = jn;
+                tj = o.t0 + j * o.spacing;
+                c = o.seg_ff + (int64_t)j * SEGFF_STRIDE;
+                const double* pref = o.seg + (int64_t)j * SEG_STRIDE;
+                D[0] = ff_from_double(xyz.x - __ldg(pref + 0));
+                D[1] = ff_from_double(xyz.y - __ldg(pref + 1));
+                D[2] = ff_from_double(xyz.z - __ldg(pref + 2));
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    const ff dv = ff_add(ff_add(ff_mul(D[0], ld_ff(c + SEGFF_B + k)), ff_mul(D[1], ld_ff(c + SEGFF_B + 7 + k))),
+                                         ff_mul(D[2], ld_ff(c + SEGFF_B + 14 + k)));
+                    cf[k] = k <= nh ? ff_add(dv, ff_neg(ld_ff(c + SEGFF_H + k))) : dv;
+                }
+            }
         }
-        const ff u = ff_add(ff_mul(s, inv_sp), {-1.5f, 0.f});
-        ff pr[3], v[3];
-        orbit_eval_ff(o, piece, u, pr, v);
-        const ff r0 = ff_add(D[0], ff_neg(pr[0])), r1 = ff_add(D[1], ff_neg(pr[1])), r2 = ff_add(D[2], ff_neg(pr[2]));
-        const ff fn = ff_add(ff_add(ff_mul(r0, v[0]), ff_mul(r1, v[1])), ff_mul(r2, v[2]));
-        const ff vv = ff_add(ff_add(ff_mul(v[0], v[0]), ff_mul(v[1], v[1])), ff_mul(v[2], v[2]));
-        const ff dt = ff_div(fn, ff_neg(vv));
+        ff fn = cf[6];
+        if (nh > 6) {
+            fn = ff_neg(ld_ff(c + SEGFF_H + nh));
+            for (int k = nh - 1; k >= 7; --k) fn = ff_fma(fn, w, ff_neg(ld_ff(c + SEGFF_H + k)));
+            fn = ff_fma(fn, w, cf[6]);
+        }
+#pragma unroll
+        for (int k = 5; k >= 0; --k) fn = ff_fma(fn, w, cf[k]);
+        ff g = ld_ff(c + SEGFF_G + ng);
+        for (int k = ng - 1; k >= 0; --k) g = ff_fma(g, w, ld_ff(c + SEGFF_G + k));
+        const ff dt = ff_neg(ff_mul(fn, g));
         if (fabsf(dt.hi) < thr) {
-            t = tidx + ((double)s.hi + (double)s.lo);
-            const double x0 = ff_to_double(r0), x1 = ff_to_double(r1), x2 = ff_to_double(r2);
-            R = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+            t = tj + ((double)w.hi + (double)w.lo + 0.5) * o.spacing;
+            double r[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                ff acc = ld_ff(c + SEGFF_A + d * 8 + 7);
+#pragma unroll
+                for (int k = 6; k >= 0; --k) acc = ff_fma(acc, w, ld_ff(c + SEGFF_A + d * 8 + k));
+                r[d] = ff_to_double(ff_add(D[d], ff_neg(acc)));
+            }
+            R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
             return true;
         }
-        s = ff_add(s, ff_neg(dt));
+        w = ff_add(w, ff_neg(ff_mul(dt, inv_sp)));
     }
     return false;
 }
@@ -1202,7 +1206,7 @@ void launch_geocode_ppt(const GeoParams& p, bool ff, cudaStream_t s) {
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches) {
     // the float-float path covers zero image-grid Doppler with the first
     // iterate at sensingMid; anything else runs in FP64
-    const bool ff = precision == 1 && p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0;
+    const bool ff = precision == 1 && ff_eligible(p);
     launch_geocode_ppt<4>(p, ff, s);     // the plain form uses 32 x 32-pixel tiles
     if (launches) ++*launches;
     return cudaGetLastError();

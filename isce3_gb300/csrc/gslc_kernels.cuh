@@ -159,6 +159,12 @@ size_t dem_stats_scratch_bytes();
 cudaError_t launch_dem_stats(const float* z, int64_t length, int64_t width, int64_t stride, void* scratch,
                              DemStats* host_out, cudaStream_t s, int64_t* launches);
 
+// The float-float Newton covers zero image-grid Doppler with the first
+// iterate at sensingMid and converged G series; anything else runs in FP64.
+inline bool ff_eligible(const GeoParams& p) {
+    return p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0 && !p.orbit.seg_div;
+}
+
 // launchers (gslc_kernels.cu)
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);

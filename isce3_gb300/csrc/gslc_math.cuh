@@ -365,7 +365,6 @@ GSLC_HD bool utm_forward(const Utm& u, double lon, double lat, double& x, double
 // u = (t - t_idx)/spacing - 1.5; velocity is its derivative.  The host
 // expands it once per interval (gslc_capi.cu) around P_ref = P_{idx+1}.
 constexpr int ORB_STRIDE = 48;   // pref[3], a[3][8], b[3][7] (b = d/dt coefficients)
-constexpr int ORB_FF_STRIDE = 45;  // a[3][8], b[3][7] split into float pairs
 
 // Newton tables per state-vector interval ("segment" j = 0..n-2, the time
 // span [t_j, t_j+1]).  Segment j uses the Hermite piece
@@ -379,21 +378,25 @@ constexpr int ORB_FF_STRIDE = 45;  // a[3][8], b[3][7] split into float pairs
 constexpr int SEG_NH = 14, SEG_NG = 13;
 constexpr int SEG_STRIDE = 76;   // pref[3], a[3][8], b[3][7], h[14], g[13], pad
 constexpr int SEG_A = 3, SEG_B = 27, SEG_H = 48, SEG_G = 62;
+// The same segment tables as float pairs (hi, lo) for the float-float Newton.
+constexpr int SEGFF_STRIDE = 72;   // float2: b[3][7], h[14], g[13], a[3][8]
+constexpr int SEGFF_B = 0, SEGFF_H = 21, SEGFF_G = 35, SEGFF_A = 48;
 
 struct Orbit {
     double t0, spacing, inv_spacing, t_end;
     int32_t n, n_pieces;
     const double* coef;          // n_pieces * ORB_STRIDE
-    const float2* coef_ff;       // n_pieces * ORB_FF_STRIDE: a[3][8], b[3][7] as (hi, lo)
     const double* seg;           // (n - 1) * SEG_STRIDE
+    const float2* seg_ff;        // (n - 1) * SEGFF_STRIDE
     int32_t seg_nh, seg_ng;      // highest H and G degree used over all segments
     int32_t seg_div, _pad;       // 1: G did not converge, divide by -|vel|^2 instead
 };
 
-// Orbit table layout in doubles: the pieces, their float pairs, then the
-// segments (16-byte aligned).
-constexpr size_t orbit_seg_offset(int n) { return ((size_t)(n - 3) * (ORB_STRIDE + ORB_FF_STRIDE) + 1) & ~(size_t)1; }
-constexpr size_t orbit_table_doubles(int n) { return orbit_seg_offset(n) + (size_t)(n - 1) * SEG_STRIDE; }
+// Orbit table layout in doubles: the pieces, then the segments (16-byte
+// aligned), then the segments' float pairs (SEG_STRIDE is even, so aligned).
+constexpr size_t orbit_seg_offset(int n) { return ((size_t)(n - 3) * ORB_STRIDE + 1) & ~(size_t)1; }
+constexpr size_t orbit_segff_offset(int n) { return orbit_seg_offset(n) + (size_t)(n - 1) * SEG_STRIDE; }
+constexpr size_t orbit_table_doubles(int n) { return orbit_segff_offset(n) + (size_t)(n - 1) * SEGFF_STRIDE; }
 
 GSLC_HD int orbit_piece(const Orbit& o, double t) {
     // core/Linspace.icc:77-89 search(t) - 2, clamped (InterpolateOrbit.icc:18-19)
