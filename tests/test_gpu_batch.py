@@ -101,3 +101,29 @@ def test_batch_rejects_host_arrays(bursts):
                          bursts.image_grid_doppler, bursts.ellipsoid, 1e-8, 25)
     with pytest.raises(ValueError):
         GeocodeBatch([req])
+
+
+def test_ff_batch_with_a_doppler_request_runs_fp64(bursts):
+    """The float-float Newton covers zero image-grid Doppler only.  A
+    float-float batch holding one request with a non-zero image-grid Doppler
+    runs every request in FP64, so each output equals its plain FP64 call."""
+    from isce3_gb300.core import LUT2d
+    b0 = bursts.bursts[0]
+    rr = np.linspace(b0.radar_grid.starting_range - 5e4, b0.radar_grid.starting_range + 2e5, 8)
+    tt = np.linspace(bursts.orbit.t0, bursts.orbit.t0 + bursts.orbit.spacing * (bursts.orbit.size - 1), 8)
+    dop = LUT2d(rr, tt, np.full((8, 8), 12.0), "bilinear", False)
+    img = [dop] + [bursts.image_grid_doppler] * (len(bursts.bursts) - 1)
+    ref = _outputs(bursts)
+    for b, (g, m), d in zip(bursts.bursts, ref, img):
+        geocode_slc(g, b.slc, bursts.dem, b.radar_grid, b.window, bursts.orbit, bursts.native_doppler, d,
+                    bursts.ellipsoid, bursts.threshold, bursts.maxiter, mask_block=m, az_carrier=b.az_carrier,
+                    rg_carrier=b.rg_carrier, geo2rdr_precision="fp64")
+    outs = _outputs(bursts)
+    reqs = [GeocodeRequest(o[0], b.slc, bursts.dem, b.radar_grid, b.window, bursts.orbit, bursts.native_doppler, d,
+                           bursts.ellipsoid, bursts.threshold, bursts.maxiter,
+                           dict(mask_block=o[1], az_carrier=b.az_carrier, rg_carrier=b.rg_carrier))
+            for b, o, d in zip(bursts.bursts, outs, img)]
+    batch = GeocodeBatch(reqs, "ff", BatchTuning(tiles_per_pop=2))
+    batch.run()
+    _same(ref, outs)
+    batch.close()
