@@ -263,6 +263,25 @@ typedef struct {
  * geogrid block of lines_per_block lines has its own DEM window, as there. */
 int gslc_geocode_rasters(gslc_ctx* ctx, const gslc_raster_geocode_args* args, void* stream);
 
+/* One raster interpolated at per-pixel radar coordinates: the interpolate
+ * kernel of the CUDA raster geocoder (cxx/isce3/cuda/geocode/Geocode.cu:203-287
+ * with the device interpolators of cxx/isce3/cuda/core/: sinc, bilinear,
+ * bicubic, nearest, biquintic) for every data type it accepts.  az_index and
+ * rg_index (device, n_px doubles) are the radar line and sample of each
+ * geogrid pixel as gslc_geocode_rasters writes them (NaN where masked);
+ * raster is the device raster (length x width samples), out n_px samples of
+ * the same type.  gdal_type: GDALDataType code (1 Byte, 2 UInt16, 4 UInt32,
+ * 6 Float32, 7 Float64, 10 CFloat32, 11 CFloat64); method: isce3
+ * dataInterpMethod (0 sinc, 1 bilinear, 2 bicubic, 3 nearest, 4 biquintic;
+ * integer types nearest only, GSLC_EINVAL otherwise).  Masked pixels and
+ * pixels within 4 samples of the raster's edge take invalid_value (both
+ * parts for complex types).  Enqueued on stream, not synchronised.  A
+ * gslc_geocode_rasters call with n_rasters = 0 and az_index / rg_index set
+ * computes the coordinates alone. */
+int gslc_interpolate_raster(gslc_ctx* ctx, const double* az_index, const double* rg_index, int64_t n_px,
+                            const void* raster, int64_t length, int64_t width, void* out, int32_t gdal_type,
+                            int32_t method, double invalid_value, void* stream);
+
 /* Number of the library's own kernels launched by the last call on ctx. */
 int64_t gslc_last_launch_count(const gslc_ctx* ctx);
 

@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBPATH = BUILD / "libgslc.so"
 HEADER = ROOT / "include" / "gslc.h"
-SOURCES = ["gslc_kernels.cu", "gslc_persistent.cu", "gslc_capi.cu", "gslc_plan.cu"]
+SOURCES = ["gslc_kernels.cu", "gslc_persistent.cu", "gslc_capi.cu", "gslc_plan.cu", "gslc_raster.cu"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(ROOT / "include")]
@@ -222,6 +222,8 @@ _EXPORTS = {
     "gslc_radar_bbox_blocks": (C.c_int, [C.c_void_p, C.POINTER(BBoxArgs), C.c_void_p, C.c_void_p]),
     "gslc_make_radar_grid_cubes": (C.c_int, [C.c_void_p, C.POINTER(CubeArgs), C.c_void_p]),
     "gslc_last_cube_passes": (C.c_int, [C.c_void_p]),
+    "gslc_interpolate_raster": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                          C.c_int64, C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_void_p]),
     "gslc_dem_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_float),
                                  C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "gslc_deramp_block": (C.c_int, [C.c_void_p, C.POINTER(RadarGrid), C.POINTER(AzRgFunc), C.POINTER(AzRgFunc),

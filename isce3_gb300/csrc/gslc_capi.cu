@@ -27,6 +27,7 @@ struct gslc_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float ms_geocode = 0.f, ms_deramp = 0.f;
     int cube_passes = 0;            // passes of the last gslc_make_radar_grid_cubes
+    double* d_sinc64 = nullptr;     // the sinc table in double (raster interpolation), on first use
     std::string err;
 };
 
@@ -44,7 +45,7 @@ int cuda_err(gslc_ctx* c, cudaError_t e, const char* where) {
 // core/Sinc2dInterpolator.cpp:12-40 and :98-115 — Hann-weighted sinc,
 // SINC_LEN taps x SINC_SUB phases, each phase normalised to unit sum, then
 // cast to float at use (Sinc2dInterpolator.cpp:88-90).
-std::vector<float> make_sinc_table() {
+std::vector<double> make_sinc_table_double() {
     const int filtercoef = SINC_SUB * SINC_LEN;
     std::vector<double> filter(filtercoef, 0.0);
     const double beta = 1.0, pedestal = 0.0;
@@ -56,15 +57,22 @@ std::vector<float> make_sinc_table() {
         const double fct = ((s != 0.) ? (std::sin(M_PI * s) / (M_PI * s)) : 1.);
         filter[i] = fct * wgt;
     }
-    std::vector<float> table((size_t)filtercoef);
+    std::vector<double> table((size_t)filtercoef);
     for (int i = 0; i < SINC_SUB; ++i) {
         double ssum = 0.0;
         for (int j = 0; j < SINC_LEN; ++j) ssum += filter[i + SINC_SUB * j];
         for (int j = 0; j < SINC_LEN; ++j) {
             filter[i + SINC_SUB * j] /= ssum;
-            table[(size_t)i * SINC_LEN + j] = (float)filter[i + SINC_SUB * j];
+            table[(size_t)i * SINC_LEN + j] = filter[i + SINC_SUB * j];
         }
     }
+    return table;
+}
+
+std::vector<float> make_sinc_table() {
+    const std::vector<double> d = make_sinc_table_double();
+    std::vector<float> table(d.size());
+    for (size_t i = 0; i < d.size(); ++i) table[i] = (float)d[i];
     return table;
 }
 
@@ -635,6 +643,7 @@ extern "C" int gslc_ctx_destroy(gslc_ctx* c) {
     if (c->d_err) cudaFree(c->d_err);
     if (c->h_err) cudaFreeHost(c->h_err);
     if (c->d_orbit) cudaFree(c->d_orbit);
+    if (c->d_sinc64) cudaFree(c->d_sinc64);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -897,7 +906,8 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
     c->err.clear();
     c->launches = 0;
     if (!r) return set_err(c, GSLC_EINVAL, "null arguments");
-    if (r->n_rasters < 1 || !r->input_rasters || !r->output_rasters || !r->invalid_values)
+    if (r->n_rasters < 0 || (r->n_rasters > 0 && (!r->input_rasters || !r->output_rasters || !r->invalid_values)) ||
+        (r->n_rasters == 0 && !r->az_index && !r->rg_index))
         return set_err(c, GSLC_EINVAL, "number of input and output rasters not equal");
     if (r->lines_per_block < 1) return set_err(c, GSLC_EINVAL, "lines_per_block must be positive");
     if (r->maxiter < 0) return set_err(c, GSLC_EINVAL, "maxiter must be non-negative");
@@ -927,6 +937,14 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
     a.rdr_width = r->radar_grid.width;
     a.rdr_blocks = r->input_rasters;
     a.geo_blocks = r->output_rasters;
+    // coordinates only: one placeholder block for the argument checks; the
+    // launches below run with no rasters
+    void* const none[1] = {nullptr};
+    if (r->n_rasters == 0) {
+        a.n_blocks = 1;
+        a.rdr_blocks = none;
+        a.geo_blocks = none;
+    }
     a.dem = r->dem;
     a.dem_margin = r->dem_margin;
     a.geo2rdr_precision = r->geo2rdr_precision;
@@ -976,7 +994,8 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
         const int64_t off = (int64_t)line_start * gg.width;
         p.az_out = r->az_index ? r->az_index + off : nullptr;
         p.rg_out = r->rg_index ? r->rg_index + off : nullptr;
-        for (int b0 = 0; b0 < r->n_rasters; b0 += MAX_BLOCKS) {
+        // no rasters: one launch for the radar coordinates alone
+        for (int b0 = 0; b0 < std::max(r->n_rasters, 1); b0 += MAX_BLOCKS) {
             p.nblk = std::min(MAX_BLOCKS, r->n_rasters - b0);
             for (int b = 0; b < p.nblk; ++b) {
                 p.rdr[b] = (const float2*)r->input_rasters[b0 + b];
@@ -1265,6 +1284,56 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
 }
 
 extern "C" int gslc_last_cube_passes(const gslc_ctx* c) { return c ? c->cube_passes : -1; }
+
+// ---- raster interpolation (cuda/geocode/Geocode.cu:203-287) ----------------
+extern "C" int gslc_interpolate_raster(gslc_ctx* c, const double* az_index, const double* rg_index, int64_t n_px,
+                                       const void* raster, int64_t length, int64_t width, void* out,
+                                       int32_t gdal_type, int32_t method, double invalid_value, void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    if (n_px < 0 || length < 0 || width < 0 || (n_px > 0 && (!az_index || !rg_index || !out || !raster)))
+        return set_err(c, GSLC_EINVAL, "invalid raster interpolation arguments");
+    int dtype;
+    switch (gdal_type) {        // GDALDataType codes
+    case 6: dtype = RASTER_F32; break;
+    case 10: dtype = RASTER_C64; break;
+    case 7: dtype = RASTER_F64; break;
+    case 11: dtype = RASTER_C128; break;
+    case 1: dtype = RASTER_U8; break;
+    case 2: dtype = RASTER_U16; break;
+    case 4: dtype = RASTER_U32; break;
+    default: return set_err(c, GSLC_EUNSUPPORTED, "raster data type not supported by the CUDA geocoder");
+    }
+    if (method < 0 || method > 4) return set_err(c, GSLC_EINVAL, "unknown interpolation method");
+    if (dtype >= RASTER_U8 && method != 3)
+        return set_err(c, GSLC_EINVAL, "int type of raster can only use nearest neighbor interp");
+    if (n_px == 0) return GSLC_OK;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    RasterInterpParams p{};
+    p.az = az_index; p.rg = rg_index; p.n = n_px;
+    p.rdr = raster; p.L = length; p.W = width;
+    p.out = out; p.dtype = dtype; p.method = method; p.invalid = invalid_value;
+    p.sinc = c->d_sinc;
+    if (method == 0 && (dtype == RASTER_F64 || dtype == RASTER_C128)) {
+        if (!c->d_sinc64) {
+            const std::vector<double> t = make_sinc_table_double();
+            e = cudaMalloc(&c->d_sinc64, t.size() * sizeof(double));
+            if (e == cudaSuccess) e = cudaMemcpy(c->d_sinc64, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                if (c->d_sinc64) cudaFree(c->d_sinc64);
+                c->d_sinc64 = nullptr;
+                return cuda_err(c, e, "sinc table");
+            }
+        }
+        p.sinc = c->d_sinc64;
+    }
+    e = launch_raster_interp(p, stream, &c->launches);
+    if (e != cudaSuccess) return cuda_err(c, e, "raster interpolation");
+    return GSLC_OK;
+}
 
 extern "C" int gslc_dem_stats(gslc_ctx* c, const float* data, int64_t length, int64_t width, int64_t row_stride,
                               float* mn, float* mx, double* mean, int64_t* n_valid, void* stream_) {

@@ -148,6 +148,24 @@ struct CubeParams {
 };
 cudaError_t launch_radar_grid_cubes(const CubeParams& p, cudaStream_t s, int64_t* launches);
 
+// Raster interpolation from per-pixel radar coordinates (gslc_raster.cu,
+// cuda/geocode/Geocode.cu:203-287).  dtype: one of RASTER_*; method: the
+// isce3 dataInterpMethod code (0 sinc, 1 bilinear, 2 bicubic, 3 nearest,
+// 4 biquintic).
+enum { RASTER_F32 = 0, RASTER_C64 = 1, RASTER_F64 = 2, RASTER_C128 = 3, RASTER_U8 = 4, RASTER_U16 = 5, RASTER_U32 = 6 };
+struct RasterInterpParams {
+    const double* az;            // radar line coordinate per geogrid pixel (NaN: masked)
+    const double* rg;            // radar sample coordinate per geogrid pixel
+    int64_t n;                   // geogrid pixels
+    const void* rdr;             // raster, L x W samples
+    int64_t L, W;
+    void* out;                   // n samples
+    int32_t dtype, method;
+    double invalid;
+    const void* sinc;            // SINC_SUB x SINC_LEN table in the component type
+};
+cudaError_t launch_raster_interp(const RasterInterpParams& p, cudaStream_t s, int64_t* launches);
+
 // DEM statistics (geometry/DEMInterpolator.cpp:515-560): min, max, sum of
 // the non-NaN samples and the NaN count.
 struct DemStats { float mn, mx; double sum; long long nan; };

@@ -8,12 +8,15 @@ geo2rdr (masking pixels whose corrections or native Doppler do not contain
 them, that fall outside the radar grid or outside the subswaths), reads the
 radar block around them and interpolates each raster.
 
-Here the whole block runs as one fused GB300 kernel per block (all rasters
-of the call at once); the per-pixel rules are the reference's, and the
-radar bounding box it reads is not needed because the rasters are resident.
-Only SINC interpolation of GDT_CFloat32 rasters (the SLC case) is provided:
-other data types and interpolation methods raise NotImplementedError after
-the reference's own argument checks.
+Here SINC rasters of GDT_CFloat32 (the SLC case) run in one fused GB300
+kernel per block, all such rasters of the call at once; the per-pixel rules
+are the reference's, and the radar bounding box it reads is not needed
+because the rasters are resident.  Every other data type the reference
+accepts (Float32, Float64, CFloat64, Byte, UInt16, UInt32) and method (SINC,
+BILINEAR, BICUBIC, NEAREST, BIQUINTIC; integer types nearest only) takes the
+reference's own two steps: the same kernel writes the radar coordinates of
+each geogrid pixel, then one interpolation kernel per raster samples it
+(gslc_interpolate_raster).
 """
 from __future__ import annotations
 
@@ -33,6 +36,10 @@ from ..product import GeoGridParameters, SubSwaths
 _INT_TYPES = (gdal.GDT_Byte, gdal.GDT_UInt16, gdal.GDT_UInt32)
 _TYPE_MAX = {gdal.GDT_Byte: 255, gdal.GDT_UInt16: 65535, gdal.GDT_UInt32: 4294967295}
 _FLT_MAX = float(np.finfo(np.float32).max)
+# the data types the reference's CUDA geocoder accepts (Geocode.cu:722-775)
+_TORCH_TYPES = {gdal.GDT_Float32: torch.float32, gdal.GDT_CFloat32: torch.complex64, gdal.GDT_Float64: torch.float64,
+                gdal.GDT_CFloat64: torch.complex128, gdal.GDT_Byte: torch.uint8, gdal.GDT_UInt16: torch.uint16,
+                gdal.GDT_UInt32: torch.uint32}
 
 
 def _samples(r):
@@ -106,18 +113,16 @@ class Geocode:
         (cuGeocode.cpp:39-90).  Rasters are ``isce3_gb300.io.Raster`` objects,
         NumPy arrays or CUDA tensors: inputs of the radar grid's shape,
         outputs of the geogrid's.  Invalid output pixels hold
-        complex(invalid, invalid).  Extra keyword-only arguments:
+        complex(invalid, invalid) for complex types.  Extra keyword-only arguments:
         ``geo2rdr_precision`` ("fp64" or "ff"), ``az_index_block`` /
         ``rg_index_block`` (f64 radar coordinates of each geo pixel, NaN where
         masked), ``dem_margin``, ``device`` and ``stream``.
         """
         self._check_consistency(output_rasters, input_rasters, data_interp_methods, raster_datatypes,
                                 invalid_values)
-        for method, dtype in zip(data_interp_methods, raster_datatypes):
-            if int(dtype) != gdal.GDT_CFloat32:
-                raise NotImplementedError("only GDT_CFloat32 rasters are geocoded on the GB300 path")
-            if DataInterpMethod(method) != DataInterpMethod.SINC:
-                raise NotImplementedError("only SINC interpolation is provided on the GB300 path")
+        for dtype in raster_datatypes:
+            if int(dtype) not in _TORCH_TYPES:
+                raise NotImplementedError(f"GDAL data type {int(dtype)} is not geocoded by the CUDA geocoder")
         if DataInterpMethod(dem_interp_method) != DataInterpMethod.BIQUINTIC:
             raise NotImplementedError("only the biquintic DEM interpolator is provided")
         if geo2rdr_precision not in ("fp64", "ff", "float-float"):
@@ -137,11 +142,16 @@ class Geocode:
         srange_correction = srange_correction if srange_correction is not None else LUT2d()
 
         dev = M.device_of(device)
+        fused = [i for i in range(n) if int(raster_datatypes[i]) == gdal.GDT_CFloat32
+                 and DataInterpMethod(data_interp_methods[i]) == DataInterpMethod.SINC]
+        others = [i for i in range(n) if i not in fused]
         with torch.cuda.device(dev):
             s = stream or torch.cuda.current_stream(dev)
             with torch.cuda.stream(s):
-                ins = [_Staged(_samples(r), dev, True, torch.complex64) for r in input_rasters]
-                outs = [_Staged(_samples(r), dev, False, torch.complex64) for r in output_rasters]
+                ins = [_Staged(_samples(r), dev, True, _TORCH_TYPES[int(t)])
+                       for r, t in zip(input_rasters, raster_datatypes)]
+                outs = [_Staged(_samples(r), dev, False, _TORCH_TYPES[int(t)])
+                        for r, t in zip(output_rasters, raster_datatypes)]
                 extra = []
                 for arr, what in ((az_index_block, "az_index_block"), (rg_index_block, "rg_index_block")):
                     if arr is None:
@@ -150,6 +160,11 @@ class Geocode:
                     if tuple(arr.shape) != (g.length, g.width):
                         raise ValueError(f"{what} shape does not match the geogrid")
                     extra.append(_Staged(arr, dev, False, torch.float64))
+                # the radar coordinates the per-raster interpolation reads
+                coords = [e.dev if e is not None else None for e in extra]
+                if others:
+                    coords = [c if c is not None else torch.empty((g.length, g.width), dtype=torch.float64,
+                                                                  device=dev) for c in coords]
                 a = L.RasterGeocodeArgs()
                 a.radar_grid = M.radar_grid_desc(rgrid)
                 a.geo_grid = M.geo_grid_desc(g)
@@ -166,20 +181,29 @@ class Geocode:
                 a.ellipsoid_a, a.ellipsoid_e2 = self.ellipsoid.a, self.ellipsoid.e2
                 a.threshold, a.delta_range = float(threshold), float(delta_range)
                 a.maxiter, a.lines_per_block = int(maxiter), self.lines_per_block
-                a.n_rasters = n
+                a.n_rasters = len(fused)
                 a.geo2rdr_precision = 0 if geo2rdr_precision == "fp64" else 1
-                in_ptrs = (C.c_void_p * n)(*[x.ptr() for x in ins])
-                out_ptrs = (C.c_void_p * n)(*[x.ptr() for x in outs])
-                invs = (C.c_double * n)(*[float(v) for v in invalid_values])
+                in_ptrs = (C.c_void_p * max(len(fused), 1))(*[ins[i].ptr() for i in fused])
+                out_ptrs = (C.c_void_p * max(len(fused), 1))(*[outs[i].ptr() for i in fused])
+                invs = (C.c_double * max(len(fused), 1))(*[float(invalid_values[i]) for i in fused])
                 a.input_rasters = C.cast(in_ptrs, C.POINTER(C.c_void_p))
                 a.output_rasters = C.cast(out_ptrs, C.POINTER(C.c_void_p))
                 a.invalid_values = C.cast(invs, C.POINTER(C.c_double))
-                a.az_index = extra[0].ptr() if extra[0] else None
-                a.rg_index = extra[1].ptr() if extra[1] else None
+                a.az_index = coords[0].data_ptr() if coords[0] is not None else None
+                a.rg_index = coords[1].data_ptr() if coords[1] is not None else None
                 a.dem_margin = int(dem_margin)
                 ctx = L.context(dev.index)
-                st = L.lib().gslc_geocode_rasters(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
-                L.check(st, ctx, "geocode_rasters")
+                lib = L.lib()
+                if fused or others or coords[0] is not None or coords[1] is not None:
+                    st = lib.gslc_geocode_rasters(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
+                    L.check(st, ctx, "geocode_rasters")
+                for i in others:
+                    st = lib.gslc_interpolate_raster(
+                        ctx, C.c_void_p(coords[0].data_ptr()), C.c_void_p(coords[1].data_ptr()), g.length * g.width,
+                        C.c_void_p(ins[i].ptr()), rgrid.length, rgrid.width, C.c_void_p(outs[i].ptr()),
+                        int(raster_datatypes[i]), int(DataInterpMethod(data_interp_methods[i])),
+                        float(invalid_values[i]), C.c_void_p(s.cuda_stream))
+                    L.check(st, ctx, "geocode_rasters")
                 for o in outs + [e for e in extra if e is not None]:
                     o.copy_back()
                 del dem_keep, ss, ins

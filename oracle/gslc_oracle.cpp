@@ -1458,3 +1458,204 @@ extern "C" int orc_radar_grid_cubes(const orc_radar_grid* rg, const orc_geo_grid
     if (proj_fail) return fail("Inverse projection transformation failed");
     return 0;
 }
+
+// ---------------------------------------------------------------- raster interpolators
+// The device interpolators of the CUDA raster geocoder (cuda/core/
+// gpuNearestNeighborInterpolator.cu:8-15, gpuBilinearInterpolator.cu:78-108,
+// gpuBicubicInterpolator.cu:104-188, gpuSpline2dInterpolator.cu _initSpline /
+// _spline / interpolate with order 6, gpuSinc2dInterpolator.cu:103-140 over
+// the chip of cuda/geocode/Geocode.cu:243-277), on one real component of a
+// sample: the reference's complex (thrust) arithmetic meets only real
+// weights, so each component follows the real arithmetic.
+namespace {
+template <typename S>
+struct RView {
+    const S* z;
+    int64_t nx;
+    int nc, c;
+    S operator()(int64_t r, int64_t col) const { return z[(r * nx + col) * nc + c]; }
+};
+
+template <typename S>
+S r_nearest(double x, double y, const RView<S>& z) {
+    return z((int64_t)std::round(y), (int64_t)std::round(x));
+}
+
+template <typename S>
+S r_bilinear(double x, double y, const RView<S>& z) {
+    const size_t x1 = std::floor(x), x2 = std::ceil(x), y1 = std::floor(y), y2 = std::ceil(y);
+    const S q11 = z(y1, x1), q12 = z(y2, x1), q21 = z(y1, x2), q22 = z(y2, x2);
+    if ((y1 == y2) && (x1 == x2)) return q11;
+    if (y1 == y2) return ((S)((x2 - x) / (x2 - x1)) * q11) + ((S)((x - x1) / (x2 - x1)) * q21);
+    if (x1 == x2) return ((S)((y2 - y) / (y2 - y1)) * q11) + ((S)((y - y1) / (y2 - y1)) * q12);
+    return ((q11 * (S)((x2 - x) * (y2 - y))) / (S)((x2 - x1) * (y2 - y1))) +
+           ((q21 * (S)((x - x1) * (y2 - y))) / (S)((x2 - x1) * (y2 - y1))) +
+           ((q12 * (S)((x2 - x) * (y - y1))) / (S)((x2 - x1) * (y2 - y1))) +
+           ((q22 * (S)((x - x1) * (y - y1))) / (S)((x2 - x1) * (y2 - y1)));
+}
+
+const double BICUBIC_W[256] = {
+    1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,     0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0,
+    -3, 0, 0, 3, 0, 0, 0, 0, -2, 0, 0, -1, 0, 0, 0, 0,  2, 0, 0, -2, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 0,
+    0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,     0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0,
+    0, 0, 0, 0, -3, 0, 0, 3, 0, 0, 0, 0, -2, 0, 0, -1,  0, 0, 0, 0, 2, 0, 0, -2, 0, 0, 0, 0, 1, 0, 0, 1,
+    -3, 3, 0, 0, -2, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,  0, 0, 0, 0, 0, 0, 0, 0, -3, 3, 0, 0, -2, -1, 0, 0,
+    9, -9, 9, -9, 6, 3, -3, -6, 6, -6, -3, 3, 4, 2, 1, 2,
+    -6, 6, -6, 6, -4, -2, 2, 4, -3, 3, 3, -3, -2, -1, -1, -2,
+    2, -2, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,    0, 0, 0, 0, 0, 0, 0, 0, 2, -2, 0, 0, 1, 1, 0, 0,
+    -6, 6, -6, 6, -3, -3, 3, 3, -4, 4, 2, -2, -2, -2, -1, -1,
+    4, -4, 4, -4, 2, 2, -2, -2, 2, -2, -2, 2, 1, 1, 1, 1};
+
+template <typename S>
+S r_bicubic(double x, double y, const RView<S>& z) {
+    const int64_t x1 = std::floor(x), x2 = std::ceil(x), y1 = std::floor(y), y2 = std::ceil(y);
+    const S denom = S(2.0), scale = S(0.25);
+    const S zz[4] = {z(y1, x1), z(y1, x2), z(y2, x2), z(y2, x1)};
+    const S dzdx[4] = {(z(y1, x1 + 1) - z(y1, x1 - 1)) / denom, (z(y1, x2 + 1) - z(y1, x2 - 1)) / denom,
+                       (z(y2, x2 + 1) - z(y2, x2 - 1)) / denom, (z(y2, x1 + 1) - z(y2, x1 - 1)) / denom};
+    // the reference's y-derivative stencils, as written there
+    const S dzdy[4] = {(z(y1 + 1, x1) - z(y1 - 1, x1)) / denom, (z(y1 + 1, x2 + 1) - z(y1 - 1, x2)) / denom,
+                       (z(y2 + 1, x2 + 1) - z(y2 - 1, x2)) / denom, (z(y2 + 1, x1 + 1) - z(y2 - 1, x1)) / denom};
+    const int64_t xs[4] = {x1, x2, x2, x1}, ys[4] = {y1, y1, y2, y2};
+    S dzdxy[4];
+    for (int k = 0; k < 4; ++k)
+        dzdxy[k] = scale * (z(ys[k] + 1, xs[k] + 1) - z(ys[k] - 1, xs[k] + 1) - z(ys[k] + 1, xs[k] - 1) +
+                            z(ys[k] - 1, xs[k] - 1));
+    S q[16];
+    for (int i = 0; i < 4; ++i) {
+        q[i] = zz[i];
+        q[i + 4] = dzdx[i];
+        q[i + 8] = dzdy[i];
+        q[i + 12] = dzdxy[i];
+    }
+    S c[16];
+    for (int i = 0; i < 16; ++i) {
+        S qq(0.0);
+        for (int j = 0; j < 16; ++j) qq += (S)(BICUBIC_W[i * 16 + j]) * q[j];
+        c[i] = qq;
+    }
+    const S t = x - x1, u = y - y1;
+    S ret = 0.0;
+    for (int i = 3; i >= 0; i--) ret = t * ret + ((c[i * 4 + 3] * u + c[i * 4 + 2]) * u + c[i * 4 + 1]) * u + c[i * 4];
+    return ret;
+}
+
+template <typename S>
+void r_init_spline(const S* Y, int n, S* R, S* Q) {
+    Q[0] = 0.0;
+    R[0] = 0.0;
+    for (int i = 1; i < n - 1; ++i) {
+        const auto p = 1.0 / (0.5 * Q[i - 1] + 2.0);
+        Q[i] = -0.5 * p;
+        R[i] = (3 * (Y[i + 1] - 2 * Y[i] + Y[i - 1]) - 0.5 * R[i - 1]) * p;
+    }
+    R[n - 1] = 0.0;
+    for (int i = (n - 2); i > 0; --i) R[i] = Q[i] * R[i + 1] + R[i];
+}
+
+template <typename S>
+S r_spline(double x, const S* Y, int n, const S* R) {
+    if (x < 1.0) return Y[0] + (x - 1.0) * (Y[1] - Y[0] - (R[1] / 6.0));
+    if (x > n) return Y[n - 1] + ((x - n) * (Y[n - 1] - Y[n - 2] + (R[n - 2] / 6.)));
+    const int j = int(std::floor(x));
+    const auto xx = x - j;
+    const auto t0 = Y[j] - Y[j - 1] - (R[j - 1] / 3.0) - (R[j] / 6.0);
+    const auto t1 = xx * ((R[j - 1] / 2.0) + (xx * ((R[j] - R[j - 1]) / 6)));
+    return Y[j - 1] + (xx * (t0 + t1));
+}
+
+template <typename S>
+S r_biquintic(double x, double y, const RView<S>& z, int64_t ny) {
+    const int order = 6;
+    int i0 = y, j0 = x;                  // order even: truncation
+    i0 = i0 - (order / 2) + 1;
+    j0 = j0 - (order / 2) + 1;
+    S A[order], R[order], Q[order], HC[order];
+    for (int i = 0; i < order; ++i) {
+        const int64_t indi = std::min(std::max((int64_t)(i0 + i), (int64_t)0), ny - 2);
+        for (int j = 0; j < order; ++j) {
+            const int64_t indj = std::min(std::max((int64_t)(j0 + j), (int64_t)0), z.nx - 2);
+            A[j] = z(indi + 1, indj + 1);
+        }
+        r_init_spline(A, order, R, Q);
+        HC[i] = r_spline(x - j0, A, order, R);
+    }
+    r_init_spline(HC, order, R, Q);
+    return (S)(r_spline(y - i0, HC, order, R));
+}
+
+template <typename S>
+S r_sinc(double x, double y, const RView<S>& z, const std::vector<double>& table) {
+    const int xi = (int)std::floor(x), yi = (int)std::floor(y);
+    const double X = SINC_HALF + (x - xi), Y = SINC_HALF + (y - yi);
+    const int ix = (int)std::floor(X), iy = (int)std::floor(Y);
+    if (!((ix >= SINC_HALF - 1) && (ix <= SINC_ONE - SINC_HALF - 1) && (iy >= SINC_HALF - 1) &&
+          (iy <= SINC_ONE - SINC_HALF - 1)))
+        return S(0.0);
+    const double frpx = X - ix, frpy = Y - iy;
+    const int intpx = ix + SINC_HALF, intpy = iy + SINC_HALF;
+    const int ifracx = std::min(std::max(0, int(frpx * SINC_SUB)), SINC_SUB - 1);
+    const int ifracy = std::min(std::max(0, int(frpy * SINC_SUB)), SINC_SUB - 1);
+    S v(0.0);
+    for (int i = 0; i < SINC_LEN; i++)
+        for (int j = 0; j < SINC_LEN; j++)
+            v += z(yi + (intpy - i) - SINC_HALF, xi + (intpx - j) - SINC_HALF) *
+                 S(table[ifracy * SINC_LEN + i]) * S(table[ifracx * SINC_LEN + j]);
+    return v;
+}
+
+template <typename S>
+void r_interpolate(const S* raster, const double* az, const double* rg, int64_t n, int64_t L, int64_t W, S* out,
+                   int nc, int method, double invalid) {
+    std::vector<double> table;
+    if (method == 0) {
+        const SincTable& T = sinc_table();
+        table.assign(T.k.begin(), T.k.end());
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        const double y = az[k], x = rg[k];
+        const bool ok = !(std::isnan(x) || std::isnan(y) || x < 4.0 || y < 4.0 || x >= W - 4.0 || y >= L - 4.0);
+        for (int c = 0; c < nc; ++c) {
+            S v = (S)invalid;
+            if (ok) {
+                const RView<S> z{raster, W, nc, c};
+                switch (method) {
+                case 0: v = r_sinc(x, y, z, table); break;
+                case 1: v = r_bilinear(x, y, z); break;
+                case 2: v = r_bicubic(x, y, z); break;
+                case 3: v = r_nearest(x, y, z); break;
+                default: v = r_biquintic(x, y, z, L); break;
+                }
+            }
+            out[k * nc + c] = v;
+        }
+    }
+}
+}  // namespace
+
+// cuda/geocode/Geocode.cu:203-287: raster samples at per-pixel radar
+// coordinates (NaN: masked).  gdal_type: 1 Byte, 2 UInt16, 4 UInt32,
+// 6 Float32, 7 Float64, 10 CFloat32, 11 CFloat64.
+extern "C" int orc_interpolate_raster(const double* az, const double* rg, int64_t n, const void* raster, int64_t L,
+                                      int64_t W, void* out, int gdal_type, int method, double invalid) {
+    auto uint_nearest = [&](auto* src, auto* dst) {
+        using U = std::remove_pointer_t<decltype(dst)>;
+        for (int64_t k = 0; k < n; ++k) {
+            const double y = az[k], x = rg[k];
+            const bool ok = !(std::isnan(x) || std::isnan(y) || x < 4.0 || y < 4.0 || x >= W - 4.0 || y >= L - 4.0);
+            dst[k] = ok ? src[(int64_t)std::round(y) * W + (int64_t)std::round(x)] : (U)invalid;
+        }
+    };
+    switch (gdal_type) {
+    case 6: r_interpolate((const float*)raster, az, rg, n, L, W, (float*)out, 1, method, invalid); break;
+    case 10: r_interpolate((const float*)raster, az, rg, n, L, W, (float*)out, 2, method, invalid); break;
+    case 7: r_interpolate((const double*)raster, az, rg, n, L, W, (double*)out, 1, method, invalid); break;
+    case 11: r_interpolate((const double*)raster, az, rg, n, L, W, (double*)out, 2, method, invalid); break;
+    case 1: uint_nearest((const uint8_t*)raster, (uint8_t*)out); break;
+    case 2: uint_nearest((const uint16_t*)raster, (uint16_t*)out); break;
+    case 4: uint_nearest((const uint32_t*)raster, (uint32_t*)out); break;
+    default: return fail("unsupported raster data type");
+    }
+    return 0;
+}

@@ -185,6 +185,13 @@ int orc_radar_grid_cubes(const orc_radar_grid* rg, const orc_geo_grid* g, const 
                          double threshold, int maxiter, double delta_range, double* slant_range,
                          double* azimuth_time, float* incidence, float* los_x, float* los_y, float* along_x,
                          float* along_y, float* elevation, double* ground_velocity, int nthreads);
+/* the CUDA raster geocoder's interpolation at per-pixel radar coordinates
+ * (cuda/geocode/Geocode.cu:203-287 and cuda/core/gpu*Interpolator.cu), NaN
+ * coordinates masked; gdal_type 1, 2, 4, 6, 7, 10, 11; method 0 sinc,
+ * 1 bilinear, 2 bicubic, 3 nearest, 4 biquintic.  Returns >0 on an
+ * unsupported type. */
+int orc_interpolate_raster(const double* az, const double* rg, int64_t n, const void* raster, int64_t L,
+                           int64_t W, void* out, int gdal_type, int method, double invalid);
 /* DEM statistics (geometry/DEMInterpolator.cpp:515-560) */
 void orc_dem_stats(const float* z, int64_t length, int64_t width, float* mn, float* mx, double* mean,
                    int64_t* n_valid);

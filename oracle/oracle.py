@@ -132,6 +132,8 @@ def lib() -> C.CDLL:
         _lib.orc_radar_grid_cubes.argtypes = [C.POINTER(RadarGrid), C.POINTER(GeoGrid), C.c_void_p, C.c_int,
                                               C.POINTER(OrbitS), C.POINTER(Lut), C.POINTER(Lut), C.c_double, C.c_int,
                                               C.c_double] + [C.c_void_p] * 9 + [C.c_int]
+        _lib.orc_interpolate_raster.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int64,
+                                                C.c_void_p, C.c_int, C.c_int, C.c_double]
         _lib.orc_dem_stats.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]
     return _lib
@@ -438,6 +440,24 @@ def radar_grid_cubes(radar_grid, geogrid, heights, orbit, native_doppler, grid_d
     if st:
         raise RuntimeError(lib().orc_last_error().decode())
     return arrs
+
+
+_GDT = {np.dtype(np.uint8): 1, np.dtype(np.uint16): 2, np.dtype(np.uint32): 4, np.dtype(np.float32): 6,
+        np.dtype(np.float64): 7, np.dtype(np.complex64): 10, np.dtype(np.complex128): 11}
+
+
+def interpolate_raster(az: np.ndarray, rg: np.ndarray, raster: np.ndarray, method: int, invalid: float) -> np.ndarray:
+    """cuda/geocode/Geocode.cu:203-287 on the CPU: ``raster`` sampled at the
+    radar coordinates (az, rg) of each output pixel (NaN: masked)."""
+    az = np.ascontiguousarray(az, dtype=np.float64)
+    rg = np.ascontiguousarray(rg, dtype=np.float64)
+    raster = np.ascontiguousarray(raster)
+    out = np.empty(az.shape, raster.dtype)
+    st = lib().orc_interpolate_raster(_ptr(az), _ptr(rg), az.size, _ptr(raster), raster.shape[0], raster.shape[1],
+                                      _ptr(out), _GDT[raster.dtype], int(method), float(invalid))
+    if st:
+        raise ValueError(lib().orc_last_error().decode())
+    return out
 
 
 def dem_stats(z: np.ndarray):

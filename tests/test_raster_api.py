@@ -60,11 +60,10 @@ def test_unsupported_cases(small):
     inp = [Raster(np.zeros((64, 64), np.complex64))]
     out = [Raster.empty(16, 16, gdal.GDT_CFloat32)]
     assert inp[0].datatype() == gdal.GDT_CFloat32
+    # data types outside the CUDA geocoder's switch (Geocode.cu:722-775)
     with pytest.raises(NotImplementedError):
-        geo.geocode_rasters(out, inp, [DataInterpMethod.BILINEAR], [gdal.GDT_CFloat32], [np.nan], sc.dem)
-    with pytest.raises(NotImplementedError):
-        geo.geocode_rasters([np.zeros((16, 16), np.float32)], [np.zeros((64, 64), np.float32)],
-                            [DataInterpMethod.SINC], [gdal.GDT_Float32], [np.nan], sc.dem)
+        geo.geocode_rasters([np.zeros((16, 16), np.int16)], [np.zeros((64, 64), np.int16)],
+                            [DataInterpMethod.NEAREST], [gdal.GDT_Int16], [0.0], sc.dem)
     with pytest.raises(NotImplementedError):
         geo.geocode_rasters(out, inp, [DataInterpMethod.SINC], [gdal.GDT_CFloat32], [np.nan], sc.dem,
                             dem_interp_method=DataInterpMethod.BILINEAR)
