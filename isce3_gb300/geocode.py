@@ -278,6 +278,16 @@ def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geo
             rg_index_block, dem_margin, rdr_deramped, rdr_format, geo_format, mantissa_bits)
 
 
+_upload_streams: dict = {}
+
+
+def _upload_stream(dev: torch.device) -> torch.cuda.Stream:
+    """One side stream per device for radar-block uploads."""
+    if dev not in _upload_streams:
+        _upload_streams[dev] = torch.cuda.Stream(dev)
+    return _upload_streams[dev]
+
+
 def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sliced_radargrid, geogrid, orbit,
                 native_doppler, image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
                 subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
@@ -287,9 +297,22 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     """Stage arrays on ``dev`` and fill a gslc_geocode_args.
 
     Returns (args, outputs to copy back, objects to keep alive)."""
-    # Small inputs first: the DEM window and LUT samples come from pageable
-    # host memory with synchronous copies, which would otherwise queue behind
-    # the radar blocks' asynchronous (pinned) upload on the same stream.
+    # Radar blocks in pinned host memory upload on a side stream while the DEM
+    # window and LUT samples (pageable host memory, synchronous copies) are
+    # prepared on the call's stream, which then waits for the upload.
+    # Pageable radar blocks upload after them, so that the small synchronous
+    # copies do not queue behind the large one.
+    s = torch.cuda.current_stream(dev)
+    raws = [_raw(r) for r in rdr_data_blocks]
+    side = None
+    if any(isinstance(r, torch.Tensor) and r.device.type == "cpu" and r.is_pinned() for r in raws):
+        side = _upload_stream(dev)
+        side.wait_stream(s)
+        with torch.cuda.stream(side):
+            rdr = [_Staged(r, dev, True, torch.complex64) for r in raws]
+        for st in rdr:
+            if st.host is not None:
+                st.dev.record_stream(s)
     holder = M.AzRgHolder()
     a = L.GeocodeArgs()
     a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
@@ -299,7 +322,10 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     a.srange_correction = M.lut_desc(srange_correction, dev)
     a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
     a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
-    rdr = [_Staged(_raw(r), dev, True, torch.complex64) for r in rdr_data_blocks]
+    if side is None:
+        rdr = [_Staged(r, dev, True, torch.complex64) for r in raws]
+    else:
+        s.wait_stream(side)
     if any(r.host is not None for r in rdr) and inplace_deramp:
         raise ValueError("inplace_deramp needs device-resident radar tensors")
     geo_t = torch.complex64 if geo_format != 1 else torch.int32
