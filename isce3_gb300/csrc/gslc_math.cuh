@@ -10,6 +10,7 @@
 #include <stddef.h>
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define GSLC_HD __host__ __device__ __forceinline__
@@ -437,6 +438,23 @@ GSLC_HD int orbit_segment(const Orbit& o, int pc, double& u) {
     return pc + 1;
 }
 
+// Bits of a double.  For |x| < c with c > 0, comparing the magnitude bits
+// (sign cleared) as unsigned integers gives the same answer as the FP64
+// compare, NaN included (its magnitude bits exceed every finite c's); the
+// Newton loop uses it to keep its tests off the FP64 pipe.
+GSLC_HD uint64_t dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    memcpy(&u, &x, sizeof(u));
+    return u;
+#endif
+}
+constexpr uint64_t DMAG = 0x7fffffffffffffffull;
+constexpr uint64_t DBITS_HALF = 0x3fe0000000000000ull;        // 0.5
+constexpr uint64_t DBITS_MINUS_HALF = 0xbfe0000000000000ull;  // -0.5
+
 GSLC_HD double seg_poly(const double* c, int deg, double w) {
     double acc = ld_gen(c + deg);
     for (int k = deg - 1; k >= 0; --k) acc = fma(acc, w, ld_gen(c + k));
@@ -461,6 +479,8 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
     double w = 0.0;
     const double* c = seg;
     const int nh = o.seg_nh;
+    // |dt| < thr as a bit compare (thr <= 0 or NaN: never, as the FP64 test)
+    const uint64_t thr_bits = thr > 0.0 ? dbits(thr) : 0ull;
     for (int i = 1; i < maxiter; ++i) {
         t -= dt;
         // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
@@ -468,7 +488,10 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
         // the first and last segment (the orbit's time span) w, the piece
         // and the span check come from t exactly as orbit interpolation does.
         w -= dt * o.inv_spacing;
-        if (cur <= 0 || cur >= o.n - 2 || !(w >= -0.5 && w < 0.5)) {
+        // w in [-0.5, 0.5): |w| < 0.5 or w == -0.5
+        const uint64_t wb = dbits(w);
+        const bool in_seg = (wb & DMAG) < DBITS_HALF || wb == DBITS_MINUS_HALF;
+        if (cur <= 0 || cur >= o.n - 2 || !in_seg) {
             if (!(t >= o.t0 && t <= o.t_end)) return false;  // FillNaN -> no convergence
             const int pc = orbit_piece(o, t);
             const double tidx = o.t0 + pc * o.spacing;
@@ -514,7 +537,7 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             fn = acc;
             dt = -fn * seg_poly(c + SEG_G, o.seg_ng, w);
         }
-        if (fabs(dt) < thr) {
+        if ((dbits(dt) & DMAG) < thr_bits) {
             double r[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
