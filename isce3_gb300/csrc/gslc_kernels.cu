@@ -296,9 +296,12 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
         }
 #pragma unroll
         for (int k = 5; k >= 0; --k) fn = ff_fma(fn, w, cf[k]);
-        ff g = ld_ff(c + SEGFF_G + ng);
-        for (int k = ng - 1; k >= 0; --k) g = ff_fma(g, w, ld_ff(c + SEGFF_G + k));
-        const ff dt = ff_neg(ff_mul(fn, g));
+        // G = 1/|vel|^2 only scales the step: in FP32 (relative error ~1e-7)
+        // each step changes by that fraction, which the next float-float
+        // residual corrects (the iteration contracts by ~0.1 per step)
+        float g = __ldg(c + SEGFF_G + ng).x;
+        for (int k = ng - 1; k >= 0; --k) g = fmaf(g, w.hi, __ldg(c + SEGFF_G + k).x);
+        const ff dt = ff_neg(ff_mul_f(fn, g));
         if (fabsf(dt.hi) < thr) {
             t = tj + ((double)w.hi + (double)w.lo + 0.5) * o.spacing;
             double r[3];

@@ -454,6 +454,7 @@ GSLC_HD uint64_t dbits(double x) {
 constexpr uint64_t DMAG = 0x7fffffffffffffffull;
 constexpr uint64_t DBITS_HALF = 0x3fe0000000000000ull;        // 0.5
 constexpr uint64_t DBITS_MINUS_HALF = 0xbfe0000000000000ull;  // -0.5
+constexpr uint64_t DBITS_1EM5 = 0x3ee4f8b588e368f1ull;        // 1e-5
 
 GSLC_HD double seg_poly(const double* c, int deg, double w) {
     double acc = ld_gen(c + deg);
@@ -481,6 +482,11 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
     const int nh = o.seg_nh;
     // |dt| < thr as a bit compare (thr <= 0 or NaN: never, as the FP64 test)
     const uint64_t thr_bits = thr > 0.0 ? dbits(thr) : 0ull;
+    // G(w) = 1/|vel|^2 changes by ~5e-5 of itself per unit w (about 10 s):
+    // after a step below 1e-5 s its last value is within ~1e-10 of the new
+    // one, which moves the next step by < 1e-15 s, so it is reused
+    double g = 0.0;
+    bool g_fresh = false;
     for (int i = 1; i < maxiter; ++i) {
         t -= dt;
         // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
@@ -535,7 +541,9 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
 #pragma unroll
             for (int k = 5; k >= 0; --k) acc = fma(acc, w, cf[k]);
             fn = acc;
-            dt = -fn * seg_poly(c + SEG_G, o.seg_ng, w);
+            if (!g_fresh) g = seg_poly(c + SEG_G, o.seg_ng, w);
+            dt = -fn * g;
+            g_fresh = (dbits(dt) & DMAG) < DBITS_1EM5;
         }
         if ((dbits(dt) & DMAG) < thr_bits) {
             double r[3];
@@ -591,6 +599,12 @@ __device__ __forceinline__ ff ff_mul(ff x, ff y) {                   // DWTimesD
     float e = fmaf(x.hi, y.hi, -p);
     e = fmaf(x.hi, y.lo, e);
     e = fmaf(x.lo, y.hi, e);
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ ff ff_mul_f(ff x, float y) {              // DWTimesFP1
+    const float p = __fmul_rn(x.hi, y);
+    float e = fmaf(x.hi, y, -p);
+    e = fmaf(x.lo, y, e);
     return ff_fast_two_sum(p, e);
 }
 __device__ __forceinline__ ff ff_fma(ff x, ff y, ff z) { return ff_add(ff_mul(x, y), z); }
