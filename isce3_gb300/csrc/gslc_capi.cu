@@ -265,11 +265,15 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
         }
         for (int k = 0; k < SEG_NH; ++k) s[SEG_H + k] = dd_round(H[k]);
         for (int k = 0; k < SEG_NG; ++k) s[SEG_G + k] = dd_round(G[k]);
-        // H degree: the tail over |w| <= 1/2 moves the Newton step by < 1e-17 s
+        // H degree: the tail over |w| <= 1/2 moves the Newton step by < 1e-13 s.
+        // On 10 s state vectors the terms above degree 5 are the rounding
+        // noise of the product (~1e-15 s), and the residual's own rounding
+        // (|D.b_0| ~ 1e10 m^2/s at 2^-53) is ~1e-14 s; the reference's
+        // azimuth times carry ~1e-11 s of orbit-interpolation rounding.
         int nh = SEG_NH - 1;
         {
             double tail = 0.0;
-            const double lim = 1e-17 * std::fabs(W[0].hi);
+            const double lim = 1e-13 * std::fabs(W[0].hi);
             while (nh > 0) {
                 const double t = tail + std::fabs(s[SEG_H + nh]) * std::ldexp(1.0, -nh);
                 if (t > lim) break;
@@ -278,7 +282,10 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
             }
         }
         // G degree: the lowest whose truncated, rounded series times W is
-        // within 2^-52 of 1 on 65 points of the segment
+        // within 2^-40 of 1 on 65 points of the segment.  G only scales the
+        // step (the iteration's fixed point is fn = 0 whatever G is): a
+        // relative error e in G changes each step by e of itself, which the
+        // next residual corrects (10 s state vectors: degree 3)
         int ng = -1;
         for (int K = 1; K < SEG_NG && ng < 0; ++K) {
             double worst = 0.0;
@@ -290,7 +297,7 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
                 const dd e = dd_add(dd_mul(gv, wv), {-1.0, 0.0});
                 worst = std::max(worst, std::fabs(e.hi));
             }
-            if (worst <= std::ldexp(1.0, -52)) ng = K;
+            if (worst <= std::ldexp(1.0, -40)) ng = K;
         }
         if (ng < 0) {
             div = 1;
