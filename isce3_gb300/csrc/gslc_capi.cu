@@ -228,11 +228,13 @@ void shift_poly_dd(const double* q, int n, int c, dd* r) {
 // G = 1/W is W's reciprocal power series.  Returns the highest H and G
 // degree needed over the segments, and div = 1 where G would need more
 // than 12 terms (the kernel then divides).
-void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, int& nh_max, int& ng_max, int& div) {
+void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, int& nh_max, int& ng_max, int& div,
+                         int& a7) {
     const int nseg = o.n - 1;
     nh_max = 0;
     ng_max = 0;
     div = 0;
+    a7 = 0;
     for (int j = 0; j < nseg; ++j) {
         const int idx = std::min(std::max(j - 1, 0), o.n - 4);
         const int c = j - idx - 1;                 // u = w + c
@@ -303,6 +305,10 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
             div = 1;
             ng = SEG_NG - 1;
         }
+        // position degree 7: kept while its term over |w| <= 1/2 reaches
+        // 1e-11 m (slant ranges of ~1e6 m round at ~1e-10 m)
+        for (int d = 0; d < 3; ++d)
+            if (std::fabs(s[SEG_A + d * 8 + 7]) * std::ldexp(1.0, -7) >= 1e-11) a7 = 1;
         nh_max = std::max(nh_max, nh);
         ng_max = std::max(ng_max, ng);
     }
@@ -314,10 +320,10 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
 void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
     make_orbit_coeffs(o, coef);
     // Newton segment tables after the pieces (orbit_seg_offset, 16-byte aligned)
-    int seg_nh = 0, seg_ng = 0, seg_div = 0;
+    int seg_nh = 0, seg_ng = 0, seg_div = 0, seg_a7 = 1;
     coef.resize(orbit_table_doubles(o.n), 0.0);
     double* seg = coef.data() + orbit_seg_offset(o.n);
-    make_orbit_segments(o, coef.data(), seg, seg_nh, seg_ng, seg_div);
+    make_orbit_segments(o, coef.data(), seg, seg_nh, seg_ng, seg_div, seg_a7);
     // their float pairs for the float-float Newton: b, h, g, a of each segment
     float2* ffs = reinterpret_cast<float2*>(coef.data() + orbit_segff_offset(o.n));
     auto split = [](double v) {
@@ -342,6 +348,7 @@ void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob
     ob.seg_nh = seg_nh;
     ob.seg_ng = seg_ng;
     ob.seg_div = seg_div;
+    ob.seg_a7 = seg_a7;
 }
 
 bool utm_setup(int code, Utm& u) {
@@ -408,6 +415,8 @@ Lut to_lut(const gslc_lut2d& l) {
     o.ref_value = l.ref_value;
     o.inv_dx = 1.0 / l.dx;
     o.inv_dy = 1.0 / l.dy;
+    o.kx_max = dkey(l.nx - 1.0);
+    o.ky_max = dkey(l.ny - 1.0);
     o.data = l.data;
     return o;
 }
@@ -765,6 +774,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
         p.inv_vv0 = 1.0 / vdot(p.vel0, p.vel0);
     }
     p.thr = a->threshold_geo2rdr;
+    p.thr_bits = p.thr > 0.0 ? dbits(p.thr) : 0ull;
     p.maxiter = a->numiter_geo2rdr;
     p.rg_t0 = rg.sensing_start; p.rg_prf = rg.prf; p.rg_r0 = rg.starting_range;
     p.rg_dr = rg.range_pixel_spacing; p.rg_wvl = rg.wavelength;
@@ -776,16 +786,23 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.s_r0 = srg.starting_range - half_rg;
     p.s_stop = grid_stop(srg) + half_az;
     p.s_end = grid_end(srg) + half_rg;
+    p.k_s_t0 = dkey(p.s_t0);
+    p.k_s_stop = dkey(p.s_stop);
+    p.k_s_r0 = dkey(p.s_r0);
+    p.k_s_end = dkey(p.s_end);
     p.nat_dop = to_lut(a->native_doppler);
     p.img_dop = to_lut(a->image_grid_doppler);
     p.az_corr = to_lut(a->az_time_correction);
     p.sr_corr = to_lut(a->srange_correction);
+    p.az_corr_on = p.az_corr.have_data || p.az_corr.ref_value != 0.0;
+    p.sr_corr_on = p.sr_corr.have_data || p.sr_corr.ref_value != 0.0;
     if ((st = to_azrg(c, a->az_carrier, p.az_car, "az_carrier"))) return st;
     if ((st = to_azrg(c, a->rg_carrier, p.rg_car, "rg_carrier"))) return st;
     p.carriers_zero = p.az_car.is_zero && p.rg_car.is_zero;
     p.flat_scale = 4.0 * (M_PI / rg.wavelength);
     p.inv_prf = 1.0 / rg.prf;
     p.two_pi_over_prf = 2.0 * M_PI / rg.prf;
+    p.two_pi_over_prf_f = (float)p.two_pi_over_prf;
     p.flatten = a->flatten; p.reramp = a->reramp; p.use_corr = a->flatten_with_corrected_srange;
     p.inv_re = a->invalid_re; p.inv_im = a->invalid_im;
     p.inL = a->rdr_length; p.inW = a->rdr_width;

@@ -175,10 +175,12 @@ __device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t
         // iteration 0 at sensingMid with the shared state: the look-side
         // test (rvec x vel) . pos > 0 as rvec . (vel x pos), the step with
         // 1/|vel|^2 (within an ulp of the quotient)
+        // (the sign and |dt| < thr tests on the bits, as in the Newton loop)
         const V3 rvec = vsub(xyz, p.pos0);
-        if ((p.look_side == -1) != (vdot(rvec, p.n0) > 0.)) return false;
+        const int64_t side = dkey(vdot(rvec, p.n0));
+        if ((p.look_side == -1) != (side > 0 && side <= DKEY_INF)) return false;
         const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
-        if (fabs(dt) < p.thr) {
+        if ((dbits(dt) & DMAG) < p.thr_bits) {
             R = vnorm(rvec);
             return true;
         }
@@ -245,9 +247,10 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
     t = p.t_mid;
     {
         const V3 rvec = vsub(xyz, p.pos0);
-        if ((p.look_side == -1) != (vdot(rvec, p.n0) > 0.)) return false;
+        const int64_t side = dkey(vdot(rvec, p.n0));
+        if ((p.look_side == -1) != (side > 0 && side <= DKEY_INF)) return false;
         const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
-        if (fabs(dt) < p.thr) {
+        if ((dbits(dt) & DMAG) < p.thr_bits) {
             R = vnorm(rvec);
             return true;
         }
@@ -307,9 +310,10 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
             double r[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                ff acc = ld_ff(c + SEGFF_A + d * 8 + 7);
+                ff acc = ld_ff(c + SEGFF_A + d * 8 + 6);
+                if (o.seg_a7) acc = ff_fma(ld_ff(c + SEGFF_A + d * 8 + 7), w, acc);
 #pragma unroll
-                for (int k = 6; k >= 0; --k) acc = ff_fma(acc, w, ld_ff(c + SEGFF_A + d * 8 + k));
+                for (int k = 5; k >= 0; --k) acc = ff_fma(acc, w, ld_ff(c + SEGFF_A + d * 8 + k));
                 r[d] = ff_to_double(ff_add(D[d], ff_neg(acc)));
             }
             R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
@@ -342,7 +346,7 @@ __device__ __forceinline__ float2 ld_sample(const __half2* q) {
 
 template <typename S>
 __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg,
-                             double fracAz, double fracRg, double doppFreq) {
+                             double fracAz, double fracRg, float doppFreq) {
     const double x = 4.0 + fracRg, y = 4.0 + fracAz;
     const int ix = (int)floor(x), iy = (int)floor(y);
     const double fx = x - ix, fy = y - iy;
@@ -357,12 +361,12 @@ __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int 
         kx[0] = a.x; kx[1] = a.y; kx[2] = a.z; kx[3] = a.w; kx[4] = b.x; kx[5] = b.y; kx[6] = b.z; kx[7] = b.w;
         ky[0] = c.x; ky[1] = c.y; ky[2] = c.z; ky[3] = c.w; ky[4] = d.x; ky[5] = d.y; ky[6] = d.z; ky[7] = d.w;
     }
-    const bool demod = doppFreq != 0.0;
+    const bool demod = doppFreq != 0.f;
     // demodulation phasors for row offsets m = 0..4 (doppPhase = doppFreq*m)
     float dc[5], ds[5];
     if (demod) {
 #pragma unroll
-        for (int m = 0; m < 5; ++m) sincosf((float)(doppFreq * m), &ds[m], &dc[m]);
+        for (int m = 0; m < 5; ++m) sincosf(doppFreq * (float)m, &ds[m], &dc[m]);
     }
     // chip row r9 = iy + 4 - i maps to radar row intAz + iy - i; col c9 = ix + 4 - j
     const S* base = rdr + (int64_t)(intAz + iy) * p.inW + (intRg + ix);
@@ -391,7 +395,7 @@ __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int 
     float2 cval = make_float2(sre, sim);
     if (demod) {
         float s, c;
-        sincosf((float)(doppFreq * fracAz), &s, &c);
+        sincosf(doppFreq * (float)fracAz, &s, &c);
         cval = cmul(cval, make_float2(c, s));
     }
     return cval;
@@ -399,7 +403,7 @@ __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int 
 
 // block b of the request, in its sample format
 __device__ __forceinline__ float2 sinc_block(const GeoParams& p, int b, int intAz, int intRg, double fracAz,
-                                             double fracRg, double doppFreq) {
+                                             double fracRg, float doppFreq) {
     if (p.rdr_c32) return sinc_pixel(p, reinterpret_cast<const __half2*>(p.rdr[b]), intAz, intRg, fracAz, fracRg, doppFreq);
     return sinc_pixel(p, p.rdr[b], intAz, intRg, fracAz, fracRg, doppFreq);
 }
@@ -828,9 +832,11 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
             }
         } else if (conv) {
             if (!p.use_corr) R_uncorr = R;
-            if (lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
-            if (lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
-            const bool in_grid = t >= p.s_t0 && R >= p.s_r0 && t <= p.s_stop && R <= p.s_end;
+            // (a table without data adds its reference value; adding zero is skipped)
+            if (p.az_corr_on && lut_contains(p.az_corr, t, R)) t += lut_eval(p.az_corr, t, R);
+            if (p.sr_corr_on && lut_contains(p.sr_corr, t, R)) R += lut_eval(p.sr_corr, t, R);
+            const int64_t kt = dkey(t), kr = dkey(R);
+            const bool in_grid = kt >= p.k_s_t0 && kr >= p.k_s_r0 && kt <= p.k_s_stop && kr <= p.k_s_end;
             if (in_grid && lut_contains(p.nat_dop, t, R)) {
                 azc = (t - p.rg_t0) * p.rg_prf;
                 rgc = (R - p.rg_r0) / p.rg_dr;
@@ -867,7 +873,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         }
         const int xi = (int)floor(rgc), yi = (int)floor(azc);
         const double fx = rgc - (double)xi, fy = azc - (double)yi;
-        for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, sinc_block(p, b, yi, xi, fy, fx, 0.0));
+        for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, sinc_block(p, b, yi, xi, fy, fx, 0.f));
         return;
     }
     const float2 invalid = make_float2(p.inv_re, p.inv_im);
@@ -891,7 +897,8 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         return;
     }
     // Doppler in radians per line: eval * 2 * pi / prf (geocodeSlc.cpp:473-474)
-    const double doppFreq = lut_eval(p.nat_dop, az, rng) * p.two_pi_over_prf;
+    // (FP32: it only sets the float phases of the chip's demodulation)
+    const float doppFreq = lut_eval_f32(p.nat_dop, az, rng) * p.two_pi_over_prf_f;
     // reramp + flatten phase (geocodeSlc.cpp:362-392)
     const double carrier = p.carriers_zero ? 0.0 : azrg_eval(p.rg_car, az, rng) + azrg_eval(p.az_car, az, rng);
     const double flat = p.flat_scale * (p.use_corr ? rng : R_uncorr);

@@ -45,6 +45,10 @@ struct GeoParams {
     double inv_prf, two_pi_over_prf;
     int32_t flatten, reramp, use_corr, carriers_zero;
     float inv_re, inv_im;
+    float two_pi_over_prf_f, _pad_f;
+    int32_t az_corr_on, sr_corr_on;   // the correction LUT can change a value (data, or a nonzero reference value)
+    uint64_t thr_bits;                // bits of thr if thr > 0, else 0 (|x| < thr as a magnitude-bit compare)
+    int64_t k_s_t0, k_s_stop, k_s_r0, k_s_end;   // dkey of the sliced grid's bounds
     // radar blocks
     int32_t nblk, _pad2;
     int64_t inL, inW, az_first, rg_first;

@@ -52,11 +52,41 @@ GSLC_HD double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 GSLC_HD V3 vcross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 GSLC_HD double vnorm(V3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
+// Bits of a double.  For |x| < c with c > 0, comparing the magnitude bits
+// (sign cleared) as unsigned integers gives the same answer as the FP64
+// compare, NaN included (its magnitude bits exceed every finite c's); the
+// Newton loop uses it to keep its tests off the FP64 pipe.
+GSLC_HD uint64_t dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    memcpy(&u, &x, sizeof(u));
+    return u;
+#endif
+}
+constexpr uint64_t DMAG = 0x7fffffffffffffffull;
+constexpr uint64_t DBITS_HALF = 0x3fe0000000000000ull;        // 0.5
+constexpr uint64_t DBITS_MINUS_HALF = 0xbfe0000000000000ull;  // -0.5
+constexpr uint64_t DBITS_1EM5 = 0x3ee4f8b588e368f1ull;        // 1e-5
+
+// Order key of a double: for finite x, y (and -0.0 == +0.0), x <= y exactly
+// when dkey(x) <= dkey(y) as signed integers.  A NaN's key lies above every
+// finite key (positive sign) or below it (negative sign), so a two-sided
+// test lo <= x <= hi is false for it, as the FP64 test is.  Range tests use
+// it to stay off the FP64 pipe.
+GSLC_HD int64_t dkey(double x) {
+    const int64_t b = (int64_t)dbits(x);
+    return b < 0 ? -(b & (int64_t)DMAG) : b;
+}
+constexpr int64_t DKEY_INF = 0x7ff0000000000000ll;   // dkey(+inf); above it: NaN
+
 // ---- LUT2d (core/LUT2d.{h,cpp}) ------------------------------------------
 struct Lut {
     int32_t have_data, bounds_error, method, nx, ny, _pad;
     double x0, y0, dx, dy, ref_value;
     double inv_dx, inv_dy;      // 1/dx, 1/dy
+    int64_t kx_max, ky_max;     // dkey(nx - 1), dkey(ny - 1)
     const double* data;
 };
 
@@ -65,9 +95,9 @@ struct Lut {
 // a point within an ulp of the table's edge.
 GSLC_HD bool lut_contains(const Lut& l, double y, double x) {
     if (!l.have_data) return true;
-    const double i = (x - l.x0) * l.inv_dx;
-    const double j = (y - l.y0) * l.inv_dy;
-    return (i >= 0.0 && i <= l.nx - 1.0) && (j >= 0.0 && j <= l.ny - 1.0);
+    const int64_t i = dkey((x - l.x0) * l.inv_dx);
+    const int64_t j = dkey((y - l.y0) * l.inv_dy);
+    return (i >= 0 && i <= l.kx_max) && (j >= 0 && j <= l.ky_max);
 }
 
 // a load through a pointer that may address shared memory
@@ -117,6 +147,28 @@ struct Poly {
     double inv_x_norm, inv_y_norm;
     double c[POLY_MAX];
 };
+
+// lut_eval in FP32 after the offsets from the table origin (FP64): for
+// values that only set float phases (the native Doppler of the sinc chip,
+// whose phasors are float angles).  Relative error ~1e-7 of the value;
+// nearest-neighbour tables take the FP64 form, whose rounding picks the cell.
+GSLC_HD float lut_eval_f32(const Lut& l, double y, double x) {
+    if (!l.have_data) return (float)l.ref_value;
+    if (l.method == 3) return (float)lut_eval(l, y, x);
+    float xi = (float)((x - l.x0) * l.inv_dx);
+    float yi = (float)((y - l.y0) * l.inv_dy);
+    xi = fminf(fmaxf(xi, 0.f), (float)(l.nx - 1));
+    yi = fminf(fmaxf(yi, 0.f), (float)(l.ny - 1));
+    const int x1 = (int)floorf(xi), x2 = (int)ceilf(xi);
+    const int y1 = (int)floorf(yi), y2 = (int)ceilf(yi);
+    const float q11 = (float)ld_ro(l.data + (long)y1 * l.nx + x1), q12 = (float)ld_ro(l.data + (long)y2 * l.nx + x1);
+    const float q21 = (float)ld_ro(l.data + (long)y1 * l.nx + x2), q22 = (float)ld_ro(l.data + (long)y2 * l.nx + x2);
+    const float wx2 = (float)x2 - xi, wx1 = xi - (float)x1, wy2 = (float)y2 - yi, wy1 = yi - (float)y1;
+    if (y1 == y2 && x1 == x2) return q11;
+    if (y1 == y2) return wx2 * q11 + wx1 * q21;
+    if (x1 == x2) return wy2 * q11 + wy1 * q12;
+    return q11 * (wx2 * wy2) + q21 * (wx1 * wy2) + q12 * (wx2 * wy1) + q22 * (wx1 * wy1);
+}
 
 // core/Poly2d.cpp:8-24, normalised with reciprocals
 GSLC_HD double poly_eval(const Poly& p, double y, double x) {
@@ -390,7 +442,8 @@ struct Orbit {
     const double* seg;           // (n - 1) * SEG_STRIDE
     const float2* seg_ff;        // (n - 1) * SEGFF_STRIDE
     int32_t seg_nh, seg_ng;      // highest H and G degree used over all segments
-    int32_t seg_div, _pad;       // 1: G did not converge, divide by -|vel|^2 instead
+    int32_t seg_div;             // 1: G did not converge, divide by -|vel|^2 instead
+    int32_t seg_a7;              // 1: the position's degree-7 term matters (else degree 6)
 };
 
 // Orbit table layout in doubles: the pieces, then the segments (16-byte
@@ -438,23 +491,6 @@ GSLC_HD int orbit_segment(const Orbit& o, int pc, double& u) {
     return pc + 1;
 }
 
-// Bits of a double.  For |x| < c with c > 0, comparing the magnitude bits
-// (sign cleared) as unsigned integers gives the same answer as the FP64
-// compare, NaN included (its magnitude bits exceed every finite c's); the
-// Newton loop uses it to keep its tests off the FP64 pipe.
-GSLC_HD uint64_t dbits(double x) {
-#if defined(__CUDA_ARCH__)
-    return (uint64_t)__double_as_longlong(x);
-#else
-    uint64_t u;
-    memcpy(&u, &x, sizeof(u));
-    return u;
-#endif
-}
-constexpr uint64_t DMAG = 0x7fffffffffffffffull;
-constexpr uint64_t DBITS_HALF = 0x3fe0000000000000ull;        // 0.5
-constexpr uint64_t DBITS_MINUS_HALF = 0xbfe0000000000000ull;  // -0.5
-constexpr uint64_t DBITS_1EM5 = 0x3ee4f8b588e368f1ull;        // 1e-5
 
 GSLC_HD double seg_poly(const double* c, int deg, double w) {
     double acc = ld_gen(c + deg);
@@ -550,9 +586,9 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const double* a = c + SEG_A + d * 8;
-                double acc = ld_gen(a + 7);
+                double acc = o.seg_a7 ? fma(ld_gen(a + 7), w, ld_gen(a + 6)) : ld_gen(a + 6);
 #pragma unroll
-                for (int k = 6; k >= 0; --k) acc = fma(acc, w, ld_gen(a + k));
+                for (int k = 5; k >= 0; --k) acc = fma(acc, w, ld_gen(a + k));
                 r[d] = D[d] - acc;
             }
             R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
