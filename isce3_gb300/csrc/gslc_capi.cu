@@ -778,6 +778,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.maxiter = a->numiter_geo2rdr;
     p.rg_t0 = rg.sensing_start; p.rg_prf = rg.prf; p.rg_r0 = rg.starting_range;
     p.rg_dr = rg.range_pixel_spacing; p.rg_wvl = rg.wavelength;
+    p.rg_inv_dr = 1.0 / p.rg_dr;
     p.rg_len = rg.length; p.rg_wid = rg.width;
     p.look_side = rg.look_side;
     // sliced grid contains() bounds (RadarGridParameters.cpp:27-35)
@@ -807,6 +808,8 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.inv_re = a->invalid_re; p.inv_im = a->invalid_im;
     p.inL = a->rdr_length; p.inW = a->rdr_width;
     p.az_first = a->first_azimuth_line; p.rg_first = a->first_range_sample;
+    p.az_first_d = (double)p.az_first;
+    p.rg_first_d = (double)p.rg_first;
     p.mask = a->mask;
     p.carrier_out = a->carrier_phase;
     p.flatten_out = a->flatten_phase;

@@ -344,15 +344,30 @@ __device__ __forceinline__ float2 ld_sample(const __half2* q) {
     return __half22float2(__ldg(q));
 }
 
+// Sinc2dInterpolator's integer position and table phase of x = 4 + frac:
+// i = floor(x), f = min(max(0, int((x - i) * SINC_SUB)), SINC_SUB - 1).  For
+// x in [4, 8) both are bit fields of x (x = 4 (1 + m 2^-52): i = 4 + m >> 50
+// and, for i = 4, (x - 4) SINC_SUB = m 2^-37, so f = m >> 37); other x take
+// the FP64 form.
+__device__ __forceinline__ void sinc_index(double x, int& i, int& f) {
+    const uint64_t b = dbits(x);
+    if ((b >> 52) == 0x401) {
+        const uint64_t m = b & 0xfffffffffffffull;
+        i = 4 + (int)(m >> 50);
+        f = (int)((m >> 37) & (uint64_t)(SINC_SUB - 1));
+        return;
+    }
+    i = (int)floor(x);
+    f = min(max(0, (int)((x - i) * SINC_SUB)), SINC_SUB - 1);
+}
+
 template <typename S>
 __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg,
                              double fracAz, double fracRg, float doppFreq) {
-    const double x = 4.0 + fracRg, y = 4.0 + fracAz;
-    const int ix = (int)floor(x), iy = (int)floor(y);
-    const double fx = x - ix, fy = y - iy;
+    int ix, iy, ifx, ify;
+    sinc_index(4.0 + fracRg, ix, ifx);
+    sinc_index(4.0 + fracAz, iy, ify);
     if (ix < 3 || ix > 4 || iy < 3 || iy > 4) return make_float2(0.f, 0.f);
-    const int ifx = min(max(0, (int)(fx * SINC_SUB)), SINC_SUB - 1);
-    const int ify = min(max(0, (int)(fy * SINC_SUB)), SINC_SUB - 1);
     float kx[8], ky[8];
     const float4* kxp = reinterpret_cast<const float4*>(p.sinc + ifx * SINC_LEN);
     const float4* kyp = reinterpret_cast<const float4*>(p.sinc + ify * SINC_LEN);
@@ -794,6 +809,16 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     }
 }
 
+// (R - r0) / dr, correctly rounded as the quotient, in Markstein's form
+// (q0 = a/dr by the correctly rounded reciprocal, one FMA residual, one FMA
+// correction: Markstein 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, sec. 4.9), without the division's longer FP64 sequence.
+__device__ __forceinline__ double range_index(const GeoParams& p, double R) {
+    const double a = R - p.rg_r0;
+    const double q0 = a * p.rg_inv_dr;
+    return fma(fma(-q0, p.rg_dr, a), p.rg_inv_dr, q0);
+}
+
 // Everything after the ground point: geo2rdr, corrections, masks, the
 // radar-coordinate outputs, the sinc interpolation of every block, reramp
 // and flattening, for output pixel k.
@@ -820,7 +845,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
                 if (!lut_contains(p.nat_dop, t, R)) masked = true;
             }
             const double yv = (t - p.rg_t0) * p.rg_prf;
-            const double xv = (R - p.rg_r0) / p.rg_dr;
+            const double xv = range_index(p, R);
             const int yi = (int)floor(yv), xi = (int)floor(xv);
             if (!masked && p.have_subsw && !subswath_contains_gpu(p, yi, xi)) masked = true;
             const bool outside = yi < 0 || yi >= p.rg_len || xi < 0 || xi >= p.rg_wid;
@@ -839,7 +864,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
             const bool in_grid = kt >= p.k_s_t0 && kr >= p.k_s_r0 && kt <= p.k_s_stop && kr <= p.k_s_end;
             if (in_grid && lut_contains(p.nat_dop, t, R)) {
                 azc = (t - p.rg_t0) * p.rg_prf;
-                rgc = (R - p.rg_r0) / p.rg_dr;
+                rgc = range_index(p, R);
                 valid = true;
                 const int intAz = (int)floor(azc), intRg = (int)floor(rgc);
                 const bool corners = !(intRg < 4 || intRg >= p.rg_wid - 4 || intAz < 4 || intAz >= p.rg_len - 4);
@@ -882,7 +907,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         return;
     }
     // block-relative chip position (geocodeSlc.cpp:440-458, 335-348)
-    const double RgIndex = rgc - (double)p.rg_first, AzIndex = azc - (double)p.az_first;
+    const double RgIndex = rgc - p.rg_first_d, AzIndex = azc - p.az_first_d;
     const int intRgB = (int)RgIndex, intAzB = (int)AzIndex;
     const double fracRg = RgIndex - intRgB, fracAz = AzIndex - intAzB;
     bool interp = !(intRgB < 4 || intRgB >= p.inW - 4 || intAzB < 4 || intAzB >= p.inL - 4);

@@ -49,6 +49,8 @@ struct GeoParams {
     int32_t az_corr_on, sr_corr_on;   // the correction LUT can change a value (data, or a nonzero reference value)
     uint64_t thr_bits;                // bits of thr if thr > 0, else 0 (|x| < thr as a magnitude-bit compare)
     int64_t k_s_t0, k_s_stop, k_s_r0, k_s_end;   // dkey of the sliced grid's bounds
+    double rg_inv_dr;                 // 1 / rg_dr (correctly rounded), for the quotient's Markstein form
+    double az_first_d, rg_first_d;    // az_first, rg_first
     // radar blocks
     int32_t nblk, _pad2;
     int64_t inL, inW, az_first, rg_first;

@@ -503,10 +503,13 @@ GSLC_HD double seg_poly(const double* c, int deg, double w) {
 // iterates t <- t - fn/fn', fn = (xyz - pos).vel, fn' = -|vel|^2, with fn
 // formed on the segment tables (Orbit::seg) instead of subtracting the
 // interpolated position: fn(w) = D.v(w) - H(w) with D = xyz - P_ref is one
-// degree-13 polynomial whose coefficients k <= 6 are D.b_k - h_k (formed
-// when the iterate enters a segment) and whose others are -h_k; 1/|vel|^2 is
-// G(w).  Rounding differs from the direct form by ~1e-13 s in azimuth time,
-// below the reference's own orbit interpolation noise (~1e-11 s).
+// polynomial whose coefficients k <= 6 are D.b_k - h_k (formed when the
+// iterate enters a segment) and whose others are -h_k (H truncated where its
+// tail stops mattering); 1/|vel|^2 is G(w).  Inside a segment the iterate is
+// carried by its coordinate w alone, t = t_j + (w + 1/2) spacing being
+// formed where it is needed (segment changes and the returned iterate).
+// Rounding differs from the direct form by ~1e-13 s in azimuth time, below
+// the reference's own orbit interpolation noise (~1e-11 s).
 // seg: the segment tables (Orbit::seg, or a copy of them in shared memory).
 GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz, double thr, int maxiter, double& t,
                                        double dt, double& R) {
@@ -523,17 +526,20 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
     // one, which moves the next step by < 1e-15 s, so it is reused
     double g = 0.0;
     bool g_fresh = false;
+    double tj = 0.0;                     // start time of segment cur
     for (int i = 1; i < maxiter; ++i) {
-        t -= dt;
-        // Inside an interior segment w follows t (w -= dt / spacing, ~1e-15 s
-        // from the exact coordinate); entering a segment, leaving it, and on
-        // the first and last segment (the orbit's time span) w, the piece
-        // and the span check come from t exactly as orbit interpolation does.
+        // Inside an interior segment the iterate moves as w -= dt / spacing
+        // (~1e-15 s from the exact coordinate); entering a segment, leaving
+        // it, and on the first and last segment (the orbit's time span) the
+        // time, the span check, the piece and w come from it as orbit
+        // interpolation forms them.
         w -= dt * o.inv_spacing;
         // w in [-0.5, 0.5): |w| < 0.5 or w == -0.5
         const uint64_t wb = dbits(w);
         const bool in_seg = (wb & DMAG) < DBITS_HALF || wb == DBITS_MINUS_HALF;
         if (cur <= 0 || cur >= o.n - 2 || !in_seg) {
+            if (cur < 0) t -= dt;        // the first step, from the caller's iterate
+            else t = tj + (w + 0.5) * o.spacing;
             if (!(t >= o.t0 && t <= o.t_end)) return false;  // FillNaN -> no convergence
             const int pc = orbit_piece(o, t);
             const double tidx = o.t0 + pc * o.spacing;
@@ -542,6 +548,7 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             c = seg + (int64_t)j * SEG_STRIDE;
             if (j != cur) {
                 cur = j;
+                tj = o.t0 + j * o.spacing;
                 D[0] = xyz.x - ld_gen(c + 0);
                 D[1] = xyz.y - ld_gen(c + 1);
                 D[2] = xyz.z - ld_gen(c + 2);
@@ -582,6 +589,7 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             g_fresh = (dbits(dt) & DMAG) < DBITS_1EM5;
         }
         if ((dbits(dt) & DMAG) < thr_bits) {
+            t = tj + (w + 0.5) * o.spacing;
             double r[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
