@@ -83,12 +83,14 @@ __device__ __forceinline__ bool dem_coords_utm(const Dem& d, double lon, double 
 // spline in FP32 (core/Spline2dInterpolator.cpp:32-67).
 __device__ double dem_spline(const Dem& d, double row, double col) {
     const double ref = 0.0;
-    const int irow = (int)floor(row), icol = (int)floor(col);
+    // truncation equals floor wherever the bounds below pass (row, col >= 2);
+    // (col - j0) - 2 is col - icol, both steps exact for col >= 2
+    const int irow = (int)row, icol = (int)col;
     if (irow < 2 || irow >= d.length - 1) return ref;
     if (icol < 2 || icol >= d.width - 1) return ref;
-    const int i0 = (int)row - 2, j0 = (int)col - 2;
-    const float xx = (float)((col - (double)j0) - 2.0);
-    const float yy = (float)((row - (double)i0) - 2.0);
+    const int i0 = irow - 2, j0 = icol - 2;
+    const float xx = (float)(col - (double)icol);
+    const float yy = (float)(row - (double)irow);
     int cidx[6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) cidx[j] = min(max(j0 + j, 0), d.width - 2) + 1;
@@ -912,18 +914,19 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
     const double fracRg = RgIndex - intRgB, fracAz = AzIndex - intAzB;
     bool interp = !(intRgB < 4 || intRgB >= p.inW - 4 || intAzB < 4 || intAzB >= p.inL - 4);
     double rng = 0.0, az = 0.0;
+    float dop = 0.f;
     if (interp) {
         rng = dadd(p.rg_r0, dmul(rgc, p.rg_dr));
         az = p.rg_t0 + azc * p.inv_prf;
-        interp = lut_contains(p.nat_dop, az, rng);
+        // the Doppler in FP32: it only sets the float phases of the chip's demodulation
+        interp = lut_contains_eval_f32(p.nat_dop, az, rng, dop);
     }
     if (!interp) {
         for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);
         return;
     }
     // Doppler in radians per line: eval * 2 * pi / prf (geocodeSlc.cpp:473-474)
-    // (FP32: it only sets the float phases of the chip's demodulation)
-    const float doppFreq = lut_eval_f32(p.nat_dop, az, rng) * p.two_pi_over_prf_f;
+    const float doppFreq = dop * p.two_pi_over_prf_f;
     // reramp + flatten phase (geocodeSlc.cpp:362-392)
     const double carrier = p.carriers_zero ? 0.0 : azrg_eval(p.rg_car, az, rng) + azrg_eval(p.az_car, az, rng);
     const double flat = p.flat_scale * (p.use_corr ? rng : R_uncorr);

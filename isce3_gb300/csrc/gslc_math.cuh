@@ -152,11 +152,30 @@ struct Poly {
 // values that only set float phases (the native Doppler of the sinc chip,
 // whose phasors are float angles).  Relative error ~1e-7 of the value;
 // nearest-neighbour tables take the FP64 form, whose rounding picks the cell.
+GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi);
+
 GSLC_HD float lut_eval_f32(const Lut& l, double y, double x) {
     if (!l.have_data) return (float)l.ref_value;
     if (l.method == 3) return (float)lut_eval(l, y, x);
-    float xi = (float)((x - l.x0) * l.inv_dx);
-    float yi = (float)((y - l.y0) * l.inv_dy);
+    return lut_bilinear_f32(l, (float)((x - l.x0) * l.inv_dx), (float)((y - l.y0) * l.inv_dy));
+}
+
+// lut_contains(l, y, x), and where it holds v = lut_eval_f32(l, y, x), the
+// table coordinates formed once
+GSLC_HD bool lut_contains_eval_f32(const Lut& l, double y, double x, float& v) {
+    if (!l.have_data) {
+        v = (float)l.ref_value;
+        return true;
+    }
+    const double xd = (x - l.x0) * l.inv_dx, yd = (y - l.y0) * l.inv_dy;
+    const int64_t i = dkey(xd), j = dkey(yd);
+    if (!((i >= 0 && i <= l.kx_max) && (j >= 0 && j <= l.ky_max))) return false;
+    v = l.method == 3 ? (float)lut_eval(l, y, x) : lut_bilinear_f32(l, (float)xd, (float)yd);
+    return true;
+}
+
+// the bilinear (BilinearInterpolator.cpp:12-49) at table coordinates (xi, yi), in FP32
+GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi) {
     xi = fminf(fmaxf(xi, 0.f), (float)(l.nx - 1));
     yi = fminf(fmaxf(yi, 0.f), (float)(l.ny - 1));
     const int x1 = (int)floorf(xi), x2 = (int)ceilf(xi);
@@ -170,14 +189,22 @@ GSLC_HD float lut_eval_f32(const Lut& l, double y, double x) {
     return q11 * (wx2 * wy2) + q21 * (wx1 * wy2) + q12 * (wx2 * wy1) + q22 * (wx1 * wy1);
 }
 
-// core/Poly2d.cpp:8-24, normalised with reciprocals
+// core/Poly2d.cpp:8-24, normalised with reciprocals.  Products with a
+// factor that is exactly 1 (the first power of each variable) are taken as
+// the other factor, and powers past the last are not formed: the same values
+// with fewer FP64 operations.
 GSLC_HD double poly_eval(const Poly& p, double y, double x) {
-    const double xval = (x - p.x_mean) * p.inv_x_norm;
-    const double yval = (y - p.y_mean) * p.inv_y_norm;
+    const double xval = p.x_order > 0 ? (x - p.x_mean) * p.inv_x_norm : 0.0;
+    const double yval = p.y_order > 0 ? (y - p.y_mean) * p.inv_y_norm : 0.0;
     double scaley = 1., val = 0.;
-    for (int i = 0; i <= p.y_order; i++, scaley *= yval) {
+    for (int i = 0; i <= p.y_order; i++) {
+        if (i > 0) scaley = i == 1 ? yval : scaley * yval;
         double scalex = 1.;
-        for (int j = 0; j <= p.x_order; j++, scalex *= xval) val += scalex * scaley * p.c[i * (p.x_order + 1) + j];
+        for (int j = 0; j <= p.x_order; j++) {
+            if (j > 0) scalex = j == 1 ? xval : scalex * xval;
+            const double sc = j == 0 ? scaley : (i == 0 ? scalex : scalex * scaley);
+            val += sc * p.c[i * (p.x_order + 1) + j];
+        }
     }
     return val;
 }
