@@ -570,9 +570,36 @@ struct FitNodes {
 };
 
 struct FitWeights {
-    double x[GBX][4];          // Lagrange weights of the column nodes
+    double xs[GBX];            // column / (GBX - 1), the variable of the per-line cubic
+    double m[3][3];            // column-node differences -> cubic coefficients 1..3
     double y8[8][4], y16[16][4], y32[32][4];
 };
+
+// Inverse of V[i][k] = x_i^(k+1) (i, k = 0..2) for the three column nodes
+// after the first, x_i = node / (GBX - 1): the cubic through the node
+// values g_0..g_3 of one line is g_0 + c1 x + c2 x^2 + c3 x^3 with
+// c = V^-1 (g_1 - g_0, g_2 - g_0, g_3 - g_0).
+constexpr void fit_cubic_matrix(double (&m)[3][3]) {
+    const FitNodes<GBX> nd;
+    double v[3][3] = {};
+    for (int i = 0; i < 3; ++i) {
+        const double x = (double)nd.v[i + 1] / (double)(GBX - 1);
+        v[i][0] = x;
+        v[i][1] = x * x;
+        v[i][2] = x * x * x;
+    }
+    const double det = v[0][0] * (v[1][1] * v[2][2] - v[1][2] * v[2][1]) -
+                       v[0][1] * (v[1][0] * v[2][2] - v[1][2] * v[2][0]) +
+                       v[0][2] * (v[1][0] * v[2][1] - v[1][1] * v[2][0]);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            // cofactor of v[j][i] (transposed), over det
+            const int r0 = j == 0 ? 1 : 0, r1 = j == 2 ? 1 : 2;
+            const int c0 = i == 0 ? 1 : 0, c1 = i == 2 ? 1 : 2;
+            const double minor = v[r0][c0] * v[r1][c1] - v[r0][c1] * v[r1][c0];
+            m[i][j] = (((i + j) & 1) ? -minor : minor) / det;
+        }
+}
 
 template <int N>
 constexpr void fit_weights(double (&w)[N][4]) {
@@ -588,7 +615,8 @@ constexpr void fit_weights(double (&w)[N][4]) {
 
 constexpr FitWeights make_fit_weights() {
     FitWeights f{};
-    fit_weights<GBX>(f.x);
+    for (int t = 0; t < GBX; ++t) f.xs[t] = (double)t / (double)(GBX - 1);
+    fit_cubic_matrix(f.m);
     fit_weights<8>(f.y8);
     fit_weights<16>(f.y16);
     fit_weights<32>(f.y32);
@@ -685,13 +713,26 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
         for (int n = 1; n < 16; ++n) fit = fit && s_nb[n] == s_nb[0];
         if (fit) {
             // the node values reduced over the line nodes, per tile line:
-            // G[r][q][i] = sum_j F[j][i][q] * wy[r][j]
-            for (int idx = tid; idx < TY * FIT_Q * 4; idx += GBX * GBY) {
-                const int r = idx / (FIT_Q * 4), q = (idx >> 2) % FIT_Q, i = idx & 3;
-                double g = 0.0;
+            // g_i = sum_j F[j][i][q] * wy[r][j] at the four column nodes, then
+            // the line's cubic in x = column / (GBX - 1):
+            // G[r][q] = (g_0, c1, c2, c3), c = m (g_1 - g_0, g_2 - g_0, g_3 - g_0).
+            // The differences are exact (Sterbenz) for the slowly varying
+            // quantities, so a pixel's value rounds once at its magnitude.
+            for (int idx = tid; idx < TY * FIT_Q; idx += GBX * GBY) {
+                const int r = idx / FIT_Q, q = idx % FIT_Q;
+                double g[4];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) g = fma(s_F[j * 4 + i][q], fit_wy<TY>(r, j), g);
-                s_G[r][q][i] = g;
+                for (int i = 0; i < 4; ++i) {
+                    double a = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) a = fma(s_F[j * 4 + i][q], fit_wy<TY>(r, j), a);
+                    g[i] = a;
+                }
+                const double d1 = g[1] - g[0], d2 = g[2] - g[0], d3 = g[3] - g[0];
+                s_G[r][q][0] = g[0];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    s_G[r][q][k + 1] = fma(c_fit.m[k][0], d1, fma(c_fit.m[k][1], d2, c_fit.m[k][2] * d3));
             }
             __syncthreads();
         }
@@ -746,11 +787,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
     }
     if (pixel >= p.gw) return;
     const double* seg = stage_ready(st, p) ? st.buf : p.orbit.seg;
-    double wx[4];
-    if (fit) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) wx[i] = c_fit.x[tx][i];
-    }
+    const double xs = c_fit.xs[tx];
 #pragma unroll 1
     for (int kk = 0; kk < PPT; ++kk) {
         const int r = ty + GBY * kk;       // tile line
@@ -763,7 +800,7 @@ __device__ __forceinline__ void geocode_block(const GeoParams& p, int bx, int by
             double f[FIT_Q];
 #pragma unroll
             for (int q = 0; q < FIT_Q; ++q)
-                f[q] = fma(s_G[r][q][0], wx[0], fma(s_G[r][q][1], wx[1], fma(s_G[r][q][2], wx[2], s_G[r][q][3] * wx[3])));
+                f[q] = fma(fma(fma(s_G[r][q][3], xs, s_G[r][q][2]), xs, s_G[r][q][1]), xs, s_G[r][q][0]);
             double h = 0.0;
             if (p.dem.have_raster && (s_nb[0] & 3) != 3) h = dem_height<RASTER>(p.dem, f[0], f[1]);
             xyz = {fma(h, f[5], f[2]), fma(h, f[6], f[3]), fma(h, f[7], f[4])};
