@@ -1102,18 +1102,69 @@ __device__ __forceinline__ double carrier_at(const AzRg& f, const CarrierLine& c
 
 // geocodeSlc.cpp:240-274: rdr *= exp(-i * float(rg_carrier + az_carrier)),
 // the FP64 phase bit-for-bit in the reference's order, so that its float
-// rounding agrees.  Grid: x covers a line in chunks of 4 * blockDim.x
-// samples, y the lines.
-__device__ __forceinline__ bool carrier_line_constant(const AzRg& f) {
+// rounding agrees.  Grid: x covers a line in chunks of 1024 samples, y the
+// lines (per-sample carriers) or tiles of DR_LINES lines (line-constant).
+__host__ __device__ __forceinline__ bool carrier_line_constant(const AzRg& f) {
     return f.is_zero || (f.kind == 1 && f.poly.x_order == 0);
 }
 
+// e^(-i phase) of line i of the block (both carriers constant along lines)
+__device__ __forceinline__ float2 deramp_line_phasor(const DerampParams& p, int64_t i) {
+    const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
+    const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
+    const float phase = (float)dadd(lr.mode ? lr.val : 0.0, la.mode ? la.val : 0.0);
+    float sn, cs;
+    sincosf(phase, &sn, &cs);
+    return make_float2(cs, -sn);
+}
+
+// Carriers constant along lines: tiles of DR_LINES lines x 1024 samples per
+// block.  Lane l of every warp forms the phasor of the tile's line l (the
+// FP64 carrier and its float phase, as the per-sample form), so the
+// phasors of 32 lines cost one evaluation's latency; each warp then streams
+// its 128-sample slice of the tile's lines, four lines' loads in flight
+// before their stores (in place, each sample is read and written by one
+// thread).
+constexpr int DR_LINES = 32;
+
+__global__ void __launch_bounds__(256) deramp_lines_kernel(const __grid_constant__ DerampParams p) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t c0 = (int64_t)blockIdx.x * 1024 + warp * 128 + lane;
+    for (int64_t i0 = (int64_t)blockIdx.y * DR_LINES; i0 < p.inL; i0 += (int64_t)gridDim.y * DR_LINES) {
+        const float2 rot_l = i0 + lane < p.inL ? deramp_line_phasor(p, i0 + lane) : make_float2(1.f, 0.f);
+        const int nl = (int)(p.inL - i0 < DR_LINES ? p.inL - i0 : DR_LINES);
+        for (int l0 = 0; l0 < nl; l0 += 4) {
+            float2 v[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int64_t i = i0 + l0 + a;
+                const float2* src = p.src + i * p.inW;
+                const __half2* src16 = reinterpret_cast<const __half2*>(p.src) + i * p.inW;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t j = c0 + 32 * u;
+                    v[a][u] = (l0 + a < nl && j < p.inW) ? (p.src_c32 ? ld_sample(src16 + j) : __ldg(src + j))
+                                                         : make_float2(0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float2 rot = make_float2(__shfl_sync(0xffffffffu, rot_l.x, l0 + a),
+                                               __shfl_sync(0xffffffffu, rot_l.y, l0 + a));
+                if (l0 + a >= nl) break;
+                float2* dst = p.dst + (i0 + l0 + a) * p.inW;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t j = c0 + 32 * u;
+                    if (j < p.inW) dst[j] = cmul(v[a][u], rot);
+                }
+            }
+        }
+    }
+}
+
+// Carriers that vary along lines: one phase per sample.
 __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ DerampParams p) {
-    __shared__ float2 s_rot;
-    // carriers constant along each line (zero, or azimuth-only polynomials):
-    // the line's phasor is formed once per block and line, the same value the
-    // per-sample form gives, so the pass streams at HBM rate
-    const bool line_const = carrier_line_constant(p.rg_car) && carrier_line_constant(p.az_car);
     for (int64_t i = blockIdx.y; i < p.inL; i += gridDim.y) {
         const float2* src = p.src + i * p.inW;
         const __half2* src16 = reinterpret_cast<const __half2*>(p.src) + i * p.inW;
@@ -1124,25 +1175,6 @@ __global__ void __launch_bounds__(256) deramp_kernel(const __grid_constant__ Der
         for (int u = 0; u < 4; ++u) {     // loads first: four samples in flight per thread
             const int64_t j = j0 + (int64_t)u * blockDim.x;
             v[u] = j < p.inW ? (p.src_c32 ? ld_sample(src16 + j) : __ldg(src + j)) : make_float2(0.f, 0.f);
-        }
-        if (line_const) {
-            if (threadIdx.x == 0) {
-                const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
-                const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
-                const float phase = (float)dadd(lr.mode ? lr.val : 0.0, la.mode ? la.val : 0.0);
-                float sn, cs;
-                sincosf(phase, &sn, &cs);
-                s_rot = make_float2(cs, -sn);
-            }
-            __syncthreads();
-            const float2 rot = s_rot;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t j = j0 + (int64_t)u * blockDim.x;
-                if (j < p.inW) dst[j] = cmul(v[u], rot);
-            }
-            __syncthreads();              // s_rot is rewritten for the next line
-            continue;
         }
         const double az = dadd(p.rg_t0, ddiv((double)(i + p.az_first), p.rg_prf));
         const CarrierLine lr = carrier_line(p.rg_car, az), la = carrier_line(p.az_car, az);
@@ -1326,6 +1358,13 @@ cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits
 
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches) {
     const int64_t chunks = (p.inW + 1023) / 1024;
+    if (carrier_line_constant(p.rg_car) && carrier_line_constant(p.az_car)) {
+        const int64_t tiles = (p.inL + DR_LINES - 1) / DR_LINES;
+        if (chunks < 1 || tiles < 1) return cudaSuccess;
+        deramp_lines_kernel<<<dim3((unsigned)chunks, (unsigned)(tiles < 65535 ? tiles : 65535)), 256, 0, s>>>(p);
+        if (launches) ++*launches;
+        return cudaGetLastError();
+    }
     const int64_t lines = p.inL < 65535 ? p.inL : 65535;
     if (chunks < 1 || lines < 1) return cudaSuccess;
     deramp_kernel<<<dim3((unsigned)chunks, (unsigned)lines), 256, 0, s>>>(p);
