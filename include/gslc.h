@@ -203,6 +203,20 @@ int gslc_sinc_table(float* out);
  * python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:218-334). */
 int gslc_geocode_slc(gslc_ctx* ctx, const gslc_geocode_args* args, void* stream);
 
+/* gslc_geocode_slc with the results delivered to host memory: args' geo
+ * blocks and mask (device) are filled as gslc_geocode_slc fills them, and
+ * each geo block (geo_format's bytes per pixel) and the mask (if host_mask
+ * and args->mask are set) are also copied to host_geo_blocks[b] and
+ * host_mask.  The geogrid runs in row bands whose copies proceed on a
+ * context-owned stream while the next bands compute; results are those of
+ * gslc_geocode_slc bit for bit (band edges fall on tile edges).  Returns
+ * after the copies completed.  Page-locked host buffers let the copies
+ * overlap; pageable ones are copied too, without overlap.  Serves the same
+ * reference call as gslc_geocode_slc (geocodeSlc.cpp:831-968, whose
+ * outputs are host arrays) for callers holding host outputs. */
+int gslc_geocode_slc_to_host(gslc_ctx* ctx, const gslc_geocode_args* args, void* const* host_geo_blocks,
+                             uint8_t* host_mask, void* stream);
+
 /* carrierPhaseDeramp (cxx/isce3/geocode/geocodeSlc.cpp:240-274) on its own:
  * dst = src * exp(-i float(rg_carrier(t, r) + az_carrier(t, r))) for a
  * length x width block starting at (first_line, first_sample) of radar_grid.

@@ -192,6 +192,8 @@ _EXPORTS = {
     "gslc_compute_dem_window_block": (C.c_int, [C.POINTER(DemRaster), C.POINTER(GeoGrid), C.c_int32, C.c_int32,
                                                 C.c_int32, C.c_int32, C.POINTER(DemWindow)]),
     "gslc_geocode_slc": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.c_void_p]),
+    "gslc_geocode_slc_to_host": (C.c_int, [C.c_void_p, C.POINTER(GeocodeArgs), C.POINTER(C.c_void_p),
+                                           C.c_void_p, C.c_void_p]),
     "gslc_geocode_rasters": (C.c_int, [C.c_void_p, C.POINTER(RasterGeocodeArgs), C.c_void_p]),
     "gslc_last_launch_count": (C.c_int64, [C.c_void_p]),
     "gslc_orbit_interpolate": (C.c_int, [C.POINTER(OrbitDesc), C.c_double, C.POINTER(C.c_double),

@@ -15,6 +15,9 @@
 
 using namespace gslc;
 
+// row bands of gslc_geocode_slc_to_host (copies of a band overlap the next bands' kernels)
+constexpr int GSLC_HOST_BANDS = 4;
+
 struct gslc_ctx {
     int device = 0;
     float* d_sinc = nullptr;        // SINC_SUB * SINC_LEN
@@ -28,6 +31,8 @@ struct gslc_ctx {
     float ms_geocode = 0.f, ms_deramp = 0.f;
     int cube_passes = 0;            // passes of the last gslc_make_radar_grid_cubes
     double* d_sinc64 = nullptr;     // the sinc table in double (raster interpolation), on first use
+    cudaStream_t copy_stream = nullptr;   // device-to-host copies of gslc_geocode_slc_to_host, on first use
+    cudaEvent_t band_ev[GSLC_HOST_BANDS + 1] = {};
     std::string err;
 };
 
@@ -662,6 +667,9 @@ extern "C" int gslc_ctx_destroy(gslc_ctx* c) {
     if (c->d_sinc64) cudaFree(c->d_sinc64);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->band_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     delete c;
     return GSLC_OK;
 }
@@ -836,11 +844,21 @@ void bind_orbit(GeoParams& p, const double* d_coef) {
 
 }  // namespace
 
-extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream_) {
+namespace {
+
+// bytes per output pixel of the geo blocks in format f (gslc_geocode_args.geo_format)
+size_t geo_pixel_bytes(int f) { return f == 1 ? 4 : 8; }
+
+// gslc_geocode_slc, and with host_geo set the copies of the geo blocks (and
+// of the mask, with host_mask) to host memory: the geogrid runs in row bands
+// whose boundaries are multiples of every tile height (so every tile, and
+// every pixel's value, is the one of the single launch), each band's copies
+// queued on the context's copy stream behind its kernels.
+int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t stream, void* const* host_geo,
+                     uint8_t* host_mask) {
     if (!c) return GSLC_EINVAL;
     c->err.clear();
     c->launches = 0;
-    cudaStream_t stream = (cudaStream_t)stream_;
     GeoParams p;
     std::vector<double> coef;
     int st = prepare_geocode(c, a, p, coef);
@@ -904,14 +922,58 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
         cudaEventRecord(c->ev[3], stream);
         cudaEventRecord(c->ev[0], stream);
     }
-    for (int b0 = 0; b0 < a->n_blocks; b0 += MAX_BLOCKS) {
-        p.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
-        for (int b = 0; b < p.nblk; ++b) {
-            p.rdr[b] = rdr[b0 + b];
-            p.geo[b] = (float2*)a->geo_blocks[b0 + b];
+    const int64_t gl = p.gl, gw = p.gw;
+    int nband = 1;
+    int64_t band_rows = gl;
+    if (host_geo) {
+        if (!c->copy_stream) {
+            e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) { c->copy_stream = nullptr; return cuda_err(c, e, "copy stream"); }
         }
-        e = launch_geocode(p, a->geo2rdr_precision, stream, &c->launches);
-        if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
+        for (auto& ev : c->band_ev)
+            if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+                ev = nullptr;
+                return cuda_err(c, e, "band event");
+            }
+        band_rows = ((gl + GSLC_HOST_BANDS - 1) / GSLC_HOST_BANDS + 31) / 32 * 32;
+        nband = (int)((gl + band_rows - 1) / band_rows);
+    }
+    const size_t esz = geo_pixel_bytes(a->geo_format);
+    for (int band = 0; band < nband; ++band) {
+        const int64_t row0 = (int64_t)band * band_rows;
+        const int64_t rows = std::min(band_rows, gl - row0);
+        const int64_t off = row0 * gw;
+        p.geo_row0 = row0;
+        p.gl = rows;
+        p.mask = a->mask ? a->mask + off : nullptr;
+        p.carrier_out = a->carrier_phase ? a->carrier_phase + off : nullptr;
+        p.flatten_out = a->flatten_phase ? a->flatten_phase + off : nullptr;
+        p.az_out = a->az_index ? a->az_index + off : nullptr;
+        p.rg_out = a->rg_index ? a->rg_index + off : nullptr;
+        for (int b0 = 0; b0 < a->n_blocks; b0 += MAX_BLOCKS) {
+            p.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
+            for (int b = 0; b < p.nblk; ++b) {
+                p.rdr[b] = rdr[b0 + b];
+                p.geo[b] = (float2*)((char*)a->geo_blocks[b0 + b] + off * esz);
+            }
+            e = launch_geocode(p, a->geo2rdr_precision, stream, &c->launches);
+            if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
+        }
+        if (!host_geo) continue;
+        e = cudaEventRecord(c->band_ev[band], stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->band_ev[band], 0);
+        for (int b = 0; b < a->n_blocks && e == cudaSuccess; ++b)
+            e = cudaMemcpyAsync((char*)host_geo[b] + off * esz, (const char*)a->geo_blocks[b] + off * esz,
+                                (size_t)(rows * gw) * esz, cudaMemcpyDeviceToHost, c->copy_stream);
+        if (e == cudaSuccess && host_mask && a->mask)
+            e = cudaMemcpyAsync(host_mask + off, a->mask + off, (size_t)(rows * gw), cudaMemcpyDeviceToHost,
+                                c->copy_stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "band copy");
+    }
+    if (host_geo) {
+        e = cudaEventRecord(c->band_ev[GSLC_HOST_BANDS], c->copy_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, c->band_ev[GSLC_HOST_BANDS], 0);
+        if (e != cudaSuccess) return cuda_err(c, e, "band copy");
     }
     if (c->timing) cudaEventRecord(c->ev[1], stream);
     for (void* s : scratch) cudaFreeAsync(s, stream);
@@ -925,6 +987,22 @@ extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* s
     if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
     if (c->h_err[0] & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
     return GSLC_OK;
+}
+
+}  // namespace
+
+extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream) {
+    return geocode_slc_impl(c, a, (cudaStream_t)stream, nullptr, nullptr);
+}
+
+extern "C" int gslc_geocode_slc_to_host(gslc_ctx* c, const gslc_geocode_args* a, void* const* host_geo_blocks,
+                                        uint8_t* host_mask, void* stream) {
+    if (!c) return GSLC_EINVAL;
+    if (!a || !host_geo_blocks) return set_err(c, GSLC_EINVAL, "null arguments");
+    const bool empty = (int64_t)a->geo_grid.length * a->geo_grid.width <= 0;   // nothing to copy
+    for (int b = 0; b < a->n_blocks && !empty; ++b)
+        if (!host_geo_blocks[b]) return set_err(c, GSLC_EINVAL, "null host geo block");
+    return geocode_slc_impl(c, a, (cudaStream_t)stream, host_geo_blocks, host_mask);
 }
 
 // ---- raster geocoder (cuda/geocode/Geocode.cu:652-864) --------------------

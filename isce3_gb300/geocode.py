@@ -386,8 +386,23 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
 
 def _geocode_on_stream(lib, ctx, s, dev, *args):
     a, outs, keep = _build_args(dev, *args)
-    st = lib.gslc_geocode_slc(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
-    L.check(st, ctx, "geocode_slc")
-    for o in outs:
-        o.copy_back()
+    geo = keep[2]
+    if all(g.host is not None for g in geo):
+        # host geo blocks (and mask): the library copies them back band by
+        # band while later bands compute
+        mask = next((o for o in outs if a.mask and o.ptr() == a.mask and o.host is not None), None)
+        host_ptrs = (C.c_void_p * len(geo))(*[g.host.data_ptr() for g in geo])
+        st = lib.gslc_geocode_slc_to_host(ctx, C.byref(a), host_ptrs,
+                                          C.c_void_p(mask.host.data_ptr() if mask else None),
+                                          C.c_void_p(s.cuda_stream))
+        L.check(st, ctx, "geocode_slc")
+        done = set(map(id, geo)) | ({id(mask)} if mask else set())
+        for o in outs:
+            if id(o) not in done:
+                o.copy_back()
+    else:
+        st = lib.gslc_geocode_slc(ctx, C.byref(a), C.c_void_p(s.cuda_stream))
+        L.check(st, ctx, "geocode_slc")
+        for o in outs:
+            o.copy_back()
     del keep

@@ -101,6 +101,37 @@ def test_c1_device_tensors_match_host_arrays(c1):
     np.testing.assert_array_equal(dev_in.cpu().numpy(), c1.slc)   # input not mutated
 
 
+@pytest.mark.parametrize("pinned", [False, True])
+def test_utm_host_outputs_equal_device_outputs(pinned):
+    """Host geo blocks and mask, copied back by the library in row bands while
+    later bands compute (gslc_geocode_slc_to_host), equal the device outputs
+    of one launch bit for bit: a ragged last band, two blocks, carriers."""
+    sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0)
+    g = sc.geogrid
+    shape = (g.length, g.width)
+    common = (sc.dem, sc.radar_grid, g, sc.orbit, sc.native_doppler, sc.image_grid_doppler, sc.ellipsoid,
+              sc.threshold, sc.maxiter)
+    kw = dict(az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    slc2 = (sc.slc * np.complex64(0.5 - 0.25j)).astype(np.complex64)
+    if pinned:
+        host = [torch.zeros(shape, dtype=torch.complex64).pin_memory() for _ in range(2)]
+        hmask = torch.zeros(shape, dtype=torch.uint8).pin_memory()
+    else:
+        host = [np.zeros(shape, np.complex64) for _ in range(2)]
+        hmask = np.zeros(shape, np.uint8)
+    geocode_slc(host, [sc.slc, slc2], *common, mask_block=hmask, **kw)
+    dev = [torch.zeros(shape, dtype=torch.complex64, device="cuda") for _ in range(2)]
+    dmask = torch.zeros(shape, dtype=torch.uint8, device="cuda")
+    geocode_slc(dev, [torch.from_numpy(sc.slc).cuda(), torch.from_numpy(slc2).cuda()], *common,
+                mask_block=dmask, **kw)
+    dm = dmask.cpu().numpy()
+    assert (dm == 1).sum() > 100000
+    for h, d in zip(host, dev):
+        hn = h.numpy() if pinned else h
+        np.testing.assert_array_equal(d.cpu().numpy().view(np.uint64), hn.view(np.uint64))
+    np.testing.assert_array_equal(dm, hmask.numpy() if pinned else hmask)
+
+
 def test_c1_doppler_carriers_corrections_blocks(oracle_mod, c1):
     """Squinted grid (image-grid Doppler = native), Poly2d carriers, correction
     LUTs, two blocks of a radar sub-block with offsets, flatten with the
