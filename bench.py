@@ -49,7 +49,6 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gslc", "reference"], default="gslc")
     p.add_argument("--workload", choices=["frame", "medium", "small"], default="frame")
-    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the burst (batched vs plain) measurement")
@@ -178,23 +177,23 @@ def run_oracle_sample(oracle, sc, g, box, outputs=False):
     return dt, phases, dict(geo=geo, mask=mask, az=az, rg=rg)
 
 
-def calibrate_rows(oracle, sc, target_s, max_rows=None):
-    """Geogrid rows (centred) whose oracle run takes about target_s seconds."""
-    max_rows = max_rows or sc.geogrid.length
-    mid = sc.geogrid.length // 2
-    rows = 4
-    g, box = sample_rows_block(oracle, sc, mid - rows // 2, rows)
-    dt, _, _ = run_oracle_sample(oracle, sc, g, box)
-    rows = int(np.clip(rows * target_s / max(dt, 1e-3), 4, max_rows))
-    row0 = max(0, min(mid - rows // 2, sc.geogrid.length - rows))
-    g, box = sample_rows_block(oracle, sc, row0, rows)
-    return row0, rows, g, box
+def cpu_sample_rows(sc, steps: int, warmup: int):
+    """Geogrid rows of both CPU timings (the cpu_baseline leg and the
+    reference arm): the whole geogrid when at most 12 oracle runs are timed,
+    else its centred half, so that the reference arm's warm-up and timed
+    steps end within about two minutes on the frame."""
+    n = sc.geogrid.length
+    if steps + warmup <= 12:
+        return 0, n
+    rows = n // 2
+    return (n - rows) // 2, rows
 
 
-def cpu_baseline(sc, target_s):
+def cpu_baseline(sc, steps: int, warmup: int):
     from oracle import oracle
     oracle.build()
-    row0, rows, g, box = calibrate_rows(oracle, sc, target_s)
+    row0, rows = cpu_sample_rows(sc, steps, warmup)
+    g, box = sample_rows_block(oracle, sc, row0, rows)
     dt, phases, out = run_oracle_sample(oracle, sc, g, box, outputs=True)
     npx = g.length * g.width
     info = {"value": npx / dt, "unit": UNIT, "cores": oracle.ncores(), "kind": "port",
@@ -203,6 +202,12 @@ def cpu_baseline(sc, target_s):
             "phase_seconds": {"index": phases[0], "deramp": phases[1], "interpolate": phases[2],
                               "reramp": phases[3]},
             "arch": os.uname().machine}
+    if rows < sc.geogrid.length:
+        # the whole frame once as well (the DEM window and blocks as one call)
+        gw, boxw = sample_rows_block(oracle, sc, 0, sc.geogrid.length)
+        dtw = run_oracle_sample(oracle, sc, gw, boxw)[0]
+        info["whole_frame"] = {"value": gw.length * gw.width / dtw, "seconds": dtw,
+                               "sample": f"all {gw.length} geogrid rows with the radar block they need"}
     return info, (row0, rows, box, out)
 
 
@@ -321,22 +326,16 @@ def run_gpu(args, rank, world):
     return sc, res
 
 
-PROFILE = ROOT / "profiles" / "geocode_kernel_medium.md"
+PROFILE = ROOT / "profiles" / "geocode_kernel_medium.json"
 
 
 def profile_per_px() -> dict:
     """Per-output-pixel figures of the committed ncu capture of the fused
-    kernel on the medium workload (lines "name: value" at its end)."""
-    vals = {}
-    if PROFILE.exists():
-        for line in PROFILE.read_text().splitlines():
-            k, _, v = line.partition(":")
-            if k.endswith("_per_output_px") and v.strip():
-                try:
-                    vals[k.strip()] = float(v)
-                except ValueError:
-                    pass
-    return vals
+    kernel on the medium workload: {"<name>_per_output_px": value}."""
+    if not PROFILE.exists():
+        return {}
+    d = json.loads(PROFILE.read_text())
+    return {f"{k}_per_output_px": float(v) for k, v in d.get("per_output_px", {}).items()}
 
 
 def fp64_roofline(prof_vals: dict, variant: str, npx: int, kernel_ms: float, peak_gflops: float) -> dict:
@@ -487,8 +486,10 @@ def run_bursts(args):
 
 
 def run_serving(args):
-    """Poisson arrivals (200 req/s) of geocode requests over 8 resident SLCs:
-    continuous-batching server against the plain per-request path."""
+    """Geocode requests over 8 resident SLCs, continuous-batching server
+    against the plain per-request path, on two traces of the same requests:
+    Poisson arrivals at 200 req/s (bound by the arrival rate) and every
+    request arriving at t = 0 (saturated: throughput is the GPU's)."""
     import torch
     from isce3_gb300 import synth
     from isce3_gb300.serve import GeocodeServer, ResidentStore, ServeRequest, serve_plain
@@ -509,18 +510,21 @@ def run_serving(args):
     out = {"slcs": len(sc.slcs), "resident_bytes": store.nbytes, "requests": n_req, "rate_hz": 200.0,
            "side_px": [256, 4096], "spacing_m": [10, 30], "budget_bytes": 150 * 10 ** 9,
            "slc_shapes": [list(s_.radar_grid.shape) for s_ in sc.slcs]}
+    traces = {"poisson_200hz": trace, "saturated_t0": [(k, g, 0.0) for k, g, _t in trace]}
     for prec in ("fp64", "ff"):
         warm_server = GeocodeServer(store, geo2rdr_precision=prec)
         warm_server.serve([ServeRequest(k, g, t) for k, g, t in warm])
         warm_server.close()
         serve_plain(store, [ServeRequest(k, g, t) for k, g, t in warm], prec)
-        server = GeocodeServer(store, budget_bytes=150 * 10 ** 9, max_in_flight=3, max_batch=64,
-                               geo2rdr_precision=prec, per_request_completion=True)
-        served = server.serve([ServeRequest(k, g, t) for k, g, t in trace])
-        server.close()
-        plain = serve_plain(store, [ServeRequest(k, g, t) for k, g, t in trace], prec)
-        out[prec] = {"served": served, "plain": plain,
-                     "px_per_s_ratio": served["px_per_s"] / plain["px_per_s"] if plain["px_per_s"] else None}
+        out[prec] = {}
+        for name, tr in traces.items():
+            server = GeocodeServer(store, budget_bytes=150 * 10 ** 9, max_in_flight=3, max_batch=64,
+                                   geo2rdr_precision=prec, per_request_completion=True)
+            served = server.serve([ServeRequest(k, g, t) for k, g, t in tr])
+            server.close()
+            plain = serve_plain(store, [ServeRequest(k, g, t) for k, g, t in tr], prec)
+            out[prec][name] = {"served": served, "plain": plain,
+                               "px_per_s_ratio": served["px_per_s"] / plain["px_per_s"] if plain["px_per_s"] else None}
     return out
 
 
@@ -694,8 +698,8 @@ def run_reference(args, rank, world):
     from oracle import oracle
     oracle.build()
     sc = make_scene(args.workload)
-    target = max(1.0, min(args.cpu_seconds, 120.0 / max(args.steps + args.warmup, 1)))
-    row0, rows, g, box = calibrate_rows(oracle, sc, target)
+    row0, rows = cpu_sample_rows(sc, args.steps, args.warmup)
+    g, box = sample_rows_block(oracle, sc, row0, rows)
     for _ in range(args.warmup):
         run_oracle_sample(oracle, sc, g, box)
     times = [run_oracle_sample(oracle, sc, g, box)[0] for _ in range(args.steps)]
@@ -740,7 +744,7 @@ def main():
     cpu, par = None, None
     par_ff = None
     if not args.no_cpu:
-        cpu, (row0, rows, box, out) = cpu_baseline(sc, args.cpu_seconds)
+        cpu, (row0, rows, box, out) = cpu_baseline(sc, args.steps, args.warmup)
         par = parity_sample(res, row0, rows, box, out)
         par_ff = parity_sample(res["ff"], row0, rows, box, out)
     batched = None

@@ -217,6 +217,21 @@ int gslc_geocode_slc(gslc_ctx* ctx, const gslc_geocode_args* args, void* stream)
 int gslc_geocode_slc_to_host(gslc_ctx* ctx, const gslc_geocode_args* args, void* const* host_geo_blocks,
                              uint8_t* host_mask, void* stream);
 
+/* Raster mode of geocodeSlc (geocode/geocodeSlc.cpp:605-828 and
+ * python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:26-102, whose
+ * rasters are GDAL datasets): rdr_blocks are the input raster's bands over
+ * the whole radar grid (rdr_length x rdr_width = the grid, first_azimuth_line
+ * and first_range_sample 0), geo_blocks the output raster's bands over the
+ * whole geogrid, carrier_phase / flatten_phase optional output rasters.  The
+ * geogrid is processed in blocks of lines_per_block lines (the reference's
+ * default is 1000), each with the DEM window of that block alone
+ * (DEMRasterToInterpolator with the block's lines, :653-656); pixels without
+ * a result hold invalid_value and the phase rasters invalid_value's real
+ * part.  The DEM samples must cover every block's window.  A mask, when
+ * given, is written as in array mode (the reference's raster mode has
+ * none).  Synchronises the stream. */
+int gslc_geocode_slc_raster(gslc_ctx* ctx, const gslc_geocode_args* args, int32_t lines_per_block, void* stream);
+
 /* carrierPhaseDeramp (cxx/isce3/geocode/geocodeSlc.cpp:240-274) on its own:
  * dst = src * exp(-i float(rg_carrier(t, r) + az_carrier(t, r))) for a
  * length x width block starting at (first_line, first_sample) of radar_grid.
@@ -304,6 +319,18 @@ int64_t gslc_last_launch_count(const gslc_ctx* ctx);
  * gslc_last_kernel_ms reads their durations after the call returns. */
 int gslc_ctx_set_timing(gslc_ctx* ctx, int32_t enable);
 int gslc_last_kernel_ms(const gslc_ctx* ctx, float* geocode_ms, float* deramp_ms);
+
+/* Failure handling of the one device-side wait: each block of the fused and
+ * persistent kernels copies the orbit's Newton tables into shared memory
+ * (cp.async.bulk, an mbarrier counting the bytes) and every thread waits for
+ * them at most `clocks` SM clocks (default, and for clocks <= 0: 2^31,
+ * about a second).  A thread whose wait runs out reads the tables from
+ * global memory instead, so the outputs stay complete and identical, and
+ * the call returns GSLC_ETIMEOUT; before a block finishes one thread waits
+ * (bounded) for its copy still in flight.  No counterpart in the reference,
+ * whose kernels do not stage (cuda/geocode/Geocode.cu:87-287); the setting
+ * exists so that the failure path can be exercised. */
+int gslc_ctx_set_stage_wait(gslc_ctx* ctx, int64_t clocks);
 
 /* Measurement: sustained FP64 FMA rate of this GPU (GFLOP/s, 2 flops per
  * FMA) from a dependent-chain DFMA loop over all SMs; the denominator of the
@@ -466,17 +493,21 @@ int gslc_last_cube_passes(const gslc_ctx* ctx);
  * arguments, kernels and results as gslc_geocode_slc, but no context: its
  * scratch lives in file-scope device arrays of the library (about 32.4 MiB
  * per GPU that loads it, held until exit):
- *  - the deramped copy of the radar blocks when carriers are present and
- *    inplace_deramp is 0: at most 4194304 complex samples over all blocks;
+ *  - the deramped copy of the radar blocks (complex64, written by the
+ *    deramp straight from the caller's complex64 or complex32 blocks) when
+ *    carriers are present and inplace_deramp is 0: at most 4194304 complex
+ *    samples over all blocks;
  *  - orbit polynomials for at most 256 state vectors; the sinc table; an
  *    error word cleared by every call.
  * Larger inputs are rejected with GSLC_EINVAL and a message in errbuf.  It
  * calls no cudaMalloc, cudaFree or other allocating routine.  The first call
  * on a device (the current one) looks up the arrays' device addresses and
  * uploads the sinc table synchronously, so make it before any stream
- * capture.  All calls share the arrays: calls that overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * errbuf (may be NULL) receives the error message, errbuf_len bytes at most. */
+ * capture.  Like gslc_geocode_slc, every call synchronises `stream` before
+ * it returns (it reads the error word back).  All calls share the arrays:
+ * calls that overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  errbuf (may be NULL) receives the error
+ * message, errbuf_len bytes at most. */
 int gslc_geocode_slc_noalloc(const gslc_geocode_args* args, void* stream, char* errbuf, size_t errbuf_len);
 
 #ifdef __cplusplus

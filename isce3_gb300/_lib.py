@@ -206,6 +206,8 @@ _EXPORTS = {
     "gslc_truncate_mantissa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p]),
     "gslc_sinc_table": (C.c_int, [C.c_void_p]),
     "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gslc_ctx_set_stage_wait": (C.c_int, [C.c_void_p, C.c_int64]),
+    "gslc_geocode_slc_raster": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),
@@ -270,7 +272,12 @@ def lib() -> C.CDLL:
 
 
 class GslcError(RuntimeError):
-    pass
+    """A CUDA error (GSLC_ECUDA) or a device-side wait that ran out
+    (GSLC_ETIMEOUT); ``status`` holds the C-ABI code."""
+
+    def __init__(self, msg: str, status: int = GSLC_ECUDA):
+        super().__init__(msg)
+        self.status = status
 
 
 def check(status: int, ctx=None, what: str = "gslc") -> None:
@@ -283,10 +290,18 @@ def check(status: int, ctx=None, what: str = "gslc") -> None:
         raise ValueError(msg)
     if status == GSLC_EUNSUPPORTED:
         raise NotImplementedError(msg)
-    raise GslcError(msg)
+    raise GslcError(msg, status)
 
 
 _ctx_local = threading.local()
+
+
+def set_stage_wait(clocks: int, device: int = 0) -> None:
+    """SM clocks each thread waits for the orbit tables' copy into shared
+    memory (gslc_ctx_set_stage_wait) on this thread's context of ``device``;
+    0 restores the default (2^31)."""
+    ctx = context(device)
+    check(lib().gslc_ctx_set_stage_wait(ctx, int(clocks)), ctx, "gslc_ctx_set_stage_wait")
 
 
 def context(device: int = 0) -> C.c_void_p:

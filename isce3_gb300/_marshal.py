@@ -104,6 +104,8 @@ def orbit_desc(o: Orbit) -> L.OrbitDesc:
 def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.device):
     """Descriptor with only the DEM window of ``geogrid`` resident on ``dev``
     (or the whole raster, when ``raster.to_device`` made it resident)."""
+    if raster.data.ndim != 2:
+        raise ValueError("a DEM raster has one band")
     res = getattr(raster, "resident", None)
     if res is not None and res.device == dev:
         return dem_raster_desc_resident(res, raster.get_geotransform(), raster.get_epsg()), res
@@ -130,7 +132,8 @@ def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.
     key = (str(dev), "win", w.x_off, w.y_off, w.width, w.length)
 
     def make():
-        sub = np.ascontiguousarray(raster.data[w.y_off:w.y_off + w.length, w.x_off:w.x_off + w.width])
+        sub = np.ascontiguousarray(raster.data[w.y_off:w.y_off + w.length, w.x_off:w.x_off + w.width],
+                                   dtype=np.float32)
         return torch.from_numpy(sub).to(dev)
 
     t = _cached_device(raster, key, make)
@@ -141,11 +144,14 @@ def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.
 
 
 def dem_raster_desc_blocks(raster, geogrid: GeoGridParameters, lines_per_block: int, margin: int,
-                           dev: torch.device):
+                           dev: torch.device, whole_window: bool = False):
     """Descriptor whose device samples cover the DEM window of every block of
     ``lines_per_block`` geogrid lines (each block loads its own window, as
-    cuda/geocode/Geocode.cu:402-407 does): the union of those windows is
-    uploaded once, or the resident raster is used."""
+    cuda/geocode/Geocode.cu:402-407 and geocode/geocodeSlc.cpp:653-656 do):
+    the union of those windows (and, with ``whole_window``, of the whole
+    geogrid's window) is uploaded once, or the resident raster is used."""
+    if raster.data.ndim != 2:
+        raise ValueError("a DEM raster has one band")
     res = getattr(raster, "resident", None)
     if res is not None and res.device == dev:
         return dem_raster_desc_resident(res, raster.get_geotransform(), raster.get_epsg()), res
@@ -159,9 +165,11 @@ def dem_raster_desc_blocks(raster, geogrid: GeoGridParameters, lines_per_block: 
     lib = L.lib()
     x0 = y0 = None
     x1 = y1 = None
-    for line_start in range(0, geogrid.length, lines_per_block):
+    blocks = [(ls, min(lines_per_block, geogrid.length - ls)) for ls in range(0, geogrid.length, lines_per_block)]
+    if whole_window:
+        blocks.append((0, geogrid.length))
+    for line_start, n in blocks:
         w = L.DemWindow()
-        n = min(lines_per_block, geogrid.length - line_start)
         st = lib.gslc_compute_dem_window_block(C.byref(d), C.byref(g), int(line_start), int(n), int(geogrid.width),
                                                int(margin), C.byref(w))
         if st == L.GSLC_EPROJ:
@@ -184,7 +192,7 @@ def dem_raster_desc_blocks(raster, geogrid: GeoGridParameters, lines_per_block: 
     key = (str(dev), "win", x0, y0, x1 - x0, y1 - y0)
 
     def make():
-        sub = np.ascontiguousarray(raster.data[y0:y1, x0:x1])
+        sub = np.ascontiguousarray(raster.data[y0:y1, x0:x1], dtype=np.float32)
         return torch.from_numpy(sub).to(dev)
 
     t = _cached_device(raster, key, make)

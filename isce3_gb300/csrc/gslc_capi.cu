@@ -33,6 +33,7 @@ struct gslc_ctx {
     double* d_sinc64 = nullptr;     // the sinc table in double (raster interpolation), on first use
     cudaStream_t copy_stream = nullptr;   // device-to-host copies of gslc_geocode_slc_to_host, on first use
     cudaEvent_t band_ev[GSLC_HOST_BANDS + 1] = {};
+    int64_t stage_wait = 0;         // SM clocks of the orbit-table wait; 0: STAGE_WAIT_DEFAULT
     std::string err;
 };
 
@@ -45,6 +46,17 @@ int set_err(gslc_ctx* c, int code, const std::string& m) {
 
 int cuda_err(gslc_ctx* c, cudaError_t e, const char* where) {
     return set_err(c, GSLC_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// The kernels' device error word: bit 0 a projection inverse failed; bit 1
+// a wait for the orbit tables' copy into shared memory ran out (the global
+// tables were read instead, so the outputs are complete and correct); bit 2
+// a block's final wait for its copy ran out too.
+int device_status(gslc_ctx* c, int32_t word) {
+    if (word & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
+    if (word & 4) return set_err(c, GSLC_ETIMEOUT, "an orbit table copy into shared memory did not complete");
+    if (word & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
+    return GSLC_OK;
 }
 
 // core/Sinc2dInterpolator.cpp:12-40 and :98-115 — Hann-weighted sinc,
@@ -756,6 +768,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.rdr_c32 = a->rdr_format == 1 ? 1 : 0;
     p.geo_fmt = a->geo_format;
     p.mant_bits = a->geo_format == 2 ? a->mantissa_bits : 23;
+    p.stage_wait = c && c->stage_wait > 0 ? c->stage_wait : STAGE_WAIT_DEFAULT;
 
     // DEM window the reference would load (loadDem.cpp:22-133)
     gslc_dem_window w;
@@ -853,9 +866,19 @@ size_t geo_pixel_bytes(int f) { return f == 1 ? 4 : 8; }
 // of the mask, with host_mask) to host memory: the geogrid runs in row bands
 // whose boundaries are multiples of every tile height (so every tile, and
 // every pixel's value, is the one of the single launch), each band's copies
-// queued on the context's copy stream behind its kernels.
+// queued on the context's copy stream behind its kernels.  deramp_buf, when
+// given, receives the deramped copies of the radar blocks (block b at
+// b * rdr_length * rdr_width, complex64) in place of stream-ordered scratch.
+// lines_per_block > 0 is the raster mode (geocode/geocodeSlc.cpp:605-828):
+// the geogrid runs in blocks of that many lines, each with its own DEM
+// window (DEMRasterToInterpolator of the block, :653-656), and the phase
+// outputs start as the invalid value's real part (:713-723).  The reference
+// reads each block's radar bounding box widened by 5 samples (:740-750);
+// the interpolator's chip tests then reject exactly the pixels they reject
+// on the whole radar raster (the box is clamped only at the raster's edges),
+// so the whole raster, deramped once, is read here.
 int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t stream, void* const* host_geo,
-                     uint8_t* host_mask) {
+                     uint8_t* host_mask, float2* deramp_buf = nullptr, int32_t lines_per_block = 0) {
     if (!c) return GSLC_EINVAL;
     c->err.clear();
     c->launches = 0;
@@ -887,19 +910,27 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
     // to stream-ordered scratch.
     const int64_t nrdr = a->rdr_length * a->rdr_width;
     std::vector<void*> scratch;
+    // every failure after this point: hand back the scratch, and let copies
+    // already queued to the caller's host buffers finish before returning
+    auto fail = [&](int code) {
+        for (void* s : scratch) cudaFreeAsync(s, stream);
+        if (host_geo && c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+        return code;
+    };
     std::vector<const float2*> rdr(a->n_blocks);
     for (int b = 0; b < a->n_blocks; ++b) rdr[b] = (const float2*)a->rdr_blocks[b];
     if (c->timing) cudaEventRecord(c->ev[2], stream);
     if (!p.carriers_zero && nrdr > 0 && !a->rdr_deramped) {
         for (int b = 0; b < a->n_blocks; ++b) {
             float2* dst = (float2*)a->rdr_blocks[b];
-            if (!a->inplace_deramp) {
+            if (a->inplace_deramp) {
+                // the caller's block (the reference's behaviour)
+            } else if (deramp_buf) {
+                dst = deramp_buf + (int64_t)b * nrdr;
+            } else {
                 void* buf = nullptr;
                 e = cudaMallocAsync(&buf, nrdr * sizeof(float2), stream);
-                if (e != cudaSuccess) {
-                    for (void* s : scratch) cudaFreeAsync(s, stream);
-                    return cuda_err(c, e, "cudaMallocAsync deramp scratch");
-                }
+                if (e != cudaSuccess) return fail(cuda_err(c, e, "cudaMallocAsync deramp scratch"));
                 scratch.push_back(buf);
                 dst = (float2*)buf;
             }
@@ -913,7 +944,7 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
             dp.inv_prf = 1.0 / rg.prf;
             dp.az_car = p.az_car; dp.rg_car = p.rg_car;
             e = launch_deramp(dp, stream, &c->launches);
-            if (e != cudaSuccess) return cuda_err(c, e, "deramp launch");
+            if (e != cudaSuccess) return fail(cuda_err(c, e, "deramp launch"));
             rdr[b] = dst;
         }
         p.rdr_c32 = 0;      // the deramped copies are complex64
@@ -925,15 +956,22 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
     const int64_t gl = p.gl, gw = p.gw;
     int nband = 1;
     int64_t band_rows = gl;
-    if (host_geo) {
+    if (lines_per_block > 0) {
+        band_rows = lines_per_block;
+        nband = (int)((gl + band_rows - 1) / band_rows);
+        const double fill = (double)a->invalid_re;
+        for (double* ph : {a->carrier_phase, a->flatten_phase})
+            if (ph && (e = launch_fill_f64(ph, gl * gw, fill, stream, &c->launches)) != cudaSuccess)
+                return fail(cuda_err(c, e, "phase fill"));
+    } else if (host_geo) {
         if (!c->copy_stream) {
             e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
-            if (e != cudaSuccess) { c->copy_stream = nullptr; return cuda_err(c, e, "copy stream"); }
+            if (e != cudaSuccess) { c->copy_stream = nullptr; return fail(cuda_err(c, e, "copy stream")); }
         }
         for (auto& ev : c->band_ev)
             if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
                 ev = nullptr;
-                return cuda_err(c, e, "band event");
+                return fail(cuda_err(c, e, "band event"));
             }
         band_rows = ((gl + GSLC_HOST_BANDS - 1) / GSLC_HOST_BANDS + 31) / 32 * 32;
         nband = (int)((gl + band_rows - 1) / band_rows);
@@ -945,6 +983,16 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
         const int64_t off = row0 * gw;
         p.geo_row0 = row0;
         p.gl = rows;
+        if (lines_per_block > 0) {
+            gslc_dem_window w;
+            const gslc_geo_grid& gg = a->geo_grid;
+            int st = gslc_compute_dem_window_block(&a->dem, &gg, (int32_t)row0, (int32_t)rows, gg.width, a->dem_margin, &w);
+            if (st == GSLC_EPROJ) st = set_err(c, GSLC_EINVAL, "projection transformation between geogrid and DEM failed");
+            else if (st != GSLC_OK) st = set_err(c, st, "unsupported or invalid DEM raster");
+            else if (w.wraps) st = set_err(c, GSLC_EUNSUPPORTED, "DEM window crossing the DEM file discontinuity");
+            else st = bind_dem_window(c, a->dem, w, p.dem);
+            if (st != GSLC_OK) return fail(st);
+        }
         p.mask = a->mask ? a->mask + off : nullptr;
         p.carrier_out = a->carrier_phase ? a->carrier_phase + off : nullptr;
         p.flatten_out = a->flatten_phase ? a->flatten_phase + off : nullptr;
@@ -957,7 +1005,7 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
                 p.geo[b] = (float2*)((char*)a->geo_blocks[b0 + b] + off * esz);
             }
             e = launch_geocode(p, a->geo2rdr_precision, stream, &c->launches);
-            if (e != cudaSuccess) return cuda_err(c, e, "geocode launch");
+            if (e != cudaSuccess) return fail(cuda_err(c, e, "geocode launch"));
         }
         if (!host_geo) continue;
         e = cudaEventRecord(c->band_ev[band], stream);
@@ -968,12 +1016,12 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
         if (e == cudaSuccess && host_mask && a->mask)
             e = cudaMemcpyAsync(host_mask + off, a->mask + off, (size_t)(rows * gw), cudaMemcpyDeviceToHost,
                                 c->copy_stream);
-        if (e != cudaSuccess) return cuda_err(c, e, "band copy");
+        if (e != cudaSuccess) return fail(cuda_err(c, e, "band copy"));
     }
     if (host_geo) {
         e = cudaEventRecord(c->band_ev[GSLC_HOST_BANDS], c->copy_stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, c->band_ev[GSLC_HOST_BANDS], 0);
-        if (e != cudaSuccess) return cuda_err(c, e, "band copy");
+        if (e != cudaSuccess) return fail(cuda_err(c, e, "band copy"));
     }
     if (c->timing) cudaEventRecord(c->ev[1], stream);
     for (void* s : scratch) cudaFreeAsync(s, stream);
@@ -984,15 +1032,26 @@ int geocode_slc_impl(gslc_ctx* c, const gslc_geocode_args* a, cudaStream_t strea
         cudaEventElapsedTime(&c->ms_geocode, c->ev[0], c->ev[1]);
         cudaEventElapsedTime(&c->ms_deramp, c->ev[2], c->ev[3]);
     }
-    if (c->h_err[0] & 1) return set_err(c, GSLC_EPROJ, "Inverse projection transformation failed");
-    if (c->h_err[0] & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
-    return GSLC_OK;
+    return device_status(c, c->h_err[0]);
 }
 
 }  // namespace
 
 extern "C" int gslc_geocode_slc(gslc_ctx* c, const gslc_geocode_args* a, void* stream) {
     return geocode_slc_impl(c, a, (cudaStream_t)stream, nullptr, nullptr);
+}
+
+extern "C" int gslc_geocode_slc_raster(gslc_ctx* c, const gslc_geocode_args* a, int32_t lines_per_block,
+                                       void* stream) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    if (!a) return set_err(c, GSLC_EINVAL, "null arguments");
+    if (lines_per_block < 1) return set_err(c, GSLC_EINVAL, "lines_per_block must be positive");
+    if (a->rdr_length != a->radar_grid.length || a->rdr_width != a->radar_grid.width)
+        return set_err(c, GSLC_EINVAL, "input raster shape differs from the radar grid");
+    if (a->first_azimuth_line != 0 || a->first_range_sample != 0)
+        return set_err(c, GSLC_EINVAL, "the input raster starts at the radar grid's first line and sample");
+    return geocode_slc_impl(c, a, (cudaStream_t)stream, nullptr, nullptr, nullptr, lines_per_block);
 }
 
 extern "C" int gslc_geocode_slc_to_host(gslc_ctx* c, const gslc_geocode_args* a, void* const* host_geo_blocks,
@@ -1120,7 +1179,12 @@ extern "C" int gslc_geocode_rasters(gslc_ctx* c, const gslc_raster_geocode_args*
         cudaEventElapsedTime(&c->ms_geocode, c->ev[0], c->ev[1]);
         c->ms_deramp = 0.f;
     }
-    if (c->h_err[0] & 2) return set_err(c, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
+    return device_status(c, c->h_err[0]);
+}
+
+extern "C" int gslc_ctx_set_stage_wait(gslc_ctx* c, int64_t clocks) {
+    if (!c) return GSLC_EINVAL;
+    c->stage_wait = clocks > 0 ? clocks : 0;
     return GSLC_OK;
 }
 
@@ -1483,6 +1547,7 @@ extern "C" int gslc_dem_stats(gslc_ctx* c, const float* data, int64_t length, in
     return GSLC_OK;
 }
 
+#include <atomic>
 #include <mutex>
 
 // ===========================================================================
@@ -1514,7 +1579,7 @@ static __device__ __align__(256) double g_noalloc_orbit[orbit_table_doubles(NOAL
 static __device__ __align__(256) int32_t g_noalloc_err[4];
 
 struct NoallocDevice {
-    bool ready = false;
+    std::atomic<bool> ready{false};   // set (release) once the fields below hold
     float2* deramp = nullptr;
     float* sinc = nullptr;
     double* orbit = nullptr;
@@ -1537,7 +1602,7 @@ int noalloc_fail(char* buf, size_t len, int code, const char* msg) {
 // inside a stream capture.
 int noalloc_setup(int dev, NoallocDevice& d, char* buf, size_t len) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (d.ready) return GSLC_OK;
+    if (d.ready.load(std::memory_order_acquire)) return GSLC_OK;
     cudaError_t e = cudaGetSymbolAddress((void**)&d.deramp, g_noalloc_deramp);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.sinc, g_noalloc_sinc);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.orbit, g_noalloc_orbit);
@@ -1546,7 +1611,7 @@ int noalloc_setup(int dev, NoallocDevice& d, char* buf, size_t len) {
     const std::vector<float> table = make_sinc_table();
     e = cudaMemcpy(d.sinc, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return noalloc_fail(buf, len, GSLC_ECUDA, cudaGetErrorString(e));
-    d.ready = true;
+    d.ready.store(true, std::memory_order_release);
     (void)dev;
     return GSLC_OK;
 }
@@ -1562,7 +1627,7 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return noalloc_fail(errbuf, errbuf_len, GSLC_EUNSUPPORTED, "device index beyond 64");
     NoallocDevice& d = g_noalloc_dev[dev];
-    if (!d.ready) {
+    if (!d.ready.load(std::memory_order_acquire)) {
         if (int st = noalloc_setup(dev, d, errbuf, errbuf_len)) return st;
     }
     if (a->orbit.n > NOALLOC_MAX_STATE_VECTORS)
@@ -1582,32 +1647,17 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     c.d_orbit = d.orbit;
     c.orbit_cap = orbit_table_doubles(NOALLOC_MAX_STATE_VECTORS);
 
-    gslc_geocode_args args = *a;
-    std::vector<const void*> blocks(a->rdr_blocks, a->rdr_blocks + a->n_blocks);
     AzRg az{}, rg{};
     bool carriers = false;
     if (!to_azrg(&c, a->az_carrier, az, "az_carrier") && !to_azrg(&c, a->rg_carrier, rg, "rg_carrier"))
         carriers = !(az.is_zero && rg.is_zero);
     const int64_t nrdr = a->rdr_length * a->rdr_width;
-    if (carriers && !a->rdr_deramped && nrdr > 0 && a->rdr_format == 1)
-        return noalloc_fail(errbuf, errbuf_len, GSLC_EUNSUPPORTED,
-                            "complex32 radar blocks with carriers need the deramp scratch of gslc_geocode_slc");
-    if (carriers && !a->inplace_deramp && !a->rdr_deramped && nrdr > 0) {
-        // deramp works on a copy in the static scratch; the caller's blocks stay as given
-        if (nrdr * a->n_blocks > NOALLOC_MAX_DERAMP)
-            return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL,
-                                "radar blocks exceed the allocation-free deramp scratch (4194304 complex samples)");
-        for (int b = 0; b < a->n_blocks; ++b) {
-            float2* dst = d.deramp + (int64_t)b * nrdr;
-            e = cudaMemcpyAsync(dst, a->rdr_blocks[b], nrdr * sizeof(float2), cudaMemcpyDeviceToDevice,
-                                (cudaStream_t)stream);
-            if (e != cudaSuccess) return noalloc_fail(errbuf, errbuf_len, GSLC_ECUDA, cudaGetErrorString(e));
-            blocks[b] = dst;
-        }
-        args.inplace_deramp = 1;
-    }
-    args.rdr_blocks = blocks.data();
-    const int st = gslc_geocode_slc(&c, &args, stream);
+    // the deramp reads the caller's blocks (complex64 or complex32) and
+    // writes the complex64 copies into the static scratch
+    if (carriers && !a->inplace_deramp && !a->rdr_deramped && nrdr > 0 && nrdr * a->n_blocks > NOALLOC_MAX_DERAMP)
+        return noalloc_fail(errbuf, errbuf_len, GSLC_EINVAL,
+                            "radar blocks exceed the allocation-free deramp scratch (4194304 complex samples)");
+    const int st = geocode_slc_impl(&c, a, (cudaStream_t)stream, nullptr, nullptr, d.deramp);
     c.d_sinc = nullptr;   // the static arrays are not the context's to free
     c.d_err = nullptr;
     c.d_orbit = nullptr;
@@ -1908,9 +1958,8 @@ extern "C" int gslc_batch_status(gslc_batch* b, void* stream) {
     // (a pageable destination: the copy has completed when the call returns)
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return batch_fail(b, b->ctx, GSLC_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
-    if (b->h_err[0] & 1) return batch_fail(b, b->ctx, GSLC_EPROJ, "Inverse projection transformation failed");
-    if (b->h_err[0] & 2)
-        return batch_fail(b, b->ctx, GSLC_ETIMEOUT, "the wait for the orbit table copy into shared memory ran out");
+    gslc_ctx probe;
+    if (const int st = device_status(&probe, b->h_err[0])) return batch_fail(b, b->ctx, st, probe.err);
     return GSLC_OK;
 }
 

@@ -476,9 +476,13 @@ constexpr int GBX = 32, GBY = 8;
 // mbarrier) issued by one thread when the tile starts; it overlaps the
 // tile's ground-point work and is waited for before the first Newton
 // iteration.  Orbits whose tables exceed SEG_SMEM read them from global
-// memory.  The wait is bounded: if it runs out the block reads the global
-// tables, raises error bit 1 (GSLC_ETIMEOUT on the host) and stages nothing
-// more.
+// memory.  The wait is bounded: the copy must land within
+// GeoParams::stage_wait SM clocks of its issue (a deadline, checked before
+// each poll); a thread whose wait runs out reads the global tables, raises
+// error bit 1 (GSLC_ETIMEOUT on the host) and the block stages nothing more.  Before the
+// block finishes, one thread waits (bounded again) for a copy still in
+// flight, so that the copy never writes shared memory the block has left;
+// if that wait runs out too, error bit 2 is raised.
 constexpr int SEG_SMEM = 4096;   // doubles (32 KiB): orbits of up to 54 state vectors
 
 struct OrbitStage {
@@ -487,6 +491,7 @@ struct OrbitStage {
     int* off;             // shared flag: a wait ran out, stage nothing more
     uint32_t phase;       // parity of the copy to wait for
     int issued;           // a copy of this request's tables was issued
+    long long deadline;   // SM clock by which the copy must have landed
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
@@ -531,21 +536,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// wait for a copy, at most ~2^31 SM clocks (about a second)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// wait for a copy, at most `limit` SM clocks
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > (1ll << 31)) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
-// every thread: true when the staged tables can be read
+// every thread: true when the staged tables can be read.  Past the deadline
+// the wait has run out whether or not the copy landed meanwhile.
 __device__ __forceinline__ bool stage_ready(const OrbitStage& st, const GeoParams& p) {
     if (!st.issued) return false;
-    if (mbar_wait_bounded(st.bar, st.phase)) return true;
+    while (clock64() <= st.deadline)
+        if (mbar_try_wait(st.bar, st.phase)) return true;
     atomicOr(p.err, 2);
     *st.off = 1;
     return false;
+}
+
+// one thread, before the block finishes: the copy of parity `parity` has
+// landed (immediate when a wait already saw it), at most STAGE_WAIT_DEFAULT
+// clocks
+__device__ __forceinline__ void stage_drain(uint64_t* bar, uint32_t parity, int32_t* err) {
+    if (!mbar_wait_bounded(bar, parity, STAGE_WAIT_DEFAULT)) atomicOr(err, 4);
 }
 
 // ---- tile fit of the projection inverse (UTM geogrids) --------------------
@@ -991,13 +1005,17 @@ __global__ void __launch_bounds__(GBX * GBY, 2) geocode_kernel(const __grid_cons
     __shared__ int s_off;
     // the float-float path reads only the piece tables
     const bool stage = !FF && seg_fits(p);
+    const long long deadline = clock64() + p.stage_wait;
     if (stage && threadIdx.x == 0 && threadIdx.y == 0) {
         stage_init(&s_bar);
         stage_issue(p, s_seg, &s_bar);
     }
     // geocode_block synchronises the block before any thread waits
-    const OrbitStage st{s_seg, &s_bar, &s_off, 0u, stage ? 1 : 0};
+    const OrbitStage st{s_seg, &s_bar, &s_off, 0u, stage ? 1 : 0, deadline};
     geocode_block<GEO_LONLAT, FF, RASTER, PPT>(p, blockIdx.x, blockIdx.y, st);
+    // thread (0, 0) always has pixels (tiles start inside the geogrid), so
+    // it reaches this point; the block's shared memory outlives the copy
+    if (stage && threadIdx.x == 0 && threadIdx.y == 0) stage_drain(&s_bar, 0u, p.err);
 }
 
 // Persistent form: blocks pop runs of tiles of any request in the batch from
@@ -1014,9 +1032,10 @@ __global__ void __launch_bounds__(GBX * GBY, 2) geocode_persistent(const __grid_
         s_off = 0;
         if (!FF) stage_init(&s_bar);
     }
-    int staged = -1;            // items[] entry whose tables are in s_seg
+    int staged = -1;            // items[] entry the block last prepared for
     uint32_t phase = 0;         // parity of the next copy
-    OrbitStage st{s_seg, &s_bar, &s_off, 0u, 0};
+    bool any_issued = false;    // a copy was issued (the last one has parity phase ^ 1)
+    OrbitStage st{s_seg, &s_bar, &s_off, 0u, 0, 0};
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0)
             s_base = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(q.counter),
@@ -1024,7 +1043,11 @@ __global__ void __launch_bounds__(GBX * GBY, 2) geocode_persistent(const __grid_
         __syncthreads();
         const long long base = s_base;
         __syncthreads();
-        if (base >= q.n_tiles) return;
+        if (base >= q.n_tiles) {
+            // the block's shared memory outlives its last copy
+            if (!FF && lead && any_issued) stage_drain(&s_bar, phase ^ 1u, q.items[0].err);
+            return;
+        }
         const long long end = min(base + (long long)q.tiles_per_pop, q.n_tiles);
         for (long long tile = base; tile < end; ++tile) {
             // request owning the tile: last prefix start <= tile (warp-uniform search)
@@ -1038,14 +1061,18 @@ __global__ void __launch_bounds__(GBX * GBY, 2) geocode_persistent(const __grid_
             const long long local = tile - q.tile_start[lo];
             const int tiles_x = (p.gw + GBX - 1) / GBX;
             // every thread finished the previous tile (barrier below), so
-            // the tables of a new request may overwrite s_seg
-            if (!FF && lo != staged && !s_off) {
+            // the tables of a new request may overwrite s_seg; after a wait
+            // ran out (s_off) nothing more is staged and the new request
+            // reads its global tables
+            if (!FF && lo != staged) {
                 staged = lo;
-                st.issued = seg_fits(p) ? 1 : 0;
+                st.issued = (!s_off && seg_fits(p)) ? 1 : 0;
                 if (st.issued) {
+                    st.deadline = clock64() + p.stage_wait;
                     if (lead) stage_issue(p, s_seg, &s_bar);
                     st.phase = phase;
                     phase ^= 1u;
+                    any_issued = true;
                 }
             }
             geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x), st);
@@ -1279,6 +1306,13 @@ __global__ void __launch_bounds__(256) mask_words_kernel(W* __restrict__ data, i
     }
 }
 
+// every element of p set to v (the invalid fill of the raster mode's phase
+// outputs); grid-stride, coalesced 8-byte stores
+__global__ void __launch_bounds__(256) fill_f64_kernel(double* __restrict__ p, int64_t n, double v) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
+}
+
 #endif  // GSLC_PERSISTENT_TU
 
 }  // namespace
@@ -1352,6 +1386,13 @@ cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits
         const unsigned long long m = ~0ull << (52 - bits);
         mask_words_kernel<unsigned long long><<<g, 256, 0, s>>>((unsigned long long*)dst, n, m);
     }
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_f64(double* p, int64_t n, double v, cudaStream_t s, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    fill_f64_kernel<<<codec_grid(n), 256, 0, s>>>(p, n, v);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -78,7 +78,14 @@ struct GeoParams {
     // sample formats: rdr 0 complex64, 1 complex32; geo 0 complex64,
     // 1 complex32, 2 complex64 keeping mant_bits mantissa bits
     int32_t rdr_c32, geo_fmt, mant_bits;
+    int32_t _pad3;
+    // SM clocks a thread waits for the orbit tables' copy into shared memory
+    // before it reads the global tables instead (error bit 1)
+    int64_t stage_wait;
 };
+
+// default of GeoParams::stage_wait: ~2^31 SM clocks, about a second
+constexpr int64_t STAGE_WAIT_DEFAULT = 1ll << 31;
 
 struct DerampParams {
     const float2* src;          // complex64, or complex32 when src_c32
@@ -192,6 +199,7 @@ inline bool ff_eligible(const GeoParams& p) {
 // launchers (gslc_kernels.cu)
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);
+cudaError_t launch_fill_f64(double* p, int64_t n, double v, cudaStream_t s, int64_t* launches);
 // op 0: complex64 -> complex32, 1: complex32 -> complex64, 2: keep `bits`
 // mantissa bits of n words of word_bytes (4 or 8) at dst, in place
 cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits, int word_bytes, cudaStream_t s,

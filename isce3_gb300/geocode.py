@@ -207,6 +207,75 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid: RadarGr
             _geocode_on_stream(lib, ctx, s, dev, *call)
 
 
+def geocode_slc_raster(output_raster, input_raster, dem_raster, radargrid: RadarGridParameters,
+                       geogrid: GeoGridParameters, orbit: Orbit, native_doppler: LUT2d, image_grid_doppler: LUT2d,
+                       ellipsoid: Ellipsoid, threshold_geo2rdr: float = 1.0e-9, numiter_geo2rdr: int = 25,
+                       lines_per_block: int = 1000, flatten: bool = True, reramp: bool = True,
+                       azimuth_carrier=None, range_carrier=None, az_time_correction=None, srange_correction=None,
+                       flatten_with_corrected_srange: bool = False, invalid_value=np.nan + np.nan * 1j,
+                       carrier_phase_raster=None, flatten_phase_raster=None, *, geo2rdr_precision: str = "fp64",
+                       az_index_block=None, rg_index_block=None, dem_margin: int = 50, device=None,
+                       stream: torch.cuda.Stream | None = None) -> None:
+    """Raster overload of geocode_slc: geocode every band of ``input_raster``
+    (the SLC over the whole radar grid) into the same band of
+    ``output_raster`` (the whole geogrid), block by block.
+
+    Names and defaults are those of the pybind overload
+    (python/extensions/pybind_isce3/geocode/GeocodeSlc.cpp:26-102) of
+    isce3::geocode::geocodeSlc's raster mode (cxx/isce3/geocode/geocodeSlc.cpp:
+    605-828): blocks of ``lines_per_block`` geogrid lines, each with the DEM
+    window of that block alone; pixels without a result hold
+    ``invalid_value``, and the optional float64 phase rasters its real part.
+    Rasters are ``isce3_gb300.io.Raster`` objects (GDAL's file I/O has no
+    place here); results are written into their samples.  The input raster is
+    not modified.  Extra keyword-only arguments as in ``geocode_slc``.
+    """
+    from .io import Raster
+    for r, what in ((output_raster, "output_raster"), (input_raster, "input_raster")):
+        if not isinstance(r, Raster):
+            raise TypeError(f"{what} must be an isce3_gb300.io.Raster")
+    if output_raster.num_bands() != input_raster.num_bands():
+        raise ValueError("input and output rasters have different numbers of bands")
+    if (input_raster.length, input_raster.width) != (radargrid.length, radargrid.width):
+        raise ValueError("input raster shape differs from the radar grid")
+    if (output_raster.length, output_raster.width) != (geogrid.length, geogrid.width):
+        raise ValueError("output raster shape differs from the geogrid")
+    if int(lines_per_block) < 1:
+        raise ValueError("lines_per_block must be positive")
+    phases = []
+    for ph, what in ((carrier_phase_raster, "carrier_phase_raster"), (flatten_phase_raster, "flatten_phase_raster")):
+        if ph is None:
+            phases.append(None)
+            continue
+        if not isinstance(ph, Raster) or ph.data.dtype != np.float64 or ph.num_bands() != 1:
+            raise TypeError(f"{what} must be a single-band float64 isce3_gb300.io.Raster")
+        if (ph.length, ph.width) != (geogrid.length, geogrid.width):
+            raise ValueError(f"{what} shape differs from the geogrid")
+        phases.append(ph.data)
+    azimuth_carrier = Poly2d() if azimuth_carrier is None else azimuth_carrier
+    range_carrier = Poly2d() if range_carrier is None else range_carrier
+    n = input_raster.num_bands()
+    rdr = [input_raster.band(i) for i in range(n)]
+    geo = [output_raster.band(i) for i in range(n)]
+    call = _normalize_call(geo, rdr, dem_raster, radargrid, geogrid, orbit, native_doppler, image_grid_doppler,
+                           ellipsoid, threshold_geo2rdr, numiter_geo2rdr, None, None, None, 0, 0, flatten, reramp,
+                           azimuth_carrier, range_carrier, az_time_correction, srange_correction,
+                           flatten_with_corrected_srange, invalid_value, phases[0], phases[1], geo2rdr_precision,
+                           False, az_index_block, rg_index_block, dem_margin)
+    dev = M.device_of(device)
+    lib = L.lib()
+    ctx = L.context(dev.index)
+    with torch.cuda.device(dev):
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        with torch.cuda.stream(s):
+            a, outs, keep = _build_args(dev, *call, dem_lines_per_block=int(lines_per_block))
+            st = lib.gslc_geocode_slc_raster(ctx, C.byref(a), int(lines_per_block), C.c_void_p(s.cuda_stream))
+            L.check(st, ctx, "geocode_slc")
+            for o in outs:
+                o.copy_back()
+            del keep
+
+
 def _normalize_call(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid, orbit, native_doppler,
                     image_grid_doppler, ellipsoid, threshold_geo2rdr, num_iter_geo2rdr, mask_block,
                     sliced_radargrid, subswaths, first_azimuth_line, first_range_sample, flatten, reramp,
@@ -293,8 +362,11 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
                 subswaths, first_azimuth_line, first_range_sample, flatten, reramp, az_carrier, rg_carrier,
                 az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
                 carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
-                rg_index_block, dem_margin, rdr_deramped=False, rdr_format=0, geo_format=0, mantissa_bits=23):
-    """Stage arrays on ``dev`` and fill a gslc_geocode_args.
+                rg_index_block, dem_margin, rdr_deramped=False, rdr_format=0, geo_format=0, mantissa_bits=23,
+                *, dem_lines_per_block=0):
+    """Stage arrays on ``dev`` and fill a gslc_geocode_args.  With
+    ``dem_lines_per_block`` the device DEM samples cover the window of every
+    block of that many geogrid lines (the raster mode).
 
     Returns (args, outputs to copy back, objects to keep alive)."""
     # Radar blocks in pinned host memory upload on a side stream while the DEM
@@ -315,7 +387,11 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
                 st.dev.record_stream(s)
     holder = M.AzRgHolder()
     a = L.GeocodeArgs()
-    a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
+    if dem_lines_per_block > 0:
+        a.dem, dem_keep = M.dem_raster_desc_blocks(dem_raster, geogrid, dem_lines_per_block, dem_margin, dev,
+                                                   whole_window=True)
+    else:
+        a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
     a.native_doppler = M.lut_desc(native_doppler, dev)
     a.image_grid_doppler = M.lut_desc(image_grid_doppler, dev)
     a.az_time_correction = M.lut_desc(az_time_correction, dev)

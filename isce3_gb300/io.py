@@ -39,13 +39,14 @@ def gdal_type_of(arr) -> int:
 
 
 class Raster:
-    """A single-band raster with a GDAL-style geotransform.
+    """A raster of one or more bands with a GDAL-style geotransform.
 
     ``geotransform = [x0, dx, 0, y0, 0, dy]`` gives the outer corner of pixel
-    (0, 0) and the pixel spacing, as ``GDALGetGeoTransform`` would.  Real
-    samples are held as float32 (a DEM), complex ones as complex64 (an SLC);
-    the geotransform and EPSG code are needed only where the raster is used
-    as a DEM.
+    (0, 0) and the pixel spacing, as ``GDALGetGeoTransform`` would.  Samples
+    are ``(length, width)`` for one band or ``(bands, length, width)``.  Real
+    samples are held as float32 (a DEM, which has one band) or float64 (a
+    phase raster), complex ones as complex64 (an SLC); the geotransform and
+    EPSG code are needed only where the raster is used as a DEM.
     """
 
     def __init__(self, path_or_data, geotransform=None, epsg: int | None = None):
@@ -58,10 +59,15 @@ class Raster:
         else:
             data = path_or_data
         arr = np.asarray(data)
-        self.data = np.ascontiguousarray(arr.astype(np.complex64 if np.iscomplexobj(arr) else np.float32,
-                                                    copy=False))
-        if self.data.ndim != 2:
-            raise ValueError("Raster data must be 2-D")
+        if np.iscomplexobj(arr):
+            dt = np.complex64
+        elif arr.dtype == np.float64:
+            dt = np.float64
+        else:
+            dt = np.float32
+        self.data = np.ascontiguousarray(arr.astype(dt, copy=False))
+        if self.data.ndim not in (2, 3):
+            raise ValueError("Raster data must be 2-D, or 3-D with the bands first")
         self._gt = None
         if geotransform is not None:
             gt = [float(v) for v in geotransform]
@@ -74,13 +80,15 @@ class Raster:
         self._device_cache = {}
 
     @classmethod
-    def empty(cls, width: int, length: int, datatype: int = gdal.GDT_CFloat32, geotransform=None, epsg=None):
+    def empty(cls, width: int, length: int, datatype: int = gdal.GDT_CFloat32, geotransform=None, epsg=None,
+              bands: int = 1):
         """A zero-filled raster to write into (isce3.io.Raster(path, width,
-        length, 1, datatype, driver) without the file)."""
+        length, bands, datatype, driver) without the file)."""
         inv = {v: k for k, v in _NP_TO_GDT.items()}
-        if datatype not in (gdal.GDT_Float32, gdal.GDT_CFloat32):
-            raise NotImplementedError("only GDT_Float32 and GDT_CFloat32 rasters are held")
-        return cls(np.zeros((int(length), int(width)), inv[datatype]), geotransform, epsg)
+        if datatype not in (gdal.GDT_Float32, gdal.GDT_Float64, gdal.GDT_CFloat32):
+            raise NotImplementedError("only GDT_Float32, GDT_Float64 and GDT_CFloat32 rasters are held")
+        shape = (int(length), int(width)) if bands == 1 else (int(bands), int(length), int(width))
+        return cls(np.zeros(shape, inv[datatype]), geotransform, epsg)
 
     def datatype(self) -> int:
         """GDALDataType of the samples (isce3.io.Raster.datatype())."""
@@ -89,11 +97,23 @@ class Raster:
     # isce3.io.Raster-like accessors
     @property
     def width(self) -> int:
-        return int(self.data.shape[1])
+        return int(self.data.shape[-1])
 
     @property
     def length(self) -> int:
-        return int(self.data.shape[0])
+        return int(self.data.shape[-2])
+
+    def num_bands(self) -> int:
+        """Number of bands (isce3.io.Raster.num_bands)."""
+        return 1 if self.data.ndim == 2 else int(self.data.shape[0])
+
+    def band(self, i: int) -> np.ndarray:
+        """Samples of band i (0-based; GDAL numbers bands from 1), a view."""
+        if self.data.ndim == 2:
+            if i != 0:
+                raise IndexError("single-band raster")
+            return self.data
+        return self.data[i]
 
     def get_geotransform(self):
         if self._gt is None:

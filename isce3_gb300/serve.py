@@ -3,8 +3,9 @@
 - ``ResidentStore`` keeps SLCs (deramped once, with their orbit, Doppler LUTs
   and carriers) and one shared DEM resident in HBM.
 - ``AdmissionPolicy`` admits queued requests first-in first-out while their
-  HBM footprint (outputs + batch metadata) fits the budget and a batch slot
-  is free; a request larger than the whole budget is rejected.
+  HBM footprint (outputs + batch metadata) fits what the budget leaves after
+  the resident store and the requests in flight, and a batch slot is free; a
+  request larger than the budget less the resident store is rejected.
 - ``GeocodeServer.serve`` runs an arrival trace: each scheduling tick it
   moves arrived requests into the queue, marks finished requests, retires
   finished batches (CUDA event polling, no device synchronisation), and
@@ -101,11 +102,16 @@ class ResidentStore:
 
 @dataclass
 class ServeRequest:
-    """One geocode request against a resident SLC."""
+    """One geocode request against a resident SLC.  ``threshold_geo2rdr`` and
+    ``num_iter_geo2rdr`` are the request's geo2rdr convergence arguments
+    (geocode_slc's of the same names); ``kwargs`` adds other geocode_slc
+    keyword arguments (outputs such as ``az_index_block`` included)."""
     slc_key: Any
     geogrid: Any
     arrival: float = 0.0              # seconds from the start of the trace
     kwargs: dict = field(default_factory=dict)
+    threshold_geo2rdr: float = 1e-8
+    num_iter_geo2rdr: int = 25
     # filled in by the server
     geo: torch.Tensor | None = None
     mask: torch.Tensor | None = None
@@ -136,17 +142,19 @@ class AdmissionPolicy:
         self.max_in_flight = max_in_flight
         self.max_batch = max_batch
 
-    def select(self, pending: collections.deque, used_bytes: int, in_flight: int):
-        """Pop and return (admitted, rejected) requests from the head of ``pending``."""
+    def select(self, pending: collections.deque, used_bytes: int, in_flight: int, resident_bytes: int = 0):
+        """Pop and return (admitted, rejected) requests from the head of
+        ``pending``.  ``resident_bytes`` (the resident store) and
+        ``used_bytes`` (requests in flight) are held against the budget."""
         admitted, rejected = [], []
         if in_flight >= self.max_in_flight:
             return admitted, rejected
-        free = self.budget - used_bytes
+        free = self.budget - resident_bytes - used_bytes
         while pending and len(admitted) < self.max_batch:
             r = pending[0]
-            if r.footprint > self.budget:
+            if r.footprint > self.budget - resident_bytes:
                 pending.popleft()
-                r.error = "request larger than the HBM budget"
+                r.error = "request larger than the HBM budget left by the resident store"
                 rejected.append(r)
                 continue
             if r.footprint > free:
@@ -200,7 +208,8 @@ class GeocodeServer:
         kw = dict(mask_block=r.mask, az_carrier=s.az_carrier, rg_carrier=s.rg_carrier, rdr_deramped=True)
         kw.update(r.kwargs)
         return GeocodeRequest(r.geo, s.slc, self.store.dem, s.radar_grid, g, s.orbit, s.native_doppler,
-                              s.image_grid_doppler, r.kwargs.get("ellipsoid") or _default_ellipsoid(), 1e-8, 25,
+                              s.image_grid_doppler, r.kwargs.get("ellipsoid") or _default_ellipsoid(),
+                              r.threshold_geo2rdr, r.num_iter_geo2rdr,
                               {k: v for k, v in kw.items() if k != "ellipsoid"})
 
     def _retire(self, now_fn) -> int:
@@ -242,7 +251,7 @@ class GeocodeServer:
     def _admit(self, now_fn, finished: list) -> int:
         if not self.free_slots or not self.pending:
             return 0
-        admitted, rejected = self.policy.select(self.pending, self.used, len(self.in_flight))
+        admitted, rejected = self.policy.select(self.pending, self.used, len(self.in_flight), self.store.nbytes)
         for r in rejected:
             r.t_done = now_fn()
             finished.append(r)
@@ -341,10 +350,11 @@ def serve_plain(store: ResidentStore, trace: list[ServeRequest], geo2rdr_precisi
         r.geo = torch.empty((g.length, g.width), dtype=torch.complex64, device=store.dev)
         r.mask = torch.empty((g.length, g.width), dtype=torch.uint8, device=store.dev)
         r.t_admit = time.perf_counter() - t0
+        kw = dict(mask_block=r.mask, az_carrier=s.az_carrier, rg_carrier=s.rg_carrier, rdr_deramped=True)
+        kw.update({k: v for k, v in r.kwargs.items() if k != "ellipsoid"})
         geocode_slc(r.geo, s.slc, store.dem, s.radar_grid, g, s.orbit, s.native_doppler, s.image_grid_doppler,
-                    r.kwargs.get("ellipsoid") or _default_ellipsoid(), 1e-8, 25, mask_block=r.mask,
-                    az_carrier=s.az_carrier, rg_carrier=s.rg_carrier, rdr_deramped=True,
-                    geo2rdr_precision=geo2rdr_precision)
+                    r.kwargs.get("ellipsoid") or _default_ellipsoid(), r.threshold_geo2rdr, r.num_iter_geo2rdr,
+                    geo2rdr_precision=geo2rdr_precision, **kw)
         r.t_done = time.perf_counter() - t0
         if not keep_outputs:
             r.geo = r.mask = None

@@ -852,6 +852,176 @@ double now() {
 }  // namespace
 
 // ================================================================ geocode
+namespace {
+
+// Radar bounding box of a block's valid pixels (geocodeSlc.cpp:79-85, 210-221)
+struct Bbox {
+    int az0, az1, rg0, rg1;
+};
+
+// computeGeogridRadarIndicesAndMask (geocodeSlc.cpp:55-228) over geogrid
+// lines [line0, line0 + nlines) with the block's DEM interpolator.  Indices,
+// uncorrected slant range, mask and iteration counts are block-relative
+// (row blockLine = line - line0).  Returns 1 if a projection inverse failed.
+int radar_indices(const orc_geocode_args* a, const Proj& proj, const DEM& dem, long line0, long nlines,
+                  std::vector<double>& rgIdx, std::vector<double>& azIdx, std::vector<double>& uncorr,
+                  uint8_t* mask, const orc_subswaths* subswaths, uint8_t* out_niter, Bbox& bb) {
+    const orc_radar_grid& rg = a->radar_grid;
+    const orc_radar_grid& srg = a->sliced_radar_grid;
+    const orc_geo_grid& gg = a->geo_grid;
+    const size_t W = gg.width;
+    const bool useCorr = a->flatten_with_corrected_srange != 0;
+    const int chipHalf = SINC_ONE / 2;
+    int az0 = (int)rg.length - 1, az1 = 0, rg0 = (int)rg.width - 1, rg1 = 0;
+    int proj_fail = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(min : az0, rg0) reduction(max : az1, rg1)
+    for (long blockLine = 0; blockLine < nlines; ++blockLine) {
+        const long line = line0 + blockLine;
+        for (size_t pixel = 0; pixel < W; ++pixel) {
+            const size_t k = (size_t)blockLine * W + pixel;
+            double y = gg.start_y + gg.spacing_y * (line + 0.5);
+            double x = gg.start_x + gg.spacing_x * (pixel + 0.5);
+            double aztime = rg_sensing_mid(rg), srange = 0.0;
+            V3 llh;
+            if (proj.inverse({x, y, 0.0}, llh) != 0) {
+#pragma omp atomic write
+                proj_fail = 1;
+                continue;
+            }
+            llh.z = dem_interp_lonlat(dem, llh.x, llh.y);
+            int niter = 0;
+            int st = geo2rdr_detail(&aztime, &srange, llh, a->ell_a, a->ell_e2, &a->orbit,
+                                    &a->image_grid_doppler, rg.wavelength, rg.look_side, aztime,
+                                    a->threshold_geo2rdr, a->numiter_geo2rdr, 1.0e-8, &niter);
+            if (out_niter) out_niter[k] = st == G_OK ? (uint8_t)std::min(niter, 255) : 0;
+            if (st != G_OK) continue;
+            if (!useCorr) uncorr[k] = srange;
+            if (lut_contains(&a->az_time_correction, aztime, srange))
+                aztime += lut_eval(&a->az_time_correction, aztime, srange);
+            if (lut_contains(&a->srange_correction, aztime, srange))
+                srange += lut_eval(&a->srange_correction, aztime, srange);
+            if (!rg_contains(srg, aztime, srange) || !lut_contains(&a->native_doppler, aztime, srange))
+                continue;
+            double azc = (aztime - rg.sensing_start) * rg.prf;
+            double rgc = (srange - rg.starting_range) / rg.range_pixel_spacing;
+            const int intAz = (int)std::floor(azc);
+            const int intRg = (int)std::floor(rgc);
+            bool corners = true;
+            if ((intRg < chipHalf) || (intRg >= (rg.width - chipHalf)) || (intAz < chipHalf) ||
+                (intAz >= (rg.length - chipHalf)))
+                corners = false;
+            if (subswaths && mask) {
+                unsigned char m = (unsigned char)subswath_of(subswaths, intAz, intRg);
+                if (m != 0) {
+                    const int ext[2] = {-chipHalf, chipHalf};
+                    for (int ai = 0; ai < 2; ++ai)
+                        for (int ri = 0; ri < 2; ++ri)
+                            if (subswath_of(subswaths, intAz + ext[ai], intRg + ext[ri]) == 0) { m = 0; break; }
+                }
+                mask[k] = m;
+            } else if (corners && mask) {
+                mask[k] = 1;
+            }
+            az0 = std::min(az0, (int)std::floor(azc));
+            az1 = std::max(az1, (int)(std::ceil(azc) - 1));
+            rg0 = std::min(rg0, (int)std::floor(rgc));
+            rg1 = std::max(rg1, (int)(std::ceil(rgc) - 1));
+            rgIdx[k] = rgc;
+            azIdx[k] = azc;
+        }
+    }
+    bb = Bbox{az0, az1, rg0, rg1};
+    return proj_fail;
+}
+
+// carrierPhaseDeramp (geocodeSlc.cpp:240-274) of an inL x inW radar block
+// whose first sample is line azFirst, sample rgFirst of the radar grid
+void deramp_block(const orc_geocode_args* a, cf* rdr, long inL, long inW, size_t azFirst, size_t rgFirst) {
+    const orc_radar_grid& rg = a->radar_grid;
+#pragma omp parallel for
+    for (long ii = 0; ii < inL * inW; ++ii) {
+        size_t i = ii / inW, j = ii % inW;
+        const size_t i_az = i + azFirst;
+        const double az = rg.sensing_start + i_az / rg.prf;
+        const size_t j_rg = j + rgFirst;
+        const double r = rg.starting_range + j_rg * rg.range_pixel_spacing;
+        const float carrierPhase = azrg_eval(&a->rg_carrier, az, r) + azrg_eval(&a->az_carrier, az, r);
+        const cf c{std::cos(carrierPhase), -std::sin(carrierPhase)};
+        rdr[ii] = cmul(rdr[ii], c);
+    }
+}
+
+// interpolate (geocodeSlc.cpp:409-511): N geo pixels from the deramped block
+void interpolate_block(const orc_geocode_args* a, const cf* rdr, long inL, long inW, size_t azFirst,
+                       size_t rgFirst, const double* rgIdx, const double* azIdx, size_t N, cf* geo) {
+    const orc_radar_grid& rg = a->radar_grid;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long ii = 0; ii < (long)N; ++ii) {
+        const double uRg = rgIdx[ii], uAz = azIdx[ii];
+        if (std::isnan(uRg) || std::isnan(uAz)) continue;
+        double RgIndex = uRg - (double)rgFirst;
+        double AzIndex = uAz - (double)azFirst;
+        const int intRg = (int)RgIndex, intAz = (int)AzIndex;
+        const double fracRg = RgIndex - intRg, fracAz = AzIndex - intAz;
+        if ((intRg < SINC_HALF) || (intRg >= (inW - SINC_HALF))) continue;
+        if ((intAz < SINC_HALF) || (intAz >= (inL - SINC_HALF))) continue;
+        const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
+        const double az = rg.sensing_start + uAz / rg.prf;
+        if (!lut_contains(&a->native_doppler, az, rng)) continue;
+        const double doppFreq = lut_eval(&a->native_doppler, az, rng) * 2 * M_PI / rg.prf;
+        cf chip[SINC_ONE * SINC_ONE];
+        for (int r9 = 0; r9 < SINC_ONE; ++r9) {
+            const int chipRow = intAz + r9 - SINC_HALF;
+            const double doppPhase = doppFreq * (r9 - SINC_HALF);
+            const cf dv{(float)std::cos(doppPhase), (float)-std::sin(doppPhase)};
+            for (int c9 = 0; c9 < SINC_ONE; ++c9) {
+                const int chipCol = intRg + c9 - SINC_HALF;
+                chip[r9 * SINC_ONE + c9] = cmul(rdr[(size_t)chipRow * inW + chipCol], dv);
+            }
+        }
+        const cf cval = sinc2d_chip(chip, SINC_ONE, SINC_ONE, SINC_HALF + fracRg, SINC_HALF + fracAz);
+        const double back = doppFreq * fracAz;
+        const cf bv{(float)std::cos(back), (float)std::sin(back)};
+        geo[ii] = cmul(cval, bv);
+    }
+}
+
+// carrierPhaseRerampAndFlatten (geocodeSlc.cpp:298-394)
+void reramp_block(const orc_geocode_args* a, long inL, long inW, size_t azFirst, size_t rgFirst,
+                  const double* rgIdx, const double* azIdx, const double* uncorr, size_t N, cf* geo,
+                  double* carrier_phase, double* flatten_phase) {
+    const orc_radar_grid& rg = a->radar_grid;
+    const bool useCorr = a->flatten_with_corrected_srange != 0;
+    const int chipHalf = SINC_ONE / 2;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long ii = 0; ii < (long)N; ++ii) {
+        const double uRg = rgIdx[ii], uAz = azIdx[ii];
+        if (std::isnan(uRg) || std::isnan(uAz)) continue;
+        const double RgIndex = uRg - (double)rgFirst, AzIndex = uAz - (double)azFirst;
+        const int intRg = (int)RgIndex, intAz = (int)AzIndex;
+        if ((intRg < chipHalf) || (intRg >= (inW - chipHalf))) continue;
+        if ((intAz < chipHalf) || (intAz >= (inL - chipHalf))) continue;
+        const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
+        const double az = rg.sensing_start + uAz / rg.prf;
+        if (!lut_contains(&a->native_doppler, az, rng)) continue;
+        const double carrierPhase = azrg_eval(&a->rg_carrier, az, rng) + azrg_eval(&a->az_carrier, az, rng);
+        const double sRngFlatten = useCorr ? rng : uncorr[ii];
+        const double flattenPhase = 4.0 * (M_PI / rg.wavelength) * sRngFlatten;
+        double totalPhase = 0.0;
+        if (a->reramp) totalPhase += carrierPhase;
+        if (a->flatten) totalPhase += flattenPhase;
+        if (carrier_phase) carrier_phase[ii] = carrierPhase;
+        if (flatten_phase) flatten_phase[ii] = flattenPhase;
+        const cf c{(float)std::cos(totalPhase), (float)std::sin(totalPhase)};
+        geo[ii] = cmul(geo[ii], c);
+    }
+}
+
+}  // namespace
+
+// Array mode (geocodeSlc.cpp:831-968): the whole geogrid is one block with
+// one DEM window; the caller's radar blocks start at (first_azimuth_line,
+// first_range_sample).
 extern "C" int orc_geocode_slc(orc_geocode_args* a) {
     g_err.clear();
     const orc_radar_grid& rg = a->radar_grid;
@@ -879,62 +1049,10 @@ extern "C" int orc_geocode_slc(orc_geocode_args* a) {
     const bool useCorr = a->flatten_with_corrected_srange != 0;
     if (!useCorr) uncorr.assign(N, (double)a->invalid_re);
 
-    // ---- computeGeogridRadarIndicesAndMask, geocodeSlc.cpp:55-228
     double t_start = now();
-    const int chipHalf = SINC_ONE / 2;
-    int proj_fail = 0;
-#pragma omp parallel for schedule(dynamic, 4)
-    for (long line = 0; line < (long)L; ++line) {
-        for (size_t pixel = 0; pixel < W; ++pixel) {
-            const size_t k = (size_t)line * W + pixel;
-            double y = gg.start_y + gg.spacing_y * (line + 0.5);
-            double x = gg.start_x + gg.spacing_x * (pixel + 0.5);
-            double aztime = rg_sensing_mid(rg), srange = 0.0;
-            V3 llh;
-            if (proj.inverse({x, y, 0.0}, llh) != 0) {
-#pragma omp atomic write
-                proj_fail = 1;
-                continue;
-            }
-            llh.z = dem_interp_lonlat(dem, llh.x, llh.y);
-            int niter = 0;
-            int st = geo2rdr_detail(&aztime, &srange, llh, a->ell_a, a->ell_e2, &a->orbit,
-                                    &a->image_grid_doppler, rg.wavelength, rg.look_side, aztime,
-                                    a->threshold_geo2rdr, a->numiter_geo2rdr, 1.0e-8, &niter);
-            if (a->out_niter) a->out_niter[k] = st == G_OK ? (uint8_t)std::min(niter, 255) : 0;
-            if (st != G_OK) continue;
-            if (!useCorr) uncorr[k] = srange;
-            if (lut_contains(&a->az_time_correction, aztime, srange))
-                aztime += lut_eval(&a->az_time_correction, aztime, srange);
-            if (lut_contains(&a->srange_correction, aztime, srange))
-                srange += lut_eval(&a->srange_correction, aztime, srange);
-            if (!rg_contains(srg, aztime, srange) || !lut_contains(&a->native_doppler, aztime, srange))
-                continue;
-            double azc = (aztime - rg.sensing_start) * rg.prf;
-            double rgc = (srange - rg.starting_range) / rg.range_pixel_spacing;
-            const int intAz = (int)std::floor(azc);
-            const int intRg = (int)std::floor(rgc);
-            bool corners = true;
-            if ((intRg < chipHalf) || (intRg >= (rg.width - chipHalf)) || (intAz < chipHalf) ||
-                (intAz >= (rg.length - chipHalf)))
-                corners = false;
-            if (a->subswaths && a->mask) {
-                unsigned char m = (unsigned char)subswath_of(a->subswaths, intAz, intRg);
-                if (m != 0) {
-                    const int ext[2] = {-chipHalf, chipHalf};
-                    for (int ai = 0; ai < 2; ++ai)
-                        for (int ri = 0; ri < 2; ++ri)
-                            if (subswath_of(a->subswaths, intAz + ext[ai], intRg + ext[ri]) == 0) { m = 0; break; }
-                }
-                a->mask[k] = m;
-            } else if (corners && a->mask) {
-                a->mask[k] = 1;
-            }
-            rgIdx[k] = rgc;
-            azIdx[k] = azc;
-        }
-    }
-    if (proj_fail) return fail("Inverse projection transformation failed");
+    Bbox bb;
+    if (radar_indices(a, proj, dem, 0, (long)L, rgIdx, azIdx, uncorr, a->mask, a->subswaths, a->out_niter, bb))
+        return fail("Inverse projection transformation failed");
     a->phase_seconds[0] = now() - t_start;
     a->phase_seconds[1] = a->phase_seconds[2] = a->phase_seconds[3] = 0.0;
 
@@ -947,77 +1065,93 @@ extern "C" int orc_geocode_slc(orc_geocode_args* a) {
     for (int b = 0; b < a->n_blocks; ++b) {
         cf* rdr = reinterpret_cast<cf*>(a->rdr_blocks[b]);
         cf* geo = reinterpret_cast<cf*>(a->geo_blocks[b]);
-        // ---- carrierPhaseDeramp, geocodeSlc.cpp:240-274
         t_start = now();
-#pragma omp parallel for
-        for (long ii = 0; ii < inL * inW; ++ii) {
-            size_t i = ii / inW, j = ii % inW;
-            const size_t i_az = i + azFirst;
-            const double az = rg.sensing_start + i_az / rg.prf;
-            const size_t j_rg = j + rgFirst;
-            const double r = rg.starting_range + j_rg * rg.range_pixel_spacing;
-            const float carrierPhase = azrg_eval(&a->rg_carrier, az, r) + azrg_eval(&a->az_carrier, az, r);
-            const cf c{std::cos(carrierPhase), -std::sin(carrierPhase)};
-            rdr[ii] = cmul(rdr[ii], c);
-        }
+        deramp_block(a, rdr, inL, inW, azFirst, rgFirst);
         a->phase_seconds[1] += now() - t_start;
-        // ---- interpolate, geocodeSlc.cpp:409-511
         t_start = now();
-#pragma omp parallel for schedule(dynamic, 4096)
-        for (long ii = 0; ii < (long)N; ++ii) {
-            const double uRg = rgIdx[ii], uAz = azIdx[ii];
-            if (std::isnan(uRg) || std::isnan(uAz)) continue;
-            double RgIndex = uRg - (double)rgFirst;
-            double AzIndex = uAz - (double)azFirst;
-            const int intRg = (int)RgIndex, intAz = (int)AzIndex;
-            const double fracRg = RgIndex - intRg, fracAz = AzIndex - intAz;
-            if ((intRg < SINC_HALF) || (intRg >= (inW - SINC_HALF))) continue;
-            if ((intAz < SINC_HALF) || (intAz >= (inL - SINC_HALF))) continue;
-            const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
-            const double az = rg.sensing_start + uAz / rg.prf;
-            if (!lut_contains(&a->native_doppler, az, rng)) continue;
-            const double doppFreq = lut_eval(&a->native_doppler, az, rng) * 2 * M_PI / rg.prf;
-            cf chip[SINC_ONE * SINC_ONE];
-            for (int r9 = 0; r9 < SINC_ONE; ++r9) {
-                const int chipRow = intAz + r9 - SINC_HALF;
-                const double doppPhase = doppFreq * (r9 - SINC_HALF);
-                const cf dv{(float)std::cos(doppPhase), (float)-std::sin(doppPhase)};
-                for (int c9 = 0; c9 < SINC_ONE; ++c9) {
-                    const int chipCol = intRg + c9 - SINC_HALF;
-                    chip[r9 * SINC_ONE + c9] = cmul(rdr[(size_t)chipRow * inW + chipCol], dv);
-                }
-            }
-            const cf cval = sinc2d_chip(chip, SINC_ONE, SINC_ONE, SINC_HALF + fracRg, SINC_HALF + fracAz);
-            const double back = doppFreq * fracAz;
-            const cf bv{(float)std::cos(back), (float)std::sin(back)};
-            geo[ii] = cmul(cval, bv);
-        }
+        interpolate_block(a, rdr, inL, inW, azFirst, rgFirst, rgIdx.data(), azIdx.data(), N, geo);
         a->phase_seconds[2] += now() - t_start;
-        // ---- carrierPhaseRerampAndFlatten, geocodeSlc.cpp:298-394
         t_start = now();
-#pragma omp parallel for schedule(dynamic, 4096)
-        for (long ii = 0; ii < (long)N; ++ii) {
-            const double uRg = rgIdx[ii], uAz = azIdx[ii];
-            if (std::isnan(uRg) || std::isnan(uAz)) continue;
-            const double RgIndex = uRg - (double)rgFirst, AzIndex = uAz - (double)azFirst;
-            const int intRg = (int)RgIndex, intAz = (int)AzIndex;
-            if ((intRg < chipHalf) || (intRg >= (inW - chipHalf))) continue;
-            if ((intAz < chipHalf) || (intAz >= (inL - chipHalf))) continue;
-            const double rng = rg.starting_range + uRg * rg.range_pixel_spacing;
-            const double az = rg.sensing_start + uAz / rg.prf;
-            if (!lut_contains(&a->native_doppler, az, rng)) continue;
-            const double carrierPhase = azrg_eval(&a->rg_carrier, az, rng) + azrg_eval(&a->az_carrier, az, rng);
-            const double sRngFlatten = useCorr ? rng : uncorr[ii];
-            const double flattenPhase = 4.0 * (M_PI / rg.wavelength) * sRngFlatten;
-            double totalPhase = 0.0;
-            if (a->reramp) totalPhase += carrierPhase;
-            if (a->flatten) totalPhase += flattenPhase;
-            if (a->carrier_phase) a->carrier_phase[ii] = carrierPhase;
-            if (a->flatten_phase) a->flatten_phase[ii] = flattenPhase;
-            const cf c{(float)std::cos(totalPhase), (float)std::sin(totalPhase)};
-            geo[ii] = cmul(geo[ii], c);
-        }
+        reramp_block(a, inL, inW, azFirst, rgFirst, rgIdx.data(), azIdx.data(), useCorr ? nullptr : uncorr.data(), N,
+                     geo, a->carrier_phase, a->flatten_phase);
         a->phase_seconds[3] += now() - t_start;
+    }
+    return 0;
+}
+
+// Raster mode (geocodeSlc.cpp:605-828).  rdr_blocks are the input raster's
+// bands over the whole radar grid (rdr_length x rdr_width = the grid), read
+// only; geo_blocks, carrier_phase and flatten_phase the output rasters over
+// the whole geogrid.  Per block of lines_per_block geogrid lines: the
+// block's own DEM window, the radar indices and their bounding box, the box
+// widened by 5 samples and clamped to the radar grid, invalid fill (and
+// invalid_re in the phase rasters), then per band the box read out of the
+// input raster, deramped, interpolated and reramped.  mask, the offsets and
+// subswaths are not used (the reference's raster mode has none).
+extern "C" int orc_geocode_slc_raster(orc_geocode_args* a, int32_t lines_per_block) {
+    g_err.clear();
+    const orc_radar_grid& rg = a->radar_grid;
+    const orc_geo_grid& gg = a->geo_grid;
+    const long W = gg.width, Lg = gg.length;
+    if (lines_per_block < 1) return fail("lines_per_block must be positive");
+    if (a->n_blocks < 1) return fail("number of input and output bands differ");
+    if (a->rdr_length != rg.length || a->rdr_width != rg.width)
+        return fail("input raster shape differs from the radar grid");
+#ifdef _OPENMP
+    if (a->nthreads > 0) omp_set_num_threads(a->nthreads);
+#endif
+    if (validate_slice(rg, a->sliced_radar_grid)) return 1;
+    Proj proj;
+    if (!proj.init(gg.epsg)) return fail("Unknown EPSG code (in factory): " + std::to_string(gg.epsg));
+    (void)sinc_table();
+    const bool useCorr = a->flatten_with_corrected_srange != 0;
+    const long nBlocks = (Lg + lines_per_block - 1) / lines_per_block;
+    for (long block = 0; block < nBlocks; ++block) {
+        const long lineStart = block * lines_per_block;
+        const long geoBlockLength = (block == nBlocks - 1) ? Lg - lineStart : lines_per_block;
+        const size_t n = (size_t)geoBlockLength * W;
+        const size_t off = (size_t)lineStart * W;
+        DEM dem;
+        if (dem_raster_to_interp(dem, &a->dem, &gg, (int)lineStart, (int)geoBlockLength, (int)W, a->dem_margin))
+            return 1;
+        std::vector<double> rgIdx(n, NaN), azIdx(n, NaN), uncorr;
+        if (!useCorr) uncorr.assign(n, (double)a->invalid_re);
+        std::vector<uint8_t> dummy_mask(n, 0);
+        Bbox bb;
+        if (radar_indices(a, proj, dem, lineStart, geoBlockLength, rgIdx, azIdx, uncorr, dummy_mask.data(), nullptr,
+                          nullptr, bb))
+            return fail("Inverse projection transformation failed");
+        if (a->out_az_index) std::memcpy(a->out_az_index + off, azIdx.data(), n * sizeof(double));
+        if (a->out_rg_index) std::memcpy(a->out_rg_index + off, rgIdx.data(), n * sizeof(double));
+        // invalid fill of the block and its phase rasters
+        for (int b = 0; b < a->n_blocks; ++b)
+            for (size_t k = 0; k < n; ++k) {
+                a->geo_blocks[b][2 * (off + k)] = a->invalid_re;
+                a->geo_blocks[b][2 * (off + k) + 1] = a->invalid_im;
+            }
+        if (a->carrier_phase) std::fill(a->carrier_phase + off, a->carrier_phase + off + n, (double)a->invalid_re);
+        if (a->flatten_phase) std::fill(a->flatten_phase + off, a->flatten_phase + off + n, (double)a->invalid_re);
+        // geocodeSlc.cpp:740-750: interpolation margin, clamped to the radar grid
+        const int interp_margin = 5;
+        const int az0 = std::max(bb.az0 - interp_margin, 0);
+        const int rg0 = std::max(bb.rg0 - interp_margin, 0);
+        const int az1 = std::min(bb.az1 + interp_margin, (int)(rg.length - 1));
+        const int rg1 = std::min(bb.rg1 + interp_margin, (int)(rg.width - 1));
+        if (az0 > az1 || rg0 > rg1) continue;       // :752-770, no valid pixels
+        const long inL = az1 - az0 + 1, inW = rg1 - rg0 + 1;
+        std::vector<cf> rdr((size_t)inL * inW);
+        for (int b = 0; b < a->n_blocks; ++b) {
+            const cf* band = reinterpret_cast<const cf*>(a->rdr_blocks[b]);
+            for (long i = 0; i < inL; ++i)
+                std::memcpy(&rdr[(size_t)i * inW], band + (size_t)(az0 + i) * rg.width + rg0, inW * sizeof(cf));
+            cf* geo = reinterpret_cast<cf*>(a->geo_blocks[b]) + off;
+            deramp_block(a, rdr.data(), inL, inW, (size_t)az0, (size_t)rg0);
+            interpolate_block(a, rdr.data(), inL, inW, (size_t)az0, (size_t)rg0, rgIdx.data(), azIdx.data(), n, geo);
+            // the phase rasters are written for every band, with the same values
+            reramp_block(a, inL, inW, (size_t)az0, (size_t)rg0, rgIdx.data(), azIdx.data(),
+                         useCorr ? nullptr : uncorr.data(), n, geo, a->carrier_phase ? a->carrier_phase + off : nullptr,
+                         a->flatten_phase ? a->flatten_phase + off : nullptr);
+        }
     }
     return 0;
 }

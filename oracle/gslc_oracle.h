@@ -116,6 +116,13 @@ typedef struct {
 /* Returns 0 on success; >0 argument error (message via orc_last_error). */
 int orc_geocode_slc(orc_geocode_args* a);
 
+/* Raster mode of geocodeSlc (geocode/geocodeSlc.cpp:605-828): rdr_blocks
+ * are the input raster's bands over the whole radar grid (read only),
+ * geo_blocks / carrier_phase / flatten_phase the output rasters over the
+ * whole geogrid; processed in blocks of lines_per_block geogrid lines, each
+ * with its own DEM window and radar bounding box (+-5 samples). */
+int orc_geocode_slc_raster(orc_geocode_args* a, int32_t lines_per_block);
+
 /* isce3::cuda::geocode::Geocode::geocodeRasters for SINC_METHOD and
  * GDT_CFloat32 (cxx/isce3/cuda/geocode/Geocode.cu:87-287, 378-864), restated
  * on the CPU block by block, bounding boxes included. */

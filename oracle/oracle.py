@@ -17,15 +17,22 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libgslc_oracle.so"
+# Build variants: "" is the oracle proper (-ffp-contract=off, the reference's
+# x86-64 arithmetic on any host); "fma" is the same source with
+# floating-point contraction on (oracle/Makefile, target fma), used only to
+# measure how far two correct builds of one code disagree.
+_VARIANTS = {"": ("all", LIB), "fma": ("fma", HERE / "_build" / "libgslc_oracle_fma.so")}
 
 
-def build(force: bool = False) -> Path:
+def build(force: bool = False, variant: str = "") -> Path:
+    target, lib_path = _VARIANTS[variant]
     src = [HERE / "gslc_oracle.cpp", HERE / "gslc_oracle.h"]
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(p.stat().st_mtime for p in src):
-        r = subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], capture_output=True, text=True)
+    if force or not lib_path.exists() or lib_path.stat().st_mtime < max(p.stat().st_mtime for p in src):
+        cmd = ["make", "-C", str(HERE)] + (["-B"] if force else []) + [target]
+        r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    return LIB
+    return lib_path
 
 
 class Lut(C.Structure):
@@ -96,16 +103,18 @@ class RasterArgs(C.Structure):
                 ("out_rg_index", C.c_void_p), ("nthreads", C.c_int32)]
 
 
-_lib = None
+_libs: dict = {}
 
 
-def lib() -> C.CDLL:
-    global _lib
+def lib(variant: str = "") -> C.CDLL:
+    _lib = _libs.get(variant)
     if _lib is None:
-        build()
-        _lib = C.CDLL(str(LIB))
+        _lib = C.CDLL(str(build(variant=variant)))
+        _libs[variant] = _lib
         _lib.orc_geocode_slc.restype = C.c_int
         _lib.orc_geocode_slc.argtypes = [C.POINTER(Args)]
+        _lib.orc_geocode_slc_raster.restype = C.c_int
+        _lib.orc_geocode_slc_raster.argtypes = [C.POINTER(Args), C.c_int32]
         _lib.orc_geocode_rasters.restype = C.c_int
         _lib.orc_geocode_rasters.argtypes = [C.POINTER(RasterArgs)]
         _lib.orc_last_error.restype = C.c_char_p
@@ -225,11 +234,13 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid
                 reramp=True, az_carrier=None, rg_carrier=None, az_time_correction=None, srange_correction=None,
                 flatten_with_corrected_srange=False, invalid_value=np.nan + np.nan * 1j,
                 carrier_phase_block=None, flatten_phase_block=None, *, az_index_block=None, rg_index_block=None,
-                uncorrected_srange_block=None, dem_margin=50, nthreads=0, inplace_deramp=False, niter_block=None):
+                uncorrected_srange_block=None, dem_margin=50, nthreads=0, inplace_deramp=False, niter_block=None,
+                build_variant=""):
     """Run the oracle with geocode_slc's arguments; outputs are written in place.
 
     Radar blocks are deramped on copies unless ``inplace_deramp``.  Returns
     the per-phase wall times (index pass, deramp, interpolate, reramp) in s.
+    ``build_variant`` selects the oracle build ("" or "fma").
     """
     from isce3_gb300.core import LUT2d
     az_carrier = az_carrier if az_carrier is not None else LUT2d()
@@ -285,10 +296,71 @@ def geocode_slc(geo_data_blocks, rdr_data_blocks, dem_raster, radargrid, geogrid
         ss.valid = _ptr(packed)
         keep.append(ss)
         a.subswaths = C.pointer(ss)
-    st = lib().orc_geocode_slc(C.byref(a))
+    L = lib(build_variant)
+    st = L.orc_geocode_slc(C.byref(a))
     if st != 0:
-        raise ValueError(lib().orc_last_error().decode())
+        raise ValueError(L.orc_last_error().decode())
     return list(a.phase_seconds)
+
+
+def geocode_slc_raster(output_raster, input_raster, dem_raster, radargrid, geogrid, orbit, native_doppler,
+                       image_grid_doppler, ellipsoid, threshold_geo2rdr=1.0e-9, numiter_geo2rdr=25,
+                       lines_per_block=1000, flatten=True, reramp=True, azimuth_carrier=None, range_carrier=None,
+                       az_time_correction=None, srange_correction=None, flatten_with_corrected_srange=False,
+                       invalid_value=np.nan + np.nan * 1j, carrier_phase_raster=None, flatten_phase_raster=None, *,
+                       az_index_block=None, rg_index_block=None, dem_margin=50, nthreads=0):
+    """The raster mode of geocodeSlc (geocode/geocodeSlc.cpp:605-828) on the
+    CPU, with the pybind overload's arguments: every band of
+    ``input_raster`` (read only) into ``output_raster``, written in place."""
+    from isce3_gb300.core import LUT2d, Poly2d
+    azimuth_carrier = azimuth_carrier if azimuth_carrier is not None else Poly2d()
+    range_carrier = range_carrier if range_carrier is not None else Poly2d()
+    az_time_correction = az_time_correction if az_time_correction is not None else LUT2d()
+    srange_correction = srange_correction if srange_correction is not None else LUT2d()
+    keep = _Keep()
+    n = input_raster.num_bands()
+    rdr = [np.ascontiguousarray(input_raster.band(i), dtype=np.complex64) for i in range(n)]
+    geo = [output_raster.band(i) for i in range(n)]
+    for g in geo:
+        assert g.flags.c_contiguous and g.dtype == np.complex64
+    keep.extend(rdr)
+    a = Args()
+    a.radar_grid = radar_struct(radargrid)
+    a.sliced_radar_grid = radar_struct(radargrid)
+    a.geo_grid = geo_struct(geogrid)
+    a.orbit = orbit_struct(orbit, keep)
+    a.native_doppler = lut_struct(native_doppler, keep)
+    a.image_grid_doppler = lut_struct(image_grid_doppler, keep)
+    a.az_time_correction = lut_struct(az_time_correction, keep)
+    a.srange_correction = lut_struct(srange_correction, keep)
+    a.az_carrier = azrg_struct(azimuth_carrier, keep)
+    a.rg_carrier = azrg_struct(range_carrier, keep)
+    a.ell_a, a.ell_e2 = ellipsoid.a, ellipsoid.e2
+    a.threshold_geo2rdr, a.numiter_geo2rdr = threshold_geo2rdr, numiter_geo2rdr
+    a.flatten, a.reramp = int(flatten), int(reramp)
+    a.flatten_with_corrected_srange = int(flatten_with_corrected_srange)
+    inv = complex(invalid_value)
+    a.invalid_re, a.invalid_im = np.float32(inv.real), np.float32(inv.imag)
+    a.n_blocks = n
+    a.rdr_length, a.rdr_width = rdr[0].shape
+    rp = (C.c_void_p * n)(*[_ptr(r) for r in rdr])
+    gp = (C.c_void_p * n)(*[_ptr(g) for g in geo])
+    a.rdr_blocks = C.cast(rp, C.POINTER(C.c_void_p))
+    a.geo_blocks = C.cast(gp, C.POINTER(C.c_void_p))
+
+    def opt(x):
+        return _ptr(x) if x is not None and x.size else None
+    a.carrier_phase = opt(carrier_phase_raster.data if carrier_phase_raster is not None else None)
+    a.flatten_phase = opt(flatten_phase_raster.data if flatten_phase_raster is not None else None)
+    a.out_az_index = opt(az_index_block)
+    a.out_rg_index = opt(rg_index_block)
+    a.dem = dem_struct(dem_raster, keep)
+    a.dem_margin = dem_margin
+    a.nthreads = nthreads
+    L = lib()
+    st = L.orc_geocode_slc_raster(C.byref(a), int(lines_per_block))
+    if st != 0:
+        raise ValueError(L.orc_last_error().decode())
 
 
 def geocode_rasters(output_rasters, input_rasters, radar_geometry, geogrid, dem_raster, lines_per_block=1000,

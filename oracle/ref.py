@@ -1,0 +1,115 @@
+"""ctypes front end of the reference's own geometry code — TEST INFRASTRUCTURE.
+
+oracle/Makefile's "ref" target compiles the reference's geo2rdr
+(geometry/detail/Geo2Rdr.icc), Hermite orbit interpolation
+(core/detail/InterpolateOrbit.icc, core/Linspace.icc), Ellipsoid::lonLatToXyz
+(core/Ellipsoid.h) and UTM projection (core/Projections.cpp) from the
+reference checkout, behind oracle/ref_geo.cpp's C ABI, into oracle/_ref/.
+Tests use it to pin the oracle's restatement of those functions bit for bit.
+The checkout exists only where the reference is mounted; elsewhere
+``available()`` is False and the pins are skipped.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF = Path(os.environ.get("ISCE3_REFERENCE", "/root/reference"))
+LIBS = {"": HERE / "_ref" / "libref_geo.so", "fma": HERE / "_ref" / "libref_geo_fma.so"}
+_SRC = [HERE / "ref_geo.cpp", HERE / "ref_shim" / "Eigen" / "Dense"]
+_libs: dict = {}
+
+
+def available() -> bool:
+    return (REF / "cxx" / "isce3" / "geometry" / "detail" / "Geo2Rdr.icc").exists()
+
+
+def build(force: bool = False) -> bool:
+    """Compile both builds (plain and contracting) if the checkout is present."""
+    if not available():
+        return False
+    newest = max(p.stat().st_mtime for p in _SRC)
+    if force or any(not p.exists() or p.stat().st_mtime < newest for p in LIBS.values()):
+        cmd = ["make", "-C", str(HERE)] + (["-B"] if force else []) + ["ref", f"REF={REF}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
+    return True
+
+
+def lib(variant: str = "") -> C.CDLL:
+    L = _libs.get(variant)
+    if L is None:
+        if not build():
+            raise RuntimeError("the reference checkout is not available")
+        L = C.CDLL(str(LIBS[variant]))
+        L.ref_orbit_interpolate.restype = C.c_int64
+        L.ref_orbit_interpolate.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p,
+                                            C.c_int64, C.c_void_p, C.c_void_p]
+        L.ref_lonlat_to_xyz.restype = None
+        L.ref_lonlat_to_xyz.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_int64, C.c_void_p]
+        L.ref_geo2rdr.restype = None
+        L.ref_geo2rdr.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                  C.c_void_p, C.c_int64, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+                                  C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_utm_inverse.restype = C.c_int64
+        L.ref_utm_inverse.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p]
+        L.ref_utm_forward.restype = C.c_int64
+        L.ref_utm_forward.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p]
+        _libs[variant] = L
+    return L
+
+
+def _orbit_arrays(orbit):
+    return (np.ascontiguousarray(orbit.position, np.float64), np.ascontiguousarray(orbit.velocity, np.float64))
+
+
+def orbit_interpolate(orbit, t, variant: str = ""):
+    """Orbit::interpolate (FillNaN) at the times t: (pos, vel) of shape (m, 3)."""
+    pos, vel = _orbit_arrays(orbit)
+    t = np.ascontiguousarray(t, np.float64)
+    P, V = np.zeros((t.size, 3)), np.zeros((t.size, 3))
+    lib(variant).ref_orbit_interpolate(pos.ctypes.data, vel.ctypes.data, orbit.size, orbit.t0, orbit.spacing,
+                                       t.ctypes.data, t.size, P.ctypes.data, V.ctypes.data)
+    return P, V
+
+
+def lonlat_to_xyz(ellipsoid, llh, variant: str = ""):
+    llh = np.ascontiguousarray(llh, np.float64).reshape(-1, 3)
+    xyz = np.zeros_like(llh)
+    lib(variant).ref_lonlat_to_xyz(ellipsoid.a, ellipsoid.e2, llh.ctypes.data, len(llh), xyz.ctypes.data)
+    return xyz
+
+
+def geo2rdr(llh, ellipsoid, orbit, wavelength, side, t_guess, threshold, maxiter, delta_range,
+            doppler_ref_value=0.0, bounds_error=True, variant: str = ""):
+    """isce3::geometry::geo2rdr at m points with an image-grid Doppler table
+    without data (reference value ``doppler_ref_value``): (t, r, status)."""
+    pos, vel = _orbit_arrays(orbit)
+    llh = np.ascontiguousarray(llh, np.float64).reshape(-1, 3)
+    m = len(llh)
+    t, r, st = np.zeros(m), np.zeros(m), np.zeros(m, np.int32)
+    lib(variant).ref_geo2rdr(pos.ctypes.data, vel.ctypes.data, orbit.size, orbit.t0, orbit.spacing, ellipsoid.a,
+                             ellipsoid.e2, llh.ctypes.data, m, wavelength, int(side), t_guess, threshold,
+                             int(maxiter), delta_range, doppler_ref_value, int(bounds_error), t.ctypes.data,
+                             r.ctypes.data, st.ctypes.data)
+    return t, r, st
+
+
+def utm_inverse(epsg, xy, variant: str = ""):
+    xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+    out = np.zeros_like(xy)
+    bad = lib(variant).ref_utm_inverse(int(epsg), xy.ctypes.data, len(xy), out.ctypes.data)
+    return out, int(bad)
+
+
+def utm_forward(epsg, lonlat, variant: str = ""):
+    ll = np.ascontiguousarray(lonlat, np.float64).reshape(-1, 2)
+    out = np.zeros_like(ll)
+    bad = lib(variant).ref_utm_forward(int(epsg), ll.ctypes.data, len(ll), out.ctypes.data)
+    return out, int(bad)

@@ -264,3 +264,52 @@ def test_projection_failure_raises(c1):
     geo = np.zeros((8, 8), np.complex64)
     with pytest.raises(ValueError):
         geocode_slc(geo, c1.slc, c1.dem, c1.radar_grid, g, c1.orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-8, 25)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+@pytest.mark.parametrize("name", ["c1", "c2r"])
+def test_split_flip_fraction_within_cross_build(oracle_mod, name, precision):
+    """On the stored cross-build scenes (tests/xbuild_scenes.py) the GPU's
+    geometry splits and sinc-table flips against the oracle are at most 1.5x
+    the fraction by which the oracle's own contracting build (the reference's
+    aarch64 arithmetic, tests/test_oracle_cross_build.py) departs from it,
+    and at most 1e-3 of valid pixels; everything else within tolerance."""
+    import xbuild_scenes as xs
+    sc = xs.unpack(dict(np.load(xs.GOLDEN)), name)
+    plain = xs.run_oracle(oracle_mod, sc, "")
+    fused = xs.run_oracle(oracle_mod, sc, "fma")
+    r_x = xs.report(fused, plain)
+    g = sc.geogrid
+    shape = (g.length, g.width)
+    gpu = dict(geo=np.zeros(shape, np.complex64), mask=np.zeros(shape, np.uint8), az=np.zeros(shape),
+               rg=np.zeros(shape))
+    geocode_slc(gpu["geo"], sc.slc, sc.dem, sc.radar_grid, g, sc.orbit, sc.native_doppler, sc.image_grid_doppler,
+                sc.ellipsoid, sc.threshold, sc.maxiter, mask_block=gpu["mask"], az_index_block=gpu["az"],
+                rg_index_block=gpu["rg"], geo2rdr_precision=precision, **xs.carriers(sc))
+    r_g = xs.report(gpu, plain)
+    print(name, precision, "gpu:", r_g, "fused build:", r_x)
+    assert_parity(r_g, max_flip_fraction=1e-3)
+    assert r_g["flip_fraction"] <= 1.5 * r_x["flip_fraction"], (r_g["flip_fraction"], r_x["flip_fraction"])
+
+
+@pytest.mark.parametrize("method,precision", [("bilinear", "fp64"), ("bilinear", "ff"), ("nearest", "fp64")])
+def test_lut2d_carriers(oracle_mod, c1, method, precision):
+    """Data-bearing LUT2d azimuth and range carriers (the pybind overload for
+    AzRgFunc = LUT2d<double>, GeocodeSlc.cpp:337): the deramp evaluates them
+    at every radar sample (geocodeSlc.cpp:240-274) and the reramp at every
+    output pixel (:298-394).  The tables cover the radar grid with a margin;
+    the azimuth carrier is a TOPS-like quadratic in time, the range carrier
+    a slow ramp in range."""
+    rg = c1.radar_grid
+    rr = np.linspace(rg.starting_range - 20 * rg.range_pixel_spacing, rg.end_range + 20 * rg.range_pixel_spacing, 24)
+    tt = np.linspace(rg.sensing_start - 20 / rg.prf, rg.sensing_stop + 20 / rg.prf, 20)
+    T, R = np.meshgrid(tt - rg.sensing_mid, rr - rg.mid_range, indexing="ij")
+    az_car = LUT2d(rr, tt, 2 * np.pi * 180.0 * T + np.pi * 900.0 * T ** 2 + 1e-5 * R, method)
+    rg_car = LUT2d(rr, tt, 2e-3 * R + 0.3 * T, method)
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], az_carrier=az_car, rg_carrier=rg_car,
+                         geo2rdr_precision=precision)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 100000
+    # the carrier output holds the table values at the pixels' radar positions
+    w = np.isfinite(gpu["az"]) & (gpu["carrier"] != -7.0)
+    assert np.abs(gpu["carrier"][w]).max() > 1.0

@@ -6,6 +6,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from isce3_gb300 import synth  # noqa: E402
+from isce3_gb300.core import Ellipsoid, LUT2d  # noqa: E402
 from isce3_gb300.serve import GeocodeServer, ResidentStore, ServeRequest, serve_plain  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -48,7 +49,50 @@ def test_budget_limits_concurrency(served):
     sc, store, trace = served
     reqs = [ServeRequest(k, g, 0.0) for k, g, _ in trace[:8]]
     biggest = max(r.footprint for r in reqs)
-    server = GeocodeServer(store, budget_bytes=biggest, max_in_flight=3, max_batch=8)
+    # the resident store counts against the budget: room for one request at a time
+    server = GeocodeServer(store, budget_bytes=store.nbytes + biggest, max_in_flight=3, max_batch=8)
     stats = server.serve(reqs)
     assert stats["completed"] == 8
     assert stats["max_concurrent_batches"] >= 1
+
+
+def test_served_requests_match_oracle(oracle_mod):
+    """Requests on 30 m UTM grids, served by continuous batching over
+    resident SLCs deramped once at load, against the oracle geocoding the
+    original SLC with its carriers: masks exact, values within tolerance."""
+    import numpy as np
+    from oracle.compare import assert_parity, compare
+    sc = synth.scene_serving(seed=12, n_slc=2, lines=(1536, 2048), samples=(1536, 2048), device="cuda")
+    store = ResidentStore(sc.dem)
+    for s in sc.slcs:
+        store.add(s.key, s.slc, s.radar_grid, s.orbit, native_doppler=s.native_doppler, az_carrier=s.az_carrier,
+                  rg_carrier=s.rg_carrier)
+    trace = synth.serving_trace(sc, n_requests=6, rate_hz=5000.0, side=(128, 384), spacing=(30.0, 30.0), seed=13)
+    reqs = []
+    for key, g, t in trace:
+        shape = (g.length, g.width)
+        reqs.append(ServeRequest(key, g, t, dict(az_index_block=torch.empty(shape, dtype=torch.float64, device="cuda"),
+                                                 rg_index_block=torch.empty(shape, dtype=torch.float64, device="cuda"))))
+    server = GeocodeServer(store, budget_bytes=2 * 10 ** 9, max_in_flight=2, max_batch=4)
+    stats = server.serve(reqs, keep_outputs=True)
+    server.close()
+    assert stats["completed"] == len(reqs)
+    n_valid = 0
+    for r in reqs:
+        s = sc.slcs[r.slc_key]
+        g = r.geogrid
+        shape = (g.length, g.width)
+        ora = dict(geo=np.zeros(shape, np.complex64), mask=np.zeros(shape, np.uint8), az=np.zeros(shape),
+                   rg=np.zeros(shape))
+        oracle_mod.geocode_slc(ora["geo"], s.slc.cpu().numpy(), sc.dem, s.radar_grid, g, s.orbit,
+                               s.native_doppler, LUT2d(), Ellipsoid(), r.threshold_geo2rdr, r.num_iter_geo2rdr,
+                               mask_block=ora["mask"], az_index_block=ora["az"], rg_index_block=ora["rg"],
+                               az_carrier=s.az_carrier, rg_carrier=s.rg_carrier)
+        gg, gm = r.geo.cpu().numpy(), r.mask.cpu().numpy()
+        ga, gr = r.kwargs["az_index_block"].cpu().numpy(), r.kwargs["rg_index_block"].cpu().numpy()
+        rep = compare(gg, ora["geo"], ga, ora["az"], gr, ora["rg"], gm, ora["mask"])
+        print(g.spacing_x, shape, rep)
+        assert g.spacing_x == 30.0
+        assert_parity(rep, max_flip_fraction=1e-3)
+        n_valid += rep["n_valid"]
+    assert n_valid > 50000

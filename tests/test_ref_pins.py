@@ -1,0 +1,116 @@
+"""The oracle's geometry against the reference's own source, bit for bit.
+
+oracle/ref.py compiles the reference's geo2rdr (geometry/detail/Geo2Rdr.icc,
+called as geometry/geometry.cpp:241-251 does for geocodeSlc.cpp:120-123),
+Hermite orbit interpolation (core/detail/InterpolateOrbit.icc:10-109,
+core/Linspace.icc:77-89), Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190)
+and UTM::inverse / forward (core/Projections.cpp:171-232) where they lie in
+the reference checkout.  The oracle's restatement of each must return the
+same bits on the same inputs: these are the functions whose rounding decides
+the sinc-table rows and Newton stops the parity checker classifies.
+
+Skipped where the reference checkout is not mounted.
+"""
+import numpy as np
+import pytest
+
+from isce3_gb300 import synth
+from isce3_gb300.core import LUT2d
+
+from oracle import ref
+
+pytestmark = pytest.mark.skipif(not ref.available(), reason="reference checkout not mounted")
+
+
+@pytest.fixture(scope="module", params=["c1", "c2"])
+def scene(request):
+    if request.param == "c1":
+        return synth.scene_c1(seed=1, slc=False)
+    return synth.scene_c2(seed=2, length=16384, width=8192, geo=64, slc=False, dem_arcsec=30.0)
+
+
+def _ground_points(sc, m, seed):
+    """llh (rad, rad, m) spread over the geogrid's footprint, 0-3000 m high."""
+    rng = np.random.default_rng(seed)
+    g = sc.geogrid
+    x = g.start_x + g.spacing_x * rng.uniform(0, g.width, m)
+    y = g.start_y + g.spacing_y * rng.uniform(0, g.length, m)
+    if g.epsg == 4326:
+        lon, lat = np.radians(x), np.radians(y)
+    else:
+        ll, bad = ref.utm_inverse(g.epsg, np.stack([x, y], 1))
+        assert bad == 0
+        lon, lat = ll[:, 0], ll[:, 1]
+    return np.stack([lon, lat, rng.uniform(0.0, 3000.0, m)], 1)
+
+
+def test_orbit_interpolation_bits(oracle_mod, scene):
+    o = scene.orbit
+    span = o.spacing * (o.size - 1)
+    t = np.concatenate([np.linspace(o.t0 - 2.0, o.t0 + span + 2.0, 4001), o.t0 + o.spacing * np.arange(o.size)])
+    P, V = ref.orbit_interpolate(o, t)
+    for k in range(t.size):
+        po, vo, _st = oracle_mod.orbit_interpolate(o, t[k])
+        np.testing.assert_array_equal(po, P[k])
+        np.testing.assert_array_equal(vo, V[k])
+
+
+def test_lonlat_to_xyz_bits(oracle_mod, scene):
+    llh = _ground_points(scene, 2000, 3)
+    xyz = ref.lonlat_to_xyz(scene.ellipsoid, llh)
+    for k in range(len(llh)):
+        out = np.zeros(3)
+        oracle_mod.lib().orc_lonlat_to_xyz(scene.ellipsoid.a, scene.ellipsoid.e2, np.ascontiguousarray(llh[k]).ctypes.data,
+                                           out.ctypes.data)
+        np.testing.assert_array_equal(out, xyz[k])
+
+
+@pytest.mark.parametrize("doppler", [0.0, 37.5])
+def test_geo2rdr_bits(oracle_mod, scene, doppler):
+    """t, r and convergence identical, from sensingMid with deltaRange 1e-8
+    (geocodeSlc's call), for a zero and a constant image-grid Doppler."""
+    rg = scene.radar_grid
+    llh = _ground_points(scene, 4000, 5)
+    t, r, st = ref.geo2rdr(llh, scene.ellipsoid, scene.orbit, rg.wavelength, int(rg.lookside), rg.sensing_mid,
+                           scene.threshold, scene.maxiter, 1e-8, doppler)
+    dop = LUT2d()
+    dop.ref_value = doppler
+    assert (st == 0).sum() > 0.9 * len(llh)
+    for k in range(len(llh)):
+        to, ro, ok = oracle_mod.geo2rdr(llh[k], scene.ellipsoid, scene.orbit, dop, rg.wavelength, int(rg.lookside),
+                                        rg.sensing_mid, scene.threshold, scene.maxiter, 1e-8)
+        assert bool(ok) == (st[k] == 0), k
+        if ok:
+            assert to == t[k] and ro == r[k], (k, to - t[k], ro - r[k])
+
+
+def test_geo2rdr_outside_orbit_start_bits(oracle_mod):
+    """A start guess outside the orbit takes the coarse search
+    (Geo2Rdr.icc:50-112) on both sides."""
+    sc = synth.scene_c1(seed=1, slc=False)
+    rg = sc.radar_grid
+    llh = _ground_points(sc, 300, 7)
+    t_out = sc.orbit.t0 - 50.0
+    t, r, st = ref.geo2rdr(llh, sc.ellipsoid, sc.orbit, rg.wavelength, int(rg.lookside), t_out, 1e-8, 50, 10.0)
+    for k in range(len(llh)):
+        to, ro, ok = oracle_mod.geo2rdr(llh[k], sc.ellipsoid, sc.orbit, LUT2d(), rg.wavelength, int(rg.lookside),
+                                        t_out, 1e-8, 50, 10.0)
+        assert bool(ok) == (st[k] == 0)
+        if ok:
+            assert to == t[k] and ro == r[k]
+
+
+@pytest.mark.parametrize("epsg", [32611, 32601, 32660, 32733, 32718])
+def test_utm_bits(oracle_mod, epsg):
+    rng = np.random.default_rng(epsg)
+    m = 3000
+    xy = np.stack([rng.uniform(2.0e5, 8.0e5, m), rng.uniform(1.0e5, 9.3e6, m)], 1)
+    ll, bad = ref.utm_inverse(epsg, xy)
+    assert bad == 0
+    back, bad = ref.utm_forward(epsg, ll)
+    assert bad == 0
+    for k in range(m):
+        lon, lat, st = oracle_mod.proj_inverse(epsg, xy[k, 0], xy[k, 1])
+        assert st == 0 and lon == ll[k, 0] and lat == ll[k, 1]
+        x, y, st = oracle_mod.proj_forward(epsg, ll[k, 0], ll[k, 1])
+        assert st == 0 and x == back[k, 0] and y == back[k, 1]

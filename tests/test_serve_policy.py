@@ -53,3 +53,24 @@ def test_summary_percentiles():
     assert s["completed"] == 100 and s["output_px"] == 100 * 100
     assert abs(s["p50_ms"] - 50.5) < 1e-6 and abs(s["p99_ms"] - 99.01) < 1e-6
     assert s["mean_batch_requests"] == 10
+
+
+def test_resident_store_counts_against_budget():
+    """The resident store's bytes are held against the budget: a request that
+    fits the budget alone but not beside the store is rejected, and the room
+    left for admission shrinks by the store's size."""
+    reqs = [_req(100), _req(100)]
+    fp = reqs[0].footprint
+    pol = AdmissionPolicy(budget_bytes=3 * fp, max_in_flight=2, max_batch=8)
+    q = collections.deque(reqs)
+    adm, rej = pol.select(q, used_bytes=0, in_flight=0, resident_bytes=2 * fp)
+    assert adm == [reqs[0]] and not rej and list(q) == [reqs[1]]
+    adm, rej = pol.select(q, used_bytes=0, in_flight=0, resident_bytes=3 * fp - 1)
+    assert adm == [] and rej == [reqs[1]] and "resident" in reqs[1].error
+
+
+def test_request_geo2rdr_arguments_default_to_reference_values():
+    r = _req(10)
+    assert r.threshold_geo2rdr == 1e-8 and r.num_iter_geo2rdr == 25
+    r = ServeRequest(0, SimpleNamespace(length=4, width=4), 0.0, {}, 1e-9, 40)
+    assert r.threshold_geo2rdr == 1e-9 and r.num_iter_geo2rdr == 40

@@ -25,14 +25,14 @@ if not torch.cuda.is_available():
     pytest.skip("needs a CUDA GPU", allow_module_level=True)
 
 
-def _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep):
+def _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep, orbit=None, c32=False):
     """GeocodeArgs for device tensors, as isce3_gb300.geocode builds them."""
     holder = M.AzRgHolder()
     a = L.GeocodeArgs()
     a.radar_grid = M.radar_grid_desc(sc.radar_grid)
     a.sliced_radar_grid = M.radar_grid_desc(sc.radar_grid)
     a.geo_grid = M.geo_grid_desc(sc.geogrid)
-    a.orbit = M.orbit_desc(sc.orbit)
+    a.orbit = M.orbit_desc(orbit if orbit is not None else sc.orbit)
     a.native_doppler = M.lut_desc(sc.native_doppler, dev)
     a.image_grid_doppler = M.lut_desc(sc.image_grid_doppler, dev)
     a.az_time_correction = M.lut_desc(LUT2d(), dev)
@@ -52,20 +52,33 @@ def _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep):
     a.mask = mask.data_ptr()
     a.dem, dem_t = M.dem_raster_desc(sc.dem, sc.geogrid, 50, dev)
     a.dem_margin = 50
+    a.rdr_format = 1 if c32 else 0
     keep.extend([holder, rp, gp, dem_t])
     return a
 
 
-def _run(sc, az_carrier, rg_carrier, noalloc):
+def _run(sc, az_carrier, rg_carrier, noalloc, c32=False, inplace=False, measure=False):
+    """One call through the C ABI; returns (geo, mask[, radar block after])."""
     dev = torch.device("cuda", torch.cuda.current_device())
     g = sc.geogrid
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    lib = L.lib()
     slc = torch.from_numpy(sc.slc).to(dev)
+    if c32:
+        # complex32 samples (float16 pairs) as 32-bit words, by the library's codec
+        words = torch.empty(slc.shape, dtype=torch.int32, device=dev)
+        ctx = L.context(dev.index)
+        L.check(lib.gslc_complex64_to_complex32(ctx, C.c_void_p(slc.data_ptr()), C.c_void_p(words.data_ptr()),
+                                                 slc.numel(), stream), ctx)
+        slc = words
+    before = slc.clone()
     geo = torch.zeros((g.length, g.width), dtype=torch.complex64, device=dev)
     mask = torch.zeros((g.length, g.width), dtype=torch.uint8, device=dev)
     keep = []
-    a = _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep)
-    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-    lib = L.lib()
+    a = _args(sc, slc, geo, mask, az_carrier, rg_carrier, dev, keep, c32=c32)
+    a.inplace_deramp = int(inplace)
+    torch.cuda.synchronize()
+    mem0 = _memory(dev.index) if measure else None
     if noalloc:
         err = C.create_string_buffer(512)
         st = lib.gslc_geocode_slc_noalloc(C.byref(a), stream, err, len(err))
@@ -74,8 +87,34 @@ def _run(sc, az_carrier, rg_carrier, noalloc):
         ctx = L.context(dev.index)
         L.check(lib.gslc_geocode_slc(ctx, C.byref(a), stream), ctx)
     torch.cuda.synchronize()
-    assert torch.equal(slc.cpu(), torch.from_numpy(sc.slc)), "radar input modified"
-    return geo.cpu().numpy(), mask.cpu().numpy()
+    if measure:
+        mem1 = _memory(dev.index)
+        # nothing was allocated: device free memory, the default pool's use and
+        # reservation, and the pool's high-water mark (reset before the call)
+        assert mem1 == dict(mem0, used_high=mem0["used"]), (mem0, mem1)
+    if not inplace:
+        assert torch.equal(slc, before), "radar input modified"
+    return geo.cpu().numpy(), mask.cpu().numpy(), slc.cpu().numpy()
+
+
+def _memory(device: int) -> dict:
+    """cudaMemGetInfo's free bytes and the default memory pool's use (the
+    pool serves cudaMallocAsync), with the pool's used high-water mark reset
+    so that a transient allocation inside a call would show."""
+    cu = C.CDLL("libcuda.so.1")
+    d, pool = C.c_int(), C.c_void_p()
+    assert cu.cuDeviceGet(C.byref(d), device) == 0
+    assert cu.cuDeviceGetDefaultMemPool(C.byref(pool), d) == 0
+    vals = {}
+    for name, attr in (("reserved", 5), ("used", 7), ("used_high", 8)):
+        v = C.c_uint64()
+        assert cu.cuMemPoolGetAttribute(pool, attr, C.byref(v)) == 0
+        vals[name] = v.value
+    zero = C.c_uint64(0)
+    assert cu.cuMemPoolSetAttribute(pool, 8, C.byref(zero)) == 0     # reset the high-water mark
+    vals["used_high"] = vals["used"]
+    vals["free"] = torch.cuda.mem_get_info(device)[0]
+    return vals
 
 
 def _compare(ref, got):
@@ -100,7 +139,65 @@ def test_noalloc_matches_regular_entry_point_twice():
     for sc, azc, rgc in cases:             # two calls in a row, different sizes
         ref = _run(sc, azc, rgc, noalloc=False)
         got = _run(sc, azc, rgc, noalloc=True)
-        _compare(ref, got)
+        _compare(ref[:2], got[:2])
+
+
+def test_noalloc_allocates_nothing():
+    """A call that is not the first on the device (the first one uploads the
+    sinc table, and the first launch of each kernel loads its code) changes
+    neither the device's free memory nor the default pool's use, reservation
+    or high-water mark."""
+    sc = synth.scene_c1(seed=14, length=768, width=768, geo=192, dem_px=96)
+    azc = Poly2d([[0.0], [2 * np.pi * 150.0]], y_mean=sc.radar_grid.sensing_mid)
+    rgc = Poly2d([[0.2, 1e-3]], x_mean=sc.radar_grid.mid_range)
+    _run(sc, azc, rgc, noalloc=True)
+    got = _run(sc, azc, rgc, noalloc=True, measure=True)
+    ref = _run(sc, azc, rgc, noalloc=False)
+    _compare(ref[:2], got[:2])
+
+
+def test_noalloc_complex32_blocks_with_carriers():
+    """complex32 radar blocks with carriers: the deramp reads them and writes
+    complex64 copies into the static scratch, as gslc_geocode_slc does into
+    its stream-ordered scratch."""
+    sc = synth.scene_c1(seed=15, length=640, width=704, geo=160, dem_px=96)
+    azc = Poly2d([[0.0], [2 * np.pi * 120.0]], y_mean=sc.radar_grid.sensing_mid)
+    rgc = Poly2d([[0.1, -1e-3]], x_mean=sc.radar_grid.mid_range)
+    ref = _run(sc, azc, rgc, noalloc=False, c32=True)
+    got = _run(sc, azc, rgc, noalloc=True, c32=True)
+    _compare(ref[:2], got[:2])
+
+
+def test_noalloc_inplace_deramp():
+    """inplace_deramp=1 deramps the caller's block itself (the reference's
+    behaviour) and uses no scratch: same outputs and same deramped block as
+    the regular entry point."""
+    sc = synth.scene_c1(seed=16, length=512, width=512, geo=128, dem_px=96)
+    azc = Poly2d([[0.0], [2 * np.pi * 80.0]], y_mean=sc.radar_grid.sensing_mid)
+    rgc = Poly2d([[0.0]])
+    ref = _run(sc, azc, rgc, noalloc=False, inplace=True)
+    got = _run(sc, azc, rgc, noalloc=True, inplace=True)
+    _compare(ref[:2], got[:2])
+    np.testing.assert_array_equal(ref[2], got[2])
+    assert not np.array_equal(got[2], sc.slc)
+
+
+def test_noalloc_rejects_long_orbit():
+    """More state vectors than the static orbit table holds (256)."""
+    sc = synth.scene_c1(seed=17, length=256, width=256, geo=64, dem_px=96)
+    orbit = sc.model.orbit(sc.radar_grid.sensing_mid, 257, 2.0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = sc.geogrid
+    slc = torch.from_numpy(sc.slc).to(dev)
+    geo = torch.zeros((g.length, g.width), dtype=torch.complex64, device=dev)
+    mask = torch.zeros((g.length, g.width), dtype=torch.uint8, device=dev)
+    keep = []
+    a = _args(sc, slc, geo, mask, Poly2d(), Poly2d(), dev, keep, orbit=orbit)
+    err = C.create_string_buffer(512)
+    st = L.lib().gslc_geocode_slc_noalloc(C.byref(a), C.c_void_p(torch.cuda.current_stream().cuda_stream), err,
+                                          len(err))
+    assert st == L.GSLC_EINVAL
+    assert b"256 state vectors" in err.value
 
 
 def test_noalloc_rejects_oversized_input():
