@@ -232,6 +232,40 @@ int gslc_geocode_slc_to_host(gslc_ctx* ctx, const gslc_geocode_args* args, void*
  * none).  Synchronises the stream. */
 int gslc_geocode_slc_raster(gslc_ctx* ctx, const gslc_geocode_args* args, int32_t lines_per_block, void* stream);
 
+/* gslc_geocode_slc for radar blocks (and optionally a DEM window) in host
+ * memory, uploaded while the geogrid computes.  Serves the same reference
+ * call (geocodeSlc.cpp:831-968 on host arrays) for callers holding host
+ * inputs.  args' radar blocks and DEM samples are device buffers of the
+ * same shapes that the call fills: the geogrid runs in `bands` row bands
+ * (0: 6); each band's radar lines and DEM rows are planned on the host from
+ * the zero-Doppler geometry of its perimeter at -500 m and 9000 m (plus
+ * `margin` lines and rows; a negative margin shrinks the plan), uploaded in
+ * band order on a context stream with the carrier deramp of each chunk, and
+ * the band's kernel starts when they have arrived, on one of two streams
+ * that alternate so that band tails overlap.  Everything is uploaded by the
+ * end of the call.  A sinc chip or DEM spline that reaches beyond what had
+ * arrived is flagged by the kernel and every band runs again once all has
+ * arrived (gslc_last_io_reruns reports it), so the results equal
+ * gslc_geocode_slc's on the same inputs whatever the plan.  Outputs stay in
+ * args' device buffers and, when geo_blocks is given, are also copied to host
+ * memory band by band.  Host buffers may be pageable; page-locked ones let
+ * the copies overlap fully.  Not with inplace_deramp.  Synchronises the
+ * stream. */
+typedef struct {
+    const void* const* rdr_blocks;  /* n_blocks host radar blocks, args' shape and sample format */
+    const float* dem;               /* host samples at the first row and column of the DEM window that args->dem's
+                                       device samples hold, or NULL when those are on the device already */
+    int64_t dem_stride;             /* row stride of dem, in samples */
+    void* const* geo_blocks;        /* n_blocks host outputs (args' geo_format), or NULL */
+    uint8_t* mask;                  /* host mask output (needs args->mask), or NULL */
+    int32_t bands;                  /* geogrid row bands; 0: 6 */
+    int32_t margin;                 /* extra radar lines and DEM rows planned around each band */
+} gslc_host_io;
+
+int gslc_geocode_slc_host_io(gslc_ctx* ctx, const gslc_geocode_args* args, const gslc_host_io* io, void* stream);
+/* 1 if the last gslc_geocode_slc_host_io call on ctx ran its bands again. */
+int gslc_last_io_reruns(const gslc_ctx* ctx);
+
 /* carrierPhaseDeramp (cxx/isce3/geocode/geocodeSlc.cpp:240-274) on its own:
  * dst = src * exp(-i float(rg_carrier(t, r) + az_carrier(t, r))) for a
  * length x width block starting at (first_line, first_sample) of radar_grid.

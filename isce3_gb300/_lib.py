@@ -148,6 +148,12 @@ class RasterGeocodeArgs(C.Structure):
                 ("dem_margin", C.c_int32), ("_pad", C.c_int32)]
 
 
+class HostIo(C.Structure):
+    _fields_ = [("rdr_blocks", C.POINTER(C.c_void_p)), ("dem", C.c_void_p), ("dem_stride", C.c_int64),
+                ("geo_blocks", C.POINTER(C.c_void_p)), ("mask", C.c_void_p), ("bands", C.c_int32),
+                ("margin", C.c_int32)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("tiles_per_pop", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
                 ("rows_per_thread", C.c_int32)]
@@ -208,6 +214,8 @@ _EXPORTS = {
     "gslc_ctx_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "gslc_ctx_set_stage_wait": (C.c_int, [C.c_void_p, C.c_int64]),
     "gslc_geocode_slc_raster": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "gslc_geocode_slc_host_io": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gslc_last_io_reruns": (C.c_int, [C.c_void_p]),
     "gslc_last_kernel_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gslc_probe_fp64_gflops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gslc_geocode_slc_noalloc": (C.c_int, [C.POINTER(GeocodeArgs), C.c_void_p, C.c_char_p, C.c_size_t]),

@@ -143,6 +143,59 @@ def dem_raster_desc(raster, geogrid: GeoGridParameters, margin: int, dev: torch.
     return d, t
 
 
+def dem_raster_desc_deferred(raster, geogrid: GeoGridParameters, margin: int, dev: torch.device):
+    """As dem_raster_desc, but a window that is not on the device yet is only
+    allocated there: the geocode call uploads it (gslc_geocode_slc_host_io).
+    Returns (descriptor, device tensor, host address of the window's first
+    sample or None, host row stride in samples, commit) where commit() keeps
+    the device window cached on the raster once the call has filled it."""
+    res = getattr(raster, "resident", None)
+    if (res is not None and res.device == dev) or raster.data.dtype != np.float32 or \
+            not raster.data.flags.c_contiguous:
+        d, t = dem_raster_desc(raster, geogrid, margin, dev)
+        return d, t, None, 0, lambda: None
+    if raster.data.ndim != 2:
+        raise ValueError("a DEM raster has one band")
+    d = L.DemRaster()
+    d.width, d.length = raster.width, raster.length
+    gt = raster.get_geotransform()
+    for i in range(6):
+        d.gt[i] = gt[i]
+    d.epsg = raster.get_epsg()
+    w = L.DemWindow()
+    g = geo_grid_desc(geogrid)
+    st = L.lib().gslc_compute_dem_window(C.byref(d), C.byref(g), int(margin), C.byref(w))
+    if st == L.GSLC_EPROJ:
+        raise ValueError("projection transformation between geogrid and DEM failed")
+    if st == L.GSLC_EUNSUPPORTED:
+        raise NotImplementedError("DEM and geogrid EPSG must be 4326 or UTM, without rotation")
+    if st != L.GSLC_OK:
+        raise ValueError(f"invalid DEM raster (status {st})")
+    if not w.have_raster:
+        d.data = None
+        return d, None, None, 0, lambda: None
+    if w.wraps:
+        raise NotImplementedError("DEM window crossing the DEM file discontinuity")
+    key = (str(dev), "win", w.x_off, w.y_off, w.width, w.length)
+    cache = raster.__dict__.setdefault("_gslc_dev", {})
+    host = None
+    if key in cache:
+        t = cache[key]
+
+        def commit():
+            return None
+    else:
+        t = torch.empty((w.length, w.width), dtype=torch.float32, device=dev)
+        host = raster.data.ctypes.data + (w.y_off * raster.width + w.x_off) * 4
+
+        def commit():
+            cache[key] = t
+    d.data = t.data_ptr()
+    d.data_x_off, d.data_y_off = w.x_off, w.y_off
+    d.data_width, d.data_length, d.data_stride = w.width, w.length, w.width
+    return d, t, host, raster.width, commit
+
+
 def dem_raster_desc_blocks(raster, geogrid: GeoGridParameters, lines_per_block: int, margin: int,
                            dev: torch.device, whole_window: bool = False):
     """Descriptor whose device samples cover the DEM window of every block of

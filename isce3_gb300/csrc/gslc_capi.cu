@@ -34,6 +34,10 @@ struct gslc_ctx {
     cudaStream_t copy_stream = nullptr;   // device-to-host copies of gslc_geocode_slc_to_host, on first use
     cudaEvent_t band_ev[GSLC_HOST_BANDS + 1] = {};
     int64_t stage_wait = 0;         // SM clocks of the orbit-table wait; 0: STAGE_WAIT_DEFAULT
+    // gslc_geocode_slc_host_io: upload stream, second compute stream, events, re-runs of the last call
+    cudaStream_t h2d_stream = nullptr, aux_stream = nullptr;
+    std::vector<cudaEvent_t> io_ev;
+    int io_reruns = 0;
     std::string err;
 };
 
@@ -682,6 +686,10 @@ extern "C" int gslc_ctx_destroy(gslc_ctx* c) {
     for (auto& e : c->band_ev)
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (auto& e : c->io_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+    if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
     delete c;
     return GSLC_OK;
 }
@@ -720,6 +728,9 @@ int bind_dem_window(gslc_ctx* c, const gslc_dem_raster& d, const gslc_dem_window
         dem.dx = w.dx; dem.dy = w.dy;
     }
     dem.sc = make_spline_const();
+    dem.avail_lo = 0;
+    dem.avail_hi = INT32_MAX;
+    dem.err = nullptr;
     return GSLC_OK;
 }
 
@@ -769,6 +780,8 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.geo_fmt = a->geo_format;
     p.mant_bits = a->geo_format == 2 ? a->mantissa_bits : 23;
     p.stage_wait = c && c->stage_wait > 0 ? c->stage_wait : STAGE_WAIT_DEFAULT;
+    p.avail_az_lo = INT64_MIN / 2;
+    p.avail_az_hi = INT64_MAX / 2;
 
     // DEM window the reference would load (loadDem.cpp:22-133)
     gslc_dem_window w;
@@ -1053,6 +1066,361 @@ extern "C" int gslc_geocode_slc_raster(gslc_ctx* c, const gslc_geocode_args* a, 
         return set_err(c, GSLC_EINVAL, "the input raster starts at the radar grid's first line and sample");
     return geocode_slc_impl(c, a, (cudaStream_t)stream, nullptr, nullptr, nullptr, lines_per_block);
 }
+
+// ---------------------------------------------------------------------------
+// Host radar blocks and DEM window uploaded while the geogrid's row bands
+// compute (gslc_geocode_slc_host_io).
+namespace {
+
+struct IoBand {
+    int64_t row0, rows;
+    int64_t az_lo, az_hi;     // radar lines of the blocks (block-relative) the band's chips read
+    int64_t dem_lo, dem_hi;   // DEM window rows its splines read
+};
+
+// The lines and rows a band of geogrid rows reads, from the pixel centres of
+// its perimeter (every eighth of each edge) at the lowest and highest
+// heights a DEM can hold (-500 and 9000 m), by the zero-Doppler geo2rdr on
+// the host: the sinc chip adds 4 lines on each side, the spline rows -1..+4
+// of the point's row.  A band whose points all fail takes everything.  The
+// plan only orders the uploads: a chip or spline outside the uploaded rows
+// raises error bit 3 and the call repeats its bands.
+void plan_io_band(const GeoParams& p, const Orbit& ob, const gslc_geocode_args* a, int64_t margin, IoBand& b) {
+    const int64_t inL = a->rdr_length;
+    const int64_t demL = p.dem.have_raster ? p.dem.length : 0;
+    double az_min = INFINITY, az_max = -INFINITY, r_min = INFINITY, r_max = -INFINITY;
+    bool any = false;
+    const int64_t W = p.gw;
+    for (int e = 0; e < 4; ++e) {
+        for (int k = 0; k <= 8; ++k) {
+            int64_t line, pix;
+            if (e == 0) { line = b.row0; pix = (W - 1) * k / 8; }
+            else if (e == 1) { line = b.row0 + b.rows - 1; pix = (W - 1) * k / 8; }
+            else if (e == 2) { line = b.row0 + (b.rows - 1) * k / 8; pix = 0; }
+            else { line = b.row0 + (b.rows - 1) * k / 8; pix = W - 1; }
+            const double x = p.gx0 + p.gdx * ((double)pix + 0.5);
+            const double y = p.gy0 + p.gdy * ((double)line + 0.5);
+            double lon, lat;
+            if (p.geo_is_lonlat) {
+                lon = x * PI / 180.0;
+                lat = y * PI / 180.0;
+            } else if (!utm_inverse(p.utm, x, y, lon, lat)) {
+                continue;
+            }
+            if (demL > 0) {
+                double row = NAN;
+                if (p.dem.epsg_is_lonlat) {
+                    row = ((lat * 180.0) / PI - p.dem.y_start) / p.dem.dy;
+                } else {
+                    double X, Y;
+                    if (utm_forward(p.dem.utm, lon, lat, X, Y)) row = (Y - p.dem.y_start) / p.dem.dy;
+                }
+                if (std::isfinite(row)) {
+                    r_min = std::min(r_min, row);
+                    r_max = std::max(r_max, row);
+                }
+            }
+            for (const double h : {-500.0, 9000.0}) {
+                const V3 xyz = lonlat_to_xyz(p.ell_a, p.ell_e2, lon, lat, h);
+                if (!p.t_mid_in_orbit) continue;
+                const V3 rvec = vsub(xyz, p.pos0);
+                double t = p.t_mid, R = 0.0;
+                const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
+                bool ok = std::fabs(dt) < p.thr;
+                if (!ok) ok = geo2rdr_zero_doppler_seg(ob, ob.seg, xyz, p.thr, std::max(p.maxiter, 2), t, dt, R);
+                if (!ok) continue;
+                const double azc = (t - p.rg_t0) * p.rg_prf - p.az_first_d;
+                az_min = std::min(az_min, azc);
+                az_max = std::max(az_max, azc);
+                any = true;
+            }
+        }
+    }
+    if (any) {
+        b.az_lo = std::max<int64_t>(0, (int64_t)std::floor(az_min) - 4 - margin);
+        b.az_hi = std::min<int64_t>(inL - 1, (int64_t)std::ceil(az_max) + 4 + margin);
+        if (b.az_lo > b.az_hi) b.az_lo = b.az_hi = std::min<int64_t>(std::max<int64_t>(0, b.az_lo), inL - 1);
+    } else {
+        b.az_lo = 0;
+        b.az_hi = inL - 1;
+    }
+    if (demL > 0 && std::isfinite(r_min)) {
+        b.dem_lo = std::max<int64_t>(0, (int64_t)std::floor(r_min) - 1 - margin);
+        b.dem_hi = std::min<int64_t>(demL - 1, (int64_t)std::ceil(r_max) + 4 + margin);
+        if (b.dem_lo > b.dem_hi) b.dem_lo = b.dem_hi = std::min<int64_t>(std::max<int64_t>(0, b.dem_lo), demL - 1);
+    } else {
+        b.dem_lo = 0;
+        b.dem_hi = std::max<int64_t>(demL - 1, 0);
+    }
+}
+
+cudaEvent_t io_event(gslc_ctx* c, size_t i) {
+    while (c->io_ev.size() <= i) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        c->io_ev.push_back(e);
+    }
+    return c->io_ev[i];
+}
+
+}  // namespace
+
+extern "C" int gslc_geocode_slc_host_io(gslc_ctx* c, const gslc_geocode_args* a, const gslc_host_io* io,
+                                        void* stream_) {
+    if (!c) return GSLC_EINVAL;
+    c->err.clear();
+    c->launches = 0;
+    c->io_reruns = 0;
+    if (!a || !io || !io->rdr_blocks) return set_err(c, GSLC_EINVAL, "null arguments");
+    if (a->inplace_deramp) return set_err(c, GSLC_EINVAL, "in-place deramp needs device radar blocks");
+    if (io->dem && io->dem_stride < a->dem.data_width)
+        return set_err(c, GSLC_EINVAL, "host DEM row stride shorter than the DEM window");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    GeoParams p;
+    std::vector<double> coef;
+    int st = prepare_geocode(c, a, p, coef);
+    if (st == GSLC_EMPTY_GRID) return GSLC_OK;
+    if (st != GSLC_OK) return st;
+    const gslc_radar_grid& rg = a->radar_grid;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaSetDevice");
+    for (cudaStream_t* s : {&c->h2d_stream, &c->aux_stream, &c->copy_stream})
+        if (!*s && (e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking)) != cudaSuccess) {
+            *s = nullptr;
+            return cuda_err(c, e, "stream");
+        }
+    if (coef.size() > c->orbit_cap) {
+        if (c->d_orbit) cudaFree(c->d_orbit);
+        c->d_orbit = nullptr;
+        e = cudaMalloc(&c->d_orbit, coef.size() * sizeof(double));
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc orbit");
+        c->orbit_cap = coef.size();
+    }
+    // host copy of the orbit tables for the band plan
+    GeoParams ph = p;
+    bind_orbit(ph, coef.data());
+    e = cudaMemcpyAsync(c->d_orbit, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "orbit upload");
+    bind_orbit(p, c->d_orbit);
+    p.sinc = c->d_sinc;
+    p.err = c->d_err;
+    p.dem.err = c->d_err;
+    e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "memset");
+
+    const int64_t inL = a->rdr_length, inW = a->rdr_width, nrdr = inL * inW;
+    const size_t sbytes = p.rdr_c32 ? 4 : 8;
+    const int64_t gl = p.gl, gw = p.gw;
+    const bool deramp = !p.carriers_zero && nrdr > 0 && !a->rdr_deramped;
+    std::vector<void*> scratch;
+    std::vector<const float2*> rdr(a->n_blocks);
+    for (int b = 0; b < a->n_blocks; ++b) rdr[b] = (const float2*)a->rdr_blocks[b];
+    std::vector<float2*> deramp_dst(a->n_blocks, nullptr);
+    auto fail = [&](int code) {
+        for (void* s : scratch) cudaFreeAsync(s, stream);
+        cudaStreamSynchronize(c->h2d_stream);
+        cudaStreamSynchronize(c->aux_stream);
+        cudaStreamSynchronize(c->copy_stream);
+        return code;
+    };
+    if (deramp) {
+        // complex64 staging is deramped where it lies; complex32 into complex64 scratch
+        for (int b = 0; b < a->n_blocks; ++b) {
+            if (!p.rdr_c32) {
+                deramp_dst[b] = (float2*)a->rdr_blocks[b];
+                continue;
+            }
+            void* buf = nullptr;
+            e = cudaMallocAsync(&buf, nrdr * sizeof(float2), stream);
+            if (e != cudaSuccess) return fail(cuda_err(c, e, "cudaMallocAsync deramp scratch"));
+            scratch.push_back(buf);
+            deramp_dst[b] = (float2*)buf;
+            rdr[b] = (const float2*)buf;
+        }
+    }
+
+    // bands, planned and ordered by the first radar line they read
+    const int nb_want = io->bands > 0 ? io->bands : 6;
+    int64_t band_rows = ((gl + nb_want - 1) / nb_want + 31) / 32 * 32;
+    const int nb = (int)((gl + band_rows - 1) / band_rows);
+    std::vector<IoBand> bands(nb);
+    for (int i = 0; i < nb; ++i) {
+        bands[i].row0 = (int64_t)i * band_rows;
+        bands[i].rows = std::min(band_rows, gl - bands[i].row0);
+        plan_io_band(ph, ph.orbit, a, io->margin, bands[i]);
+    }
+    std::stable_sort(bands.begin(), bands.end(), [](const IoBand& x, const IoBand& y) { return x.az_lo < y.az_lo; });
+
+    // uploads on h2d_stream: a band's missing lines (deramped there) and DEM rows, then an event
+    const int64_t demL = (io->dem && p.dem.have_raster) ? p.dem.length : 0;
+    const int64_t demW = p.dem.have_raster ? p.dem.width : 0;
+    int64_t u0 = 0, u1 = -1, d0 = 0, d1 = -1;   // uploaded lines [u0, u1] and DEM rows [d0, d1]
+    size_t evn = 0;
+    cudaEvent_t ev_start = io_event(c, evn++);
+    if (!ev_start) return fail(set_err(c, GSLC_ECUDA, "event"));
+    e = cudaEventRecord(ev_start, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->h2d_stream, ev_start, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->aux_stream, ev_start, 0);
+    if (e != cudaSuccess) return fail(cuda_err(c, e, "stream order"));
+    const int32_t src_c32 = p.rdr_c32;
+    auto upload_lines = [&](int64_t l0, int64_t l1) -> cudaError_t {   // [l0, l1]
+        if (l1 < l0) return cudaSuccess;
+        cudaError_t r = cudaSuccess;
+        for (int b = 0; b < a->n_blocks && r == cudaSuccess; ++b)
+            r = cudaMemcpyAsync((char*)a->rdr_blocks[b] + l0 * inW * sbytes,
+                                (const char*)io->rdr_blocks[b] + l0 * inW * sbytes, (size_t)((l1 - l0 + 1) * inW) * sbytes,
+                                cudaMemcpyHostToDevice, c->h2d_stream);
+        if (r != cudaSuccess || !deramp) return r;
+        for (int b = 0; b < a->n_blocks && r == cudaSuccess; ++b) {
+            DerampParams dp;
+            std::memset(&dp, 0, sizeof(dp));
+            dp.src = (const float2*)((const char*)a->rdr_blocks[b] + l0 * inW * sbytes);
+            dp.dst = deramp_dst[b] + l0 * inW;
+            dp.src_c32 = src_c32;
+            dp.inL = l1 - l0 + 1; dp.inW = inW;
+            dp.az_first = a->first_azimuth_line + l0; dp.rg_first = a->first_range_sample;
+            dp.rg_t0 = rg.sensing_start; dp.rg_prf = rg.prf; dp.rg_r0 = rg.starting_range;
+            dp.rg_dr = rg.range_pixel_spacing;
+            dp.inv_prf = 1.0 / rg.prf;
+            dp.az_car = p.az_car; dp.rg_car = p.rg_car;
+            r = launch_deramp(dp, c->h2d_stream, &c->launches);
+        }
+        return r;
+    };
+    auto upload_dem = [&](int64_t r0, int64_t r1) -> cudaError_t {
+        if (r1 < r0 || demL == 0) return cudaSuccess;
+        return cudaMemcpy2DAsync((float*)p.dem.data + r0 * p.dem.stride, p.dem.stride * sizeof(float),
+                                 io->dem + r0 * io->dem_stride, io->dem_stride * sizeof(float), demW * sizeof(float),
+                                 (size_t)(r1 - r0 + 1), cudaMemcpyHostToDevice, c->h2d_stream);
+    };
+    if (deramp) p.rdr_c32 = 0;
+    const size_t esz = geo_pixel_bytes(a->geo_format);
+    std::vector<cudaEvent_t> band_done(nb);
+    for (int i = 0; i < nb && e == cudaSuccess; ++i) {
+        IoBand& B = bands[i];
+        if (u1 < u0) {
+            e = upload_lines(B.az_lo, B.az_hi);
+            u0 = B.az_lo; u1 = B.az_hi;
+        } else {
+            if (B.az_lo < u0) { e = upload_lines(B.az_lo, u0 - 1); u0 = B.az_lo; }
+            if (e == cudaSuccess && B.az_hi > u1) { e = upload_lines(u1 + 1, B.az_hi); u1 = B.az_hi; }
+        }
+        if (e == cudaSuccess && demL > 0) {
+            if (d1 < d0) {
+                e = upload_dem(B.dem_lo, B.dem_hi);
+                d0 = B.dem_lo; d1 = B.dem_hi;
+            } else {
+                if (B.dem_lo < d0) { e = upload_dem(B.dem_lo, d0 - 1); d0 = B.dem_lo; }
+                if (e == cudaSuccess && B.dem_hi > d1) { e = upload_dem(d1 + 1, B.dem_hi); d1 = B.dem_hi; }
+            }
+        }
+        cudaEvent_t ready = io_event(c, evn++);
+        if (!ready) return fail(set_err(c, GSLC_ECUDA, "event"));
+        if (e == cudaSuccess) e = cudaEventRecord(ready, c->h2d_stream);
+        cudaStream_t s = (i & 1) ? c->aux_stream : stream;
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ready, 0);
+        if (e != cudaSuccess) break;
+        // the band's kernel, reading only what has arrived
+        GeoParams q = p;
+        q.avail_az_lo = u0; q.avail_az_hi = u1;
+        if (demL > 0) { q.dem.avail_lo = (int32_t)d0; q.dem.avail_hi = (int32_t)d1; }
+        q.geo_row0 = B.row0;
+        q.gl = B.rows;
+        const int64_t off = B.row0 * gw;
+        q.mask = a->mask ? a->mask + off : nullptr;
+        q.carrier_out = a->carrier_phase ? a->carrier_phase + off : nullptr;
+        q.flatten_out = a->flatten_phase ? a->flatten_phase + off : nullptr;
+        q.az_out = a->az_index ? a->az_index + off : nullptr;
+        q.rg_out = a->rg_index ? a->rg_index + off : nullptr;
+        for (int b0 = 0; b0 < a->n_blocks && e == cudaSuccess; b0 += MAX_BLOCKS) {
+            q.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
+            for (int b = 0; b < q.nblk; ++b) {
+                q.rdr[b] = rdr[b0 + b];
+                q.geo[b] = (float2*)((char*)a->geo_blocks[b0 + b] + off * esz);
+            }
+            e = launch_geocode(q, a->geo2rdr_precision, s, &c->launches);
+        }
+        band_done[i] = io_event(c, evn++);
+        if (!band_done[i]) return fail(set_err(c, GSLC_ECUDA, "event"));
+        if (e == cudaSuccess) e = cudaEventRecord(band_done[i], s);
+    }
+    if (e != cudaSuccess) return fail(cuda_err(c, e, "pipelined geocode"));
+    // the rest of the radar blocks and DEM window (left complete on the device)
+    if (u1 < u0) { e = upload_lines(0, inL - 1); u0 = 0; u1 = inL - 1; }
+    if (e == cudaSuccess && u0 > 0) e = upload_lines(0, u0 - 1);
+    if (e == cudaSuccess && u1 < inL - 1) e = upload_lines(u1 + 1, inL - 1);
+    if (e == cudaSuccess && demL > 0) {
+        if (d1 < d0) e = upload_dem(0, demL - 1);
+        else {
+            if (d0 > 0) e = upload_dem(0, d0 - 1);
+            if (e == cudaSuccess && d1 < demL - 1) e = upload_dem(d1 + 1, demL - 1);
+        }
+    }
+    // each band's outputs to the host behind its kernel (queued after every
+    // launch: a pageable destination makes the call wait for its copy)
+    for (int i = 0; i < nb && e == cudaSuccess && io->geo_blocks; ++i) {
+        const IoBand& B = bands[i];
+        const int64_t off = B.row0 * gw;
+        e = cudaStreamWaitEvent(c->copy_stream, band_done[i], 0);
+        for (int b = 0; b < a->n_blocks && e == cudaSuccess; ++b)
+            e = cudaMemcpyAsync((char*)io->geo_blocks[b] + off * esz, (const char*)a->geo_blocks[b] + off * esz,
+                                (size_t)(B.rows * gw) * esz, cudaMemcpyDeviceToHost, c->copy_stream);
+        if (e == cudaSuccess && io->mask && a->mask)
+            e = cudaMemcpyAsync(io->mask + off, a->mask + off, (size_t)(B.rows * gw), cudaMemcpyDeviceToHost,
+                                c->copy_stream);
+    }
+    if (e != cudaSuccess) return fail(cuda_err(c, e, "pipelined geocode"));
+    cudaEvent_t all_in = io_event(c, evn++), aux_done = io_event(c, evn++), out_done = io_event(c, evn++);
+    if (!all_in || !aux_done || !out_done) return fail(set_err(c, GSLC_ECUDA, "event"));
+    if (e == cudaSuccess) e = cudaEventRecord(all_in, c->h2d_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(aux_done, c->aux_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(out_done, c->copy_stream);
+    for (cudaEvent_t ev : {all_in, aux_done, out_done})
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ev, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return fail(cuda_err(c, e, "pipelined geocode"));
+    if (c->h_err[0] & 8) {
+        // a chip or spline read beyond what had arrived: every band again,
+        // now that all has (the same values wherever the first pass was right)
+        c->io_reruns = 1;
+        e = cudaMemsetAsync(c->d_err, 0, sizeof(int32_t), stream);
+        for (int i = 0; i < nb && e == cudaSuccess; ++i) {
+            const IoBand& B = bands[i];
+            GeoParams q = p;
+            q.geo_row0 = B.row0;
+            q.gl = B.rows;
+            const int64_t off = B.row0 * gw;
+            q.mask = a->mask ? a->mask + off : nullptr;
+            q.carrier_out = a->carrier_phase ? a->carrier_phase + off : nullptr;
+            q.flatten_out = a->flatten_phase ? a->flatten_phase + off : nullptr;
+            q.az_out = a->az_index ? a->az_index + off : nullptr;
+            q.rg_out = a->rg_index ? a->rg_index + off : nullptr;
+            for (int b0 = 0; b0 < a->n_blocks && e == cudaSuccess; b0 += MAX_BLOCKS) {
+                q.nblk = std::min(MAX_BLOCKS, a->n_blocks - b0);
+                for (int b = 0; b < q.nblk; ++b) {
+                    q.rdr[b] = rdr[b0 + b];
+                    q.geo[b] = (float2*)((char*)a->geo_blocks[b0 + b] + off * esz);
+                }
+                e = launch_geocode(q, a->geo2rdr_precision, stream, &c->launches);
+            }
+        }
+        if (e == cudaSuccess && io->geo_blocks) {
+            for (int b = 0; b < a->n_blocks && e == cudaSuccess; ++b)
+                e = cudaMemcpyAsync(io->geo_blocks[b], a->geo_blocks[b], (size_t)(gl * gw) * esz, cudaMemcpyDeviceToHost,
+                                    stream);
+            if (e == cudaSuccess && io->mask && a->mask)
+                e = cudaMemcpyAsync(io->mask, a->mask, (size_t)(gl * gw), cudaMemcpyDeviceToHost, stream);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return fail(cuda_err(c, e, "pipelined geocode re-run"));
+    }
+    for (void* s : scratch) cudaFreeAsync(s, stream);
+    return device_status(c, c->h_err[0]);
+}
+
+extern "C" int gslc_last_io_reruns(const gslc_ctx* c) { return c ? c->io_reruns : 0; }
 
 extern "C" int gslc_geocode_slc_to_host(gslc_ctx* c, const gslc_geocode_args* a, void* const* host_geo_blocks,
                                         uint8_t* host_mask, void* stream) {

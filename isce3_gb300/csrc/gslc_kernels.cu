@@ -89,6 +89,10 @@ __device__ double dem_spline(const Dem& d, double row, double col) {
     if (irow < 2 || irow >= d.length - 1) return ref;
     if (icol < 2 || icol >= d.width - 1) return ref;
     const int i0 = irow - 2, j0 = icol - 2;
+    // rows i0 + 1 .. min(i0 + 6, length - 1) (the clamp below) must be on the device
+    if (i0 + 1 < d.avail_lo || min(i0 + 6, d.length - 1) > d.avail_hi) {
+        if (d.err) atomicOr(d.err, 8);
+    }
     const float xx = (float)(col - (double)icol);
     const float yy = (float)(row - (double)irow);
     int cidx[6];
@@ -976,6 +980,8 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);
         return;
     }
+    // the chip's lines intAzB - 4 .. intAzB + 4 must be on the device
+    if (intAzB - 4 < p.avail_az_lo || intAzB + 4 > p.avail_az_hi) atomicOr(p.err, 8);
     // Doppler in radians per line: eval * 2 * pi / prf (geocodeSlc.cpp:473-474)
     const float doppFreq = dop * p.two_pi_over_prf_f;
     // reramp + flatten phase (geocodeSlc.cpp:362-392)

@@ -15,6 +15,11 @@ struct Dem {
     double x_start, y_start, dx, dy;
     Utm utm;                    // DEM projection when it is UTM
     SplineConst sc;
+    // window rows whose samples are on the device (all of them unless the
+    // window is still being uploaded); a spline reaching outside raises bit 3
+    // of *err (the launch must be repeated once every row has arrived)
+    int32_t avail_lo, avail_hi;
+    int32_t* err;
 };
 
 struct GeoParams {
@@ -82,6 +87,9 @@ struct GeoParams {
     // SM clocks a thread waits for the orbit tables' copy into shared memory
     // before it reads the global tables instead (error bit 1)
     int64_t stage_wait;
+    // radar lines of the blocks (block-relative) on the device; a sinc chip
+    // reaching outside raises error bit 3, as for the DEM rows
+    int64_t avail_az_lo, avail_az_hi;
 };
 
 // default of GeoParams::stage_wait: ~2^31 SM clocks, about a second

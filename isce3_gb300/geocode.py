@@ -363,10 +363,13 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
                 az_time_correction, srange_correction, flatten_with_corrected_srange, invalid_value,
                 carrier_phase_block, flatten_phase_block, precision, inplace_deramp, az_index_block,
                 rg_index_block, dem_margin, rdr_deramped=False, rdr_format=0, geo_format=0, mantissa_bits=23,
-                *, dem_lines_per_block=0):
+                *, dem_lines_per_block=0, host_io=None):
     """Stage arrays on ``dev`` and fill a gslc_geocode_args.  With
     ``dem_lines_per_block`` the device DEM samples cover the window of every
-    block of that many geogrid lines (the raster mode).
+    block of that many geogrid lines (the raster mode).  With ``host_io`` (a
+    dict) host radar blocks and a DEM window not yet on the device are only
+    allocated there, and ``host_io`` receives what gslc_geocode_slc_host_io
+    needs to upload them.
 
     Returns (args, outputs to copy back, objects to keep alive)."""
     # Radar blocks in pinned host memory upload on a side stream while the DEM
@@ -377,7 +380,9 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     s = torch.cuda.current_stream(dev)
     raws = [_raw(r) for r in rdr_data_blocks]
     side = None
-    if any(isinstance(r, torch.Tensor) and r.device.type == "cpu" and r.is_pinned() for r in raws):
+    if host_io is not None:
+        rdr = [_Staged(r, dev, False, torch.complex64) for r in raws]
+    elif any(isinstance(r, torch.Tensor) and r.device.type == "cpu" and r.is_pinned() for r in raws):
         side = _upload_stream(dev)
         side.wait_stream(s)
         with torch.cuda.stream(side):
@@ -390,6 +395,9 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     if dem_lines_per_block > 0:
         a.dem, dem_keep = M.dem_raster_desc_blocks(dem_raster, geogrid, dem_lines_per_block, dem_margin, dev,
                                                    whole_window=True)
+    elif host_io is not None:
+        a.dem, dem_keep, host_io["dem"], host_io["dem_stride"], host_io["dem_commit"] = \
+            M.dem_raster_desc_deferred(dem_raster, geogrid, dem_margin, dev)
     else:
         a.dem, dem_keep = M.dem_raster_desc(dem_raster, geogrid, dem_margin, dev)
     a.native_doppler = M.lut_desc(native_doppler, dev)
@@ -398,7 +406,9 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     a.srange_correction = M.lut_desc(srange_correction, dev)
     a.az_carrier = M.azrg_desc(az_carrier, dev, holder)
     a.rg_carrier = M.azrg_desc(rg_carrier, dev, holder)
-    if side is None:
+    if host_io is not None:
+        pass
+    elif side is None:
         rdr = [_Staged(r, dev, True, torch.complex64) for r in raws]
     else:
         s.wait_stream(side)
@@ -460,7 +470,21 @@ def _build_args(dev, rdr_data_blocks, geo_data_blocks, dem_raster, radargrid, sl
     return a, outs, keep
 
 
+# geogrid row bands of the pipelined host-input call, and the radar lines and
+# DEM rows planned around each band beyond its perimeter's footprint
+HOST_IO_BANDS = 6
+HOST_IO_MARGIN = 16
+
+
+def _host_inputs(call) -> bool:
+    """Radar blocks all in host memory, deramped on copies (not in place)."""
+    rdr, inplace = call[0], call[27]
+    return not inplace and all(not (isinstance(r, torch.Tensor) and r.device.type == "cuda") for r in rdr)
+
+
 def _geocode_on_stream(lib, ctx, s, dev, *args):
+    if _host_inputs(args):
+        return _geocode_host_inputs(lib, ctx, s, dev, *args)
     a, outs, keep = _build_args(dev, *args)
     geo = keep[2]
     if all(g.host is not None for g in geo):
@@ -482,3 +506,34 @@ def _geocode_on_stream(lib, ctx, s, dev, *args):
         for o in outs:
             o.copy_back()
     del keep
+
+
+def _geocode_host_inputs(lib, ctx, s, dev, *args):
+    """Host radar blocks: gslc_geocode_slc_host_io uploads them (and a DEM
+    window not yet on the device) band by band while earlier bands compute,
+    and copies host geo blocks and mask back behind each band."""
+    hio = {}
+    a, outs, keep = _build_args(dev, *args, host_io=hio)
+    rdr, geo = keep[1], keep[2]
+    io = L.HostIo()
+    rp = (C.c_void_p * len(rdr))(*[r.host.data_ptr() for r in rdr])
+    io.rdr_blocks = C.cast(rp, C.POINTER(C.c_void_p))
+    io.dem = hio.get("dem")
+    io.dem_stride = int(hio.get("dem_stride") or 0)
+    host_geo = all(g.host is not None for g in geo)
+    mask = next((o for o in outs if a.mask and o.ptr() == a.mask and o.host is not None), None)
+    gp = None
+    if host_geo:
+        gp = (C.c_void_p * len(geo))(*[g.host.data_ptr() for g in geo])
+        io.geo_blocks = C.cast(gp, C.POINTER(C.c_void_p))
+        io.mask = mask.host.data_ptr() if mask else None
+    io.bands = HOST_IO_BANDS
+    io.margin = HOST_IO_MARGIN
+    st = lib.gslc_geocode_slc_host_io(ctx, C.byref(a), C.byref(io), C.c_void_p(s.cuda_stream))
+    L.check(st, ctx, "geocode_slc")
+    hio["dem_commit"]()
+    done = (set(map(id, geo)) | ({id(mask)} if mask else set())) if host_geo else set()
+    for o in outs:
+        if id(o) not in done:
+            o.copy_back()
+    del keep, rp, gp
