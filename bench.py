@@ -24,6 +24,7 @@ the same workload, metric and units.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -54,6 +55,10 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true", help="skip the burst (batched vs plain) measurement")
     p.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
     p.add_argument("--no-geometry", action="store_true", help="skip the block-planner and metadata-cube legs")
+    p.add_argument("--profile-summary", nargs=2, metavar=("FP64_CSV", "FF_CSV"),
+                   help="instead of timing: write profiles/geocode_kernel_medium.json from the raw-page CSV "
+                        "exports (ncu -i REPORT --page raw --csv) of the medium captures of the FP64 and "
+                        "float-float geocode_kernel launches")
     p.add_argument("--precision-study", action="store_true",
                    help="instead of timing: fp64 and float-float geo2rdr against the oracle over the whole "
                         "workload (error histograms, Newton iteration counts); writes one JSON line")
@@ -338,6 +343,63 @@ def profile_per_px() -> dict:
     return {f"{k}_per_output_px": float(v) for k, v in d.get("per_output_px", {}).items()}
 
 
+MEDIUM_PX = 4000 * 4000     # output pixels of the medium workload (the captures' launches)
+
+
+def _ncu_raw(path) -> dict:
+    """Metric name -> value of the one launch in an ncu raw-page CSV export."""
+    import csv
+    rows = list(csv.reader(Path(path).read_text().splitlines()))
+    head = next(i for i, r in enumerate(rows) if "gpu__time_duration.sum" in r)
+    names, units = rows[head], rows[head + 1]
+    vals = rows[head + 2]
+    out = {}
+    for n, u, v in zip(names, units, vals):
+        try:
+            x = float(v.replace(",", ""))
+        except ValueError:
+            continue
+        scale = {"Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "byte": 1.0, "msecond": 1e-3, "usecond": 1e-6,
+                 "nsecond": 1e-9, "ms": 1e-3, "us": 1e-6, "ns": 1e-9, "s": 1.0, "second": 1.0}.get(u.strip(), 1.0)
+        out[n] = x * scale
+    return out
+
+
+def write_profile_summary(fp64_csv, ff_csv) -> dict:
+    """profiles/geocode_kernel_medium.json from the two captures."""
+    f, g = _ncu_raw(fp64_csv), _ncu_raw(ff_csv)
+
+    def count(m, op):
+        # the raw page gives the summed rate; times the elapsed cycles, the count
+        return m[f"smsp__sass_thread_inst_executed_op_{op}_pred_on.sum.per_cycle_elapsed"] * \
+            m["smsp__cycles_elapsed.avg"]
+
+    def flop(m):
+        return (2 * count(m, "dfma") + count(m, "dadd") + count(m, "dmul")) / MEDIUM_PX
+    d = {"kernel": "geocode_kernel (fused SLC geocoder)",
+         "workload": "medium: 8192 x 4096 c64 SLC -> 4000 x 4000 UTM EPSG:32611 10 m (16,000,000 output px)",
+         "command": "M='python bench.py --workload medium --steps 2 --warmup 1 --no-cpu --no-e2e --no-batched "
+                    "--no-served --no-geometry'; ncu --set full --clock-control none -k regex:geocode_kernel -s 2 "
+                    "-c 1 -o prof_med_fp64 $M; ncu --set full --clock-control none -k regex:geocode_kernel -s 6 "
+                    "-c 1 -o prof_med_ff $M; python bench.py --profile-summary fp64.csv ff.csv (the raw-page "
+                    "CSV exports)",
+         "per_output_px": {
+             "dram_bytes": round((f["dram__bytes_read.sum"] + f["dram__bytes_write.sum"]) / MEDIUM_PX, 3),
+             "fp64_flop_fp64": round(flop(f), 1),
+             "fp64_flop_ff": round(flop(g), 1)},
+         "duration_ms": {"fp64": round(f["gpu__time_duration.sum"] * 1e3, 3),
+                         "ff": round(g["gpu__time_duration.sum"] * 1e3, 3)},
+         "fp64_inst_per_output_px": {v: {op: round(count(m, op) / MEDIUM_PX, 1) for op in ("dfma", "dadd", "dmul")}
+                                     for v, m in (("fp64", f), ("ff", g))},
+         "definitions": {
+             "dram_bytes": "(dram__bytes_read.sum + dram__bytes_write.sum) of the FP64 launch / 16,000,000",
+             "fp64_flop_<variant>": "(2 x DFMA + DADD + DMUL thread instructions) / 16,000,000, each count "
+                                    "smsp__sass_thread_inst_executed_op_<op>_pred_on.sum.per_cycle_elapsed x "
+                                    "smsp__cycles_elapsed.avg"}}
+    PROFILE.write_text(json.dumps(d, indent=2) + "\n")
+    return d
+
+
 def fp64_roofline(prof_vals: dict, variant: str, npx: int, kernel_ms: float, peak_gflops: float) -> dict:
     """FP64 roofline of the fused kernel: FP64 FLOP per output pixel counted
     by ncu (2 x DFMA + DADD + DMUL thread instructions of the medium capture)
@@ -383,8 +445,9 @@ def run_e2e(args, sc, dev, common, kw):
     for _ in range(max(1, args.warmup)):
         step()
     torch.cuda.synchronize()
+    gc.collect()
     t = []
-    for _ in range(max(args.steps, 10)):     # at least 10 drop-in calls: single outliers weigh less
+    for _ in range(max(args.steps, 20)):     # at least 20 drop-in calls: single outliers weigh less
         t0 = time.perf_counter()
         step()
         torch.cuda.synchronize()
@@ -743,6 +806,9 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse_args()
+    if args.profile_summary:
+        print(json.dumps(write_profile_summary(*args.profile_summary)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

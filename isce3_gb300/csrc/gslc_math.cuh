@@ -68,7 +68,7 @@ GSLC_HD uint64_t dbits(double x) {
 constexpr uint64_t DMAG = 0x7fffffffffffffffull;
 constexpr uint64_t DBITS_HALF = 0x3fe0000000000000ull;        // 0.5
 constexpr uint64_t DBITS_MINUS_HALF = 0xbfe0000000000000ull;  // -0.5
-constexpr uint64_t DBITS_1EM5 = 0x3ee4f8b588e368f1ull;        // 1e-5
+constexpr uint64_t DBITS_0P1 = 0x3fb999999999999aull;         // 0.1
 
 // Order key of a double: for finite x, y (and -0.0 == +0.0), x <= y exactly
 // when dkey(x) <= dkey(y) as signed integers.  A NaN's key lies above every
@@ -548,9 +548,14 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
     const int nh = o.seg_nh;
     // |dt| < thr as a bit compare (thr <= 0 or NaN: never, as the FP64 test)
     const uint64_t thr_bits = thr > 0.0 ? dbits(thr) : 0ull;
-    // G(w) = 1/|vel|^2 changes by ~5e-5 of itself per unit w (about 10 s):
-    // after a step below 1e-5 s its last value is within ~1e-10 of the new
-    // one, which moves the next step by < 1e-15 s, so it is reused
+    // G(w) = 1/|vel|^2 changes by ~5e-6 of itself per second of the
+    // iterate's travel.  Once a step falls below 0.1 s the iterate travels
+    // at most ~0.014 s more (the steps shrink by ~0.12 each), so the last G
+    // stays within ~7e-8 of the current one and is reused: each later step
+    // changes by at most that fraction of itself, a change the contraction
+    // shrinks to ~1e-14 s in the returned iterate, well below the ~1e-13 s
+    // the segment form already differs by; the fixed point fn = 0 does not
+    // depend on G at all.
     double g = 0.0;
     bool g_fresh = false;
     double tj = 0.0;                     // start time of segment cur
@@ -613,7 +618,7 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             fn = acc;
             if (!g_fresh) g = seg_poly(c + SEG_G, o.seg_ng, w);
             dt = -fn * g;
-            g_fresh = (dbits(dt) & DMAG) < DBITS_1EM5;
+            g_fresh = (dbits(dt) & DMAG) < DBITS_0P1;
         }
         if ((dbits(dt) & DMAG) < thr_bits) {
             t = tj + (w + 0.5) * o.spacing;
