@@ -40,7 +40,7 @@ typedef struct gslc_ctx gslc_ctx;
 typedef struct {
     int32_t have_data;      /* 0: default LUT — contains() is true, eval() = ref_value */
     int32_t bounds_error;   /* LUT2d::boundsError() */
-    int32_t method;         /* 1 bilinear, 3 nearest (isce3 dataInterpMethod) */
+    int32_t method;         /* isce3 dataInterpMethod: 0 sinc, 1 bilinear, 2 bicubic, 3 nearest, 4 biquintic */
     int32_t nx, ny;         /* width, length */
     int32_t _pad;
     double x0, y0, dx, dy;  /* x = slant range (m), y = azimuth time (s) */
@@ -525,18 +525,19 @@ int gslc_last_cube_passes(const gslc_ctx* ctx);
  * loops that reserve HBM up front under a fixed budget, hosts that forbid
  * allocation after start-up, frameworks that own the memory pool).  Same
  * arguments, kernels and results as gslc_geocode_slc, but no context: its
- * scratch lives in file-scope device arrays of the library (about 32.4 MiB
+ * scratch lives in file-scope device arrays of the library (about 33.1 MiB
  * per GPU that loads it, held until exit):
  *  - the deramped copy of the radar blocks (complex64, written by the
  *    deramp straight from the caller's complex64 or complex32 blocks) when
  *    carriers are present and inplace_deramp is 0: at most 4194304 complex
  *    samples over all blocks;
- *  - orbit polynomials for at most 256 state vectors; the sinc table; an
- *    error word cleared by every call.
+ *  - orbit polynomials for at most 256 state vectors; the sinc table (in
+ *    float for the SLC, in double for sinc-method LUT2d tables); an error
+ *    word cleared by every call.
  * Larger inputs are rejected with GSLC_EINVAL and a message in errbuf.  It
  * calls no cudaMalloc, cudaFree or other allocating routine.  The first call
  * on a device (the current one) looks up the arrays' device addresses and
- * uploads the sinc table synchronously, so make it before any stream
+ * uploads the sinc tables synchronously, so make it before any stream
  * capture.  Like gslc_geocode_slc, every call synchronises `stream` before
  * it returns (it reads the error word back).  All calls share the arrays:
  * calls that overlap on the GPU (other streams, other host threads) race and

@@ -38,6 +38,7 @@ struct gslc_ctx {
     cudaStream_t h2d_stream = nullptr, aux_stream = nullptr;
     std::vector<cudaEvent_t> io_ev;
     int io_reruns = 0;
+    bool no_alloc = false;          // the allocation-free entry point's stand-in context
     std::string err;
 };
 
@@ -425,7 +426,7 @@ bool proj_forward(int epsg, const Utm& u, double lon, double lat, double& x, dou
     return utm_forward(u, lon, lat, x, y);
 }
 
-Lut to_lut(const gslc_lut2d& l) {
+Lut to_lut(const gslc_lut2d& l, const double* sinc64 = nullptr) {
     Lut o{};
     o.have_data = l.have_data;
     o.bounds_error = l.bounds_error;
@@ -439,14 +440,35 @@ Lut to_lut(const gslc_lut2d& l) {
     o.kx_max = dkey(l.nx - 1.0);
     o.ky_max = dkey(l.ny - 1.0);
     o.data = l.data;
+    o.sinc = sinc64;
     return o;
 }
 
+// The sinc kernel table in double on the device (a LUT2d with the sinc
+// method, the raster interpolators), made on first use.
+int ensure_sinc64(gslc_ctx* c) {
+    if (c->d_sinc64) return GSLC_OK;
+    if (c->no_alloc) return set_err(c, GSLC_EUNSUPPORTED, "a sinc LUT2d needs the context's sinc table");
+    const std::vector<double> t = make_sinc_table_double();
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_sinc64, t.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_sinc64, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (c->d_sinc64) cudaFree(c->d_sinc64);
+        c->d_sinc64 = nullptr;
+        return cuda_err(c, e, "sinc table");
+    }
+    return GSLC_OK;
+}
+
+// LUT2d interpolation methods (isce3 dataInterpMethod): 0 sinc, 1 bilinear,
+// 2 bicubic, 3 nearest, 4 biquintic
 int check_lut(gslc_ctx* c, const gslc_lut2d& l, const char* name) {
     if (!l.have_data) return 0;
-    if (l.method != 1 && l.method != 3)
-        return set_err(c, GSLC_EUNSUPPORTED, std::string(name) + ": only bilinear and nearest LUT2d interpolation");
+    if (l.method < 0 || l.method > 4)
+        return set_err(c, GSLC_EINVAL, std::string(name) + ": unknown LUT2d interpolation method");
     if (l.nx < 1 || l.ny < 1 || !l.data) return set_err(c, GSLC_EINVAL, std::string(name) + ": LUT2d without data");
+    if (l.method == 0) return ensure_sinc64(c);
     return 0;
 }
 
@@ -455,7 +477,7 @@ int to_azrg(gslc_ctx* c, const gslc_azrg_func& f, AzRg& o, const char* name) {
     o.kind = f.kind;
     if (f.kind == 0) {
         if (int st = check_lut(c, f.lut, name)) return st;
-        o.lut = to_lut(f.lut);
+        o.lut = to_lut(f.lut, c->d_sinc64);
         o.is_zero = (!f.lut.have_data && f.lut.ref_value == 0.0) ? 1 : 0;
     } else if (f.kind == 1) {
         const gslc_poly2d& p = f.poly;
@@ -825,10 +847,10 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.k_s_stop = dkey(p.s_stop);
     p.k_s_r0 = dkey(p.s_r0);
     p.k_s_end = dkey(p.s_end);
-    p.nat_dop = to_lut(a->native_doppler);
-    p.img_dop = to_lut(a->image_grid_doppler);
-    p.az_corr = to_lut(a->az_time_correction);
-    p.sr_corr = to_lut(a->srange_correction);
+    p.nat_dop = to_lut(a->native_doppler, c->d_sinc64);
+    p.img_dop = to_lut(a->image_grid_doppler, c->d_sinc64);
+    p.az_corr = to_lut(a->az_time_correction, c->d_sinc64);
+    p.sr_corr = to_lut(a->srange_correction, c->d_sinc64);
     p.az_corr_on = p.az_corr.have_data || p.az_corr.ref_value != 0.0;
     p.sr_corr_on = p.sr_corr.have_data || p.sr_corr.ref_value != 0.0;
     if ((st = to_azrg(c, a->az_carrier, p.az_car, "az_carrier"))) return st;
@@ -1641,7 +1663,7 @@ extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc
     p.n_blocks = a->n_blocks;
     p.geo_is_lonlat = a->epsg == 4326;
     if (!p.geo_is_lonlat) utm_setup(a->epsg, p.utm);
-    p.dop = to_lut(a->doppler);
+    p.dop = to_lut(a->doppler, c->d_sinc64);
     p.ell_a = WGS84_A;
     p.ell_e2 = WGS84_E2;
     p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));     // RadarGridParameters::sensingMid
@@ -1729,8 +1751,8 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     p.width = gg.width; p.length = gg.length; p.n_heights = a->n_heights;
     p.geo_is_lonlat = gg.epsg == 4326;
     if (!p.geo_is_lonlat) utm_setup(gg.epsg, p.utm);
-    p.grid_dop = to_lut(a->grid_doppler);
-    p.nat_dop = to_lut(a->native_doppler);
+    p.grid_dop = to_lut(a->grid_doppler, c->d_sinc64);
+    p.nat_dop = to_lut(a->native_doppler, c->d_sinc64);
     p.t_mid = 0.5 * (rg.sensing_start + grid_stop(rg));
     p.mid_range = 0.5 * (rg.starting_range + grid_end(rg));      // RadarGridParameters::midRange
     p.wvl = rg.wavelength;
@@ -1855,16 +1877,7 @@ extern "C" int gslc_interpolate_raster(gslc_ctx* c, const double* az_index, cons
     p.out = out; p.dtype = dtype; p.method = method; p.invalid = invalid_value;
     p.sinc = c->d_sinc;
     if (method == 0 && (dtype == RASTER_F64 || dtype == RASTER_C128)) {
-        if (!c->d_sinc64) {
-            const std::vector<double> t = make_sinc_table_double();
-            e = cudaMalloc(&c->d_sinc64, t.size() * sizeof(double));
-            if (e == cudaSuccess) e = cudaMemcpy(c->d_sinc64, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
-            if (e != cudaSuccess) {
-                if (c->d_sinc64) cudaFree(c->d_sinc64);
-                c->d_sinc64 = nullptr;
-                return cuda_err(c, e, "sinc table");
-            }
-        }
+        if (int st = ensure_sinc64(c)) return st;
         p.sinc = c->d_sinc64;
     }
     e = launch_raster_interp(p, stream, &c->launches);
@@ -1929,7 +1942,7 @@ extern "C" int gslc_dem_stats(gslc_ctx* c, const float* data, int64_t length, in
 // gslc_geocode_slc needs a context, and its constructor and the carrier
 // deramp allocate; this variant runs the same kernels with all of its
 // scratch in the file-scope device arrays below, held by every GPU that
-// loads the library until the process exits (about 32.4 MiB in total).
+// loads the library until the process exits (about 33.1 MiB in total).
 // ===========================================================================
 namespace {
 
@@ -1939,8 +1952,10 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 
 // deramped radar samples, all blocks back to back
 static __device__ __align__(256) float2 g_noalloc_deramp[NOALLOC_MAX_DERAMP];
-// sinc kernel table, SINC_SUB x SINC_LEN
+// sinc kernel table, SINC_SUB x SINC_LEN, in float (the SLC interpolation)
+// and in double (LUT2d tables with the sinc method)
 static __device__ __align__(256) float g_noalloc_sinc[SINC_SUB * SINC_LEN];
+static __device__ __align__(256) double g_noalloc_sinc64[SINC_SUB * SINC_LEN];
 // orbit polynomial pieces
 static __device__ __align__(256) double g_noalloc_orbit[orbit_table_doubles(NOALLOC_MAX_STATE_VECTORS)];
 // error word (bit 0: projection inverse failed); cleared at every call
@@ -1950,6 +1965,7 @@ struct NoallocDevice {
     std::atomic<bool> ready{false};   // set (release) once the fields below hold
     float2* deramp = nullptr;
     float* sinc = nullptr;
+    double* sinc64 = nullptr;
     double* orbit = nullptr;
     int32_t* err = nullptr;
 };
@@ -1973,11 +1989,15 @@ int noalloc_setup(int dev, NoallocDevice& d, char* buf, size_t len) {
     if (d.ready.load(std::memory_order_acquire)) return GSLC_OK;
     cudaError_t e = cudaGetSymbolAddress((void**)&d.deramp, g_noalloc_deramp);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.sinc, g_noalloc_sinc);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.sinc64, g_noalloc_sinc64);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.orbit, g_noalloc_orbit);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&d.err, g_noalloc_err);
     if (e != cudaSuccess) return noalloc_fail(buf, len, GSLC_ECUDA, cudaGetErrorString(e));
     const std::vector<float> table = make_sinc_table();
+    const std::vector<double> table64 = make_sinc_table_double();
     e = cudaMemcpy(d.sinc, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d.sinc64, table64.data(), table64.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return noalloc_fail(buf, len, GSLC_ECUDA, cudaGetErrorString(e));
     d.ready.store(true, std::memory_order_release);
     (void)dev;
@@ -2008,7 +2028,9 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
     // has nothing to allocate (orbit capacity suffices, deramp is in place).
     gslc_ctx c;
     c.device = dev;
+    c.no_alloc = true;
     c.d_sinc = d.sinc;
+    c.d_sinc64 = d.sinc64;
     c.d_err = d.err;
     static thread_local int32_t h_err[4];
     c.h_err = h_err;
@@ -2027,6 +2049,7 @@ extern "C" int gslc_geocode_slc_noalloc(const gslc_geocode_args* a, void* stream
                             "radar blocks exceed the allocation-free deramp scratch (4194304 complex samples)");
     const int st = geocode_slc_impl(&c, a, (cudaStream_t)stream, nullptr, nullptr, d.deramp);
     c.d_sinc = nullptr;   // the static arrays are not the context's to free
+    c.d_sinc64 = nullptr;
     c.d_err = nullptr;
     c.d_orbit = nullptr;
     c.h_err = nullptr;

@@ -14,8 +14,10 @@
 
 #ifdef __CUDACC__
 #define GSLC_HD __host__ __device__ __forceinline__
+#define GSLC_HD_COLD __host__ __device__ __noinline__ inline
 #else
 #define GSLC_HD inline
+#define GSLC_HD_COLD inline
 #endif
 
 namespace gslc {
@@ -88,6 +90,7 @@ struct Lut {
     double inv_dx, inv_dy;      // 1/dx, 1/dy
     int64_t kx_max, ky_max;     // dkey(nx - 1), dkey(ny - 1)
     const double* data;
+    const double* sinc;         // method 0: the sinc kernel table in double, [SINC_SUB][SINC_LEN]
 };
 
 // core/LUT2d.h:84-95.  The index is formed with the reciprocal spacing; it
@@ -115,6 +118,109 @@ GSLC_HD T ld_ro(const T* p) {
 #endif
 }
 
+// ---- LUT2d's other interpolators, FP64 in the reference's operation order,
+// at table coordinates already clamped to the table (LUT2d.cpp:151-152) ----
+GSLC_HD double lut_at(const Lut& l, int r, int c) {
+    r = r < 0 ? 0 : (r > l.ny - 1 ? l.ny - 1 : r);
+    c = c < 0 ? 0 : (c > l.nx - 1 ? l.nx - 1 : c);
+    return ld_ro(l.data + (long)r * l.nx + c);
+}
+
+// core/BicubicInterpolator.cpp:37-42 (cubicInterpolate, T = double)
+GSLC_HD double lut_cubic(double p0, double p1, double p2, double p3, double t) {
+    const double tc = dsub(1.0, t);
+    const double inner = dadd(dsub(p2, dmul(p0, dmul(tc, tc))),
+                              dmul(dsub(dmul(p2, dadd(dmul(tc, 3.0), 1.0)), dmul(p3, tc)), t));
+    const double tail = dmul(p1, dadd(dmul(dmul(t, t), dsub(dmul(t, 3.0), 5.0)), 2.0));
+    return ddiv(dadd(dmul(t, inner), tail), 2.0);
+}
+
+// core/BicubicInterpolator.cpp:47-64: rows y0-1..y0+2, columns x0-1..x0+2.
+// The reference reads that neighbourhood unchecked, which at a table's edge
+// rows and columns falls outside the table; those reads are clamped here.
+GSLC_HD double lut_bicubic(const Lut& l, double xi, double yi) {
+    const int x0 = (int)floor(xi), y0 = (int)floor(yi);
+    const double fx = dsub(xi, (double)x0), fy = dsub(yi, (double)y0);
+    double v[4];
+    for (int i = -1; i < 3; ++i)
+        v[i + 1] = lut_cubic(lut_at(l, y0 + i, x0 - 1), lut_at(l, y0 + i, x0), lut_at(l, y0 + i, x0 + 1),
+                             lut_at(l, y0 + i, x0 + 2), fx);
+    return lut_cubic(v[0], v[1], v[2], v[3], fy);
+}
+
+// core/Spline2dInterpolator.cpp:89-108 (_initSpline, U = double, n = 6)
+GSLC_HD void lut_init_spline6(const double Y[6], double R[6]) {
+    double Q[6];
+    Q[0] = 0.0;
+    R[0] = 0.0;
+    for (int i = 1; i < 5; ++i) {
+        const double p = ddiv(1.0, dadd(dmul(0.5, Q[i - 1]), 2.0));
+        Q[i] = dmul(-0.5, p);
+        R[i] = dmul(dsub(dmul(3.0, dadd(dsub(Y[i + 1], dmul(2.0, Y[i])), Y[i - 1])), dmul(0.5, R[i - 1])), p);
+    }
+    R[5] = 0.0;
+    for (int i = 4; i > 0; --i) R[i] = dadd(dmul(Q[i], R[i + 1]), R[i]);
+}
+
+// core/Spline2dInterpolator.cpp:69-87 (_spline) on the branch x in [2, 3)
+// that LUT2d's clamped coordinates always take (x - j0 = 2 + frac)
+GSLC_HD double lut_spline6_at(double x, const double Y[6], const double R[6]) {
+    const int j = (int)floor(x);
+    const double xx = dsub(x, (double)j);
+    const double t0 = dsub(dsub(dsub(Y[j], Y[j - 1]), ddiv(R[j - 1], 3.0)), ddiv(R[j], 6.0));
+    const double t1 = dmul(xx, dadd(ddiv(R[j - 1], 2.0), dmul(xx, ddiv(dsub(R[j], R[j - 1]), 6.0))));
+    return dadd(Y[j - 1], dmul(xx, dadd(t0, t1)));
+}
+
+// core/Spline2dInterpolator.cpp:32-67 (interp_impl, order 6): window rows and
+// columns clamped to [0, n - 2], read at index + 1
+GSLC_HD double lut_biquintic(const Lut& l, double xi, double yi) {
+    const int i0 = (int)yi - 2, j0 = (int)xi - 2;
+    double A[6], R[6], HC[6];
+    for (int i = 0; i < 6; ++i) {
+        int indi = i0 + i;
+        indi = (indi < 0 ? 0 : (indi > l.ny - 2 ? l.ny - 2 : indi)) + 1;
+        for (int j = 0; j < 6; ++j) {
+            int indj = j0 + j;
+            indj = (indj < 0 ? 0 : (indj > l.nx - 2 ? l.nx - 2 : indj)) + 1;
+            A[j] = ld_ro(l.data + (long)indi * l.nx + indj);
+        }
+        lut_init_spline6(A, R);
+        HC[i] = lut_spline6_at(dsub(xi, (double)j0), A, R);
+    }
+    lut_init_spline6(HC, R);
+    return lut_spline6_at(dsub(yi, (double)i0), HC, R);
+}
+
+// core/Sinc2dInterpolator.cpp:45-96 (U = double): 8 x 8 taps, 0 within 3-4
+// samples of the table's edges
+GSLC_HD double lut_sinc(const Lut& l, double xi, double yi) {
+    const int ix = (int)floor(xi), iy = (int)floor(yi);
+    const double fx = dsub(xi, (double)ix), fy = dsub(yi, (double)iy);
+    if (ix < SINC_HALF - 1 || ix > l.nx - SINC_HALF - 1) return 0.0;
+    if (iy < SINC_HALF - 1 || iy > l.ny - SINC_HALF - 1) return 0.0;
+    const int xx = ix + SINC_HALF, yy = iy + SINC_HALF;
+    int fxi = (int)dmul(fx, (double)SINC_SUB), fyi = (int)dmul(fy, (double)SINC_SUB);
+    fxi = fxi < 0 ? 0 : (fxi > SINC_SUB - 1 ? SINC_SUB - 1 : fxi);
+    fyi = fyi < 0 ? 0 : (fyi > SINC_SUB - 1 ? SINC_SUB - 1 : fyi);
+    double ret = 0.0;
+    for (int i = 0; i < SINC_LEN; ++i)
+        for (int j = 0; j < SINC_LEN; ++j)
+            ret = dadd(ret, dmul(dmul(ld_ro(l.data + (long)(yy - i) * l.nx + (xx - j)),
+                                      ld_ro(l.sinc + fyi * SINC_LEN + i)),
+                                 ld_ro(l.sinc + fxi * SINC_LEN + j)));
+    return ret;
+}
+
+// methods 0 (sinc), 2 (bicubic) and 4 (biquintic) at clamped table
+// coordinates; out of line, so that the geocode kernels' register allocation
+// does not carry these rarely taken paths
+GSLC_HD_COLD double lut_interp_other(const Lut& l, double xi, double yi) {
+    if (l.method == 2) return lut_bicubic(l, xi, yi);
+    if (l.method == 4) return lut_biquintic(l, xi, yi);
+    return lut_sinc(l, xi, yi);
+}
+
 // core/LUT2d.cpp:124-158 with core/BilinearInterpolator.cpp:12-49 or
 // core/NearestNeighborInterpolator.cpp:12-22.  The bilinear divisions by
 // (x2-x1)*(y2-y1) == 1 are exact and omitted.
@@ -124,6 +230,7 @@ GSLC_HD double lut_eval(const Lut& l, double y, double x) {
     double yi = (y - l.y0) * l.inv_dy;
     xi = fmin(fmax(xi, 0.0), l.nx - 1.0);
     yi = fmin(fmax(yi, 0.0), l.ny - 1.0);
+    if (l.method != 1 && l.method != 3) return lut_interp_other(l, xi, yi);
     if (l.method == 3) {
         long r = (long)round(yi), c = (long)round(xi);
         return ld_ro(l.data + r * l.nx + c);
@@ -156,7 +263,7 @@ GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi);
 
 GSLC_HD float lut_eval_f32(const Lut& l, double y, double x) {
     if (!l.have_data) return (float)l.ref_value;
-    if (l.method == 3) return (float)lut_eval(l, y, x);
+    if (l.method != 1) return (float)lut_eval(l, y, x);
     return lut_bilinear_f32(l, (float)((x - l.x0) * l.inv_dx), (float)((y - l.y0) * l.inv_dy));
 }
 
@@ -170,7 +277,7 @@ GSLC_HD bool lut_contains_eval_f32(const Lut& l, double y, double x, float& v) {
     const double xd = (x - l.x0) * l.inv_dx, yd = (y - l.y0) * l.inv_dy;
     const int64_t i = dkey(xd), j = dkey(yd);
     if (!((i >= 0 && i <= l.kx_max) && (j >= 0 && j <= l.ky_max))) return false;
-    v = l.method == 3 ? (float)lut_eval(l, y, x) : lut_bilinear_f32(l, (float)xd, (float)yd);
+    v = l.method != 1 ? (float)lut_eval(l, y, x) : lut_bilinear_f32(l, (float)xd, (float)yd);
     return true;
 }
 
@@ -219,6 +326,7 @@ GSLC_HD double lut_eval_exact(const Lut& l, double y, double x) {
     double yi = ddiv(dsub(y, l.y0), l.dy);
     xi = fmin(fmax(xi, 0.0), l.nx - 1.0);
     yi = fmin(fmax(yi, 0.0), l.ny - 1.0);
+    if (l.method != 1 && l.method != 3) return lut_interp_other(l, xi, yi);
     if (l.method == 3) {
         long r = (long)round(yi), c = (long)round(xi);
         return ld_ro(l.data + r * l.nx + c);

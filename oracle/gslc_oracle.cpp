@@ -201,7 +201,37 @@ double nearest(const double* z, int nx, double x, double y) {
     return z[(size_t)row * nx + col];
 }
 
-// core/LUT2d.cpp:124-158 (out-of-bounds only logs; index is clamped)
+// core/BicubicInterpolator.cpp:37-42 (cubicInterpolate, T = double)
+double cubic_interpolate(double p0, double p1, double p2, double p3, double tfrac) {
+    const double tconj = 1. - tfrac;
+    return (tfrac * (p2 - p0 * (tconj * tconj) + (p2 * (tconj * 3. + 1.) - p3 * tconj) * tfrac) +
+            p1 * (tfrac * tfrac * (tfrac * 3. - 5.) + 2.)) / 2.;
+}
+
+// core/BicubicInterpolator.cpp:47-64 (U = double).  The reference reads the
+// 4 x 4 neighbourhood unchecked, outside its matrix at the edge rows and
+// columns (undefined there); here those reads are clamped to the matrix.
+double bicubic(const double* z, int ny, int nx, double x, double y) {
+    const int x0 = (int)std::floor(x), y0 = (int)std::floor(y);
+    auto at = [&](int r, int c) {
+        r = std::min(std::max(r, 0), ny - 1);
+        c = std::min(std::max(c, 0), nx - 1);
+        return z[(size_t)r * nx + c];
+    };
+    double intp[4];
+    for (int i = -1; i < 3; i++)
+        intp[i + 1] = cubic_interpolate(at(y0 + i, x0 - 1), at(y0 + i, x0), at(y0 + i, x0 + 1), at(y0 + i, x0 + 2),
+                                        x - x0);
+    return cubic_interpolate(intp[0], intp[1], intp[2], intp[3], y - y0);
+}
+
+template <typename U>
+U spline2d(const U* z, int ny, int nx, double x, double y);
+double sinc2d_double(const double* z, int rows, int cols, double x, double y);
+
+// core/LUT2d.cpp:124-158 (out-of-bounds only logs; index is clamped), with
+// the interpolator of the table's method (core/LUT2d.cpp _setInterpolator):
+// 0 sinc, 1 bilinear, 2 bicubic, 3 nearest, 4 biquintic
 double lut_eval(const orc_lut2d* l, double y, double x) {
     double value = l->ref_value;
     if (!l->have_data) return value;
@@ -209,8 +239,13 @@ double lut_eval(const orc_lut2d* l, double y, double x) {
     double y_idx = (y - l->y0) / l->dy;
     x_idx = std::min(std::max(x_idx, 0.0), l->nx - 1.0);
     y_idx = std::min(std::max(y_idx, 0.0), l->ny - 1.0);
-    if (l->method == 3) return nearest(l->data, l->nx, x_idx, y_idx);
-    return bilinear(l->data, l->nx, x_idx, y_idx);
+    switch (l->method) {
+        case 0: return sinc2d_double(l->data, l->ny, l->nx, x_idx, y_idx);
+        case 2: return bicubic(l->data, l->ny, l->nx, x_idx, y_idx);
+        case 3: return nearest(l->data, l->nx, x_idx, y_idx);
+        case 4: return spline2d<double>(l->data, l->ny, l->nx, x_idx, y_idx);
+        default: return bilinear(l->data, l->nx, x_idx, y_idx);
+    }
 }
 
 // ---------------------------------------------------------------- Poly2d
@@ -1318,6 +1353,7 @@ extern "C" int orc_orbit_interpolate(const orc_orbit* o, double t, double* pos, 
 extern "C" double orc_interp2d_double(int method, const double* z, int ny, int nx, double x, double y) {
     switch (method) {
         case 1: return bilinear(z, nx, x, y);
+        case 2: return bicubic(z, ny, nx, x, y);
         case 3: return nearest(z, nx, x, y);
         case 4: return spline2d<double>(z, ny, nx, x, y);
         case 5: return sinc2d_double(z, ny, nx, x, y);

@@ -313,3 +313,34 @@ def test_lut2d_carriers(oracle_mod, c1, method, precision):
     # the carrier output holds the table values at the pixels' radar positions
     w = np.isfinite(gpu["az"]) & (gpu["carrier"] != -7.0)
     assert np.abs(gpu["carrier"][w]).max() > 1.0
+
+
+@pytest.mark.parametrize("method,precision", [("sinc", "fp64"), ("bicubic", "fp64"), ("biquintic", "fp64"),
+                                              ("biquintic", "ff")])
+def test_lut2d_methods(oracle_mod, c1, method, precision):
+    """LUT2d tables with the reference's other interpolators
+    (core/LUT2d.cpp _setInterpolator: sinc 8 x 8, bicubic, biquintic order
+    6) as the image-grid and native Doppler of a squinted grid (geo2rdr's
+    Newton and the sinc chip's demodulation), as the slant-range correction
+    and as the azimuth and range carriers.  The tables reach 12 samples past
+    the radar grid on every side, so that the points the kernels evaluate
+    lie where the sinc interpolator is non-zero and the bicubic reads stay
+    inside the table."""
+    rg = c1.radar_grid
+    nr, nt = 40, 36
+    pad_r, pad_t = 12, 12
+    dr = (rg.end_range - rg.starting_range) / (nr - 1 - 2 * pad_r)
+    dt = (rg.sensing_stop - rg.sensing_start) / (nt - 1 - 2 * pad_t)
+    rr = rg.starting_range + dr * (np.arange(nr) - pad_r)
+    tt = rg.sensing_start + dt * (np.arange(nt) - pad_t)
+    T, R = np.meshgrid((tt - rg.sensing_mid) / (tt[-1] - tt[0]), (rr - rg.mid_range) / (rr[-1] - rr[0]),
+                       indexing="ij")
+    dop = LUT2d(rr, tt, -30.0 + 120.0 * R ** 2 + 25.0 * np.sin(3.0 * T) + 8.0 * R * T, method)
+    corr_r = LUT2d(rr, tt, 0.4 + 0.2 * np.cos(2.0 * R + T), method)
+    az_car = LUT2d(rr, tt, 2 * np.pi * 40.0 * T + 3.0 * T ** 2 + 0.5 * R, method)
+    rg_car = LUT2d(rr, tt, 0.8 * R + 0.2 * T * R, method)
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], native_doppler=dop, image_grid_doppler=dop,
+                         srange_correction=corr_r, az_carrier=az_car, rg_carrier=rg_car,
+                         geo2rdr_precision=precision)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 100000

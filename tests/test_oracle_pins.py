@@ -1,7 +1,8 @@
 """Pins the CPU oracle against the reference's own known-answer data.
 
 - tests/data/interpolator/data.txt of the reference (golden copy in
-  tests/golden/interpolator_data.npz): bilinear to 1e-8, biquintic MSE < 0.058,
+  tests/golden/interpolator_data.npz): bilinear to 1e-8, bicubic and
+  biquintic MSE < 0.058,
   sinc MSE < 3e-4, nearest exact (tests/cxx/isce3/core/interpolator/
   interpolator.cpp:104-236).
 - the circular-orbit Hermite KAT (tests/cxx/isce3/core/orbit/orbit.cpp:495-552),
@@ -47,6 +48,19 @@ def test_nearest_known_answer(oracle_mod, interp_case):
     for row in data:
         x, y = (row[0] - start) / delta, (row[1] - start) / delta
         assert oracle_mod.interp2d(3, M, x, y) == M[int(round(y)), int(round(x))]
+
+
+def test_bicubic_known_answer(oracle_mod, interp_case):
+    # interpolator.cpp:144-168: points at least one sample inside the left and
+    # top edges and two inside the right and bottom ones
+    data, M, start, delta = interp_case
+    err = 0.0
+    for r in data:
+        x, y = (r[0] - start) / delta, (r[1] - start) / delta
+        if x < 1 or y < 1 or x >= M.shape[1] - 2 or y >= M.shape[0] - 2:
+            continue
+        err += (oracle_mod.interp2d(2, M, x, y) - r[5]) ** 2
+    assert err / len(data) < 0.058
 
 
 def test_biquintic_known_answer(oracle_mod, interp_case):
@@ -155,3 +169,22 @@ def test_oracle_regression_golden(oracle_mod):
     np.testing.assert_array_equal(np.isnan(geo), np.isnan(gold["geo"]))
     v = np.isfinite(geo)
     assert np.max(np.abs(geo[v] - gold["geo"][v])) <= 1e-6
+
+
+@pytest.mark.parametrize("method,code", [("sinc", 0), ("bilinear", 1), ("bicubic", 2), ("nearest", 3),
+                                         ("biquintic", 4)])
+def test_lut2d_methods_use_their_interpolator(oracle_mod, interp_case, method, code):
+    # core/LUT2d.cpp:124-158 and _setInterpolator: the coordinates are
+    # clamped to the table, then the method's interpolator runs on them
+    _, M, _, _ = interp_case
+    lut = LUT2d(-3.0, 7.0, 0.5, 0.25, M, method)
+    interp_code = {0: 5, 1: 1, 2: 2, 3: 3, 4: 4}[code]
+    rng = np.random.default_rng(5)
+    for _ in range(200):
+        x = -3.0 + rng.uniform(-2.0, 0.5 * M.shape[1] + 2.0)
+        y = 7.0 + rng.uniform(-1.0, 0.25 * M.shape[0] + 1.0)
+        xi = min(max((x + 3.0) / 0.5, 0.0), M.shape[1] - 1.0)
+        yi = min(max((y - 7.0) / 0.25, 0.0), M.shape[0] - 1.0)
+        if code == 2 and not (1 <= xi < M.shape[1] - 2 and 1 <= yi < M.shape[0] - 2):
+            continue   # the reference's bicubic reads outside the table there
+        assert oracle_mod.lut_eval(lut, y, x) == oracle_mod.interp2d(interp_code, M, xi, yi)

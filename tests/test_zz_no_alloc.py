@@ -182,6 +182,22 @@ def test_noalloc_inplace_deramp():
     assert not np.array_equal(got[2], sc.slc)
 
 
+def test_noalloc_sinc_lut_carriers():
+    """Carriers given as LUT2d tables with the sinc method: their double sinc
+    table is static scratch too, uploaded with the float one at set-up."""
+    sc = synth.scene_c1(seed=17, length=512, width=576, geo=128, dem_px=96)
+    rg = sc.radar_grid
+    rr = rg.starting_range + (rg.end_range - rg.starting_range) / 11 * (np.arange(36) - 12)
+    tt = rg.sensing_start + (rg.sensing_stop - rg.sensing_start) / 11 * (np.arange(36) - 12)
+    T, R = np.meshgrid((tt - rg.sensing_mid) / (tt[-1] - tt[0]), (rr - rg.mid_range) / (rr[-1] - rr[0]),
+                       indexing="ij")
+    azc = LUT2d(rr, tt, 2 * np.pi * 30.0 * T + 0.4 * R, "sinc")
+    rgc = LUT2d(rr, tt, 0.6 * R - 0.1 * T, "sinc")
+    ref = _run(sc, azc, rgc, noalloc=False)
+    got = _run(sc, azc, rgc, noalloc=True)
+    _compare(ref[:2], got[:2])
+
+
 def test_noalloc_rejects_long_orbit():
     """More state vectors than the static orbit table holds (256)."""
     sc = synth.scene_c1(seed=17, length=256, width=256, geo=64, dem_px=96)
