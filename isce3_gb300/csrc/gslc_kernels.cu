@@ -84,8 +84,12 @@ __device__ __forceinline__ bool dem_coords_utm(const Dem& d, double lon, double 
 __device__ double dem_spline(const Dem& d, double row, double col) {
     const double ref = 0.0;
     // truncation equals floor wherever the bounds below pass (row, col >= 2);
-    // (col - j0) - 2 is col - icol, both steps exact for col >= 2
-    const int irow = (int)row, icol = (int)col;
+    // (col - j0) - 2 is col - icol, both steps exact for col >= 2.  The
+    // integer parts and the fractions come from the bits (split_bits): a row
+    // or column that is negative, NaN or at least 2^31 gives INT32_MAX and
+    // fails the bounds, as its truncation does.
+    uint64_t frow, fcol;
+    const int irow = split_bits(row, frow), icol = split_bits(col, fcol);
     if (irow < 2 || irow >= d.length - 1) return ref;
     if (icol < 2 || icol >= d.width - 1) return ref;
     const int i0 = irow - 2, j0 = icol - 2;
@@ -93,8 +97,9 @@ __device__ double dem_spline(const Dem& d, double row, double col) {
     if (i0 + 1 < d.avail_lo || min(i0 + 6, d.length - 1) > d.avail_hi) {
         if (d.err) atomicOr(d.err, 8);
     }
-    const float xx = (float)(col - (double)icol);
-    const float yy = (float)(row - (double)irow);
+    // (float)(col - icol) and (float)(row - irow)
+    const float xx = fixed64_to_float(fcol);
+    const float yy = fixed64_to_float(frow);
     int cidx[6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) cidx[j] = min(max(j0 + j, 0), d.width - 2) + 1;
@@ -175,7 +180,7 @@ __device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t
     const bool first_shared = p.t_mid_in_orbit;
     if (!p.t_mid_in_orbit && !update_aztime(p, xyz, t)) return false;
     const bool dop_data = p.img_dop.have_data;
-    const bool dop_const = !dop_data && p.img_dop.ref_value == 0.0;
+    const bool dop_const = !dop_data && (dbits(p.img_dop.ref_value) & DMAG) == 0;   // ref_value == 0.0
     if (p.maxiter < 1) return false;
     if (dop_const && first_shared) {
         // iteration 0 at sensingMid with the shared state: the look-side
@@ -275,7 +280,8 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
         // (the orbit's time span): time, span check and w from FP64
         if (j <= 0 || j >= o.n - 2 || !(wf >= -0.5f && wf < 0.5f)) {
             if (j >= 0) t = tj + ((double)w.hi + (double)w.lo + 0.5) * o.spacing;
-            if (!(t >= o.t0 && t <= o.t_end)) return false;    // FillNaN -> no convergence
+            const int64_t kt = dkey(t);                         // the span test on order keys
+            if (!(kt >= dkey(o.t0) && kt <= dkey(o.t_end))) return false;    // FillNaN -> no convergence
             const int pc = orbit_piece(o, t);
             const double tidx = o.t0 + pc * o.spacing;
             double w64 = (t - tidx) * o.inv_spacing - 1.5;
@@ -367,13 +373,11 @@ __device__ __forceinline__ void sinc_index(double x, int& i, int& f) {
     f = min(max(0, (int)((x - i) * SINC_SUB)), SINC_SUB - 1);
 }
 
+// The chip sum at integer positions ix, iy (3 or 4) and table phases ifx,
+// ify; fracAz_f is (float)fracAz, the demodulation's phase argument.
 template <typename S>
-__device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg,
-                             double fracAz, double fracRg, float doppFreq) {
-    int ix, iy, ifx, ify;
-    sinc_index(4.0 + fracRg, ix, ifx);
-    sinc_index(4.0 + fracAz, iy, ify);
-    if (ix < 3 || ix > 4 || iy < 3 || iy > 4) return make_float2(0.f, 0.f);
+__device__ __noinline__ float2 sinc_chip(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg, int ix, int iy,
+                            int ifx, int ify, float fracAz_f, float doppFreq) {
     float kx[8], ky[8];
     const float4* kxp = reinterpret_cast<const float4*>(p.sinc + ifx * SINC_LEN);
     const float4* kyp = reinterpret_cast<const float4*>(p.sinc + ify * SINC_LEN);
@@ -416,10 +420,20 @@ __device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int 
     float2 cval = make_float2(sre, sim);
     if (demod) {
         float s, c;
-        sincosf(doppFreq * (float)fracAz, &s, &c);
+        sincosf(doppFreq * fracAz_f, &s, &c);
         cval = cmul(cval, make_float2(c, s));
     }
     return cval;
+}
+
+template <typename S>
+__device__ float2 sinc_pixel(const GeoParams& p, const S* __restrict__ rdr, int intAz, int intRg,
+                             double fracAz, double fracRg, float doppFreq) {
+    int ix, iy, ifx, ify;
+    sinc_index(4.0 + fracRg, ix, ifx);
+    sinc_index(4.0 + fracAz, iy, ify);
+    if (ix < 3 || ix > 4 || iy < 3 || iy > 4) return make_float2(0.f, 0.f);
+    return sinc_chip(p, rdr, intAz, intRg, ix, iy, ifx, ify, (float)fracAz, doppFreq);
 }
 
 // block b of the request, in its sample format
@@ -427,6 +441,19 @@ __device__ __forceinline__ float2 sinc_block(const GeoParams& p, int b, int intA
                                              double fracRg, float doppFreq) {
     if (p.rdr_c32) return sinc_pixel(p, reinterpret_cast<const __half2*>(p.rdr[b]), intAz, intRg, fracAz, fracRg, doppFreq);
     return sinc_pixel(p, p.rdr[b], intAz, intRg, fracAz, fracRg, doppFreq);
+}
+
+// The same with the table phases of fractions in 64-bit fixed point
+// (split_bits): 4 + frac is exact in [4, 5) whenever the chip is
+// interpolated (the fraction's last bit is at least the ulp of an index
+// >= 4), so the integer position is 4 and the table phase the fraction's
+// top 13 bits (sinc_index), without the FP64 additions.
+__device__ __forceinline__ float2 sinc_block_fixed(const GeoParams& p, int b, int intAz, int intRg, int ify, int ifx,
+                                                   float fracAz_f, float doppFreq) {
+    if (p.rdr_c32)
+        return sinc_chip(p, reinterpret_cast<const __half2*>(p.rdr[b]), intAz, intRg, 4, 4, ifx, ify, fracAz_f,
+                         doppFreq);
+    return sinc_chip(p, p.rdr[b], intAz, intRg, 4, 4, ifx, ify, fracAz_f, doppFreq);
 }
 
 // float32 -> float16 bits as numpy's astype(float16): round to nearest even
@@ -884,7 +911,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
     bool valid = false;
     uint8_t mval = 255;
     double azc = CUDART_NAN, rgc = CUDART_NAN;
-    double R_uncorr = (double)p.inv_re;
+    double R_uncorr = 0.0;          // the uncorrected slant range, set where the pixel converges
     if (ok) {
         double t, R;
         bool conv;
@@ -963,11 +990,20 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);
         return;
     }
-    // block-relative chip position (geocodeSlc.cpp:440-458, 335-348)
-    const double RgIndex = rgc - p.rg_first_d, AzIndex = azc - p.az_first_d;
-    const int intRgB = (int)RgIndex, intAzB = (int)AzIndex;
-    const double fracRg = RgIndex - intRgB, fracAz = AzIndex - intAzB;
-    bool interp = !(intRgB < 4 || intRgB >= p.inW - 4 || intAzB < 4 || intAzB >= p.inL - 4);
+    // block-relative chip position (geocodeSlc.cpp:440-458, 335-348).
+    // RgIndex = rgc - rg_first is exact, so for rgc >= rg_first its integer
+    // part is trunc(rgc) - rg_first and its fraction that of rgc; below
+    // rg_first, under 1, or with the sign bit set every form gives an integer
+    // part under 4 or past the block, which skips the chip.  Both come from
+    // the bits of rgc and azc (split_bits); likewise in azimuth.
+    uint64_t frg, faz;
+    const int64_t intRgB64 = (int64_t)split_bits(rgc, frg) - p.rg_first;
+    const int64_t intAzB64 = (int64_t)split_bits(azc, faz) - p.az_first;
+    bool interp = !(intRgB64 < 4 || intRgB64 >= p.inW - 4 || intAzB64 < 4 || intAzB64 >= p.inL - 4);
+    const int intRgB = (int)intRgB64, intAzB = (int)intAzB64;
+    static_assert(SINC_SUB == 8192, "table phase = top 13 bits of the fraction");
+    const int ifx = (int)(frg >> 51), ify = (int)(faz >> 51);
+    const float fracAz_f = fixed64_to_float(faz);   // (float)fracAz
     double rng = 0.0, az = 0.0;
     float dop = 0.f;
     if (interp) {
@@ -987,16 +1023,17 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
     // reramp + flatten phase (geocodeSlc.cpp:362-392)
     const double carrier = p.carriers_zero ? 0.0 : azrg_eval(p.rg_car, az, rng) + azrg_eval(p.az_car, az, rng);
     const double flat = p.flat_scale * (p.use_corr ? rng : R_uncorr);
-    double total = 0.0;
-    if (p.reramp) total += carrier;
-    if (p.flatten) total += flat;
+    // 0.0 + carrier is carrier but for a -0.0 carrier, and either zero
+    // skips the rotation below; the sums are otherwise the reference's
+    double total = p.reramp ? carrier : 0.0;
+    if (p.flatten) total = p.reramp ? total + flat : flat;
     if (p.carrier_out) p.carrier_out[k] = carrier;
     if (p.flatten_out) p.flatten_out[k] = flat;
-    const bool rot = total != 0.0;
+    const bool rot = (dbits(total) & DMAG) != 0;    // total != 0.0
     float2 ph = make_float2(1.f, 0.f);
     if (rot) ph = expi_fp64(total);
     for (int b = 0; b < p.nblk; ++b) {
-        float2 v = sinc_block(p, b, intAzB, intRgB, fracAz, fracRg, doppFreq);
+        float2 v = sinc_block_fixed(p, b, intAzB, intRgB, ify, ifx, fracAz_f, doppFreq);
         if (rot) v = cmul(v, ph);
         store_geo(p, b, k, v);
     }

@@ -83,6 +83,52 @@ GSLC_HD int64_t dkey(double x) {
 }
 constexpr int64_t DKEY_INF = 0x7ff0000000000000ll;   // dkey(+inf); above it: NaN
 
+// Integer part and fraction of x from its bits, both exact, off the FP64
+// pipe: for x in [1, 2^31) returns trunc(x) and sets frac64 to
+// (x - trunc(x)) * 2^64 (the bits of x below the binary point, moved to the
+// top of the word); for x in [0, 1) returns 0; for x >= 2^31, infinite, NaN
+// or with the sign bit set returns INT32_MAX.  frac64 is 0 in the last two
+// cases.
+GSLC_HD int32_t split_bits(double x, uint64_t& frac64) {
+    const uint64_t b = dbits(x);
+    const int e = (int)(b >> 52) - 1023;
+    frac64 = 0;
+    if (e < 0) return 0;
+    if (e > 30) return 0x7fffffff;
+    const uint64_t m = (b & 0xfffffffffffffull) | (1ull << 52);
+    frac64 = m << (12 + e);
+    return (int32_t)(m >> (52 - e));
+}
+
+// frac64 * 2^-64 rounded to the nearest float, ties to even: the float of
+// a fraction split_bits formed, as converting the exact double would give.
+GSLC_HD float fixed64_to_float(uint64_t f) {
+    if (f == 0) return 0.0f;
+#if defined(__CUDA_ARCH__)
+    const int lz = __clzll((long long)f);
+#else
+    const int lz = __builtin_clzll(f);
+#endif
+    const uint64_t n = f << lz;                     // leading one at bit 63
+    uint32_t mant = (uint32_t)(n >> 40);            // 24 bits, leading one at bit 23
+    const uint64_t rest = n & 0xffffffffffull;      // the 40 bits below
+    const uint64_t half = 1ull << 39;
+    if (rest > half || (rest == half && (mant & 1u))) ++mant;
+    uint32_t expo = 126u - (uint32_t)lz;            // n * 2^(-64-lz) = (mant / 2^23) * 2^(-1-lz)
+    if (mant == (1u << 24)) {
+        mant >>= 1;
+        ++expo;
+    }
+    const uint32_t u = (expo << 23) | (mant & 0x7fffffu);
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float r;
+    memcpy(&r, &u, sizeof(r));
+    return r;
+#endif
+}
+
 // ---- LUT2d (core/LUT2d.{h,cpp}) ------------------------------------------
 struct Lut {
     int32_t have_data, bounds_error, method, nx, ny, _pad;
@@ -654,8 +700,12 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
     double w = 0.0;
     const double* c = seg;
     const int nh = o.seg_nh;
-    // |dt| < thr as a bit compare (thr <= 0 or NaN: never, as the FP64 test)
-    const uint64_t thr_bits = thr > 0.0 ? dbits(thr) : 0ull;
+    // |dt| < thr as a bit compare (thr <= 0 or NaN: never, as the FP64
+    // test); thr > 0.0 from its bits as well
+    const uint64_t tb = dbits(thr);
+    const uint64_t thr_bits = ((int64_t)tb > 0 && tb <= (uint64_t)DKEY_INF) ? tb : 0ull;
+    // the orbit's time span as order keys (the range test below)
+    const int64_t k_t0 = dkey(o.t0), k_tend = dkey(o.t_end);
     // G(w) = 1/|vel|^2 changes by ~5e-6 of itself per second of the
     // iterate's travel.  Once a step falls below 0.1 s the iterate travels
     // at most ~0.014 s more (the steps shrink by ~0.12 each), so the last G
@@ -680,7 +730,8 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
         if (cur <= 0 || cur >= o.n - 2 || !in_seg) {
             if (cur < 0) t -= dt;        // the first step, from the caller's iterate
             else t = tj + (w + 0.5) * o.spacing;
-            if (!(t >= o.t0 && t <= o.t_end)) return false;  // FillNaN -> no convergence
+            const int64_t kt = dkey(t);
+            if (!(kt >= k_t0 && kt <= k_tend)) return false;  // FillNaN -> no convergence
             const int pc = orbit_piece(o, t);
             const double tidx = o.t0 + pc * o.spacing;
             w = (t - tidx) * o.inv_spacing - 1.5;
