@@ -82,7 +82,7 @@ typedef struct {
 typedef struct {
     double t0, spacing;     /* time tag i = t0 + i*spacing (s since reference epoch) */
     int32_t n;
-    int32_t method;         /* 0 Hermite (1 Legendre: GSLC_EUNSUPPORTED) */
+    int32_t method;         /* 0 Hermite (n >= 4), 1 Legendre (n >= 9) */
     const double* pos;      /* host, n*3 (m, ECEF) */
     const double* vel;      /* host, n*3 (m/s) */
 } gslc_orbit;

@@ -340,6 +340,23 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
 // segments; orbit_table_doubles) and the Orbit descriptor, its table
 // pointers left null for bind_orbit.
 void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
+    if (o.method == 1) {
+        // Legendre: the state vectors themselves (positions, then
+        // velocities), interpolated at each iterate as the reference does;
+        // the table keeps the Hermite size so that capacities match
+        coef.assign(orbit_table_doubles(o.n), 0.0);
+        std::memcpy(coef.data(), o.pos, sizeof(double) * 3 * (size_t)o.n);
+        std::memcpy(coef.data() + 3 * (size_t)o.n, o.vel, sizeof(double) * 3 * (size_t)o.n);
+        ob = Orbit{};
+        ob.t0 = o.t0;
+        ob.spacing = o.spacing;
+        ob.inv_spacing = 1.0 / o.spacing;
+        ob.t_end = o.t0 + (o.n - 1) * o.spacing;
+        ob.n = o.n;
+        ob.n_pieces = o.n - 3;
+        ob.legendre = 1;
+        return;
+    }
     make_orbit_coeffs(o, coef);
     // Newton segment tables after the pieces (orbit_seg_offset, 16-byte aligned)
     int seg_nh = 0, seg_ng = 0, seg_div = 0, seg_a7 = 1;
@@ -424,6 +441,17 @@ bool proj_inverse(int epsg, const Utm& u, double x, double y, double& lon, doubl
 bool proj_forward(int epsg, const Utm& u, double lon, double lat, double& x, double& y) {
     if (epsg == 4326) { x = lon * 180.0 / M_PI; y = lat * 180.0 / M_PI; return true; }
     return utm_forward(u, lon, lat, x, y);
+}
+
+// Orbit descriptor checks: Hermite (4 or more state vectors) or Legendre
+// (9 or more, core/detail/InterpolateOrbit.icc:111-155); uniform spacing.
+int check_orbit(gslc_ctx* c, const gslc_orbit& o) {
+    if (o.method != 0 && o.method != 1) return set_err(c, GSLC_EINVAL, "orbit interpolation method must be 0 or 1");
+    if (o.n < 4 || !o.pos || !o.vel || !(o.spacing > 0))
+        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (o.method == 1 && o.n < 9)
+        return set_err(c, GSLC_EINVAL, "Legendre orbit interpolation needs >= 9 state vectors");
+    return GSLC_OK;
 }
 
 Lut to_lut(const gslc_lut2d& l, const double* sinc64 = nullptr) {
@@ -602,12 +630,19 @@ extern "C" int gslc_compute_dem_window_block(const gslc_dem_raster* r, const gsl
 }
 
 extern "C" int gslc_orbit_interpolate(const gslc_orbit* o, double t, double* pos, double* vel) {
-    if (!o || !pos || !vel || o->n < 4 || !(o->spacing > 0) || o->method != 0) return GSLC_EINVAL;
+    if (!o || !pos || !vel || o->n < 4 || !(o->spacing > 0) || (o->method != 0 && o->method != 1) ||
+        (o->method == 1 && o->n < 9) || !o->pos || !o->vel)
+        return GSLC_EINVAL;
     std::vector<double> coef;
-    make_orbit_coeffs(*o, coef);
     Orbit ob{};
-    ob.t0 = o->t0; ob.spacing = o->spacing; ob.inv_spacing = 1.0 / o->spacing;
-    ob.t_end = o->t0 + (o->n - 1) * o->spacing; ob.n = o->n; ob.n_pieces = o->n - 3; ob.coef = coef.data();
+    if (o->method == 1) {
+        build_orbit_table(*o, coef, ob);
+    } else {
+        make_orbit_coeffs(*o, coef);
+        ob.t0 = o->t0; ob.spacing = o->spacing; ob.inv_spacing = 1.0 / o->spacing;
+        ob.t_end = o->t0 + (o->n - 1) * o->spacing; ob.n = o->n; ob.n_pieces = o->n - 3;
+    }
+    ob.coef = coef.data();
     if (!(t >= ob.t0 && t <= ob.t_end)) return GSLC_EINVAL;
     V3 p, v;
     orbit_eval(ob, t, p, v);
@@ -619,8 +654,9 @@ extern "C" int gslc_orbit_interpolate(const gslc_orbit* o, double t, double* pos
 extern "C" int gslc_geo2rdr_zero_doppler(const gslc_orbit* o, const double* xyz, double t_guess, int32_t look_side,
                                          double threshold, int32_t maxiter, double* aztime, double* slant_range,
                                          int32_t* converged) {
-    if (!o || !xyz || !aztime || !slant_range || !converged || o->n < 4 || !(o->spacing > 0) || o->method != 0 ||
-        !o->pos || !o->vel || (look_side != -1 && look_side != 1))
+    if (!o || !xyz || !aztime || !slant_range || !converged || o->n < 4 || !(o->spacing > 0) ||
+        (o->method != 0 && o->method != 1) || (o->method == 1 && o->n < 9) || !o->pos || !o->vel ||
+        (look_side != -1 && look_side != 1))
         return GSLC_EINVAL;
     std::vector<double> coef;
     Orbit ob;
@@ -646,7 +682,8 @@ extern "C" int gslc_geo2rdr_zero_doppler(const gslc_orbit* o, const double* xyz,
         R = vnorm(rvec);
         ok = true;
     } else {
-        ok = geo2rdr_zero_doppler_seg(ob, ob.seg, x, threshold, maxiter, t, dt, R);
+        ok = ob.legendre ? geo2rdr_zero_doppler_orbit(ob, x, threshold, maxiter, t, dt, R)
+                         : geo2rdr_zero_doppler_seg(ob, ob.seg, x, threshold, maxiter, t, dt, R);
     }
     if (ok) {
         *aztime = t;
@@ -777,9 +814,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     if (srg.look_side != rg.look_side) return set_err(c, GSLC_EINVAL, "sliced grid look side != full grid look side");
     if (srg.wavelength != rg.wavelength) return set_err(c, GSLC_EINVAL, "sliced grid wavelength != full grid wavelength");
     if (!is_lonlat_or_utm(gg.epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
-    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
-    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
-        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (int st = check_orbit(c, a->orbit)) return st;
     if (a->rdr_length < 0 || a->rdr_width < 0) return set_err(c, GSLC_EINVAL, "invalid radar block shape");
     if (a->rdr_format != 0 && a->rdr_format != 1) return set_err(c, GSLC_EINVAL, "rdr_format must be 0 (complex64) or 1 (complex32)");
     if (a->geo_format < 0 || a->geo_format > 2) return set_err(c, GSLC_EINVAL, "geo_format must be 0, 1 or 2");
@@ -1149,7 +1184,9 @@ void plan_io_band(const GeoParams& p, const Orbit& ob, const gslc_geocode_args* 
                 double t = p.t_mid, R = 0.0;
                 const double dt = -vdot(rvec, p.vel0) * p.inv_vv0;
                 bool ok = std::fabs(dt) < p.thr;
-                if (!ok) ok = geo2rdr_zero_doppler_seg(ob, ob.seg, xyz, p.thr, std::max(p.maxiter, 2), t, dt, R);
+                if (!ok)
+                    ok = ob.legendre ? geo2rdr_zero_doppler_orbit(ob, xyz, p.thr, std::max(p.maxiter, 2), t, dt, R)
+                                     : geo2rdr_zero_doppler_seg(ob, ob.seg, xyz, p.thr, std::max(p.maxiter, 2), t, dt, R);
                 if (!ok) continue;
                 const double azc = (t - p.rg_t0) * p.rg_prf - p.az_first_d;
                 az_min = std::min(az_min, azc);
@@ -1646,9 +1683,7 @@ extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc
         return set_err(c, GSLC_EINVAL, "geogrid_expansion_threshold must be in [0, 10000] and maxiter in [0, 1000]");
     if (!grid_ok(a->radar_grid)) return set_err(c, GSLC_EINVAL, "invalid radar grid");
     if (!is_lonlat_or_utm(a->epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
-    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
-    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
-        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (int st = check_orbit(c, a->orbit)) return st;
     if (int st = check_lut(c, a->doppler, "doppler")) return st;
     if (a->n_blocks == 0) return GSLC_OK;
     cudaStream_t stream = (cudaStream_t)stream_;
@@ -1731,9 +1766,7 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     if (a->maxiter < 0 || a->maxiter > 1000) return set_err(c, GSLC_EINVAL, "numiter_geo2rdr must be in [0, 1000]");
     if (!grid_ok(a->radar_grid)) return set_err(c, GSLC_EINVAL, "invalid radar grid");
     if (!is_lonlat_or_utm(gg.epsg)) return set_err(c, GSLC_EUNSUPPORTED, "geogrid EPSG must be 4326 or UTM");
-    if (a->orbit.method != 0) return set_err(c, GSLC_EUNSUPPORTED, "only Hermite orbit interpolation");
-    if (a->orbit.n < 4 || !a->orbit.pos || !a->orbit.vel || !(a->orbit.spacing > 0))
-        return set_err(c, GSLC_EINVAL, "orbit needs >= 4 uniformly spaced state vectors");
+    if (int st = check_orbit(c, a->orbit)) return st;
     if (int st = check_lut(c, a->native_doppler, "native_doppler")) return st;
     if (int st = check_lut(c, a->grid_doppler, "grid_doppler")) return st;
     const int64_t npts = (int64_t)a->n_heights * gg.length * gg.width;

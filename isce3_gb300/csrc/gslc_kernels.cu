@@ -182,7 +182,10 @@ __device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t
     const bool dop_data = p.img_dop.have_data;
     const bool dop_const = !dop_data && (dbits(p.img_dop.ref_value) & DMAG) == 0;   // ref_value == 0.0
     if (p.maxiter < 1) return false;
-    if (dop_const && first_shared) {
+    // the segment tables hold the Hermite pieces; with a Legendre orbit every
+    // iteration interpolates the state vectors as the reference does
+    const bool seg_path = dop_const && !p.orbit.legendre;
+    if (seg_path && first_shared) {
         // iteration 0 at sensingMid with the shared state: the look-side
         // test (rvec x vel) . pos > 0 as rvec . (vel x pos), the step with
         // 1/|vel|^2 (within an ulp of the quotient)
@@ -211,7 +214,7 @@ __device__ bool geo2rdr(const GeoParams& p, const double* seg, V3 xyz, double& t
         }
         const V3 rvec = vsub(xyz, pos);
         if (i == 0 && ((p.look_side == -1) != (vdot(vcross(rvec, vel), pos) > 0.))) return false;
-        if (dop_const) {
+        if (seg_path) {
             // fdop == 0 and fdopder == 0 exactly: fn = rvec.vel, fn' = -vel.vel;
             // iterations after this one run on the segment tables
             dt = vdot(rvec, vel) / (-vdot(vel, vel));
@@ -534,7 +537,7 @@ __device__ __forceinline__ uint32_t seg_bytes(const GeoParams& p) {
 }
 
 __device__ __forceinline__ bool seg_fits(const GeoParams& p) {
-    return p.orbit.n - 1 <= SEG_SMEM / SEG_STRIDE;
+    return !p.orbit.legendre && p.orbit.n - 1 <= SEG_SMEM / SEG_STRIDE;
 }
 
 // one thread, once per block

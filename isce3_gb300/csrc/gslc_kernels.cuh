@@ -201,7 +201,8 @@ cudaError_t launch_dem_stats(const float* z, int64_t length, int64_t width, int6
 // The float-float Newton covers zero image-grid Doppler with the first
 // iterate at sensingMid and converged G series; anything else runs in FP64.
 inline bool ff_eligible(const GeoParams& p) {
-    return p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0 && !p.orbit.seg_div;
+    return p.t_mid_in_orbit && !p.img_dop.have_data && p.img_dop.ref_value == 0.0 && !p.orbit.seg_div &&
+           !p.orbit.legendre;
 }
 
 // launchers (gslc_kernels.cu)

@@ -625,6 +625,9 @@ struct Orbit {
     int32_t seg_nh, seg_ng;      // highest H and G degree used over all segments
     int32_t seg_div;             // 1: G did not converge, divide by -|vel|^2 instead
     int32_t seg_a7;              // 1: the position's degree-7 term matters (else degree 6)
+    int32_t legendre;            // 1: Legendre interpolation; coef holds the state vectors
+                                 // (positions 3n, then velocities 3n) and seg, seg_ff are unused
+    int32_t _pad;
 };
 
 // Orbit table layout in doubles: the pieces, then the segments (16-byte
@@ -641,7 +644,56 @@ GSLC_HD int orbit_piece(const Orbit& o, double t) {
     return idx;
 }
 
+// core/detail/InterpolateOrbit.icc:111-155 (interpolateOrbitLegendre): the
+// 9-point Lagrange interpolant of the state vectors' positions and, apart,
+// of their velocities, in the reference's operation order (no contraction);
+// Linspace::search and operator[] (core/Linspace.icc:77-89) for the window.
+// o.coef: positions (3n doubles), then velocities (3n).  t in the orbit span.
+GSLC_HD void orbit_eval_legendre(const Orbit& o, double t, V3& pos, V3& vel) {
+    const double last = dadd(o.t0, dmul((double)(o.n - 1), o.spacing));
+    int search = o.n;
+    if (t < o.t0) search = 0;
+    else if (!(t > last)) search = (int)dadd(ddiv(dsub(t, o.t0), o.spacing), 1.0);
+    int idx = search - 5;
+    idx = idx < 0 ? 0 : idx;
+    idx = idx > o.n - 9 ? o.n - 9 : idx;
+    const double t_lo = dadd(o.t0, dmul((double)idx, o.spacing));
+    const double t_hi = dadd(o.t0, dmul((double)(idx + 8), o.spacing));
+    const double trel = ddiv(dmul(8.0, dsub(t, t_lo)), dsub(t_hi, t_lo));
+    double teller = 1.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) teller = dmul(teller, dsub(trel, (double)i));
+    const double* P = o.coef;
+    const double* V = o.coef + 3 * (size_t)o.n;
+    if (teller == 0.0) {
+        const int i = idx + (int)trel;
+        pos = {ld_ro(P + 3 * i), ld_ro(P + 3 * i + 1), ld_ro(P + 3 * i + 2)};
+        vel = {ld_ro(V + 3 * i), ld_ro(V + 3 * i + 1), ld_ro(V + 3 * i + 2)};
+        return;
+    }
+    constexpr double noemer[9] = {40320.0, -5040.0, 1440.0, -720.0, 576.0, -720.0, 1440.0, -5040.0, 40320.0};
+    double px = 0.0, py = 0.0, pz = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const double coeff = ddiv(ddiv(teller, noemer[i]), dsub(trel, (double)i));
+        const double* pi = P + 3 * (size_t)(idx + i);
+        const double* vi = V + 3 * (size_t)(idx + i);
+        px = dadd(px, dmul(coeff, ld_ro(pi)));
+        py = dadd(py, dmul(coeff, ld_ro(pi + 1)));
+        pz = dadd(pz, dmul(coeff, ld_ro(pi + 2)));
+        vx = dadd(vx, dmul(coeff, ld_ro(vi)));
+        vy = dadd(vy, dmul(coeff, ld_ro(vi + 1)));
+        vz = dadd(vz, dmul(coeff, ld_ro(vi + 2)));
+    }
+    pos = {px, py, pz};
+    vel = {vx, vy, vz};
+}
+
 GSLC_HD void orbit_eval(const Orbit& o, double t, V3& pos, V3& vel) {
+    if (o.legendre) {
+        orbit_eval_legendre(o, t, pos, vel);
+        return;
+    }
     const int idx = orbit_piece(o, t);
     const double* c = o.coef + (long)idx * ORB_STRIDE;
     const double tidx = o.t0 + idx * o.spacing;
@@ -793,6 +845,26 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
             return true;
         }
+    }
+    return false;
+}
+
+// Iterations 1.. of the zero-Doppler Newton solve with the orbit
+// interpolated at every iterate (geometry/detail/Geo2Rdr.icc:114-179 with
+// fdop = fdopder = 0, where fn = rvec.vel and fn' = -vel.vel exactly): the
+// form for orbits the segment tables do not hold (Legendre).  Same
+// arguments as geo2rdr_zero_doppler_seg without the tables.
+GSLC_HD bool geo2rdr_zero_doppler_orbit(const Orbit& o, V3 xyz, double thr, int maxiter, double& t, double dt,
+                                        double& R) {
+    for (int i = 1; i < maxiter; ++i) {
+        t -= dt;
+        if (!(t >= o.t0 && t <= o.t_end)) return false;   // FillNaN -> no convergence
+        V3 pos, vel;
+        orbit_eval(o, t, pos, vel);
+        const V3 rvec = vsub(xyz, pos);
+        R = vnorm(rvec);
+        dt = vdot(rvec, vel) / (-vdot(vel, vel));
+        if (fabs(dt) < thr) return true;
     }
     return false;
 }

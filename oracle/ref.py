@@ -49,12 +49,13 @@ def lib(variant: str = "") -> C.CDLL:
             raise RuntimeError("the reference checkout is not available")
         L = C.CDLL(str(LIBS[variant]))
         L.ref_orbit_interpolate.restype = C.c_int64
-        L.ref_orbit_interpolate.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p,
-                                            C.c_int64, C.c_void_p, C.c_void_p]
+        L.ref_orbit_interpolate.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                            C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         L.ref_lonlat_to_xyz.restype = None
         L.ref_lonlat_to_xyz.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_int64, C.c_void_p]
         L.ref_geo2rdr.restype = None
-        L.ref_geo2rdr.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+        L.ref_geo2rdr.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                                  C.c_double,
                                   C.c_void_p, C.c_int64, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
                                   C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_utm_inverse.restype = C.c_int64
@@ -70,12 +71,13 @@ def _orbit_arrays(orbit):
 
 
 def orbit_interpolate(orbit, t, variant: str = ""):
-    """Orbit::interpolate (FillNaN) at the times t: (pos, vel) of shape (m, 3)."""
+    """Orbit::interpolate (FillNaN, the orbit's interpolation method) at the
+    times t: (pos, vel) of shape (m, 3)."""
     pos, vel = _orbit_arrays(orbit)
     t = np.ascontiguousarray(t, np.float64)
     P, V = np.zeros((t.size, 3)), np.zeros((t.size, 3))
     lib(variant).ref_orbit_interpolate(pos.ctypes.data, vel.ctypes.data, orbit.size, orbit.t0, orbit.spacing,
-                                       t.ctypes.data, t.size, P.ctypes.data, V.ctypes.data)
+                                       int(orbit.interp_method), t.ctypes.data, t.size, P.ctypes.data, V.ctypes.data)
     return P, V
 
 
@@ -94,7 +96,8 @@ def geo2rdr(llh, ellipsoid, orbit, wavelength, side, t_guess, threshold, maxiter
     llh = np.ascontiguousarray(llh, np.float64).reshape(-1, 3)
     m = len(llh)
     t, r, st = np.zeros(m), np.zeros(m), np.zeros(m, np.int32)
-    lib(variant).ref_geo2rdr(pos.ctypes.data, vel.ctypes.data, orbit.size, orbit.t0, orbit.spacing, ellipsoid.a,
+    lib(variant).ref_geo2rdr(pos.ctypes.data, vel.ctypes.data, orbit.size, orbit.t0, orbit.spacing,
+                             int(orbit.interp_method), ellipsoid.a,
                              ellipsoid.e2, llh.ctypes.data, m, wavelength, int(side), t_guess, threshold,
                              int(maxiter), delta_range, doppler_ref_value, int(bounds_error), t.ctypes.data,
                              r.ctypes.data, st.ctypes.data)

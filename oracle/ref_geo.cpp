@@ -11,7 +11,7 @@
 //
 // RefOrbit provides what the templated orbit interpolation and geo2rdr read
 // from isce3::core::Orbit (core/Orbit.h:94-205): the uniform time grid as a
-// Linspace, state vectors, Hermite method, start/mid/end times, and
+// Linspace, state vectors, interpolation method, start/mid/end times, and
 // interpolate() forwarding to detail::interpolateOrbit (core/Orbit.cpp:71-86).
 // ConstDoppler is a LUT2d without data (core/LUT2d.h:84-95, LUT2d.cpp:124-130:
 // contains() is true, eval() returns the reference value).
@@ -42,8 +42,10 @@ namespace {
 struct RefOrbit {
     Linspace<double> t;
     std::vector<Vec3> pos, vel;
+    OrbitInterpMethod method;
 
-    RefOrbit(const double* p, const double* v, int n, double first, double spacing) : t(first, spacing, n) {
+    RefOrbit(const double* p, const double* v, int n, double first, double spacing, int m)
+        : t(first, spacing, n), method(m == 1 ? OrbitInterpMethod::Legendre : OrbitInterpMethod::Hermite) {
         pos.resize(n);
         vel.resize(n);
         for (int i = 0; i < n; ++i) {
@@ -51,7 +53,7 @@ struct RefOrbit {
             vel[i] = Vec3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
         }
     }
-    OrbitInterpMethod interpMethod() const { return OrbitInterpMethod::Hermite; }
+    OrbitInterpMethod interpMethod() const { return method; }
     double startTime() const { return t[0]; }
     double midTime() const { return startTime() + 0.5 * (size() - 1) * spacing(); }
     double endTime() const { return t[size() - 1]; }
@@ -78,11 +80,11 @@ struct ConstDoppler {
 
 extern "C" {
 
-// Orbit::interpolate with FillNaN at m times; returns the number of times
-// outside the orbit.
+// Orbit::interpolate with FillNaN at m times (method 0 Hermite, 1 Legendre);
+// returns the number of times outside the orbit.
 int64_t ref_orbit_interpolate(const double* sv_pos, const double* sv_vel, int n, double first, double spacing,
-                              const double* t, int64_t m, double* pos, double* vel) {
-    const RefOrbit orb(sv_pos, sv_vel, n, first, spacing);
+                              int method, const double* t, int64_t m, double* pos, double* vel) {
+    const RefOrbit orb(sv_pos, sv_vel, n, first, spacing, method);
     int64_t outside = 0;
     for (int64_t k = 0; k < m; ++k) {
         Vec3 p, v;
@@ -110,11 +112,11 @@ void ref_lonlat_to_xyz(double a, double e2, const double* llh, int64_t m, double
 // deltaRange}, converged = status Success) over m points; the image-grid
 // Doppler is a table without data whose reference value is dop_ref.
 // side: -1 right, 1 left.  status[k] = the detail::geo2rdr ErrorCode.
-void ref_geo2rdr(const double* sv_pos, const double* sv_vel, int n, double first, double spacing, double a,
-                 double e2, const double* llh, int64_t m, double wvl, int side, double t_guess, double threshold,
-                 int maxiter, double delta_range, double dop_ref, int bounds_error, double* t_out, double* r_out,
-                 int* status) {
-    const RefOrbit orb(sv_pos, sv_vel, n, first, spacing);
+void ref_geo2rdr(const double* sv_pos, const double* sv_vel, int n, double first, double spacing, int method,
+                 double a, double e2, const double* llh, int64_t m, double wvl, int side, double t_guess,
+                 double threshold, int maxiter, double delta_range, double dop_ref, int bounds_error, double* t_out,
+                 double* r_out, int* status) {
+    const RefOrbit orb(sv_pos, sv_vel, n, first, spacing, method);
     const isce3::core::Ellipsoid ell(a, e2);
     const ConstDoppler dop{dop_ref, bounds_error != 0};
     const auto look = side < 0 ? isce3::core::LookSide::Right : isce3::core::LookSide::Left;

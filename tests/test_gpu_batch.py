@@ -70,6 +70,26 @@ def test_batch_equals_plain_calls(bursts, precision, graph, pop):
     batch.close()
 
 
+def test_batch_legendre_orbit_equals_plain_calls(bursts):
+    """A Legendre orbit in the persistent kernel: its tables are the state
+    vectors (no segment tables to stage), every iterate interpolates them;
+    each burst equals its plain call."""
+    import copy
+    from isce3_gb300.core import Orbit, OrbitInterpMethod
+    sc = copy.copy(bursts)
+    o = sc.orbit
+    sc.orbit = Orbit.from_arrays(o.t0, o.spacing, o.position, o.velocity, o.reference_epoch,
+                                 OrbitInterpMethod.LEGENDRE)
+    ref = _plain(sc, "ff")
+    outs = _outputs(sc)
+    batch = GeocodeBatch(_requests(sc, outs), "ff", BatchTuning(tiles_per_pop=2, use_graph=True))
+    batch.run()
+    _same(ref, outs)
+    valid = sum(int((m == 1).sum()) for _, m in outs)
+    assert valid > 0.2 * sum(m.numel() for _, m in outs)
+    batch.close()
+
+
 @pytest.mark.parametrize("graph", [True, False])
 def test_batch_request_flags(bursts, graph):
     """Per-request completion words: every request's word is 1 once the

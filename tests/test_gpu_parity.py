@@ -344,3 +344,22 @@ def test_lut2d_methods(oracle_mod, c1, method, precision):
                          geo2rdr_precision=precision)
     r = _check(gpu, ora)[0]
     assert r["n_valid"] > 100000
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+@pytest.mark.parametrize("which", ["c1", "c2"])
+def test_legendre_orbit(oracle_mod, c1, which, precision):
+    """Legendre orbit interpolation (core/detail/InterpolateOrbit.icc:111-155):
+    every Newton iterate interpolates the state vectors in the reference's
+    operation order (the segment tables hold Hermite pieces); a float-float
+    request takes the same FP64 path.  EPSG:4326 and UTM geogrids."""
+    import copy
+    from isce3_gb300.core import Orbit, OrbitInterpMethod
+    sc = copy.copy(c1 if which == "c1" else synth.scene_c2(length=2048, width=1024, geo=400, spacing=15.0))
+    o = sc.orbit
+    sc.orbit = Orbit.from_arrays(o.t0, o.spacing, o.position, o.velocity, o.reference_epoch,
+                                 OrbitInterpMethod.LEGENDRE)
+    kw = {} if which == "c1" else dict(az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier)
+    gpu, ora = _run_both(oracle_mod, sc, [sc.slc], geo2rdr_precision=precision, **kw)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 10000

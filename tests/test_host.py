@@ -40,6 +40,31 @@ def test_orbit_polynomial_matches_reference_hermite(lib, oracle_mod):
     assert lib.gslc_orbit_interpolate(C.byref(d), o.end_time + 1.0, p, v) == L.GSLC_EINVAL
 
 
+def test_orbit_legendre_matches_oracle_bits(lib, oracle_mod):
+    """Legendre orbits (core/detail/InterpolateOrbit.icc:111-155): the
+    library interpolates the state vectors in the reference's operation
+    order, so position and velocity equal the oracle's bit for bit; fewer
+    than 9 state vectors are rejected."""
+    from isce3_gb300.core import Orbit, OrbitInterpMethod
+    o0 = synth.scene_c1(slc=False).orbit
+    o = Orbit.from_arrays(o0.t0, o0.spacing, o0.position, o0.velocity, o0.reference_epoch, OrbitInterpMethod.LEGENDRE)
+    d = M.orbit_desc(o)
+    assert d.method == 1
+    ts = np.concatenate([np.linspace(o.start_time, o.end_time, 701), o.t0 + o.spacing * np.arange(o.size)])
+    for t in ts:
+        p, v = (C.c_double * 3)(), (C.c_double * 3)()
+        assert lib.gslc_orbit_interpolate(C.byref(d), t, p, v) == 0
+        po, vo, st = oracle_mod.orbit_interpolate(o, t)
+        assert st == 0
+        np.testing.assert_array_equal(np.array(p[:]), po)
+        np.testing.assert_array_equal(np.array(v[:]), vo)
+    short = Orbit.from_arrays(o0.t0, o0.spacing, o0.position[:8], o0.velocity[:8], o0.reference_epoch,
+                              OrbitInterpMethod.LEGENDRE)
+    ds = M.orbit_desc(short)
+    p, v = (C.c_double * 3)(), (C.c_double * 3)()
+    assert lib.gslc_orbit_interpolate(C.byref(ds), short.t0 + 1.0, p, v) == L.GSLC_EINVAL
+
+
 @pytest.mark.parametrize("which", ["c1", "c2"])
 def test_zero_doppler_newton_matches_oracle(lib, oracle_mod, which):
     """The kernels' Newton iterations (segment tables: residual D.vel - H,

@@ -2,8 +2,8 @@
 
 oracle/ref.py compiles the reference's geo2rdr (geometry/detail/Geo2Rdr.icc,
 called as geometry/geometry.cpp:241-251 does for geocodeSlc.cpp:120-123),
-Hermite orbit interpolation (core/detail/InterpolateOrbit.icc:10-109,
-core/Linspace.icc:77-89), Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190)
+Hermite and Legendre orbit interpolation (core/detail/InterpolateOrbit.icc:
+10-155, core/Linspace.icc:77-89), Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190)
 and UTM::inverse / forward (core/Projections.cpp:171-232) where they lie in
 the reference checkout.  The oracle's restatement of each must return the
 same bits on the same inputs: these are the functions whose rounding decides
@@ -53,6 +53,40 @@ def test_orbit_interpolation_bits(oracle_mod, scene):
         po, vo, _st = oracle_mod.orbit_interpolate(o, t[k])
         np.testing.assert_array_equal(po, P[k])
         np.testing.assert_array_equal(vo, V[k])
+
+
+def _legendre(o):
+    from isce3_gb300.core import Orbit, OrbitInterpMethod
+    return Orbit.from_arrays(o.t0, o.spacing, o.position, o.velocity, o.reference_epoch, OrbitInterpMethod.LEGENDRE)
+
+
+def test_legendre_orbit_interpolation_bits(oracle_mod, scene):
+    """core/detail/InterpolateOrbit.icc:111-155: the 9-point Lagrange form,
+    including the state-vector times where it returns the vectors as they
+    are."""
+    o = _legendre(scene.orbit)
+    span = o.spacing * (o.size - 1)
+    t = np.concatenate([np.linspace(o.t0 - 2.0, o.t0 + span + 2.0, 4001), o.t0 + o.spacing * np.arange(o.size)])
+    P, V = ref.orbit_interpolate(o, t)
+    for k in range(t.size):
+        po, vo, _st = oracle_mod.orbit_interpolate(o, t[k])
+        np.testing.assert_array_equal(po, P[k])
+        np.testing.assert_array_equal(vo, V[k])
+
+
+def test_legendre_geo2rdr_bits(oracle_mod, scene):
+    rg = scene.radar_grid
+    o = _legendre(scene.orbit)
+    llh = _ground_points(scene, 1500, 9)
+    t, r, st = ref.geo2rdr(llh, scene.ellipsoid, o, rg.wavelength, int(rg.lookside), rg.sensing_mid,
+                           scene.threshold, scene.maxiter, 1e-8)
+    assert (st == 0).sum() > 0.9 * len(llh)
+    for k in range(len(llh)):
+        to, ro, ok = oracle_mod.geo2rdr(llh[k], scene.ellipsoid, o, LUT2d(), rg.wavelength, int(rg.lookside),
+                                        rg.sensing_mid, scene.threshold, scene.maxiter, 1e-8)
+        assert bool(ok) == (st[k] == 0), k
+        if ok:
+            assert to == t[k] and ro == r[k], (k, to - t[k], ro - r[k])
 
 
 def test_lonlat_to_xyz_bits(oracle_mod, scene):
