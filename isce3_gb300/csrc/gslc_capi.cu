@@ -39,6 +39,10 @@ struct gslc_ctx {
     std::vector<cudaEvent_t> io_ev;
     int io_reruns = 0;
     bool no_alloc = false;          // the allocation-free entry point's stand-in context
+    // the last orbit's host tables (build_orbit_table), keyed by its descriptor
+    // and state vectors: calls that reuse an orbit skip rebuilding them
+    std::vector<double> orb_key, orb_coef;
+    Orbit orb_ob{};
     std::string err;
 };
 
@@ -441,6 +445,27 @@ bool proj_inverse(int epsg, const Utm& u, double x, double y, double& lon, doubl
 bool proj_forward(int epsg, const Utm& u, double lon, double lat, double& x, double& y) {
     if (epsg == 4326) { x = lon * 180.0 / M_PI; y = lat * 180.0 / M_PI; return true; }
     return utm_forward(u, lon, lat, x, y);
+}
+
+// build_orbit_table through the context's one-entry cache: a caller that
+// geocodes many blocks, bands or requests with one orbit builds its
+// polynomial pieces and Newton tables once (about 0.7 ms for 21 state
+// vectors).  The key is the descriptor's scalars and the state vectors'
+// bytes, so any change rebuilds.
+void orbit_table_cached(gslc_ctx* c, const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
+    const size_t nv = 3 * (size_t)o.n;
+    const double head[4] = {o.t0, o.spacing, (double)o.n, (double)o.method};
+    bool hit = c->orb_key.size() == 4 + 2 * nv && std::memcmp(c->orb_key.data(), head, sizeof(head)) == 0 &&
+               std::memcmp(c->orb_key.data() + 4, o.pos, nv * sizeof(double)) == 0 &&
+               std::memcmp(c->orb_key.data() + 4 + nv, o.vel, nv * sizeof(double)) == 0;
+    if (!hit) {
+        build_orbit_table(o, c->orb_coef, c->orb_ob);
+        c->orb_key.assign(head, head + 4);
+        c->orb_key.insert(c->orb_key.end(), o.pos, o.pos + nv);
+        c->orb_key.insert(c->orb_key.end(), o.vel, o.vel + nv);
+    }
+    coef = c->orb_coef;
+    ob = c->orb_ob;
 }
 
 // Orbit descriptor checks: Hermite (4 or more state vectors) or Legendre
@@ -851,7 +876,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.ell_e2 = a->ellipsoid_e2;
 
     // orbit polynomials and Newton tables
-    build_orbit_table(a->orbit, coef, p.orbit);
+    orbit_table_cached(c, a->orbit, coef, p.orbit);
     const Orbit& ob = p.orbit;
 
     // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)
@@ -1693,7 +1718,7 @@ extern "C" int gslc_radar_bbox_blocks(gslc_ctx* c, const gslc_bbox_args* a, gslc
     PlanParams p;
     std::memset(&p, 0, sizeof(p));
     std::vector<double> coef;
-    build_orbit_table(a->orbit, coef, p.orbit);
+    orbit_table_cached(c, a->orbit, coef, p.orbit);
     const gslc_radar_grid& rg = a->radar_grid;
     p.n_blocks = a->n_blocks;
     p.geo_is_lonlat = a->epsg == 4326;
@@ -1778,7 +1803,7 @@ extern "C" int gslc_make_radar_grid_cubes(gslc_ctx* c, const gslc_cube_args* a, 
     CubeParams p;
     std::memset(&p, 0, sizeof(p));
     std::vector<double> coef;
-    build_orbit_table(a->orbit, coef, p.orbit);
+    orbit_table_cached(c, a->orbit, coef, p.orbit);
     const gslc_radar_grid& rg = a->radar_grid;
     p.gx0 = gg.start_x; p.gy0 = gg.start_y; p.gdx = gg.spacing_x; p.gdy = gg.spacing_y;
     p.width = gg.width; p.length = gg.length; p.n_heights = a->n_heights;
