@@ -1361,6 +1361,14 @@ extern "C" double orc_interp2d_double(int method, const double* z, int ny, int n
     }
 }
 
+// the SLC interpolator (sinc2d_chip) on a row-major complex64 table
+// (interleaved re, im); out: re, im
+extern "C" void orc_sinc2d_cfloat(const float* z, int ny, int nx, double x, double y, float* out) {
+    const cf r = sinc2d_chip(reinterpret_cast<const cf*>(z), ny, nx, x, y);
+    out[0] = r.re;
+    out[1] = r.im;
+}
+
 extern "C" float orc_spline2d_float(const float* z, int ny, int nx, double x, double y) {
     return spline2d<float>(z, ny, nx, x, y);
 }

@@ -123,6 +123,8 @@ def lib(variant: str = "") -> C.CDLL:
         _lib.orc_interp2d_double.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         _lib.orc_spline2d_float.restype = C.c_float
         _lib.orc_spline2d_float.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        _lib.orc_sinc2d_cfloat.restype = None
+        _lib.orc_sinc2d_cfloat.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p]
         _lib.orc_lut2d_eval.restype = C.c_double
         _lib.orc_lut2d_eval.argtypes = [C.POINTER(Lut), C.c_double, C.c_double]
         _lib.orc_lut2d_contains.argtypes = [C.POINTER(Lut), C.c_double, C.c_double]
@@ -429,6 +431,14 @@ def interp2d(method: int, z: np.ndarray, x: float, y: float) -> float:
 def spline2d_float(z: np.ndarray, x: float, y: float) -> np.float32:
     z = np.ascontiguousarray(z, dtype=np.float32)
     return np.float32(lib().orc_spline2d_float(_ptr(z), z.shape[0], z.shape[1], x, y))
+
+
+def sinc2d_cfloat(z: np.ndarray, x: float, y: float) -> np.complex64:
+    """The SLC interpolator (Sinc2d on complex64) at (x, y) of the table z."""
+    z = np.ascontiguousarray(z, dtype=np.complex64)
+    out = np.zeros(2, np.float32)
+    lib().orc_sinc2d_cfloat(_ptr(z), z.shape[0], z.shape[1], x, y, _ptr(out))
+    return np.complex64(out[0] + 1j * out[1])
 
 
 def lut_eval(lut, y, x) -> float:

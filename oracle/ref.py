@@ -21,7 +21,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REF = Path(os.environ.get("ISCE3_REFERENCE", "/root/reference"))
 LIBS = {"": HERE / "_ref" / "libref_geo.so", "fma": HERE / "_ref" / "libref_geo_fma.so"}
-_SRC = [HERE / "ref_geo.cpp", HERE / "ref_shim" / "Eigen" / "Dense"]
+INTERP_LIB = HERE / "_ref" / "libref_interp.so"
+_SRC = [HERE / "ref_geo.cpp", HERE / "ref_interp.cpp", HERE / "ref_shim" / "Eigen" / "Dense",
+        HERE / "ref_shim" / "pyre" / "journal.h"]
 _libs: dict = {}
 
 
@@ -34,7 +36,7 @@ def build(force: bool = False) -> bool:
     if not available():
         return False
     newest = max(p.stat().st_mtime for p in _SRC)
-    if force or any(not p.exists() or p.stat().st_mtime < newest for p in LIBS.values()):
+    if force or any(not p.exists() or p.stat().st_mtime < newest for p in [*LIBS.values(), INTERP_LIB]):
         cmd = ["make", "-C", str(HERE)] + (["-B"] if force else []) + ["ref", f"REF={REF}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -116,3 +118,42 @@ def utm_forward(epsg, lonlat, variant: str = ""):
     out = np.zeros_like(ll)
     bad = lib(variant).ref_utm_forward(int(epsg), ll.ctypes.data, len(ll), out.ctypes.data)
     return out, int(bad)
+
+
+_interp = None
+
+
+def interp_lib() -> C.CDLL:
+    """The reference's interpolators (ref_interp.cpp)."""
+    global _interp
+    if _interp is None:
+        if not build():
+            raise RuntimeError("the reference checkout is not available")
+        L = C.CDLL(str(INTERP_LIB))
+        L.ref_interp2d_double.restype = C.c_double
+        L.ref_interp2d_double.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.ref_spline2d_float.restype = C.c_float
+        L.ref_spline2d_float.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.ref_sinc2d_cfloat.restype = None
+        L.ref_sinc2d_cfloat.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p]
+        _interp = L
+    return _interp
+
+
+def interp2d(method: int, z, x: float, y: float) -> float:
+    """createInterpolator<double>(method) at (x, y); method: isce3 dataInterpMethod
+    (0 sinc, 1 bilinear, 2 bicubic, 3 nearest, 4 biquintic)."""
+    z = np.ascontiguousarray(z, np.float64)
+    return interp_lib().ref_interp2d_double(int(method), z.ctypes.data, z.shape[0], z.shape[1], x, y)
+
+
+def spline2d_float(z, x: float, y: float) -> np.float32:
+    z = np.ascontiguousarray(z, np.float32)
+    return np.float32(interp_lib().ref_spline2d_float(z.ctypes.data, z.shape[0], z.shape[1], x, y))
+
+
+def sinc2d_cfloat(z, x: float, y: float) -> np.complex64:
+    z = np.ascontiguousarray(z, np.complex64)
+    out = np.zeros(2, np.float32)
+    interp_lib().ref_sinc2d_cfloat(z.ctypes.data, z.shape[0], z.shape[1], x, y, out.ctypes.data)
+    return np.complex64(out[0] + 1j * out[1])

@@ -1,0 +1,49 @@
+// TEST INFRASTRUCTURE: a C ABI over the reference's own interpolators
+// (core/BilinearInterpolator.cpp, BicubicInterpolator.cpp,
+// NearestNeighborInterpolator.cpp, Spline2dInterpolator.cpp,
+// Sinc2dInterpolator.cpp, built where they lie in the reference checkout by
+// oracle/Makefile, target "ref", with ref_shim/ standing in for Eigen 3.3.7
+// and pyre-journal).  The oracle's restatements of the same interpolators
+// are checked against it bit for bit.  Nothing in the product uses it.
+#include <complex>
+#include <memory>
+
+#include "isce3/core/Interpolator.h"
+
+using isce3::core::dataInterpMethod;
+
+namespace {
+template <typename U>
+using MapOf = Eigen::Map<const isce3::core::EArray2D<U>>;
+}
+
+extern "C" {
+
+// createInterpolator<double>(method) (core/Interpolator.h: biquintic of
+// order 6, sinc of SINC_LEN taps at SINC_SUB phases) at (x, y) of the
+// row-major ny x nx table z.  method: isce3 dataInterpMethod.
+double ref_interp2d_double(int method, const double* z, int ny, int nx, double x, double y) {
+    std::unique_ptr<isce3::core::Interpolator<double>> it(
+            isce3::core::createInterpolator<double>(static_cast<dataInterpMethod>(method)));
+    return it->interpolate(x, y, MapOf<double>(z, ny, nx));
+}
+
+// Spline2dInterpolator<float>(6), the DEM interpolator's spline
+// (geometry/DEMInterpolator.cpp), at (x, y) of a row-major float table.
+float ref_spline2d_float(const float* z, int ny, int nx, double x, double y) {
+    const isce3::core::Spline2dInterpolator<float> it(6);
+    return it.interpolate(x, y, MapOf<float>(z, ny, nx));
+}
+
+// Sinc2dInterpolator<std::complex<float>>(SINC_LEN, SINC_SUB), the SLC
+// interpolator of geocodeSlc.cpp:476-494, at (x, y) of a row-major complex64
+// table (interleaved re, im); out: re, im.
+void ref_sinc2d_cfloat(const float* z, int ny, int nx, double x, double y, float* out) {
+    const isce3::core::Sinc2dInterpolator<std::complex<float>> it(isce3::core::SINC_LEN, isce3::core::SINC_SUB);
+    const std::complex<float> v =
+            it.interpolate(x, y, MapOf<std::complex<float>>(reinterpret_cast<const std::complex<float>*>(z), ny, nx));
+    out[0] = v.real();
+    out[1] = v.imag();
+}
+
+}  // extern "C"

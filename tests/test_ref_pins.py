@@ -3,7 +3,8 @@
 oracle/ref.py compiles the reference's geo2rdr (geometry/detail/Geo2Rdr.icc,
 called as geometry/geometry.cpp:241-251 does for geocodeSlc.cpp:120-123),
 Hermite and Legendre orbit interpolation (core/detail/InterpolateOrbit.icc:
-10-155, core/Linspace.icc:77-89), Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190)
+10-155, core/Linspace.icc:77-89), the 2-D interpolators (core/Bilinear,
+Bicubic, NearestNeighbor, Spline2d and Sinc2dInterpolator.cpp), Ellipsoid::lonLatToXyz (core/Ellipsoid.h:177-190)
 and UTM::inverse / forward (core/Projections.cpp:171-232) where they lie in
 the reference checkout.  The oracle's restatement of each must return the
 same bits on the same inputs: these are the functions whose rounding decides
@@ -148,3 +149,57 @@ def test_utm_bits(oracle_mod, epsg):
         assert st == 0 and lon == ll[k, 0] and lat == ll[k, 1]
         x, y, st = oracle_mod.proj_forward(epsg, ll[k, 0], ll[k, 1])
         assert st == 0 and x == back[k, 0] and y == back[k, 1]
+
+
+# ---- the 2-D interpolators ----
+# the oracle's numbering of interp2d (1 bilinear, 2 bicubic, 3 nearest,
+# 4 biquintic, 5 sinc) against isce3's dataInterpMethod
+_ISCE3_METHOD = {1: 1, 2: 2, 3: 3, 4: 4, 5: 0}
+
+
+def _points(ny, nx, m, seed, lo=0.0):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(lo, nx - 1 - lo, m)
+    y = rng.uniform(lo, ny - 1 - lo, m)
+    # node coordinates and exact halves as well
+    x[:40] = np.floor(x[:40])
+    y[40:80] = np.floor(y[40:80]) + 0.5
+    return x, y
+
+
+@pytest.mark.parametrize("ora_method", [1, 2, 3, 4, 5])
+def test_interp2d_double_bits(oracle_mod, ora_method):
+    """LUT2d's interpolators on doubles, over the interior (the bicubic reads
+    one sample outside its cell, so it stays one sample inside the table)."""
+    rng = np.random.default_rng(ora_method)
+    z = rng.normal(size=(37, 41)) * 50.0 + np.linspace(0, 30, 41)[None, :]
+    lo = 1.0 if ora_method == 2 else 0.0
+    x, y = _points(37, 41 - (2 if ora_method == 2 else 0), 2000, 11 + ora_method, lo)
+    for k in range(x.size):
+        want = ref.interp2d(_ISCE3_METHOD[ora_method], z, x[k], y[k])
+        assert oracle_mod.interp2d(ora_method, z, x[k], y[k]) == want, (k, x[k], y[k])
+
+
+def test_dem_spline_float_bits(oracle_mod):
+    """Spline2dInterpolator<float> of order 6, the DEM's interpolator, on a
+    float table (edges included: its window clamps there)."""
+    rng = np.random.default_rng(3)
+    z = (rng.normal(size=(48, 52)) * 300.0 + 1500.0).astype(np.float32)
+    x, y = _points(48, 52, 3000, 4)
+    for k in range(x.size):
+        want = ref.spline2d_float(z, x[k], y[k])
+        got = oracle_mod.spline2d_float(z, x[k], y[k])
+        assert got.view(np.uint32) == want.view(np.uint32), (k, x[k], y[k])
+
+
+def test_sinc_complex64_bits(oracle_mod):
+    """Sinc2dInterpolator<complex<float>>, the SLC interpolator of
+    geocodeSlc.cpp:476-494, on 9 x 9 chips and on a larger table."""
+    rng = np.random.default_rng(5)
+    for shape, m in (((9, 9), 400), ((30, 33), 1500)):
+        z = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64)
+        x, y = _points(shape[0], shape[1], m, 6 + m)
+        for k in range(x.size):
+            want = ref.sinc2d_cfloat(z, x[k], y[k])
+            got = oracle_mod.sinc2d_cfloat(z, x[k], y[k])
+            assert np.array([got]).view(np.uint64)[0] == np.array([want]).view(np.uint64)[0], (k, x[k], y[k])
