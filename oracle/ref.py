@@ -136,6 +136,12 @@ def interp_lib() -> C.CDLL:
         L.ref_spline2d_float.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         L.ref_sinc2d_cfloat.restype = None
         L.ref_sinc2d_cfloat.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p]
+        L.ref_lut2d_eval.restype = C.c_double
+        L.ref_lut2d_eval.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_int,
+                                     C.c_int, C.c_int, C.c_double, C.c_double]
+        L.ref_poly2d_eval.restype = C.c_double
+        L.ref_poly2d_eval.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                      C.c_double, C.c_double]
         _interp = L
     return _interp
 
@@ -157,3 +163,17 @@ def sinc2d_cfloat(z, x: float, y: float) -> np.complex64:
     out = np.zeros(2, np.float32)
     interp_lib().ref_sinc2d_cfloat(z.ctypes.data, z.shape[0], z.shape[1], x, y, out.ctypes.data)
     return np.complex64(out[0] + 1j * out[1])
+
+
+def lut2d_eval(lut, y: float, x: float) -> float:
+    """LUT2d<double>::eval of a table with data (core/LUT2d.cpp:124-158)."""
+    z = np.ascontiguousarray(lut.data, np.float64)
+    return interp_lib().ref_lut2d_eval(lut.x_start, lut.y_start, lut.x_spacing, lut.y_spacing, z.ctypes.data,
+                                       z.shape[0], z.shape[1], int(lut.interp_method), int(lut.bounds_error), y, x)
+
+
+def poly2d_eval(p, y: float, x: float) -> float:
+    """Poly2d::eval (core/Poly2d.cpp:8-24)."""
+    c = np.ascontiguousarray(p.coeffs, np.float64).reshape(-1)
+    return interp_lib().ref_poly2d_eval(p.x_order, p.y_order, p.x_mean, p.y_mean, p.x_std, p.y_std, c.ctypes.data,
+                                        y, x)

@@ -1,7 +1,8 @@
 // TEST INFRASTRUCTURE: a C ABI over the reference's own interpolators
 // (core/BilinearInterpolator.cpp, BicubicInterpolator.cpp,
 // NearestNeighborInterpolator.cpp, Spline2dInterpolator.cpp,
-// Sinc2dInterpolator.cpp, built where they lie in the reference checkout by
+// Sinc2dInterpolator.cpp), LUT2d (core/LUT2d.cpp) and Poly2d
+// (core/Poly2d.cpp), built where they lie in the reference checkout by
 // oracle/Makefile, target "ref", with ref_shim/ standing in for Eigen 3.3.7
 // and pyre-journal).  The oracle's restatements of the same interpolators
 // are checked against it bit for bit.  Nothing in the product uses it.
@@ -9,6 +10,8 @@
 #include <memory>
 
 #include "isce3/core/Interpolator.h"
+#include "isce3/core/LUT2d.h"
+#include "isce3/core/Poly2d.h"
 
 using isce3::core::dataInterpMethod;
 
@@ -44,6 +47,25 @@ void ref_sinc2d_cfloat(const float* z, int ny, int nx, double x, double y, float
             it.interpolate(x, y, MapOf<std::complex<float>>(reinterpret_cast<const std::complex<float>*>(z), ny, nx));
     out[0] = v.real();
     out[1] = v.imag();
+}
+
+// LUT2d<double>(xstart, ystart, dx, dy, data, method, bounds_error).eval(y, x)
+// (core/LUT2d.cpp:18-27, 124-158) over the row-major ny x nx table z.
+double ref_lut2d_eval(double xstart, double ystart, double dx, double dy, const double* z, int ny, int nx, int method,
+                      int bounds_error, double y, double x) {
+    std::vector<double> copy(z, z + (size_t)ny * nx);
+    const isce3::core::Matrix<double> data(copy.data(), ny, nx);
+    const isce3::core::LUT2d<double> lut(xstart, ystart, dx, dy, data, static_cast<dataInterpMethod>(method),
+                                         bounds_error != 0);
+    return lut.eval(y, x);
+}
+
+// Poly2d::eval (core/Poly2d.cpp:8-24); coeffs row-major (y_order + 1) x (x_order + 1)
+double ref_poly2d_eval(int x_order, int y_order, double x_mean, double y_mean, double x_norm, double y_norm,
+                       const double* coeffs, double y, double x) {
+    isce3::core::Poly2d p(x_order, y_order, x_mean, y_mean, x_norm, y_norm);
+    for (size_t i = 0; i < p.coeffs.size(); ++i) p.coeffs[i] = coeffs[i];
+    return p.eval(y, x);
 }
 
 }  // extern "C"

@@ -203,3 +203,33 @@ def test_sinc_complex64_bits(oracle_mod):
             want = ref.sinc2d_cfloat(z, x[k], y[k])
             got = oracle_mod.sinc2d_cfloat(z, x[k], y[k])
             assert np.array([got]).view(np.uint64)[0] == np.array([want]).view(np.uint64)[0], (k, x[k], y[k])
+
+
+@pytest.mark.parametrize("method", ["sinc", "bilinear", "bicubic", "nearest", "biquintic"])
+def test_lut2d_eval_bits(oracle_mod, method):
+    """LUT2d<double>::eval (core/LUT2d.cpp:124-158): index, clamp to the
+    table, the method's interpolator; points inside and outside the table
+    (the bicubic only where its 4 x 4 reads stay in the table)."""
+    rng = np.random.default_rng(21)
+    data = rng.normal(size=(24, 30)) * 20.0
+    lut = LUT2d(-3.0, 7.0, 0.5, 0.25, data, method)
+    for _ in range(1500):
+        x = -3.0 + rng.uniform(-2.0, 0.5 * 29 + 2.0)
+        y = 7.0 + rng.uniform(-1.0, 0.25 * 23 + 1.0)
+        if method == "bicubic":
+            xi = min(max((x + 3.0) / 0.5, 0.0), 29.0)
+            yi = min(max((y - 7.0) / 0.25, 0.0), 23.0)
+            if not (1 <= xi < 27 and 1 <= yi < 21):
+                continue
+        assert oracle_mod.lut_eval(lut, y, x) == ref.lut2d_eval(lut, y, x), (x, y)
+
+
+def test_poly2d_eval_bits(oracle_mod):
+    """Poly2d::eval (core/Poly2d.cpp:8-24): the carriers' polynomials."""
+    from isce3_gb300.core import Poly2d
+    rng = np.random.default_rng(22)
+    for xo, yo in ((0, 0), (1, 0), (0, 1), (2, 3), (4, 2)):
+        p = Poly2d(rng.normal(size=(yo + 1, xo + 1)) * 10.0, x_mean=850e3, y_mean=100.0, x_std=3e3, y_std=5.0)
+        for _ in range(300):
+            x, y = rng.uniform(8.4e5, 8.7e5), rng.uniform(90.0, 110.0)
+            assert oracle_mod.poly_eval(p, y, x) == ref.poly2d_eval(p, y, x), (xo, yo, x, y)
