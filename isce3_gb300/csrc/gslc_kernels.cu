@@ -526,6 +526,7 @@ struct OrbitStage {
     uint32_t phase;       // parity of the copy to wait for
     int issued;           // a copy of this request's tables was issued
     long long deadline;   // SM clock by which the copy must have landed
+    int* landed;          // shared flag: a wait saw this copy land (later waits on it succeed at once)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
@@ -579,11 +580,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // every thread: true when the staged tables can be read.  Past the deadline
-// the wait has run out whether or not the copy landed meanwhile.
+// the wait has run out whether or not the copy landed meanwhile, unless an
+// earlier wait on the same copy (a thread of this or of an earlier tile of
+// the request) saw it land.
 __device__ __forceinline__ bool stage_ready(const OrbitStage& st, const GeoParams& p) {
     if (!st.issued) return false;
+    if (*(volatile int*)st.landed) return true;
     while (clock64() <= st.deadline)
-        if (mbar_try_wait(st.bar, st.phase)) return true;
+        if (mbar_try_wait(st.bar, st.phase)) {
+            *(volatile int*)st.landed = 1;
+            return true;
+        }
     atomicOr(p.err, 2);
     *st.off = 1;
     return false;
@@ -1048,16 +1055,17 @@ template <bool GEO_LONLAT, bool FF, bool RASTER, int PPT>
 __global__ void __launch_bounds__(GBX * GBY, 2) geocode_kernel(const __grid_constant__ GeoParams p) {
     __shared__ __align__(128) double s_seg[SEG_SMEM];
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_off;
+    __shared__ int s_off, s_landed;
     // the float-float path reads only the piece tables
     const bool stage = !FF && seg_fits(p);
     const long long deadline = clock64() + p.stage_wait;
     if (stage && threadIdx.x == 0 && threadIdx.y == 0) {
+        s_landed = 0;
         stage_init(&s_bar);
         stage_issue(p, s_seg, &s_bar);
     }
     // geocode_block synchronises the block before any thread waits
-    const OrbitStage st{s_seg, &s_bar, &s_off, 0u, stage ? 1 : 0, deadline};
+    const OrbitStage st{s_seg, &s_bar, &s_off, 0u, stage ? 1 : 0, deadline, &s_landed};
     geocode_block<GEO_LONLAT, FF, RASTER, PPT>(p, blockIdx.x, blockIdx.y, st);
     // thread (0, 0) always has pixels (tiles start inside the geogrid), so
     // it reaches this point; the block's shared memory outlives the copy
@@ -1069,69 +1077,86 @@ __global__ void __launch_bounds__(GBX * GBY, 2) geocode_kernel(const __grid_cons
 // parameters, so each request's output equals its plain call.
 template <bool GEO_LONLAT, bool FF, int PPT>
 __global__ void __launch_bounds__(GBX * GBY, 2) geocode_persistent(const __grid_constant__ BatchQueue q) {
-    __shared__ long long s_base;
+    // The block's queue position and staging state are block-uniform and
+    // live in shared memory, written by the lead thread between barriers:
+    // nothing of the loop stays in registers across a tile's body, which
+    // has the same register budget as the plain kernel's.
+    __shared__ long long s_next, s_end, s_tile;
     __shared__ __align__(128) double s_seg[SEG_SMEM];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ int s_off;
+    __shared__ int s_staged;    // items[] entry the block last prepared for
+    __shared__ int s_issued;    // a copy for it was issued
+    __shared__ uint32_t s_phase;   // parity of the next copy
+    __shared__ int s_any;       // a copy was issued (the last one has parity s_phase ^ 1)
+    __shared__ long long s_deadline;
+    __shared__ int s_landed;    // a wait saw the current copy land
     const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
     if (lead) {
         s_off = 0;
+        s_landed = 0;
+        s_next = s_end = 0;
+        s_staged = -1;
+        s_issued = 0;
+        s_phase = 0;
+        s_any = 0;
         if (!FF) stage_init(&s_bar);
     }
-    int staged = -1;            // items[] entry the block last prepared for
-    uint32_t phase = 0;         // parity of the next copy
-    bool any_issued = false;    // a copy was issued (the last one has parity phase ^ 1)
-    OrbitStage st{s_seg, &s_bar, &s_off, 0u, 0, 0};
     for (;;) {
-        if (threadIdx.x == 0 && threadIdx.y == 0)
-            s_base = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(q.counter),
-                                          (unsigned long long)q.tiles_per_pop);
+        if (lead) {
+            // the next tile of the block's current pop, or a new pop of tiles_per_pop
+            if (s_next >= s_end) {
+                s_next = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(q.counter),
+                                              (unsigned long long)q.tiles_per_pop);
+                s_end = min(s_next + (long long)q.tiles_per_pop, q.n_tiles);
+            }
+            s_tile = s_next < q.n_tiles ? s_next++ : -1;
+        }
         __syncthreads();
-        const long long base = s_base;
-        __syncthreads();
-        if (base >= q.n_tiles) {
+        const long long tile = s_tile;
+        if (tile < 0) {
             // the block's shared memory outlives its last copy
-            if (!FF && lead && any_issued) stage_drain(&s_bar, phase ^ 1u, q.items[0].err);
+            if (!FF && lead && s_any) stage_drain(&s_bar, s_phase ^ 1u, q.items[0].err);
             return;
         }
-        const long long end = min(base + (long long)q.tiles_per_pop, q.n_tiles);
-        for (long long tile = base; tile < end; ++tile) {
-            // request owning the tile: last prefix start <= tile (warp-uniform search)
-            int lo = 0, hi = q.n_items - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (q.tile_start[mid] <= tile) lo = mid;
-                else hi = mid - 1;
+        // request owning the tile: last prefix start <= tile (warp-uniform search)
+        int lo = 0, hi = q.n_items - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (q.tile_start[mid] <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        const GeoParams& p = q.items[lo];
+        const long long local = tile - q.tile_start[lo];
+        const int tiles_x = (p.gw + GBX - 1) / GBX;
+        // every thread finished the previous tile (barrier below), so the
+        // tables of a new request may overwrite s_seg; after a wait ran out
+        // (s_off) nothing more is staged and the new request reads its global
+        // tables.  The lead thread decides; the others read its decision.
+        if (!FF && lead && lo != s_staged) {
+            s_staged = lo;
+            s_issued = (!s_off && seg_fits(p)) ? 1 : 0;
+            if (s_issued) {
+                s_deadline = clock64() + p.stage_wait;
+                s_landed = 0;
+                stage_issue(p, s_seg, &s_bar);
+                s_phase ^= 1u;
+                s_any = 1;
             }
-            const GeoParams& p = q.items[lo];
-            const long long local = tile - q.tile_start[lo];
-            const int tiles_x = (p.gw + GBX - 1) / GBX;
-            // every thread finished the previous tile (barrier below), so
-            // the tables of a new request may overwrite s_seg; after a wait
-            // ran out (s_off) nothing more is staged and the new request
-            // reads its global tables
-            if (!FF && lo != staged) {
-                staged = lo;
-                st.issued = (!s_off && seg_fits(p)) ? 1 : 0;
-                if (st.issued) {
-                    st.deadline = clock64() + p.stage_wait;
-                    if (lead) stage_issue(p, s_seg, &s_bar);
-                    st.phase = phase;
-                    phase ^= 1u;
-                    any_issued = true;
-                }
-            }
-            geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x), st);
-            if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
-            __syncthreads();
-            if (q.done_flags && threadIdx.x == 0 && threadIdx.y == 0) {
-                // the block finishing a request's last tile raises its flag
-                const int r = q.item_request[lo];
-                const unsigned long long old = atomicAdd(q.request_done + r, 1ull);
-                if ((long long)old + 1 == q.request_tiles[r]) {
-                    __threadfence_system();
-                    *(volatile unsigned int*)(q.done_flags + r) = 1u;   // single writer
-                }
+        }
+        __syncthreads();
+        // (the copy just issued, if any, has parity s_phase ^ 1)
+        const OrbitStage st{s_seg, &s_bar, &s_off, s_phase ^ 1u, FF ? 0 : s_issued, s_deadline, &s_landed};
+        geocode_block<GEO_LONLAT, FF, false, PPT>(p, (int)(local % tiles_x), (int)(local / tiles_x), st);
+        if (q.done_flags) __threadfence();   // this thread's outputs before the tile count
+        __syncthreads();
+        if (q.done_flags && lead) {
+            // the block finishing a request's last tile raises its flag
+            const int r = q.item_request[lo];
+            const unsigned long long old = atomicAdd(q.request_done + r, 1ull);
+            if ((long long)old + 1 == q.request_tiles[r]) {
+                __threadfence_system();
+                *(volatile unsigned int*)(q.done_flags + r) = 1u;   // single writer
             }
         }
     }
