@@ -39,10 +39,14 @@ struct gslc_ctx {
     std::vector<cudaEvent_t> io_ev;
     int io_reruns = 0;
     bool no_alloc = false;          // the allocation-free entry point's stand-in context
-    // the last orbit's host tables (build_orbit_table), keyed by its descriptor
-    // and state vectors: calls that reuse an orbit skip rebuilding them
-    std::vector<double> orb_key, orb_coef;
-    Orbit orb_ob{};
+    // the host tables (build_orbit_table) of the last few orbits, keyed by
+    // the descriptor and the state vectors, most recent first: calls that
+    // reuse an orbit skip rebuilding them
+    struct OrbitTables {
+        std::vector<double> key, coef;
+        Orbit ob{};
+    };
+    std::vector<OrbitTables> orbit_cache;
     std::string err;
 };
 
@@ -447,25 +451,37 @@ bool proj_forward(int epsg, const Utm& u, double lon, double lat, double& x, dou
     return utm_forward(u, lon, lat, x, y);
 }
 
-// build_orbit_table through the context's one-entry cache: a caller that
-// geocodes many blocks, bands or requests with one orbit builds its
-// polynomial pieces and Newton tables once (about 0.7 ms for 21 state
-// vectors).  The key is the descriptor's scalars and the state vectors'
-// bytes, so any change rebuilds.
+// build_orbit_table through the context's cache of the last 16 orbits: a
+// caller that geocodes many blocks, bands or requests with a few orbits
+// builds their polynomial pieces and Newton tables once each (about 0.7 ms
+// for 21 state vectors).  The key is the descriptor's scalars and the state
+// vectors' bytes, so any change rebuilds.
+constexpr size_t ORBIT_CACHE_ENTRIES = 16;
 void orbit_table_cached(gslc_ctx* c, const gslc_orbit& o, std::vector<double>& coef, Orbit& ob) {
     const size_t nv = 3 * (size_t)o.n;
     const double head[4] = {o.t0, o.spacing, (double)o.n, (double)o.method};
-    bool hit = c->orb_key.size() == 4 + 2 * nv && std::memcmp(c->orb_key.data(), head, sizeof(head)) == 0 &&
-               std::memcmp(c->orb_key.data() + 4, o.pos, nv * sizeof(double)) == 0 &&
-               std::memcmp(c->orb_key.data() + 4 + nv, o.vel, nv * sizeof(double)) == 0;
-    if (!hit) {
-        build_orbit_table(o, c->orb_coef, c->orb_ob);
-        c->orb_key.assign(head, head + 4);
-        c->orb_key.insert(c->orb_key.end(), o.pos, o.pos + nv);
-        c->orb_key.insert(c->orb_key.end(), o.vel, o.vel + nv);
+    auto& cache = c->orbit_cache;
+    size_t i = 0;
+    for (; i < cache.size(); ++i) {
+        const std::vector<double>& k = cache[i].key;
+        if (k.size() == 4 + 2 * nv && std::memcmp(k.data(), head, sizeof(head)) == 0 &&
+            std::memcmp(k.data() + 4, o.pos, nv * sizeof(double)) == 0 &&
+            std::memcmp(k.data() + 4 + nv, o.vel, nv * sizeof(double)) == 0)
+            break;
     }
-    coef = c->orb_coef;
-    ob = c->orb_ob;
+    if (i == cache.size()) {
+        gslc_ctx::OrbitTables t;
+        build_orbit_table(o, t.coef, t.ob);
+        t.key.assign(head, head + 4);
+        t.key.insert(t.key.end(), o.pos, o.pos + nv);
+        t.key.insert(t.key.end(), o.vel, o.vel + nv);
+        if (cache.size() == ORBIT_CACHE_ENTRIES) cache.pop_back();
+        cache.insert(cache.begin(), std::move(t));
+    } else if (i > 0) {
+        std::rotate(cache.begin(), cache.begin() + i, cache.begin() + i + 1);   // most recent first
+    }
+    coef = cache.front().coef;
+    ob = cache.front().ob;
 }
 
 // Orbit descriptor checks: Hermite (4 or more state vectors) or Legendre
@@ -1326,13 +1342,30 @@ extern "C" int gslc_geocode_slc_host_io(gslc_ctx* c, const gslc_geocode_args* a,
     // bands, planned and ordered by the first radar line they read
     const int nb_want = io->bands > 0 ? io->bands : 6;
     int64_t band_rows = ((gl + nb_want - 1) / nb_want + 31) / 32 * 32;
-    const int nb = (int)((gl + band_rows - 1) / band_rows);
-    std::vector<IoBand> bands(nb);
-    for (int i = 0; i < nb; ++i) {
-        bands[i].row0 = (int64_t)i * band_rows;
-        bands[i].rows = std::min(band_rows, gl - bands[i].row0);
-        plan_io_band(ph, ph.orbit, a, io->margin, bands[i]);
+    const int nb0 = (int)((gl + band_rows - 1) / band_rows);
+    // the first and last row bands are split, an eighth of a band at the
+    // geogrid's edge: whichever end the uploads start from, the first
+    // kernel waits for fewer radar lines and the last band's copy back is
+    // shorter (frame: 38.0 -> 37.7 ms per call).  Every band starts on a
+    // multiple of 32 rows, the tile height, so that the tiles (and their
+    // UTM fits) are those of one launch over the whole geogrid.
+    std::vector<IoBand> bands;
+    {
+        const int64_t q = std::max<int64_t>(32, (band_rows / 8 + 31) / 32 * 32);
+        for (int i = 0; i < nb0; ++i) {
+            const int64_t r0 = (int64_t)i * band_rows, rows = std::min(band_rows, gl - r0);
+            IoBand x{};
+            if ((i == 0 || i == nb0 - 1) && rows > 2 * q) {
+                const int64_t cut = i == 0 ? q : (rows - q) / 32 * 32;
+                x.row0 = r0; x.rows = cut; bands.push_back(x);
+                x.row0 = r0 + cut; x.rows = rows - cut; bands.push_back(x);
+            } else {
+                x.row0 = r0; x.rows = rows; bands.push_back(x);
+            }
+        }
+        for (IoBand& x : bands) plan_io_band(ph, ph.orbit, a, io->margin, x);
     }
+    const int nb = (int)bands.size();
     std::stable_sort(bands.begin(), bands.end(), [](const IoBand& x, const IoBand& y) { return x.az_lo < y.az_lo; });
 
     // uploads on h2d_stream: a band's missing lines (deramped there) and DEM rows, then an event

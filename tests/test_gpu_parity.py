@@ -363,3 +363,31 @@ def test_legendre_orbit(oracle_mod, c1, which, precision):
     gpu, ora = _run_both(oracle_mod, sc, [sc.slc], geo2rdr_precision=precision, **kw)
     r = _check(gpu, ora)[0]
     assert r["n_valid"] > 10000
+
+
+def test_context_orbit_tables_follow_the_orbit(c1):
+    """A context keeps the host tables of the last orbits it used, keyed by
+    their state vectors: calls alternating between two orbits, and one whose
+    state vectors are changed in place, each give the bits of a call with
+    that orbit alone."""
+    from isce3_gb300.core import Orbit
+    g = c1.geogrid
+
+    def run(orbit):
+        out = np.zeros((g.length, g.width), np.complex64)
+        geocode_slc(out, c1.slc, c1.dem, c1.radar_grid, g, orbit, LUT2d(), LUT2d(), c1.ellipsoid, 1e-8, 25)
+        return out.view(np.uint64).copy()
+
+    o = c1.orbit
+    a = Orbit.from_arrays(o.t0, o.spacing, o.position.copy(), o.velocity.copy(), o.reference_epoch)
+    b = Orbit.from_arrays(o.t0, o.spacing, o.position + np.array([0.0, 0.0, 40.0]), o.velocity.copy(),
+                          o.reference_epoch)
+    ra = run(a)
+    rb = run(b)
+    assert not np.array_equal(ra, rb)
+    np.testing.assert_array_equal(run(a), ra)
+    saved = a.position.copy()
+    a.position[:, 2] += 40.0               # the same bytes as b now
+    np.testing.assert_array_equal(run(a), rb)
+    a.position[...] = saved
+    np.testing.assert_array_equal(run(a), ra)
