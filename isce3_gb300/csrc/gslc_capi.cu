@@ -259,12 +259,14 @@ void shift_poly_dd(const double* q, int n, int c, dd* r) {
 // degree needed over the segments, and div = 1 where G would need more
 // than 12 terms (the kernel then divides).
 void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, int& nh_max, int& ng_max, int& div,
-                         int& a7) {
+                         int& a7, double& b6s, double& h6s) {
     const int nseg = o.n - 1;
     nh_max = 0;
     ng_max = 0;
     div = 0;
     a7 = 0;
+    b6s = 0.0;
+    h6s = 0.0;
     for (int j = 0; j < nseg; ++j) {
         const int idx = std::min(std::max(j - 1, 0), o.n - 4);
         const int c = j - idx - 1;                 // u = w + c
@@ -339,6 +341,14 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
         // 1e-11 m (slant ranges of ~1e6 m round at ~1e-10 m)
         for (int d = 0; d < 3; ++d)
             if (std::fabs(s[SEG_A + d * 8 + 7]) * std::ldexp(1.0, -7) >= 1e-11) a7 = 1;
+        // the residual's degree-6 term D.b_6 - h_6 over |w| <= 1/2, as a step
+        // (divided by |v|^2): |D| b6s + h6s seconds at most (residual_degree)
+        {
+            const double b6 = std::sqrt(b[0][6] * b[0][6] + b[1][6] * b[1][6] + b[2][6] * b[2][6]);
+            const double scale = std::ldexp(1.0, -6) / std::fabs(W[0].hi);
+            b6s = std::max(b6s, b6 * scale);
+            h6s = std::max(h6s, std::fabs(s[SEG_H + 6]) * scale);
+        }
         nh_max = std::max(nh_max, nh);
         ng_max = std::max(ng_max, ng);
     }
@@ -368,9 +378,10 @@ void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob
     make_orbit_coeffs(o, coef);
     // Newton segment tables after the pieces (orbit_seg_offset, 16-byte aligned)
     int seg_nh = 0, seg_ng = 0, seg_div = 0, seg_a7 = 1;
+    double seg_b6 = 0.0, seg_h6 = 0.0;
     coef.resize(orbit_table_doubles(o.n), 0.0);
     double* seg = coef.data() + orbit_seg_offset(o.n);
-    make_orbit_segments(o, coef.data(), seg, seg_nh, seg_ng, seg_div, seg_a7);
+    make_orbit_segments(o, coef.data(), seg, seg_nh, seg_ng, seg_div, seg_a7, seg_b6, seg_h6);
     // their float pairs for the float-float Newton: b, h, g, a of each segment
     float2* ffs = reinterpret_cast<float2*>(coef.data() + orbit_segff_offset(o.n));
     auto split = [](double v) {
@@ -396,6 +407,9 @@ void build_orbit_table(const gslc_orbit& o, std::vector<double>& coef, Orbit& ob
     ob.seg_ng = seg_ng;
     ob.seg_div = seg_div;
     ob.seg_a7 = seg_a7;
+    ob.seg_b6 = seg_b6;
+    ob.seg_h6 = seg_h6;
+    ob.seg_r6 = 1;           // without a geometry to bound |D|: kept (residual_degree)
 }
 
 bool utm_setup(int code, Utm& u) {
@@ -482,6 +496,22 @@ void orbit_table_cached(gslc_ctx* c, const gslc_orbit& o, std::vector<double>& c
     }
     coef = cache.front().coef;
     ob = cache.front().ob;
+}
+
+// The Newton residual's degree for ground points seen from the radar grid
+// rg: the degree-6 term is dropped where it moves a step by less than
+// 1e-12 s.  With |D| = |xyz - P_ref| at most the grid's far slant range
+// plus half a segment of travel (10 km/s bounds the speed), the returned
+// iterate then moves by < 1e-12 s, a tenth of the reference's own
+// orbit-interpolation rounding (~1e-11 s), and the slant range, stationary
+// at zero Doppler, does not move to first order.  Terms of H above degree 5
+// (seg_nh >= 6) keep it.
+int residual_degree6(const Orbit& ob, const gslc_radar_grid& rg) {
+    if (ob.legendre) return 1;
+    if (ob.seg_nh >= 6) return 1;
+    const double far = rg.starting_range + std::max<int64_t>(rg.width - 1, 0) * rg.range_pixel_spacing;
+    const double dmax = std::fabs(far) + 1e4 * 0.5 * ob.spacing;
+    return dmax * ob.seg_b6 + ob.seg_h6 >= 1e-12 ? 1 : 0;
 }
 
 // Orbit descriptor checks: Hermite (4 or more state vectors) or Legendre
@@ -893,6 +923,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
 
     // orbit polynomials and Newton tables
     orbit_table_cached(c, a->orbit, coef, p.orbit);
+    p.orbit.seg_r6 = residual_degree6(p.orbit, a->radar_grid);
     const Orbit& ob = p.orbit;
 
     // geo2rdr setup: initial guess sensingMid (geocodeSlc.cpp:108)

@@ -627,7 +627,10 @@ struct Orbit {
     int32_t seg_a7;              // 1: the position's degree-7 term matters (else degree 6)
     int32_t legendre;            // 1: Legendre interpolation; coef holds the state vectors
                                  // (positions 3n, then velocities 3n) and seg, seg_ff are unused
-    int32_t _pad;
+    int32_t seg_r6;              // 1: the residual's degree-6 term is kept (else degree 5)
+    // the degree-6 term's step over |w| <= 1/2, max over segments: up to
+    // |D| seg_b6 + seg_h6 seconds for |D| = |xyz - P_ref| (seconds per metre, seconds)
+    double seg_b6, seg_h6;
 };
 
 // Orbit table layout in doubles: the pieces, then the segments (16-byte
@@ -738,7 +741,8 @@ GSLC_HD double seg_poly(const double* c, int deg, double w) {
 // interpolated position: fn(w) = D.v(w) - H(w) with D = xyz - P_ref is one
 // polynomial whose coefficients k <= 6 are D.b_k - h_k (formed when the
 // iterate enters a segment) and whose others are -h_k (H truncated where its
-// tail stops mattering); 1/|vel|^2 is G(w).  Inside a segment the iterate is
+// tail stops mattering; the degree-6 term too where it does not matter,
+// Orbit::seg_r6); 1/|vel|^2 is G(w).  Inside a segment the iterate is
 // carried by its coordinate w alone, t = t_j + (w + 1/2) spacing being
 // formed where it is needed (segment changes and the returned iterate).
 // Rounding differs from the direct form by ~1e-13 s in azimuth time, below
@@ -797,6 +801,7 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
                 D[2] = xyz.z - ld_gen(c + 2);
 #pragma unroll
                 for (int k = 0; k < 7; ++k) {
+                    if (k == 6 && !o.seg_r6) break;
                     const double dv = fma(D[0], ld_gen(c + SEG_B + k), fma(D[1], ld_gen(c + SEG_B + 7 + k),
                                                                          D[2] * ld_gen(c + SEG_B + 14 + k)));
                     cf[k] = k <= nh ? dv - ld_gen(c + SEG_H + k) : dv;
@@ -818,14 +823,20 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             fn = fma(D[0], v[0], fma(D[1], v[1], D[2] * v[2])) - seg_poly(c + SEG_H, nh, w);
             dt = fn / (-(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
         } else {
-            double acc = cf[6];
-            if (nh > 6) {
-                acc = -ld_gen(c + SEG_H + nh);
-                for (int k = nh - 1; k >= 7; --k) acc = fma(acc, w, -ld_gen(c + SEG_H + k));
-                acc = fma(acc, w, cf[6]);
+            double acc;
+            if (o.seg_r6) {
+                acc = cf[6];
+                if (nh > 6) {
+                    acc = -ld_gen(c + SEG_H + nh);
+                    for (int k = nh - 1; k >= 7; --k) acc = fma(acc, w, -ld_gen(c + SEG_H + k));
+                    acc = fma(acc, w, cf[6]);
+                }
+                acc = fma(acc, w, cf[5]);
+            } else {
+                acc = cf[5];
             }
 #pragma unroll
-            for (int k = 5; k >= 0; --k) acc = fma(acc, w, cf[k]);
+            for (int k = 4; k >= 0; --k) acc = fma(acc, w, cf[k]);
             fn = acc;
             if (!g_fresh) g = seg_poly(c + SEG_G, o.seg_ng, w);
             dt = -fn * g;
