@@ -559,11 +559,13 @@ def run_bursts(args):
                      "batched_timing": "CUDA events around graph launches",
                      "batched_wall_ms": wall_batch,
                      "speedup": ms_plain / ms_batch, "valid_px": valid, "batched_equals_plain": bool(same),
-                     "tuning": {"rows_per_thread": best.rows_per_thread, "tiles_per_pop": best.tiles_per_pop,
+                     "tuning": {"form": "per-request kernels" if best.per_request else "persistent queue",
+                                "rows_per_thread": best.rows_per_thread, "tiles_per_pop": best.tiles_per_pop,
                                 "blocks_per_sm": best.blocks_per_sm,
                                 "tried_ms": {"x".join(map(str, k)) if isinstance(k, tuple) else k: v
                                              for k, v in tried.items()},
-                                "tried_key": "rows_per_thread x tiles_per_pop x blocks_per_sm"},
+                                "tried_key": "rows_per_thread x tiles_per_pop x blocks_per_sm of the "
+                                             "persistent queue; per-request: each request's own kernel"},
                      "tiles": info["tiles"], "blocks": info["blocks"], "launches_per_run": info["launches_per_run"]}
         del ref
         torch.cuda.empty_cache()

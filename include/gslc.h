@@ -389,6 +389,9 @@ typedef struct {
     int32_t blocks_per_sm;   /* persistent blocks per SM; 0: occupancy maximum */
     int32_t use_graph;       /* 1: capture and replay a CUDA graph; 0: launch directly */
     int32_t rows_per_thread; /* geogrid lines per thread: 1, 2 or 4 (tiles of 32 x 8/16/32 pixels); 0: 4 */
+    int32_t per_request;     /* 1: each request's own fused kernel (the plain call's, 32 x 32 tiles) on
+                                concurrent streams, in place of the persistent queue; the three fields
+                                above do not apply */
 } gslc_batch_tuning;
 
 /* Device buffers are allocated and filled in the order of `stream`

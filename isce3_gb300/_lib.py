@@ -156,7 +156,7 @@ class HostIo(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("tiles_per_pop", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
-                ("rows_per_thread", C.c_int32)]
+                ("rows_per_thread", C.c_int32), ("per_request", C.c_int32)]
 
 
 class GeoBlock(C.Structure):

@@ -4,7 +4,9 @@ For a batch it times a small set of persistent-kernel shapes — the tile
 shape (32 x 8, 32 x 16 or 32 x 32 output pixels, i.e. 1, 2 or 4 geogrid
 lines per thread; on UTM grids the tile is also the unit of the fitted
 projection inverse), tiles taken per counter pop, persistent blocks per SM —
-with CUDA events on the real requests, keeps the fastest, and caches the
+and the per-request form (each request's own fused kernel on concurrent
+streams, which suits few large requests), with CUDA events on the real
+requests, keeps the fastest, and caches the
 choice in JSON keyed by GPU name and a hash of the batch's shape (request
 count, tile count bucket, geogrid projection, geo2rdr precision), so later
 batches of the same kind skip the search.
@@ -70,7 +72,8 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
     if key in cache:
         c = cache[key]
         probe.close()
-        return (BatchTuning(c["tiles_per_pop"], c["blocks_per_sm"], True, c.get("rows_per_thread", 4)),
+        return (BatchTuning(c["tiles_per_pop"], c["blocks_per_sm"], True, c.get("rows_per_thread", 4),
+                            bool(c.get("per_request", False))),
                 {"cached": c["ms"]})
     occ = max(1, info["blocks"] // torch.cuda.get_device_properties(0).multi_processor_count)
     if candidates is None:
@@ -80,6 +83,7 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
         else:
             candidates = [BatchTuning(p, b, True, r) for r in (1, 2, 4) for p in (1, 2, 4)
                           for b in sorted({occ, max(1, occ - 1)})]
+        candidates.append(BatchTuning(per_request=True))
     results = {}
     best, best_ms = None, float("inf")
     probe.close()
@@ -87,14 +91,14 @@ def tune(requests, precision: str = "fp64", candidates=None, use_cache: bool = T
         b = GeocodeBatch(requests, precision, t)
         ms = time_batch(b, reps)
         b.close()
-        results[(t.rows_per_thread, t.tiles_per_pop, t.blocks_per_sm)] = ms
+        results["per-request" if t.per_request else (t.rows_per_thread, t.tiles_per_pop, t.blocks_per_sm)] = ms
         if ms < best_ms:
             best, best_ms = t, ms
     if use_cache:
         with _lock:
             cache = _load()
             cache[key] = {"tiles_per_pop": best.tiles_per_pop, "blocks_per_sm": best.blocks_per_sm,
-                          "rows_per_thread": best.rows_per_thread, "ms": best_ms,
+                          "rows_per_thread": best.rows_per_thread, "per_request": best.per_request, "ms": best_ms,
                           "gpu": torch.cuda.get_device_name(), "precision": precision, "requests": len(requests)}
             _store(cache)
     return best, results

@@ -74,11 +74,13 @@ class BatchTuning:
     blocks_per_sm: int = 0          # 0: occupancy maximum
     use_graph: bool = True
     rows_per_thread: int = 4        # geogrid lines per thread: tiles of 32 x 8*rows_per_thread pixels
+    per_request: bool = False       # each request's own fused kernel on concurrent streams, no queue
 
     def to_c(self) -> L.BatchTuning:
         t = L.BatchTuning()
         t.tiles_per_pop, t.blocks_per_sm, t.use_graph = self.tiles_per_pop, self.blocks_per_sm, int(self.use_graph)
         t.rows_per_thread = self.rows_per_thread
+        t.per_request = int(self.per_request)
         return t
 
 

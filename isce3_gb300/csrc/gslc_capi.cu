@@ -2210,6 +2210,15 @@ struct gslc_batch {
     cudaStream_t capture_stream = nullptr;
     int64_t launches_per_run = 0;
     long long n_tiles = 0;
+    // per-request mode: the launch parameters of each entry (its request
+    // owner[j]), run as the plain call's kernel on concurrent branch streams
+    bool per_request = false;
+    std::vector<GeoParams> params;
+    std::vector<int> owner;
+    std::vector<cudaStream_t> branches;
+    cudaEvent_t fork_ev = nullptr;
+    std::vector<cudaEvent_t> join_ev;
+    unsigned int* d_flags = nullptr;    // device view of h_flags
     std::string err;
 };
 
@@ -2226,7 +2235,47 @@ int batch_fail(gslc_batch* b, gslc_ctx* c, int code, const std::string& m) {
     return code;
 }
 
+// Per-request mode: after the deramps, each entry's plain kernel on one of
+// the branch streams (forked from s and joined back into it), the request's
+// completion word behind its last entry.  Concurrent kernels fill each
+// other's last waves; inside a graph capture the branches become parallel
+// graph paths.
+cudaError_t batch_enqueue_per_request(gslc_batch* b, cudaStream_t s) {
+    cudaError_t e = cudaEventRecord(b->fork_ev, s);
+    for (cudaStream_t br : b->branches)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(br, b->fork_ev, 0);
+    const size_t nb = b->branches.size();
+    for (size_t j = 0; j < b->params.size() && e == cudaSuccess; ++j) {
+        cudaStream_t br = b->branches[j % nb];
+        e = launch_geocode(b->params[j], b->ff ? 1 : 0, br, nullptr);
+        const bool last = j + 1 == b->params.size() || b->owner[j + 1] != b->owner[j];
+        // a request's entries share a branch only when it has one entry; with
+        // several, the word waits for all of them on the join below
+        if (e == cudaSuccess && b->d_flags && last && (j == 0 || b->owner[j - 1] != b->owner[j]))
+            e = launch_set_flag(b->d_flags + b->owner[j], br, nullptr);
+    }
+    for (size_t k = 0; k < nb && e == cudaSuccess; ++k) {
+        e = cudaEventRecord(b->join_ev[k], b->branches[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->join_ev[k], 0);
+    }
+    // requests split over several entries (more than MAX_BLOCKS radar blocks)
+    for (size_t j = 0; j < b->params.size() && e == cudaSuccess && b->d_flags; ++j) {
+        const bool first = j == 0 || b->owner[j - 1] != b->owner[j];
+        const bool last = j + 1 == b->params.size() || b->owner[j + 1] != b->owner[j];
+        if (last && !first) e = launch_set_flag(b->d_flags + b->owner[j], s, nullptr);
+    }
+    return e;
+}
+
 cudaError_t batch_enqueue(gslc_batch* b, cudaStream_t s) {
+    if (b->per_request) {
+        cudaError_t e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), s);
+        for (const DerampParams& dp : b->deramps) {
+            if (e != cudaSuccess) break;
+            e = launch_deramp(dp, s, nullptr);
+        }
+        return e == cudaSuccess ? batch_enqueue_per_request(b, s) : e;
+    }
     cudaError_t e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter, 0, sizeof(long long), s);
     if (e == cudaSuccess && b->q.done_flags)
@@ -2420,6 +2469,7 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
         b->q.request_tiles = b->d_request_tiles;
         b->q.request_done = b->d_request_done;
         b->q.done_flags = dflags;
+        b->d_flags = dflags;
     }
     b->n_tiles = tile_start.back();
     b->q.items = b->d_items;
@@ -2435,6 +2485,34 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
     const int per_sm = (tuning && tuning->blocks_per_sm > 0) ? std::min(tuning->blocks_per_sm, occ) : occ;
     b->blocks = sms * per_sm;
     b->launches_per_run = (int64_t)b->deramps.size() + 1;
+    if (tuning && tuning->per_request) {
+        if (ppt != 4) {
+            gslc_batch_destroy(b);
+            return set_err(c, GSLC_EINVAL, "per-request batches use the plain kernel's 32 x 32 tiles (rows_per_thread 4)");
+        }
+        b->per_request = true;
+        b->params = params;
+        b->owner = owner;
+        const int nbr = (int)std::min<size_t>(4, params.size());
+        e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+        for (int k = 0; k < nbr && e == cudaSuccess; ++k) {
+            cudaStream_t br = nullptr;
+            cudaEvent_t ev = nullptr;
+            e = cudaStreamCreateWithFlags(&br, cudaStreamNonBlocking);
+            if (e == cudaSuccess) b->branches.push_back(br);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) b->join_ev.push_back(ev);
+        }
+        if (e != cudaSuccess) {
+            gslc_batch_destroy(b);
+            return cuda_err(c, e, "batch streams");
+        }
+        int64_t flags = 0;
+        if (b->d_flags)
+            for (size_t j = 0; j < params.size(); ++j)
+                if (j + 1 == params.size() || owner[j + 1] != owner[j]) ++flags;
+        b->launches_per_run = (int64_t)b->deramps.size() + (int64_t)params.size() + flags;
+    }
     if (!tuning || tuning->use_graph) {
         e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
@@ -2492,6 +2570,9 @@ extern "C" int gslc_batch_destroy(gslc_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    for (cudaStream_t br : b->branches) cudaStreamDestroy(br);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    for (cudaEvent_t ev : b->join_ev) cudaEventDestroy(ev);
     for (void* ptr : {(void*)b->d_items, (void*)b->d_tile_start, (void*)b->d_counter, (void*)b->d_orbit,
                       (void*)b->d_scratch, (void*)b->d_err, (void*)b->d_item_request, (void*)b->d_request_tiles,
                       (void*)b->d_request_done})

@@ -1379,6 +1379,14 @@ __global__ void __launch_bounds__(256) mask_words_kernel(W* __restrict__ data, i
 
 // every element of p set to v (the invalid fill of the raster mode's phase
 // outputs); grid-stride, coalesced 8-byte stores
+// A request's completion word (mapped host memory): written once the
+// kernels before it on the stream have finished, after a system-wide fence
+// that orders their outputs before the word.
+__global__ void set_flag_kernel(unsigned int* flag) {
+    __threadfence_system();
+    *(volatile unsigned int*)flag = 1u;
+}
+
 __global__ void __launch_bounds__(256) fill_f64_kernel(double* __restrict__ p, int64_t n, double v) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
@@ -1457,6 +1465,12 @@ cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits
         const unsigned long long m = ~0ull << (52 - bits);
         mask_words_kernel<unsigned long long><<<g, 256, 0, s>>>((unsigned long long*)dst, n, m);
     }
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_flag(unsigned int* flag, cudaStream_t s, int64_t* launches) {
+    set_flag_kernel<<<1, 1, 0, s>>>(flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

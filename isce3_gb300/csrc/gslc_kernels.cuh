@@ -209,6 +209,7 @@ inline bool ff_eligible(const GeoParams& p) {
 cudaError_t launch_geocode(const GeoParams& p, int precision, cudaStream_t s, int64_t* launches);
 cudaError_t launch_deramp(const DerampParams& p, cudaStream_t s, int64_t* launches);
 cudaError_t launch_fill_f64(double* p, int64_t n, double v, cudaStream_t s, int64_t* launches);
+cudaError_t launch_set_flag(unsigned int* flag, cudaStream_t s, int64_t* launches);
 // op 0: complex64 -> complex32, 1: complex32 -> complex64, 2: keep `bits`
 // mantissa bits of n words of word_bytes (4 or 8) at dst, in place
 cudaError_t launch_codec(int op, const void* src, void* dst, int64_t n, int bits, int word_bytes, cudaStream_t s,

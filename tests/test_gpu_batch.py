@@ -52,13 +52,17 @@ def _same(a, b):
         assert torch.equal(torch.view_as_real(g0).view(torch.int32), torch.view_as_real(g1).view(torch.int32))
 
 
-@pytest.mark.parametrize("precision,graph,pop", [("fp64", True, 2), ("ff", True, 4), ("fp64", False, 1)])
-def test_batch_equals_plain_calls(bursts, precision, graph, pop):
+@pytest.mark.parametrize("precision,graph,pop,per_request", [("fp64", True, 2, False), ("ff", True, 4, False),
+                                                              ("fp64", False, 1, False), ("fp64", True, 0, True),
+                                                              ("ff", False, 0, True)])
+def test_batch_equals_plain_calls(bursts, precision, graph, pop, per_request):
     ref = _plain(bursts, precision)
     outs = _outputs(bursts)
-    batch = GeocodeBatch(_requests(bursts, outs), precision, BatchTuning(tiles_per_pop=pop, use_graph=graph))
+    batch = GeocodeBatch(_requests(bursts, outs), precision,
+                         BatchTuning(tiles_per_pop=pop or 2, use_graph=graph, per_request=per_request))
     info = batch.info()
-    assert info["tiles"] > 0 and info["launches_per_run"] == len(bursts.bursts) + 1
+    n = len(bursts.bursts)
+    assert info["tiles"] > 0 and info["launches_per_run"] == (2 * n if per_request else n + 1)
     for _ in range(2):                       # a replay recomputes the same bits
         for g, m in outs:
             g.fill_(0)
@@ -90,8 +94,8 @@ def test_batch_legendre_orbit_equals_plain_calls(bursts):
     batch.close()
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_batch_request_flags(bursts, graph):
+@pytest.mark.parametrize("graph,per_request", [(True, False), (False, False), (True, True)])
+def test_batch_request_flags(bursts, graph, per_request):
     """Per-request completion words: every request's word is 1 once the
     batch has run, cleared words are set again by a replay, and the outputs
     are those of the plain calls."""
@@ -99,8 +103,8 @@ def test_batch_request_flags(bursts, graph):
     outs = _outputs(bursts)
     n = len(bursts.bursts)
     flags = HostFlags(n + 3)
-    batch = GeocodeBatch(_requests(bursts, outs), "fp64", BatchTuning(tiles_per_pop=1, use_graph=graph),
-                         done_flags=flags)
+    batch = GeocodeBatch(_requests(bursts, outs), "fp64",
+                         BatchTuning(tiles_per_pop=1, use_graph=graph, per_request=per_request), done_flags=flags)
     for _ in range(2):
         flags.clear()
         batch.run()
