@@ -26,12 +26,18 @@ def served():
     return sc, store, trace
 
 
-@pytest.mark.parametrize("precision,signaled", [("fp64", True), ("ff", True), ("fp64", False)])
-def test_served_results_equal_alone(served, precision, signaled):
+@pytest.mark.parametrize("precision,signaled,queue", [("fp64", True, False), ("ff", True, False),
+                                                      ("fp64", False, False), ("fp64", True, True),
+                                                      ("ff", True, True)])
+def test_served_results_equal_alone(served, precision, signaled, queue):
+    """Each request's outputs equal its plain call, served in the mix by
+    per-request kernels (the default) or by the persistent queue."""
+    from isce3_gb300.batch import BatchTuning
     sc, store, trace = served
     mixed = [ServeRequest(k, g, t) for k, g, t in trace]
     server = GeocodeServer(store, budget_bytes=2 * 10 ** 9, max_in_flight=3, max_batch=6,
-                           geo2rdr_precision=precision, per_request_completion=signaled)
+                           geo2rdr_precision=precision, per_request_completion=signaled,
+                           tuning=BatchTuning(use_graph=False) if queue else None)
     stats = server.serve(mixed, keep_outputs=True)
     server.close()
     assert stats["completed"] == len(trace) and stats["batches"] >= 2
