@@ -2241,6 +2241,12 @@ int batch_fail(gslc_batch* b, gslc_ctx* c, int code, const std::string& m) {
 // other's last waves; inside a graph capture the branches become parallel
 // graph paths.
 cudaError_t batch_enqueue_per_request(gslc_batch* b, cudaStream_t s) {
+    if (b->branches.empty()) {
+        // one entry: its kernel and word on the launch stream itself
+        cudaError_t e = launch_geocode(b->params[0], b->ff ? 1 : 0, s, nullptr);
+        if (e == cudaSuccess && b->d_flags) e = launch_set_flag(b->d_flags + b->owner[0], s, nullptr);
+        return e;
+    }
     cudaError_t e = cudaEventRecord(b->fork_ev, s);
     for (cudaStream_t br : b->branches)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(br, b->fork_ev, 0);
@@ -2493,8 +2499,9 @@ extern "C" int gslc_batch_create_signaled(gslc_ctx* c, const gslc_geocode_args* 
         b->per_request = true;
         b->params = params;
         b->owner = owner;
-        const int nbr = (int)std::min<size_t>(4, params.size());
-        e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+        // branch streams for two or more entries (one entry runs on the launch stream)
+        const int nbr = params.size() > 1 ? (int)std::min<size_t>(4, params.size()) : 0;
+        if (nbr > 0) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
         for (int k = 0; k < nbr && e == cudaSuccess; ++k) {
             cudaStream_t br = nullptr;
             cudaEvent_t ev = nullptr;

@@ -9,12 +9,14 @@
 - ``GeocodeServer.serve`` runs an arrival trace: each scheduling tick it
   moves arrived requests into the queue, marks finished requests, retires
   finished batches (CUDA event polling, no device synchronisation), and
-  launches the newly admitted requests as ONE batch on a free stream: by
-  default each request's own fused kernel on the batch's branch streams
-  (``BatchTuning(per_request=True)``: on the 200-request trace at
-  saturation 1901M px/s FP64 and 2205M float-float, against 1835M and 2069M
-  for the persistent queue); ``tuning=BatchTuning()`` selects the persistent
-  queue.  Requests that arrive while earlier batches run join the next
+  launches the newly admitted requests as ONE batch on a free stream.  By
+  default a batch of two or more requests runs each request's own fused
+  kernel on the batch's branch streams (``BatchTuning(per_request=True)``:
+  on the 200-request trace at saturation 1899M px/s FP64 and 2216M
+  float-float, against 1839M and 2080M for the persistent queue) and a
+  single request runs on the persistent queue (p50 latency at 200 req/s
+  2.09 ms against 2.32 ms for its own kernel); a ``tuning`` given to the
+  server applies to every batch.  Requests that arrive while earlier batches run join the next
   batch as soon as a slot and memory free up, and batches on different
   streams overlap on the device (the next batch's blocks start on the SMs
   that the running batch's blocks leave at its tail).
@@ -191,7 +193,7 @@ class GeocodeServer:
         self.dev = store.dev
         self.policy = AdmissionPolicy(budget_bytes, max_in_flight, max_batch)
         self.precision = geo2rdr_precision
-        self.tuning = tuning or BatchTuning(use_graph=False, per_request=True)
+        self.tuning = tuning          # None: per-request kernels for 2+ requests, else the queue
         self.signaled = bool(per_request_completion)
         self.slots = [_Slot(self.dev, max_batch, self.signaled) for _ in range(max_in_flight)]
         self.free_slots = list(self.slots)
@@ -269,7 +271,8 @@ class GeocodeServer:
                 reqs.append(self._request(r))
             if slot.flags is not None:
                 slot.flags.clear()         # the slot's previous batch has retired
-            batch = GeocodeBatch(reqs, self.precision, self.tuning, self.dev, stream, done_flags=slot.flags)
+            tuning = self.tuning or BatchTuning(use_graph=False, per_request=len(reqs) > 1)
+            batch = GeocodeBatch(reqs, self.precision, tuning, self.dev, stream, done_flags=slot.flags)
             batch.launch(stream)
             ev = torch.cuda.Event()
             ev.record(stream)

@@ -30,8 +30,9 @@ def served():
                                                       ("fp64", False, False), ("fp64", True, True),
                                                       ("ff", True, True)])
 def test_served_results_equal_alone(served, precision, signaled, queue):
-    """Each request's outputs equal its plain call, served in the mix by
-    per-request kernels (the default) or by the persistent queue."""
+    """Each request's outputs equal its plain call, served in the mix with
+    the default batch forms (per-request kernels for two or more requests,
+    the persistent queue for one) or with the persistent queue throughout."""
     from isce3_gb300.batch import BatchTuning
     sc, store, trace = served
     mixed = [ServeRequest(k, g, t) for k, g, t in trace]
