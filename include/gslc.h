@@ -374,10 +374,13 @@ int gslc_probe_fp64_gflops(gslc_ctx* ctx, double* gflops);
 /* Batched form.  A batch holds many geocode requests (bursts, tiles of
  * uneven size; each a gslc_geocode_args with its own radar grid, radar
  * blocks, geogrid window and outputs).  One launch runs the deramp passes and
- * ONE persistent kernel whose blocks pop runs of 32x8-pixel tiles of any
- * request from a device counter; by default the whole sequence is captured
- * in a CUDA graph at creation and replayed by gslc_batch_launch.  Each
- * request's outputs equal its plain gslc_geocode_slc call.  Pointers in the
+ * either ONE persistent kernel whose blocks pop runs of 32 x 8/16/32-pixel
+ * tiles of any request from a device counter, or (tuning per_request) each
+ * request's own fused kernel on up to four branch streams forked from and
+ * joined into the launch stream; by default the whole sequence is captured
+ * in a CUDA graph at creation (the branches as parallel paths) and replayed
+ * by gslc_batch_launch.  Each request's outputs equal its plain
+ * gslc_geocode_slc call (with 32 x 32 tiles: rows_per_thread 4).  Pointers in the
  * requests are bound at creation: relaunching recomputes the same outputs
  * from the (possibly updated) contents of the same buffers.  No counterpart
  * in the reference, which geocodes one block per call
@@ -401,9 +404,10 @@ typedef struct {
 int gslc_batch_create(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
                       int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, void* stream, gslc_batch** out);
 /* As gslc_batch_create, with per-request completion: done_flags is
- * n_requests words of mapped host memory (gslc_host_flags_create) that the
- * kernel sets to 1 when the last tile of request i has been written, while
- * the rest of the batch still runs.  The caller clears them before a launch. */
+ * n_requests words of mapped host memory (gslc_host_flags_create) set to 1
+ * when request i's outputs have been written (by the block writing its last
+ * tile, or by a one-thread kernel behind its own kernel), while the rest of
+ * the batch still runs.  The caller clears them before a launch. */
 int gslc_batch_create_signaled(gslc_ctx* ctx, const gslc_geocode_args* requests, int32_t n_requests,
                                int32_t geo2rdr_precision, const gslc_batch_tuning* tuning, void* stream,
                                uint32_t* done_flags, gslc_batch** out);
