@@ -544,12 +544,11 @@ int gslc_last_cube_passes(const gslc_ctx* ctx);
  * Larger inputs are rejected with GSLC_EINVAL and a message in errbuf.  It
  * calls no cudaMalloc, cudaFree or other allocating routine.  The first call
  * on a device (the current one) looks up the arrays' device addresses and
- * uploads the sinc tables synchronously, so make it before any stream
- * capture.  Like gslc_geocode_slc, every call synchronises `stream` before
- * it returns (it reads the error word back).  All calls share the arrays:
- * calls that overlap on the GPU (other streams, other host threads) race and
- * must be serialised by the caller.  errbuf (may be NULL) receives the error
- * message, errbuf_len bytes at most. */
+ * uploads the sinc tables synchronously.  Like gslc_geocode_slc, every call
+ * synchronises `stream` before it returns (it reads the error word back).
+ * All calls share the arrays: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  errbuf
+ * (may be NULL) receives the error message, errbuf_len bytes at most. */
 int gslc_geocode_slc_noalloc(const gslc_geocode_args* args, void* stream, char* errbuf, size_t errbuf_len);
 
 #ifdef __cplusplus

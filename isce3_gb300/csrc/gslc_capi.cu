@@ -2117,8 +2117,7 @@ int noalloc_fail(char* buf, size_t len, int code, const char* msg) {
 
 // Once per device, with that device current: the device addresses of the
 // static arrays (the host-side names are not device addresses) and the sinc
-// table upload.  Synchronous, so the first call on a device must not be
-// inside a stream capture.
+// table upload, synchronously.
 int noalloc_setup(int dev, NoallocDevice& d, char* buf, size_t len) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (d.ready.load(std::memory_order_acquire)) return GSLC_OK;
