@@ -1410,7 +1410,14 @@ extern "C" int gslc_geocode_slc_host_io(gslc_ctx* c, const gslc_geocode_args* a,
         for (IoBand& x : bands) plan_io_band(ph, ph.orbit, a, io->margin, x);
     }
     const int nb = (int)bands.size();
-    std::stable_sort(bands.begin(), bands.end(), [](const IoBand& x, const IoBand& y) { return x.az_lo < y.az_lo; });
+    // by first line, then last: where several bands start at the radar grid's
+    // first line (the clamp), the one needing the fewest lines goes first, so
+    // the first kernel waits for the shortest upload (frame: the first band's
+    // upload 3558 -> 1125 lines, its kernel starting 0.42 instead of 1.24 ms
+    // into the call)
+    std::stable_sort(bands.begin(), bands.end(), [](const IoBand& x, const IoBand& y) {
+        return x.az_lo != y.az_lo ? x.az_lo < y.az_lo : x.az_hi < y.az_hi;
+    });
 
     // uploads on h2d_stream: a band's missing lines (deramped there) and DEM rows, then an event
     const int64_t demL = (io->dem && p.dem.have_raster) ? p.dem.length : 0;
