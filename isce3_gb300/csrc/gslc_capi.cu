@@ -525,6 +525,57 @@ int check_orbit(gslc_ctx* c, const gslc_orbit& o) {
     return GSLC_OK;
 }
 
+// The double whose order key (dkey) is k, for the keys of finite doubles.
+double key_double(int64_t k) {
+    const uint64_t b = k >= 0 ? (uint64_t)k : ((uint64_t)(-k) | 0x8000000000000000ull);
+    double x;
+    std::memcpy(&x, &b, sizeof(x));
+    return x;
+}
+
+// Order keys [lo, hi] of the finite x where g(x) >= 0.0 and g(x) <= top hold
+// together, for g monotone in x (non-decreasing when up, else
+// non-increasing) and never NaN there: each test is monotone in x, so its
+// boundary is found by bisection over the keys, evaluating g as the
+// reference writes it.  Empty: lo > hi.
+template <class G>
+void key_interval(G g, bool up, double top, int64_t& lo, int64_t& hi) {
+    const int64_t kmax = dkey(std::numeric_limits<double>::max());
+    // first key in [-kmax, kmax] where pred holds (pred false, then true), kmax + 1 if none
+    auto first = [&](auto pred) {
+        int64_t a = -kmax, b = kmax + 1;
+        while (a < b) {
+            const int64_t m = a + (int64_t)(((uint64_t)b - (uint64_t)a) / 2);
+            if (pred(key_double(m))) b = m;
+            else a = m + 1;
+        }
+        return a;
+    };
+    if (up) {
+        lo = first([&](double x) { return g(x) >= 0.0; });
+        hi = first([&](double x) { return !(g(x) <= top); }) - 1;
+    } else {
+        lo = first([&](double x) { return g(x) <= top; });
+        hi = first([&](double x) { return !(g(x) >= 0.0); }) - 1;
+    }
+}
+
+// The keys of one axis of LUT2d::contains (core/LUT2d.h:84-95):
+// (x - x0) / dx in [0, n - 1].  A spacing of zero or NaN, or an origin that
+// is not finite, contains nothing; an infinite spacing contains every
+// finite x (the quotient is zero) when n >= 1.
+void lut_axis_keys(double x0, double dx, int n, int64_t& lo, int64_t& hi) {
+    const int64_t kmax = dkey(std::numeric_limits<double>::max());
+    lo = 1;
+    hi = 0;
+    if (!std::isfinite(x0) || !(dx != 0.0)) return;
+    if (std::isinf(dx)) {
+        if (n >= 1) { lo = -kmax; hi = kmax; }
+        return;
+    }
+    key_interval([&](double x) { return (x - x0) / dx; }, dx > 0, n - 1.0, lo, hi);
+}
+
 Lut to_lut(const gslc_lut2d& l, const double* sinc64 = nullptr) {
     Lut o{};
     o.have_data = l.have_data;
@@ -536,8 +587,8 @@ Lut to_lut(const gslc_lut2d& l, const double* sinc64 = nullptr) {
     o.ref_value = l.ref_value;
     o.inv_dx = 1.0 / l.dx;
     o.inv_dy = 1.0 / l.dy;
-    o.kx_max = dkey(l.nx - 1.0);
-    o.ky_max = dkey(l.ny - 1.0);
+    lut_axis_keys(l.x0, l.dx, l.nx, o.kx_lo, o.kx_hi);
+    lut_axis_keys(l.y0, l.dy, l.ny, o.ky_lo, o.ky_hi);
     o.data = l.data;
     o.sinc = sinc64;
     return o;
@@ -868,6 +919,40 @@ int bind_dem_window(gslc_ctx* c, const gslc_dem_raster& d, const gslc_dem_window
 // the device addresses of the orbit polynomials (bind_orbit), the sinc table
 // and the error word.  GSLC_EMPTY_GRID means there is nothing to do.
 constexpr int GSLC_EMPTY_GRID = 100;
+// The sinc chip's native Doppler from the radar indices (GeoParams::chip_dop):
+// the reference's contains(az, rng) at az = t0 + azc / prf and
+// rng = r0 + rgc * dr (geocodeSlc.cpp:457-467), monotone in each index, as
+// key intervals of azc and rgc; the table's origin in radar indices and
+// its cells per index for the FP32 coordinates.  Left off (the FP64 form)
+// for other methods, tables without data, degenerate spacings, or tables
+// spanning 2^21 radar lines or samples or more.
+void chip_doppler(GeoParams& p, const gslc_lut2d& l, const gslc_radar_grid& rg) {
+    p.chip_dop = 0;
+    if (!l.have_data || l.method != 1 || l.nx < 1 || l.ny < 1) return;
+    const double prf = rg.prf, t0 = rg.sensing_start, dr = rg.range_pixel_spacing, r0 = rg.starting_range;
+    for (double v : {prf, t0, dr, r0, l.x0, l.y0, l.dx, l.dy})
+        if (!std::isfinite(v)) return;
+    if (prf == 0.0 || dr == 0.0 || l.dx == 0.0 || l.dy == 0.0) return;
+    const double saz = 1.0 / (prf * l.dy), srg = dr / l.dx;          // cells per line, per sample
+    const double caz = (l.y0 - t0) * prf, crg = (l.x0 - r0) / dr;    // the table's first cell in radar indices
+    const double lim = 2097152.0;                                    // 2^21
+    if (!((l.ny - 1.0) / std::fabs(saz) < lim && (l.nx - 1.0) / std::fabs(srg) < lim)) return;
+    if (!(std::fabs(caz) < 1e9 && std::fabs(crg) < 1e9)) return;
+    const double y0 = l.y0, dy = l.dy, x0 = l.x0, dx = l.dx;
+    key_interval([&](double azc) { return ((t0 + azc / prf) - y0) / dy; }, (prf > 0) == (dy > 0), l.ny - 1.0,
+                 p.cd_kaz_lo, p.cd_kaz_hi);
+    key_interval([&](double rgc) { return ((r0 + rgc * dr) - x0) / dx; }, (dr > 0) == (dx > 0), l.nx - 1.0,
+                 p.cd_krg_lo, p.cd_krg_hi);
+    const double iaz = std::floor(caz), irg = std::floor(crg);
+    p.cd_iaz = (int32_t)iaz;
+    p.cd_irg = (int32_t)irg;
+    p.cd_faz = (float)(caz - iaz);
+    p.cd_frg = (float)(crg - irg);
+    p.cd_saz = (float)saz;
+    p.cd_srg = (float)srg;
+    p.chip_dop = 1;
+}
+
 int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::vector<double>& coef) {
     if (!a) return set_err(c, GSLC_EINVAL, "null arguments");
     const gslc_radar_grid& rg = a->radar_grid;
@@ -955,6 +1040,7 @@ int prepare_geocode(gslc_ctx* c, const gslc_geocode_args* a, GeoParams& p, std::
     p.k_s_r0 = dkey(p.s_r0);
     p.k_s_end = dkey(p.s_end);
     p.nat_dop = to_lut(a->native_doppler, c->d_sinc64);
+    chip_doppler(p, a->native_doppler, rg);
     p.img_dop = to_lut(a->image_grid_doppler, c->d_sinc64);
     p.az_corr = to_lut(a->az_time_correction, c->d_sinc64);
     p.sr_corr = to_lut(a->srange_correction, c->d_sinc64);

@@ -1020,7 +1020,22 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
         rng = dadd(p.rg_r0, dmul(rgc, p.rg_dr));
         az = p.rg_t0 + azc * p.inv_prf;
         // the Doppler in FP32: it only sets the float phases of the chip's demodulation
-        interp = lut_contains_eval_f32(p.nat_dop, az, rng, dop);
+        if (p.chip_dop) {
+            // contains(az, rng) on the indices' keys; the table coordinates
+            // (index - origin) * cells per index, the integer parts exact
+            // (|difference| < 2^21 inside the table), one rounding each
+            const int64_t ka = dkey(azc), kr = dkey(rgc);
+            interp = ka >= p.cd_kaz_lo && ka <= p.cd_kaz_hi && kr >= p.cd_krg_lo && kr <= p.cd_krg_hi;
+            if (interp) {
+                const float naz = small_int_to_float((int32_t)(intAzB64 + p.az_first - p.cd_iaz));
+                const float nrg = small_int_to_float((int32_t)(intRgB64 + p.rg_first - p.cd_irg));
+                const float yf = fmaf(naz, p.cd_saz, (fracAz_f - p.cd_faz) * p.cd_saz);
+                const float xf = fmaf(nrg, p.cd_srg, (fixed64_to_float(frg) - p.cd_frg) * p.cd_srg);
+                dop = lut_bilinear_f32(p.nat_dop, xf, yf);
+            }
+        } else {
+            interp = lut_contains_eval_f32(p.nat_dop, az, rng, dop);
+        }
     }
     if (!interp) {
         for (int b = 0; b < p.nblk; ++b) store_geo(p, b, k, invalid);

@@ -90,6 +90,17 @@ struct GeoParams {
     // radar lines of the blocks (block-relative) on the device; a sinc chip
     // reaching outside raises error bit 3, as for the DEM rows
     int64_t avail_az_lo, avail_az_hi;
+    // The native Doppler of the sinc chip from the radar indices (azc, rgc)
+    // when chip_dop is set (a bilinear table with data, spanning fewer than
+    // 2^21 radar lines and samples): the reference's
+    // contains(t0 + azc / prf, r0 + rgc * dr) as order-key intervals of azc
+    // and rgc, and the table coordinates in FP32 as
+    // (index - origin) * cells per index, the origin (the table's first
+    // cell in radar indices) split into an integer and a fraction.
+    int32_t chip_dop, _pad4;
+    int64_t cd_kaz_lo, cd_kaz_hi, cd_krg_lo, cd_krg_hi;
+    int32_t cd_iaz, cd_irg;
+    float cd_faz, cd_frg, cd_saz, cd_srg;
 };
 
 // default of GeoParams::stage_wait: ~2^31 SM clocks, about a second

@@ -129,24 +129,67 @@ GSLC_HD float fixed64_to_float(uint64_t f) {
 #endif
 }
 
+// (float)n for |n| < 2^22: 1.5 * 2^23 + n is exact in float, so its bits
+// are those of 1.5 * 2^23 plus n; an integer add and an FP32 subtraction,
+// off the conversion unit.
+GSLC_HD float small_int_to_float(int32_t n) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(0x4B400000u + (uint32_t)n) - 12582912.0f;
+#else
+    return (float)n;
+#endif
+}
+
 // ---- LUT2d (core/LUT2d.{h,cpp}) ------------------------------------------
 struct Lut {
     int32_t have_data, bounds_error, method, nx, ny, _pad;
     double x0, y0, dx, dy, ref_value;
     double inv_dx, inv_dy;      // 1/dx, 1/dy
-    int64_t kx_max, ky_max;     // dkey(nx - 1), dkey(ny - 1)
+    // contains(y, x) (core/LUT2d.h:84-95) as order keys: it holds exactly
+    // where kx_lo <= dkey(x) <= kx_hi and ky_lo <= dkey(y) <= ky_hi (the
+    // host finds the bounds with the reference's expression)
+    int64_t kx_lo, kx_hi, ky_lo, ky_hi;
     const double* data;
     const double* sinc;         // method 0: the sinc kernel table in double, [SINC_SUB][SINC_LEN]
 };
 
-// core/LUT2d.h:84-95.  The index is formed with the reciprocal spacing; it
-// can differ from the reference's quotient by an ulp, which matters only for
-// a point within an ulp of the table's edge.
+// core/LUT2d.h:84-95: (x - xStart) / dx in [0, width - 1] and likewise in
+// y, which is monotone in x (in y), so it holds on an interval of each; the
+// test compares order keys with the interval's ends (Lut::kx_lo ...), the
+// same decision as the reference's for every x and y, off the FP64 pipe.
 GSLC_HD bool lut_contains(const Lut& l, double y, double x) {
     if (!l.have_data) return true;
-    const int64_t i = dkey((x - l.x0) * l.inv_dx);
-    const int64_t j = dkey((y - l.y0) * l.inv_dy);
-    return (i >= 0 && i <= l.kx_max) && (j >= 0 && j <= l.ky_max);
+    const int64_t kx = dkey(x), ky = dkey(y);
+    return kx >= l.kx_lo && kx <= l.kx_hi && ky >= l.ky_lo && ky <= l.ky_hi;
+}
+
+// (float)x from the bits with integer operations (off the FP64 pipe),
+// rounded to nearest even, where x is zero or rounds to a normal float;
+// other values (float subnormals, overflow, infinities, NaN) take the
+// conversion instruction.
+GSLC_HD float dbl_to_float(double x) {
+    const uint64_t b = dbits(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;   // the float's biased exponent
+    uint32_t u;
+    if ((b & DMAG) == 0) {
+        u = sign;
+    } else if (e < 1 || e > 254) {
+        return (float)x;
+    } else {
+        const uint64_t m = b & 0xfffffffffffffull;
+        u = ((uint32_t)e << 23) | (uint32_t)(m >> 29);
+        const uint64_t rest = m & 0x1fffffffull, half = 1ull << 28;
+        if (rest > half || (rest == half && (u & 1u))) ++u;   // a carry into the exponent rounds up correctly
+        u |= sign;
+    }
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float r;
+    memcpy(&r, &u, sizeof(r));
+    return r;
+#endif
 }
 
 // a load through a pointer that may address shared memory
@@ -301,29 +344,21 @@ struct Poly {
     double c[POLY_MAX];
 };
 
-// lut_eval in FP32 after the offsets from the table origin (FP64): for
-// values that only set float phases (the native Doppler of the sinc chip,
-// whose phasors are float angles).  Relative error ~1e-7 of the value;
-// nearest-neighbour tables take the FP64 form, whose rounding picks the cell.
+// The LUT's value in FP32 for values that only set float phases (the
+// native Doppler of the sinc chip, whose phasors are float angles): the
+// bilinear at table coordinates formed in FP32, relative error ~1e-7 of
+// the value; the other methods in FP64, whose rounding picks the cell.
 GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi);
 
-GSLC_HD float lut_eval_f32(const Lut& l, double y, double x) {
-    if (!l.have_data) return (float)l.ref_value;
-    if (l.method != 1) return (float)lut_eval(l, y, x);
-    return lut_bilinear_f32(l, (float)((x - l.x0) * l.inv_dx), (float)((y - l.y0) * l.inv_dy));
-}
-
-// lut_contains(l, y, x), and where it holds v = lut_eval_f32(l, y, x), the
-// table coordinates formed once
+// lut_contains(l, y, x), and where it holds v, the value in FP32 (above)
 GSLC_HD bool lut_contains_eval_f32(const Lut& l, double y, double x, float& v) {
     if (!l.have_data) {
         v = (float)l.ref_value;
         return true;
     }
-    const double xd = (x - l.x0) * l.inv_dx, yd = (y - l.y0) * l.inv_dy;
-    const int64_t i = dkey(xd), j = dkey(yd);
-    if (!((i >= 0 && i <= l.kx_max) && (j >= 0 && j <= l.ky_max))) return false;
-    v = l.method != 1 ? (float)lut_eval(l, y, x) : lut_bilinear_f32(l, (float)xd, (float)yd);
+    if (!lut_contains(l, y, x)) return false;
+    v = l.method != 1 ? (float)lut_eval(l, y, x)
+                      : lut_bilinear_f32(l, (float)((x - l.x0) * l.inv_dx), (float)((y - l.y0) * l.inv_dy));
     return true;
 }
 
@@ -333,8 +368,10 @@ GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi) {
     yi = fminf(fmaxf(yi, 0.f), (float)(l.ny - 1));
     const int x1 = (int)floorf(xi), x2 = (int)ceilf(xi);
     const int y1 = (int)floorf(yi), y2 = (int)ceilf(yi);
-    const float q11 = (float)ld_ro(l.data + (long)y1 * l.nx + x1), q12 = (float)ld_ro(l.data + (long)y2 * l.nx + x1);
-    const float q21 = (float)ld_ro(l.data + (long)y1 * l.nx + x2), q22 = (float)ld_ro(l.data + (long)y2 * l.nx + x2);
+    const float q11 = dbl_to_float(ld_ro(l.data + (long)y1 * l.nx + x1));
+    const float q12 = dbl_to_float(ld_ro(l.data + (long)y2 * l.nx + x1));
+    const float q21 = dbl_to_float(ld_ro(l.data + (long)y1 * l.nx + x2));
+    const float q22 = dbl_to_float(ld_ro(l.data + (long)y2 * l.nx + x2));
     const float wx2 = (float)x2 - xi, wx1 = xi - (float)x1, wy2 = (float)y2 - yi, wy1 = yi - (float)y1;
     if (y1 == y2 && x1 == x2) return q11;
     if (y1 == y2) return wx2 * q11 + wx1 * q21;
@@ -342,22 +379,24 @@ GSLC_HD float lut_bilinear_f32(const Lut& l, float xi, float yi) {
     return q11 * (wx2 * wy2) + q21 * (wx1 * wy2) + q12 * (wx2 * wy1) + q22 * (wx1 * wy1);
 }
 
-// core/Poly2d.cpp:8-24, normalised with reciprocals.  Products with a
-// factor that is exactly 1 (the first power of each variable) are taken as
-// the other factor, and powers past the last are not formed: the same values
-// with fewer FP64 operations.
+// core/Poly2d.cpp:8-24: the sum of c[i][j] xval^j yval^i with
+// xval = (x - xMean) / xNorm and yval likewise, here normalised with
+// reciprocals and summed in nested Horner form, one FMA per coefficient
+// (the term-by-term sum formed every power and product: 19 FP64
+// instructions per pixel for the frame's two carriers against 4).  The
+// rounding differs from the reference's by a few ulps of its largest term;
+// it serves the reramp's FP64 phase, and the deramp, whose float phase must
+// match the reference's, uses poly_eval_exact.
 GSLC_HD double poly_eval(const Poly& p, double y, double x) {
     const double xval = p.x_order > 0 ? (x - p.x_mean) * p.inv_x_norm : 0.0;
     const double yval = p.y_order > 0 ? (y - p.y_mean) * p.inv_y_norm : 0.0;
-    double scaley = 1., val = 0.;
-    for (int i = 0; i <= p.y_order; i++) {
-        if (i > 0) scaley = i == 1 ? yval : scaley * yval;
-        double scalex = 1.;
-        for (int j = 0; j <= p.x_order; j++) {
-            if (j > 0) scalex = j == 1 ? xval : scalex * xval;
-            const double sc = j == 0 ? scaley : (i == 0 ? scalex : scalex * scaley);
-            val += sc * p.c[i * (p.x_order + 1) + j];
-        }
+    const int nx = p.x_order + 1;
+    double val = 0.0;
+    for (int i = p.y_order; i >= 0; --i) {
+        const double* c = p.c + i * nx;
+        double row = c[p.x_order];
+        for (int j = p.x_order - 1; j >= 0; --j) row = fma(row, xval, c[j]);
+        val = i == p.y_order ? row : fma(val, yval, row);
     }
     return val;
 }

@@ -189,6 +189,29 @@ def test_utm_geogrid_and_lut_doppler(oracle_mod, precision):
     assert r["n_valid"] > 10000
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+def test_partial_native_doppler(oracle_mod, c1, precision):
+    """A native Doppler table covering part of the swath, its edges running
+    through the geogrid in range and azimuth: pixels whose zero-Doppler time
+    and range (geocodeSlc.cpp:200-206), or whose chip's az and rng
+    (geocodeSlc.cpp:457-467), fall outside it are left as the reference's
+    LUT2d::contains decides, and the chips inside are demodulated with the
+    table's Doppler."""
+    rg = c1.radar_grid
+    span_r = rg.end_range - rg.starting_range
+    span_t = rg.sensing_stop - rg.sensing_start
+    rr = np.linspace(rg.starting_range + 0.2 * span_r, rg.starting_range + 0.75 * span_r, 13)
+    tt = np.linspace(rg.sensing_start + 0.15 * span_t, rg.sensing_start + 0.8 * span_t, 9)
+    u = np.linspace(-1.0, 1.0, 13)
+    dop = LUT2d(rr, tt, np.tile(30.0 - 55.0 * u ** 2, (9, 1)) + 8.0 * np.linspace(-1, 1, 9)[:, None])
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], native_doppler=dop, geo2rdr_precision=precision)
+    r = _check(gpu, ora)[0]
+    m = gpu["mask"]
+    inside, outside = (m != 255).mean(), (m == 255).mean()
+    assert inside > 0.2 and outside > 0.2, (inside, outside)
+    assert r["n_valid"] > 10000
+
+
 @pytest.mark.parametrize("case", ["coarse_exact", "dem_west_edge", "utm_dem"])
 def test_utm_tile_fit_and_exact_paths(oracle_mod, case):
     """UTM geogrids through both ground-point paths of the kernel: the tile
