@@ -274,6 +274,7 @@ void make_orbit_segments(const gslc_orbit& o, const double* piece, double* out, 
         double* s = out + (size_t)j * SEG_STRIDE;
         std::fill(s, s + SEG_STRIDE, 0.0);
         for (int d = 0; d < 3; ++d) s[d] = pc[d];
+        s[SEG_T] = std::fma((double)j, o.spacing, o.t0);
         double a[3][8], b[3][7];
         for (int d = 0; d < 3; ++d) {
             dd ta[8], tb[7];

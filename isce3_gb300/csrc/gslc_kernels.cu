@@ -960,7 +960,7 @@ __device__ __forceinline__ void geocode_pixel(const GeoParams& p, const double* 
                 azc = (t - p.rg_t0) * p.rg_prf;
                 rgc = range_index(p, R);
                 valid = true;
-                const int intAz = (int)floor(azc), intRg = (int)floor(rgc);
+                const int intAz = floor_int(azc), intRg = floor_int(rgc);
                 const bool corners = !(intRg < 4 || intRg >= p.rg_wid - 4 || intAz < 4 || intAz >= p.rg_len - 4);
                 if (p.have_subsw && p.mask) {
                     int m = subswath_of(p, intAz, intRg);

@@ -140,6 +140,14 @@ GSLC_HD float small_int_to_float(int32_t n) {
 #endif
 }
 
+// (int)floor(x): the integer part from the bits where x is in [0, 2^31)
+// (split_bits, off the FP64 pipe), the FP64 floor elsewhere.
+GSLC_HD int floor_int(double x) {
+    uint64_t f;
+    const int32_t i = split_bits(x, f);
+    return i != 0x7fffffff ? (int)i : (int)floor(x);
+}
+
 // ---- LUT2d (core/LUT2d.{h,cpp}) ------------------------------------------
 struct Lut {
     int32_t have_data, bounds_error, method, nx, ny, _pad;
@@ -649,8 +657,12 @@ constexpr int ORB_STRIDE = 48;   // pref[3], a[3][8], b[3][7] (b = d/dt coeffici
 // polynomial (truncated where its tail is below 1e-9 m^2/s), G a truncated
 // power series of 1/|vel|^2 accurate to about one ulp on the segment.
 constexpr int SEG_NH = 14, SEG_NG = 13;
-constexpr int SEG_STRIDE = 76;   // pref[3], a[3][8], b[3][7], h[14], g[13], pad
+constexpr int SEG_STRIDE = 76;   // pref[3], a[3][8], b[3][7], h[14], g[13], t
 constexpr int SEG_A = 3, SEG_B = 27, SEG_H = 48, SEG_G = 62;
+// t: the segment's start time t0 + j * spacing, rounded once (an FMA), as
+// the Newton forms it; read where the iterate enters a segment instead of
+// converting the index (two FP64-pipe conversions and two FMAs saved)
+constexpr int SEG_T = 75;
 // The same segment tables as float pairs (hi, lo) for the float-float Newton.
 constexpr int SEGFF_STRIDE = 72;   // float2: b[3][7], h[14], g[13], a[3][8]
 constexpr int SEGFF_B = 0, SEGFF_H = 21, SEGFF_G = 35, SEGFF_A = 48;
@@ -827,14 +839,21 @@ GSLC_HD bool geo2rdr_zero_doppler_seg(const Orbit& o, const double* seg, V3 xyz,
             else t = tj + (w + 0.5) * o.spacing;
             const int64_t kt = dkey(t);
             if (!(kt >= k_t0 && kt <= k_tend)) return false;  // FillNaN -> no convergence
-            const int pc = orbit_piece(o, t);
-            const double tidx = o.t0 + pc * o.spacing;
+            // orbit_piece(o, t) with the truncation from the bits (the
+            // argument is at least 1 here, t >= t0), then t_idx, the start
+            // of segment pc, from the tables
+            uint64_t fb;
+            const int32_t tr = split_bits((t - o.t0) * o.inv_spacing + 1, fb);
+            int pc = tr - 2;
+            pc = pc < 0 ? 0 : pc;
+            pc = pc > o.n - 4 ? o.n - 4 : pc;
+            const double tidx = ld_gen(seg + (int64_t)pc * SEG_STRIDE + SEG_T);
             w = (t - tidx) * o.inv_spacing - 1.5;
             const int j = orbit_segment(o, pc, w);
             c = seg + (int64_t)j * SEG_STRIDE;
             if (j != cur) {
                 cur = j;
-                tj = o.t0 + j * o.spacing;
+                tj = ld_gen(c + SEG_T);
                 D[0] = xyz.x - ld_gen(c + 0);
                 D[1] = xyz.y - ld_gen(c + 1);
                 D[2] = xyz.z - ld_gen(c + 2);
