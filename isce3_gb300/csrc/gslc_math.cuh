@@ -161,6 +161,58 @@ struct Lut {
     const double* sinc;         // method 0: the sinc kernel table in double, [SINC_SUB][SINC_LEN]
 };
 
+// Host side (launch preparation): the key intervals of Lut and GeoParams.
+// The double whose order key (dkey) is k, for the keys of finite doubles.
+inline double key_double(int64_t k) {
+    const uint64_t b = k >= 0 ? (uint64_t)k : ((uint64_t)(-k) | 0x8000000000000000ull);
+    double x;
+    memcpy(&x, &b, sizeof(x));
+    return x;
+}
+
+// Order keys [lo, hi] of the finite x where g(x) >= 0.0 and g(x) <= top hold
+// together, for g monotone in x (non-decreasing when up, else
+// non-increasing) and never NaN there: each test is monotone in x, so its
+// boundary is found by bisection over the keys, evaluating g as the
+// reference writes it.  Empty: lo > hi.
+template <class G>
+inline void key_interval(G g, bool up, double top, int64_t& lo, int64_t& hi) {
+    const int64_t kmax = dkey(1.7976931348623157e308);   // the largest finite double
+    // first key in [-kmax, kmax] where pred holds (pred false, then true), kmax + 1 if none
+    auto first = [&](auto pred) {
+        int64_t a = -kmax, b = kmax + 1;
+        while (a < b) {
+            const int64_t m = a + (int64_t)(((uint64_t)b - (uint64_t)a) / 2);
+            if (pred(key_double(m))) b = m;
+            else a = m + 1;
+        }
+        return a;
+    };
+    if (up) {
+        lo = first([&](double x) { return g(x) >= 0.0; });
+        hi = first([&](double x) { return !(g(x) <= top); }) - 1;
+    } else {
+        lo = first([&](double x) { return g(x) <= top; });
+        hi = first([&](double x) { return !(g(x) >= 0.0); }) - 1;
+    }
+}
+
+// The keys of one axis of LUT2d::contains (core/LUT2d.h:84-95):
+// (x - x0) / dx in [0, n - 1].  A spacing of zero or NaN, or an origin that
+// is not finite, contains nothing; an infinite spacing contains every
+// finite x (the quotient is zero) when n >= 1.
+inline void lut_axis_keys(double x0, double dx, int n, int64_t& lo, int64_t& hi) {
+    const int64_t kmax = dkey(1.7976931348623157e308);   // the largest finite double
+    lo = 1;
+    hi = 0;
+    if (!isfinite(x0) || !(dx != 0.0)) return;
+    if (isinf(dx)) {
+        if (n >= 1) { lo = -kmax; hi = kmax; }
+        return;
+    }
+    key_interval([&](double x) { return (x - x0) / dx; }, dx > 0, n - 1.0, lo, hi);
+}
+
 // core/LUT2d.h:84-95: (x - xStart) / dx in [0, width - 1] and likewise in
 // y, which is monotone in x (in y), so it holds on an interval of each; the
 // test compares order keys with the interval's ends (Lut::kx_lo ...), the

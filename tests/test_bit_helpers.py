@@ -171,3 +171,108 @@ def test_small_int_to_float_identity():
     bits = (np.uint64(0x4B400000) + n.astype(np.int64).astype(np.uint64)) & np.uint64(0xFFFFFFFF)
     v = bits.astype(np.uint32).view(np.float32) - np.float32(12582912.0)
     np.testing.assert_array_equal(v, n.astype(np.float32))
+
+
+HARNESS3 = r"""
+#include "gslc_math.cuh"
+#include <cstdio>
+#include <cstring>
+using namespace gslc;
+static double d(unsigned long long b) { double x; memcpy(&x, &b, 8); return x; }
+int main() {
+    int mode, n;
+    unsigned long long a, b, c, e, x;
+    while (scanf("%d %d %llx %llx %llx %llx %llx", &mode, &n, &a, &b, &c, &e, &x) == 7) {
+        int64_t lo, hi;
+        if (mode == 1) {
+            lut_axis_keys(d(a), d(b), n, lo, hi);
+        } else {
+            const double t0 = d(a), prf = d(b), y0 = d(c), dy = d(e);
+            key_interval([&](double azc) { return ((t0 + azc / prf) - y0) / dy; }, (prf > 0) == (dy > 0), n - 1.0,
+                         lo, hi);
+        }
+        const int64_t k = dkey(d(x));
+        printf("%d\n", (k >= lo && k <= hi) ? 1 : 0);
+    }
+    return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def harness3(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        pytest.skip("needs nvcc")
+    d = tmp_path_factory.mktemp("bits3")
+    (d / "h.cu").write_text(HARNESS3)
+    subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-I",
+                    str(ROOT / "isce3_gb300" / "csrc"), str(d / "h.cu"), "-o", str(d / "h")],
+                   check=True, capture_output=True)
+
+    def run(rows):
+        hx = lambda v: f"{int(np.float64(v).view(np.uint64)):x}"
+        inp = "\n".join(f"{m} {n} {hx(a)} {hx(b)} {hx(c)} {hx(e)} {hx(x)}" for m, n, a, b, c, e, x in rows) + "\n"
+        out = subprocess.run([str(d / "h")], input=inp, capture_output=True, text=True, check=True).stdout
+        return [int(v) for v in out.split()]
+    return run
+
+
+def _near(v, k):
+    """v and the k doubles on each side of it"""
+    out = [v]
+    lo = hi = np.float64(v)
+    for _ in range(k):
+        lo, hi = np.nextafter(lo, -np.inf), np.nextafter(hi, np.inf)
+        out += [lo, hi]
+    return out
+
+
+def test_lut_contains_key_intervals(harness3):
+    """LUT2d::contains as order-key intervals (lut_axis_keys) decides as the
+    reference's (x - xStart) / dx in [0, width - 1] (core/LUT2d.h:84-95)
+    does, at and beside the table's edges, for both spacing signs and
+    degenerate spacings."""
+    rng = np.random.default_rng(21)
+    rows, want = [], []
+    cases = [(848750.0, 1732.0564516128507, 32), (99.86842105263158, 0.35617572156196786, 32), (0.1, 0.3, 7),
+             (5.0, -0.7, 9), (-3.0, 1e-3, 1), (1e6, 3.3, 2)]
+    cases += [(float(rng.uniform(-1e6, 1e6)), float(rng.choice([-1, 1]) * 10 ** rng.uniform(-4, 4)),
+               int(rng.integers(1, 200))) for _ in range(20)]
+    for x0, dx, n in cases:
+        x0, dx = np.float64(x0), np.float64(dx)
+        end = x0 + (n - 1) * dx
+        for x in _near(x0, 3) + _near(end, 3) + list(rng.uniform(min(x0, end) - 5 * abs(dx), max(x0, end) + 5 * abs(dx), 20)):
+            x = np.float64(x)
+            i = (x - x0) / dx
+            rows.append((1, n, x0, dx, 0.0, 0.0, x))
+            want.append(int(i >= 0.0 and i <= n - 1.0))
+    for x0, dx, n, xs in [(1.0, 0.0, 5, [1.0, 2.0, 0.5]), (1.0, np.inf, 3, [-1e300, 0.0, 5.0]),
+                          (np.inf, 1.0, 3, [1.0, 1e308]), (1.0, np.nan, 3, [1.0])]:
+        for x in xs:
+            with np.errstate(all="ignore"):
+                i = (np.float64(x) - x0) / dx
+            rows.append((1, n, x0, dx, 0.0, 0.0, x))
+            want.append(int(i >= 0.0 and i <= n - 1.0))
+    assert harness3(rows) == want
+
+
+def test_chip_doppler_key_intervals(harness3):
+    """The chip's contains(t0 + azc / prf, ...) as a key interval of azc
+    (geocodeSlc.cpp:462-467) decides as the composed FP64 expression does."""
+    rng = np.random.default_rng(22)
+    rows, want = [], []
+    for _ in range(30):
+        t0, prf = np.float64(rng.uniform(0, 1e4)), np.float64(rng.uniform(100, 3000))
+        n = int(rng.integers(2, 64))
+        dy = np.float64(rng.choice([-1, 1]) * rng.uniform(0.01, 2.0))
+        y0 = np.float64(t0 + rng.uniform(-5, 5))
+        # azc near the table's two edges
+        for edge in (y0, y0 + (n - 1) * dy):
+            a0 = (edge - t0) * prf
+            for azc in _near(a0, 4) + list(rng.uniform(a0 - 3, a0 + 3, 10)):
+                azc = np.float64(azc)
+                j = ((t0 + azc / prf) - y0) / dy
+                rows.append((2, n, t0, prf, y0, dy, azc))
+                want.append(int(j >= 0.0 and j <= n - 1.0))
+    assert harness3(rows) == want
