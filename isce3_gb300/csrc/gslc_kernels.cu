@@ -285,16 +285,20 @@ __device__ bool geo2rdr_ff(const GeoParams& p, V3 xyz, double& t, double& R) {
             if (j >= 0) t = tj + ((double)w.hi + (double)w.lo + 0.5) * o.spacing;
             const int64_t kt = dkey(t);                         // the span test on order keys
             if (!(kt >= dkey(o.t0) && kt <= dkey(o.t_end))) return false;    // FillNaN -> no convergence
-            const int pc = orbit_piece(o, t);
-            const double tidx = o.t0 + pc * o.spacing;
+            // orbit_piece(o, t) truncated from the bits (t >= t0 here) and
+            // the segment start times from the tables, as the FP64 path
+            uint64_t fb;
+            int pc = split_bits((t - o.t0) * o.inv_spacing + 1, fb) - 2;
+            pc = pc < 0 ? 0 : (pc > o.n - 4 ? o.n - 4 : pc);
+            const double tidx = __ldg(o.seg + (int64_t)pc * SEG_STRIDE + SEG_T);
             double w64 = (t - tidx) * o.inv_spacing - 1.5;
             const int jn = orbit_segment(o, pc, w64);
             w = ff_from_double(w64);
             if (jn != j) {
                 j = jn;
-                tj = o.t0 + j * o.spacing;
                 c = o.seg_ff + (int64_t)j * SEGFF_STRIDE;
                 const double* pref = o.seg + (int64_t)j * SEG_STRIDE;
+                tj = __ldg(pref + SEG_T);
                 D[0] = ff_from_double(xyz.x - __ldg(pref + 0));
                 D[1] = ff_from_double(xyz.y - __ldg(pref + 1));
                 D[2] = ff_from_double(xyz.z - __ldg(pref + 2));
