@@ -46,7 +46,7 @@ UNIT = "px/s"
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gslc", "reference"], default="gslc")
     p.add_argument("--workload", choices=["frame", "medium", "small"], default="frame")
@@ -96,16 +96,27 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.skip = 0       # samples written before the timed region
 
     def start(self):
+        """Start sampling every 50 ms and return once the first sample is
+        written (at most 3 s), so that the samples fall inside the timed
+        region that follows."""
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t_end = time.perf_counter() + 3.0
+        while time.perf_counter() < t_end and self.proc.poll() is None:
+            if Path(self.path).stat().st_size > 0:
+                break
+            time.sleep(0.005)
+        self.skip = sum(1 for ln in Path(self.path).read_text().splitlines() if ln.strip())
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -117,6 +128,10 @@ class ClockSampler:
             self.proc.kill()
         rows = [ln.split(",") for ln in Path(self.path).read_text().splitlines() if ln.strip()]
         os.unlink(self.path)
+        # samples taken before start() returned are not in the timed region,
+        # unless they are all there is
+        if len(rows) > self.skip:
+            rows = rows[self.skip:]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
