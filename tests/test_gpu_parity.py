@@ -212,6 +212,20 @@ def test_partial_native_doppler(oracle_mod, c1, precision):
     assert r["n_valid"] > 10000
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ff"])
+def test_native_doppler_table_beyond_index_range(oracle_mod, c1, precision):
+    """A bilinear native Doppler table spanning more than 2^21 range samples
+    (1000 km cells): the chip's Doppler takes the FP64-coordinate form
+    instead of the one from the radar indices, with the same results."""
+    rg = c1.radar_grid
+    rr = rg.starting_range - 8.0e6 + 1.0e6 * np.arange(17)
+    tt = np.linspace(rg.sensing_start - 1.0, rg.sensing_stop + 1.0, 5)
+    dop = LUT2d(rr, tt, np.tile(20.0 + 3.0e-6 * (rr - rg.starting_range), (5, 1)) + 4.0 * np.arange(5)[:, None])
+    gpu, ora = _run_both(oracle_mod, c1, [c1.slc], native_doppler=dop, geo2rdr_precision=precision)
+    r = _check(gpu, ora)[0]
+    assert r["n_valid"] > 10000
+
+
 @pytest.mark.parametrize("case", ["coarse_exact", "dem_west_edge", "utm_dem"])
 def test_utm_tile_fit_and_exact_paths(oracle_mod, case):
     """UTM geogrids through both ground-point paths of the kernel: the tile
