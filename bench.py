@@ -199,11 +199,12 @@ def run_oracle_sample(oracle, sc, g, box, outputs=False):
 
 def cpu_sample_rows(sc, steps: int, warmup: int):
     """Geogrid rows of both CPU timings (the cpu_baseline leg and the
-    reference arm): the whole geogrid when at most 12 oracle runs are timed,
-    else its centred half, so that the reference arm's warm-up and timed
-    steps end within about two minutes on the frame."""
+    reference arm): the whole geogrid when at most 13 oracle runs are timed
+    (the default 10 steps after 3 warm-ups), else its centred half, so that
+    the reference arm's warm-up and timed steps end within about two
+    minutes on the frame (9.6 s per whole-frame run on 16 cores)."""
     n = sc.geogrid.length
-    if steps + warmup <= 12:
+    if steps + warmup <= 13:
         return 0, n
     rows = n // 2
     return (n - rows) // 2, rows
