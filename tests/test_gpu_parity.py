@@ -226,6 +226,24 @@ def test_native_doppler_table_beyond_index_range(oracle_mod, c1, precision):
     assert r["n_valid"] > 10000
 
 
+@pytest.mark.parametrize("where", ["south_32734", "descending_32610"])
+def test_utm_south_and_descending_pass(oracle_mod, where):
+    """The reduced frame scene moved to the southern hemisphere (UTM zone 34
+    south, false northing 10,000 km: Projections.cpp's south branch) and to
+    a descending pass (the swath crossing the UTM rows the other way)."""
+    if where == "south_32734":
+        sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0, epsg=32734, lat0_deg=-33.9,
+                            lon0_deg=19.5)
+    else:
+        sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0, epsg=32610, lat0_deg=47.5,
+                            lon0_deg=-114.0, ascending=False)
+    for precision in ("fp64", "ff"):
+        gpu, ora = _run_both(oracle_mod, sc, [sc.slc], az_carrier=sc.az_carrier, rg_carrier=sc.rg_carrier,
+                             geo2rdr_precision=precision)
+        r = _check(gpu, ora)[0]
+        assert r["n_valid"] > 10000
+
+
 @pytest.mark.parametrize("case", ["coarse_exact", "dem_west_edge", "utm_dem"])
 def test_utm_tile_fit_and_exact_paths(oracle_mod, case):
     """UTM geogrids through both ground-point paths of the kernel: the tile
