@@ -209,18 +209,20 @@ def utm_forward_host(epsg, lon, lat):
 
 
 def scene_c2(seed: int = 2, length=16384, width=8192, geo=8000, spacing=10.0, dem_arcsec=1.0, slc=True,
-             epsg=32611, geo_length=None, lat0_deg=35.0, lon0_deg=-121.8, ascending=True):
+             epsg=32611, geo_length=None, lat0_deg=35.0, lon0_deg=-121.8, ascending=True,
+             look_side=LookSide.Right):
     """Frame-scale scene: 16384 x 8192 SLC onto an 8000 x 8000 UTM 10 m grid.
 
     Native Doppler: 32 x 32 LUT2d, quadratic in range, +-50 Hz; azimuth carrier:
     linear Poly2d; DEM: EPSG:4326 fBm at ``dem_arcsec`` arc-seconds, 0-3000 m.
-    The pass is centred on (``lat0_deg``, ``lon0_deg``); ``epsg`` must hold
-    that point (326zz north, 327zz south).
+    The orbit passes (``lat0_deg``, ``lon0_deg``) ascending or descending and
+    the radar looks to ``look_side``; ``epsg`` must hold the swath (326zz
+    north, 327zz south).
     """
     rng = np.random.default_rng(seed)
     model = CircularOrbitModel(lat0_deg=lat0_deg, lon0_deg=lon0_deg, ascending=ascending)
     prf, dr, r0, wvl = 1520.0, 6.25, 850e3, 0.24
-    grid = RadarGridParameters(100.0, wvl, prf, r0, dr, LookSide.Right, length, width, EPOCH)
+    grid = RadarGridParameters(100.0, wvl, prf, r0, dr, look_side, length, width, EPOCH)
     orbit = model.orbit(grid.sensing_mid, 21, 10.0)
     lon, lat = _swath_bounds(model, grid, 1500.0)
     lon_c, lat_c = lon.mean(), lat.mean()

@@ -226,12 +226,17 @@ def test_native_doppler_table_beyond_index_range(oracle_mod, c1, precision):
     assert r["n_valid"] > 10000
 
 
-@pytest.mark.parametrize("where", ["south_32734", "descending_32610"])
+@pytest.mark.parametrize("where", ["south_32734", "descending_32610", "left_32609"])
 def test_utm_south_and_descending_pass(oracle_mod, where):
     """The reduced frame scene moved to the southern hemisphere (UTM zone 34
-    south, false northing 10,000 km: Projections.cpp's south branch) and to
-    a descending pass (the swath crossing the UTM rows the other way)."""
-    if where == "south_32734":
+    south, false northing 10,000 km: Projections.cpp's south branch), to a
+    descending pass (the swath crossing the UTM rows the other way) and to
+    a left-looking radar (the first iterate's look-side test,
+    geometry/detail/Geo2Rdr.icc:156-161, with the other sign)."""
+    if where == "left_32609":
+        sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0, epsg=32609,
+                            look_side=synth.LookSide.Left)
+    elif where == "south_32734":
         sc = synth.scene_c2(length=2048, width=1024, geo=600, spacing=12.0, epsg=32734, lat0_deg=-33.9,
                             lon0_deg=19.5)
     else:
