@@ -156,6 +156,17 @@ def test_c1_doppler_carriers_corrections_blocks(oracle_mod, c1):
     _check(gpu, ora, az_first=a0, rg_first=r0)
 
 
+def test_more_blocks_than_one_launch(oracle_mod, c1):
+    """17 radar/geo block pairs: more than one launch's 16 (the call runs its
+    blocks in groups of 16 with the same geometry)."""
+    scales = [np.complex64(np.exp(0.3j * k) * (1.0 + 0.05 * k)) for k in range(17)]
+    blocks = [c1.slc * s_ for s_ in scales]
+    az_car = Poly2d([[0.0], [2 * np.pi * 100.0]], y_mean=c1.radar_grid.sensing_mid)
+    gpu, ora = _run_both(oracle_mod, c1, blocks, n_out=17, az_carrier=az_car, rg_carrier=Poly2d())
+    reports = _check(gpu, ora)
+    assert len(reports) == 17 and all(r["n_valid"] > 10000 for r in reports)
+
+
 @pytest.mark.parametrize("flatten,reramp,precision", [(False, True, "fp64"), (True, False, "fp64"),
                                                      (False, False, "fp64"), (True, True, "ff")])
 def test_c1_flags(oracle_mod, c1, flatten, reramp, precision):
